@@ -1,0 +1,193 @@
+// Shared device-side definitions of the GB300 immersed-boundary time step.
+//
+// Layout (identical to the reference, src/utils.h:8-16): every field lives
+// on the padded cell grid (Nx+4)(Ny+4)(Nz+4), k fastest, interior cell
+// (i,j,k) at ((i+2)*sx + (j+2)*sy + (k+2)).  Face fields use the same
+// padded cell layout: the x-face between cells i-1 and i is stored at cell
+// (i,j,k), so all fields share one index and one allocation size.  1-D
+// metric arrays have N+4 entries indexed i+2 (the reference's c1e()).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace ibm {
+
+enum { FLUID = 1, GHOST = 2, SOLID = 3 };
+
+// Boundary-condition types, values as in the reference (src/ibm3d.h:37-45).
+enum { BCT_VELOCITY = 0, BCT_PRESSURE = 1, BCT_WALL = 2, BCT_SLIP = 3,
+       BCT_SYMMETRIC = 4, BCT_PERIODIC = 5, BCT_VELPERIODIC = 6 };
+
+// Face order of the reference's bc[] array: north, east, south, west, down, up.
+enum { F_N = 0, F_E = 1, F_S = 2, F_W = 3, F_D = 4, F_U = 5 };
+
+struct Grid {
+    int nx, ny, nz;
+    long long sx, sy;   // strides of i and j (k stride is 1)
+    long long ncell;    // (nx+4)(ny+4)(nz+4)
+};
+
+__host__ __device__ inline long long cidx(const Grid &g, int i, int j, int k) {
+    return (long long)(i + 2) * g.sx + (long long)(j + 2) * g.sy + (k + 2);
+}
+
+__host__ __device__ inline void cijk(const Grid &g, long long idx, int &i, int &j, int &k) {
+    i = (int)(idx / g.sx) - 2;
+    long long r = idx - (long long)(i + 2) * g.sx;
+    j = (int)(r / g.sy) - 2;
+    k = (int)(r - (long long)(j + 2) * g.sy) - 2;
+}
+
+// Per-axis 1-D tables (device pointers, N+4 entries, index i+2).
+struct Axis {
+    const double *d;     // cell width
+    const double *c;     // centroid
+    const double *wm;    // face i: weight of cell i-1 = d(i)/(d(i-1)+d(i))
+    const double *wp;    // face i: weight of cell i   = d(i-1)/(d(i-1)+d(i))
+    const double *rd;    // 1/d(i)
+    const double *rdc;   // 1/(c(i)-c(i-1))        face-normal gradient
+    const double *rdcc;  // 1/(c(i+1)-c(i-1))      cell-centred gradient
+    const double *km;    // Crank-Nicolson coefficient toward i-1 (kx_W)
+    const double *kp;    // Crank-Nicolson coefficient toward i+1 (kx_E)
+};
+
+// Boundary face description with every coefficient the outer-layer rows
+// and fills need, precomputed on the host from the reference's formulas
+// (src/ibm3d_setup.c:1723-2903, src/ibm3d_fracstep.c:855-1906).
+// Index [L-1] is the layer (1 = adjacent to the boundary, 2 = outermost).
+struct BCFace {
+    int type;            // BCT_*, after set_bc's rewrites (WALL->VELOCITY, SYMMETRIC->SLIP)
+    double val[3];       // constant velocity value
+    double pval;         // constant pressure value
+    // Operator rows.
+    double dir_o[2], dir_m[2];   // Dirichlet interpolation: dir_o*x_o + dir_m*x_m
+    double ext_o[2], ext_2[2];   // 3-point extrapolation: ext_o*x_o - x_(o+1in) + ext_2*x_(o+2in)
+    // Fills (update_outer).
+    double fv_a[2], fv_b[2];     // velocity Dirichlet / slip: u_o = fv_a*bc - fv_b*u_m
+    double fe_a[2], fe_b[2];     // extrapolation: u_o = fe_a*u_(o+1in) - fe_b*u_(o+2in)
+    double fp_a[2], fp_b[2];     // pressure Dirichlet: p_o = fp_a*bc - fp_b*p_m
+};
+
+struct BCSet {
+    BCFace f[6];
+    int p_singular;      // no pressure / velocity-periodic face: pin p'(0,0,0)
+};
+
+// Which boundary face owns an outer cell (each outer cell is owned by
+// exactly one face in the reference's matrix assembly: z faces own every
+// cell with k outside, y faces every remaining cell with j outside, x faces
+// the rest).  Returns -1 for interior cells; layer is 1 or 2.
+__host__ __device__ inline int owner_face(const Grid &g, int i, int j, int k, int &layer) {
+    if (k < 0) { layer = -k; return F_D; }
+    if (k >= g.nz) { layer = k - g.nz + 1; return F_U; }
+    if (j < 0) { layer = -j; return F_S; }
+    if (j >= g.ny) { layer = j - g.ny + 1; return F_N; }
+    if (i < 0) { layer = -i; return F_W; }
+    if (i >= g.nx) { layer = i - g.nx + 1; return F_E; }
+    layer = 0;
+    return -1;
+}
+
+__host__ __device__ inline int face_axis(int f) { return (f == F_E || f == F_W) ? 0 : (f == F_N || f == F_S) ? 1 : 2; }
+__host__ __device__ inline bool face_low(int f) { return f == F_W || f == F_S || f == F_D; }
+
+// Periodic image of a padded cell: every outer coordinate wrapped into the
+// interior, as the reference's cell_idx_periodic (src/ibm3d_setup.c:892-1074).
+__host__ __device__ inline long long periodic_image(const Grid &g, int i, int j, int k) {
+    if (i < 0) i += g.nx; else if (i >= g.nx) i -= g.nx;
+    if (j < 0) j += g.ny; else if (j >= g.ny) j -= g.ny;
+    if (k < 0) k += g.nz; else if (k >= g.nz) k -= g.nz;
+    return cidx(g, i, j, k);
+}
+
+// ------------------------------------------------------------ reductions --
+// Deterministic two-level reductions: every block writes its partial sums
+// to partials[block][v]; the last block to finish adds them in block order.
+constexpr int RED_MAX = 8;
+
+template <int NV>
+__device__ inline void block_sum(double (&v)[NV], double *smem /* [32*NV] */) {
+#pragma unroll
+    for (int q = 0; q < NV; q++) {
+        double x = v[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        v[q] = x;
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; q++) smem[warp * NV + q] = v[q];
+    }
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = blockDim.x >> 5;
+#pragma unroll
+        for (int q = 0; q < NV; q++) {
+            double x = lane < nw ? smem[lane * NV + q] : 0.0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+            v[q] = x;
+        }
+    }
+}
+
+template <int NV>
+__device__ inline void block_max(double (&v)[NV], double *smem) {
+#pragma unroll
+    for (int q = 0; q < NV; q++) {
+        double x = v[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x = fmax(x, __shfl_down_sync(0xffffffffu, x, o));
+        v[q] = x;
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; q++) smem[warp * NV + q] = v[q];
+    }
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = blockDim.x >> 5;
+#pragma unroll
+        for (int q = 0; q < NV; q++) {
+            double x = lane < nw ? smem[lane * NV + q] : 0.0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) x = fmax(x, __shfl_down_sync(0xffffffffu, x, o));
+            v[q] = x;
+        }
+    }
+}
+
+// Publishes this block's NV partials; returns true in thread 0 of the last
+// block, which then finds every block's partials in `partials`.
+template <int NV>
+__device__ inline bool publish_partials(const double (&v)[NV], double *partials, unsigned int *counter) {
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; q++) partials[blockIdx.x * NV + q] = v[q];
+        __threadfence();
+        unsigned int t = atomicAdd(counter, 1u);
+        last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        __threadfence();
+        return true;
+    }
+    return false;
+}
+
+template <int NV>
+__device__ inline void sum_partials(const double *partials, int nblocks, double (&out)[NV]) {
+#pragma unroll
+    for (int q = 0; q < NV; q++) out[q] = 0.0;
+    for (int b = 0; b < nblocks; b++) {
+#pragma unroll
+        for (int q = 0; q < NV; q++) out[q] += ((volatile const double *)partials)[b * NV + q];
+    }
+}
+
+}  // namespace ibm

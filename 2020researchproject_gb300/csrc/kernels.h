@@ -1,0 +1,86 @@
+// Kernel argument structs and launch wrappers shared by the host code.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace ibm {
+
+struct ConvArgs {
+    const double *u[3];
+    const double *U[3];
+    const double *p;
+    const double *Np[3];
+    const double *tau[6];
+    double *N[3];
+    double *b[3];
+};
+
+struct TauArgs {
+    double *tau[6];
+};
+
+struct UstarArgs {
+    const double *us[3];
+    const double *p;
+    double *Us[3];
+    double *b;
+};
+
+struct NextArgs {
+    const double *us[3];
+    const double *Us[3];
+    const double *p;
+    const double *pp;
+    double *un[3];
+    double *Un[3];
+    double *pn;
+};
+
+enum { GK_ARRAY = 0, GK_OLD = 1, GK_SKIP = 2 };
+
+struct GhostArgs {
+    int nghost;
+    int nlevels;
+    const int *level_start;  // device, nlevels+1
+    const int *cell;         // padded index of each ghost (level-sorted)
+    const int *ref;          // [8*g+e]: padded index (GK_ARRAY) or ghost id (GK_OLD)
+    const int8_t *kind;      // [8*g+e]
+    const double *w;         // [8*g+e] normalised weights (0 where skipped)
+    const double *wself;     // weight of the ghost cell in its own stencil
+    double *old;             // [4*g]: snapshot of u1,u2,u3,p
+};
+
+// Operator context for the matrix-free momentum and pressure rows.
+struct OpCtx {
+    Grid g;
+    Axis ax, ay, az;
+    BCSet bc;
+    const uint8_t *flag;
+    const int *gid;          // padded index -> ghost id, -1 elsewhere
+    const int *gidx;         // [8*g+e] padded index of a stencil entry, -1 if dropped
+    const double *gw;        // [8*g+e] normalised weight
+    const double *gwself;    // [g]
+    const double *dinv;      // 1/coeffsum on fluid cells (pressure rows)
+};
+
+void launch_conv_rhs(cudaStream_t s, const Grid &g, const Axis &ax, const Axis &ay, const Axis &az,
+                     const BCSet &bc, const uint8_t *flag, const ConvArgs &a, double dt, const double f[3],
+                     int les);
+void launch_smagorinsky(cudaStream_t s, const Grid &g, const Axis &ax, const Axis &ay, const Axis &az,
+                        const uint8_t *flag, const double *lvset, const double *const u[3], const TauArgs &t,
+                        double cs);
+void launch_ustar_prhs(cudaStream_t s, const Grid &g, const Axis &ax, const Axis &ay, const Axis &az,
+                       const BCSet &bc, const uint8_t *flag, const UstarArgs &a, double dt, double Re);
+void launch_update_next(cudaStream_t s, const Grid &g, const Axis &ax, const Axis &ay, const Axis &az,
+                        const BCSet &bc, const uint8_t *flag, const NextArgs &a, double dt, double *partials,
+                        unsigned int *counter, double *maxdiv_out, int nblocks);
+void launch_fill_outer(cudaStream_t s, const Grid &g, const BCSet &bc, double *const u[3], double *p);
+void launch_interp_stag(cudaStream_t s, const Grid &g, const Axis &ax, const Axis &ay, const Axis &az,
+                        const double *const u[3], double *const U[3]);
+void launch_ghost_update(cudaStream_t s, const GhostArgs &a, double *const u[3], double *p);
+void launch_solid_nan(cudaStream_t s, const Grid &g, const uint8_t *flag, double *const u[3], double *p);
+
+}  // namespace ibm

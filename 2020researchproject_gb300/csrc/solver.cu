@@ -1,0 +1,1352 @@
+// IBMSolver C ABI on one GB300: host orchestration of the fractional step.
+//
+// Entry points mirror src/ibm3d_setup.c, src/ibm3d_init.c,
+// src/ibm3d_fracstep.c, src/ibm3d_turb.c and src/ibm3d_export.c (cited per
+// function).  All per-step work runs on the GPU; the host only sequences
+// kernels, reads Krylov convergence scalars, and prints the reference's
+// per-step table.
+#include <cmath>
+#include <ctime>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "../../include/ibm3d.h"
+#include "../../include/ibm3d_gb300.h"
+#include "common.cuh"
+#include "geo3d.h"
+#include "kernels.h"
+#include "krylov.h"
+#include "multigrid.h"
+#include "prof.h"
+#include "setup.h"
+
+using namespace ibm;
+
+struct ibm3d_device {
+    cudaStream_t s = nullptr;
+    Grid g{};
+    int dev_id = 0;
+    char dev_name[256] = "";
+    // Per-axis 1-D tables: 9 arrays of n+4 doubles each.
+    double *tab[3] = {nullptr, nullptr, nullptr};
+    Axis ax[3];
+    BCSet bc{};
+    // Fields.
+    double *fields = nullptr;
+    size_t nfields = 0;
+    double *u[3], *un[3], *ustar, *U[3], *Un[3], *Us[3], *p, *pn, *pp, *N[3], *Np[3], *tau[6], *b, *lvset, *dinv;
+    uint8_t *flag = nullptr;
+    int *gid = nullptr;
+    // Ghost cells.
+    int nghost = 0, nlevels = 0;
+    int *g_mem = nullptr;
+    double *g_dmem = nullptr;
+    int8_t *g_kind = nullptr;
+    GhostArgs gargs{};
+    int *g_gidx = nullptr;
+    double *g_gw = nullptr, *g_gwself = nullptr;
+    std::vector<GhostStencil> gst;   // lexicographic order
+    std::vector<int> gcell_lex;      // padded index, lexicographic order
+    // Solvers.
+    KrylovWork kmom, kpres;
+    GMG *mg = nullptr;
+    double *red_partials = nullptr;
+    unsigned int *red_counter = nullptr;
+    double *maxdiv_d = nullptr;
+    double *maxdiv_h = nullptr;
+    // Settings.
+    double divtol = 0.0;
+    int precision = IBM3D_FP64;
+    int les = 0;
+    int cpt_fallback = 0;
+    bool abort_on_error = true;
+    // Last-step statistics.
+    SolveReport rep_mom, rep_p;
+    double max_div = 0.0;
+    int status = IBM3D_OK;
+    bool assembled = false;
+    Prof prof;
+};
+
+namespace {
+
+constexpr double kNaN = __builtin_nan("");
+constexpr int kUpdateBlocks = 608;
+
+int ncell_of(const IBMSolver *s) { return (s->Nx + 4) * (s->Ny + 4) * (s->Nz + 4); }
+
+void set_status(IBMSolver *s, int code, const char *fmt, ...) {
+    if (s && s->dev) s->dev->status = code;
+    va_list ap;
+    va_start(ap, fmt);
+    fprintf(stderr, "error: ");
+    vfprintf(stderr, fmt, ap);
+    fprintf(stderr, "\n");
+    va_end(ap);
+    if (s && s->dev && s->dev->abort_on_error && code != IBM3D_ENOCONV) std::exit(255);
+}
+
+bool cuda_check(IBMSolver *s, cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return true;
+    set_status(s, IBM3D_ECUDA, "%s: %s", what, cudaGetErrorString(e));
+    return false;
+}
+
+bool isperiodic(IBMSolverBCType t) { return t == BC_ALL_PERIODIC || t == BC_VELOCITY_PERIODIC; }
+
+double *c1(double *a, int i) { return &a[i + 2]; }
+
+// Outer-layer coefficients of one face (see BCFace).
+void make_bcface(const IBMSolver *sv, int f, BCFace &F) {
+    const IBMSolverBC &B = sv->bc[f];
+    switch (B.type) {
+    case BC_VELOCITY_COMPONENT:
+    case BC_STATIONARY_WALL: F.type = BCT_VELOCITY; break;
+    case BC_PRESSURE: F.type = BCT_PRESSURE; break;
+    case BC_FREE_SLIP_WALL:
+    case BC_SYMMETRIC: F.type = BCT_SLIP; break;
+    case BC_ALL_PERIODIC: F.type = BCT_PERIODIC; break;
+    case BC_VELOCITY_PERIODIC: F.type = BCT_VELPERIODIC; break;
+    }
+    F.val[0] = B.const_u1;
+    F.val[1] = B.const_u2;
+    F.val[2] = B.const_u3;
+    F.pval = B.const_p;
+    const int axis = face_axis(f);
+    const bool low = face_low(f);
+    const double *d = axis == 0 ? sv->dx : axis == 1 ? sv->dy : sv->dz;
+    const double *c = axis == 0 ? sv->xc : axis == 1 ? sv->yc : sv->zc;
+    const int N = axis == 0 ? sv->Nx : axis == 1 ? sv->Ny : sv->Nz;
+    auto D = [&](int i) { return d[i + 2]; };
+    auto C = [&](int i) { return c[i + 2]; };
+    // Pressure-Dirichlet fill widths: the reference's down face reads dx here
+    // (src/ibm3d_fracstep.c:1792-1800); every other face its own axis.
+    const double *dp = (f == F_D) ? sv->dx : d;
+    auto DP = [&](int i) { return dp[i + 2]; };
+    for (int L = 1; L <= 2; L++) {
+        double a, b, ap, bp, ea, eb;
+        if (low) {
+            if (L == 1) {
+                a = D(-1) / 2; b = D(0) / 2;
+                ap = DP(-1) / 2; bp = DP(0) / 2;
+                ea = C(0) - C(-1); eb = C(1) - C(0);
+            } else {
+                a = D(-2) / 2 + D(-1); b = D(0) + D(1) / 2;
+                ap = DP(-2) / 2 + DP(-1); bp = DP(0) + DP(1) / 2;
+                ea = C(-1) - C(-2); eb = C(0) - C(-1);
+            }
+            F.dir_o[L - 1] = b / (a + b);
+            F.dir_m[L - 1] = a / (a + b);
+            F.fv_a[L - 1] = (a + b) / b;
+            F.fv_b[L - 1] = a / b;
+            F.fp_a[L - 1] = (ap + bp) / bp;
+            F.fp_b[L - 1] = ap / bp;
+            F.ext_o[L - 1] = eb / (ea + eb);
+            F.ext_2[L - 1] = ea / (ea + eb);
+            F.fe_a[L - 1] = (ea + eb) / eb;
+            F.fe_b[L - 1] = ea / eb;
+        } else {
+            if (L == 1) {
+                a = D(N - 1) / 2; b = D(N) / 2;
+                ap = DP(N - 1) / 2; bp = DP(N) / 2;
+                ea = C(N - 1) - C(N - 2); eb = C(N) - C(N - 1);
+            } else {
+                a = D(N - 2) / 2 + D(N - 1); b = D(N) + D(N + 1) / 2;
+                ap = DP(N - 2) / 2 + DP(N - 1); bp = DP(N) + DP(N + 1) / 2;
+                ea = C(N) - C(N - 1); eb = C(N + 1) - C(N);
+            }
+            F.dir_o[L - 1] = a / (a + b);
+            F.dir_m[L - 1] = b / (a + b);
+            F.fv_a[L - 1] = (a + b) / a;
+            F.fv_b[L - 1] = b / a;
+            F.fp_a[L - 1] = (ap + bp) / ap;
+            F.fp_b[L - 1] = bp / ap;
+            F.ext_o[L - 1] = ea / (ea + eb);
+            F.ext_2[L - 1] = eb / (ea + eb);
+            F.fe_a[L - 1] = (ea + eb) / ea;
+            F.fe_b[L - 1] = eb / ea;
+        }
+    }
+}
+
+OpCtx op_ctx(const ibm3d_device *d) {
+    OpCtx c{};
+    c.g = d->g;
+    c.ax = d->ax[0];
+    c.ay = d->ax[1];
+    c.az = d->ax[2];
+    c.bc = d->bc;
+    c.flag = d->flag;
+    c.gid = d->gid;
+    c.gidx = d->g_gidx;
+    c.gw = d->g_gw;
+    c.gwself = d->g_gwself;
+    c.dinv = d->dinv;
+    return c;
+}
+
+template <typename T>
+void dfree(T *&p) {
+    if (p) cudaFree((void *)p);
+    p = nullptr;
+}
+
+void release_device(ibm3d_device *d) {
+    if (!d) return;
+    delete d->mg;
+    d->mg = nullptr;
+    d->kmom.release();
+    d->kpres.release();
+    for (int a = 0; a < 3; a++) dfree(d->tab[a]);
+    dfree(d->fields);
+    dfree(d->flag);
+    dfree(d->gid);
+    dfree(d->g_mem);
+    dfree(d->g_dmem);
+    dfree(d->g_kind);
+    dfree(d->red_partials);
+    dfree(d->red_counter);
+    dfree(d->maxdiv_d);
+    if (d->maxdiv_h) cudaFreeHost(d->maxdiv_h);
+    d->maxdiv_h = nullptr;
+    d->nghost = d->nlevels = 0;
+    d->gargs = GhostArgs{};
+    d->g_gidx = nullptr;
+    d->g_gw = d->g_gwself = nullptr;
+    d->assembled = false;
+    if (d->s) cudaStreamDestroy(d->s);
+    d->s = nullptr;
+}
+
+template <typename T>
+T *dmalloc(IBMSolver *sv, size_t n, const char *what) {
+    void *p = nullptr;
+    if (!cuda_check(sv, cudaMalloc(&p, n * sizeof(T) + 16), what)) return nullptr;
+    cudaMemsetAsync(p, 0, n * sizeof(T) + 16, sv->dev->s);
+    return (T *)p;
+}
+
+// Grid extension (src/ibm3d_setup.c:535-618) and the Crank-Nicolson
+// coefficients (src/ibm3d_setup.c:620-632) on the host arrays.
+void host_metrics(IBMSolver *s) {
+    auto ext = [](double *d, double *c, int N, bool plo, bool phi) {
+        *c1(d, -1) = plo ? *c1(d, N - 1) : *c1(d, 0);
+        *c1(d, -2) = plo ? *c1(d, N - 2) : *c1(d, 1);
+        *c1(d, N) = phi ? *c1(d, 0) : *c1(d, N - 1);
+        *c1(d, N + 1) = phi ? *c1(d, 1) : *c1(d, N - 2);
+        *c1(c, -1) = *c1(c, 0) - (*c1(d, -1) + *c1(d, 0)) / 2;
+        *c1(c, -2) = *c1(c, -1) - (*c1(d, -2) + *c1(d, -1)) / 2;
+        *c1(c, N) = *c1(c, N - 1) + (*c1(d, N - 1) + *c1(d, N)) / 2;
+        *c1(c, N + 1) = *c1(c, N) + (*c1(d, N) + *c1(d, N + 1)) / 2;
+    };
+    ext(s->dx, s->xc, s->Nx, isperiodic(s->bc[3].type), isperiodic(s->bc[1].type));
+    ext(s->dy, s->yc, s->Ny, isperiodic(s->bc[2].type), isperiodic(s->bc[0].type));
+    ext(s->dz, s->zc, s->Nz, isperiodic(s->bc[4].type), isperiodic(s->bc[5].type));
+    auto kco = [&](double *km, double *kp, const double *d, const double *c, int N) {
+        for (int i = 0; i < N; i++) {
+            km[i + 2] = s->dt / (2 * s->Re * (c[i + 2] - c[i + 1]) * d[i + 2]);
+            kp[i + 2] = s->dt / (2 * s->Re * (c[i + 3] - c[i + 2]) * d[i + 2]);
+        }
+    };
+    kco(s->kx_W, s->kx_E, s->dx, s->xc, s->Nx);
+    kco(s->ky_S, s->ky_N, s->dy, s->yc, s->Ny);
+    kco(s->kz_D, s->kz_U, s->dz, s->zc, s->Nz);
+}
+
+bool upload_axes(IBMSolver *sv) {
+    ibm3d_device *d = sv->dev;
+    const double *D[3] = {sv->dx, sv->dy, sv->dz}, *Cc[3] = {sv->xc, sv->yc, sv->zc};
+    const double *KM[3] = {sv->kx_W, sv->ky_S, sv->kz_D}, *KP[3] = {sv->kx_E, sv->ky_N, sv->kz_U};
+    const int Ns[3] = {sv->Nx, sv->Ny, sv->Nz};
+    for (int a = 0; a < 3; a++) {
+        const int n = Ns[a] + 4;
+        std::vector<double> h(9 * (size_t)n, 0.0);
+        double *dd = &h[0], *cc = &h[n], *wm = &h[2 * n], *wp = &h[3 * n], *rd = &h[4 * n], *rdc = &h[5 * n],
+               *rdcc = &h[6 * n], *km = &h[7 * n], *kp = &h[8 * n];
+        for (int q = 0; q < n; q++) {
+            dd[q] = D[a][q];
+            cc[q] = Cc[a][q];
+            rd[q] = 1.0 / D[a][q];
+            km[q] = KM[a][q];
+            kp[q] = KP[a][q];
+            if (q >= 1) {
+                wm[q] = D[a][q] / (D[a][q - 1] + D[a][q]);
+                wp[q] = D[a][q - 1] / (D[a][q - 1] + D[a][q]);
+                rdc[q] = 1.0 / (Cc[a][q] - Cc[a][q - 1]);
+            }
+            if (q >= 1 && q + 1 < n) rdcc[q] = 1.0 / (Cc[a][q + 1] - Cc[a][q - 1]);
+        }
+        d->tab[a] = dmalloc<double>(sv, h.size(), "axis tables");
+        if (!d->tab[a]) return false;
+        cudaMemcpyAsync(d->tab[a], h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, d->s);
+        double *t = d->tab[a];
+        d->ax[a] = Axis{t, t + n, t + 2 * n, t + 3 * n, t + 4 * n, t + 5 * n, t + 6 * n, t + 7 * n, t + 8 * n};
+    }
+    return true;
+}
+
+bool alloc_fields(IBMSolver *sv) {
+    ibm3d_device *d = sv->dev;
+    const long long n = d->g.ncell;
+    // u, un, ustar(3), U, Un, Us, p, pn, pp, N, Np, tau(6), b(3), lvset, dinv
+    d->nfields = 3 + 3 + 3 + 3 + 3 + 3 + 1 + 1 + 1 + 3 + 3 + 6 + 3 + 1 + 1;
+    d->fields = dmalloc<double>(sv, d->nfields * (size_t)n, "field arrays");
+    if (!d->fields) return false;
+    double *q = d->fields;
+    auto take = [&](int k) {
+        double *r = q;
+        q += (size_t)k * n;
+        return r;
+    };
+    for (int l = 0; l < 3; l++) d->u[l] = take(1);
+    for (int l = 0; l < 3; l++) d->un[l] = take(1);
+    d->ustar = take(3);
+    for (int l = 0; l < 3; l++) d->U[l] = take(1);
+    for (int l = 0; l < 3; l++) d->Un[l] = take(1);
+    for (int l = 0; l < 3; l++) d->Us[l] = take(1);
+    d->p = take(1);
+    d->pn = take(1);
+    d->pp = take(1);
+    for (int l = 0; l < 3; l++) d->N[l] = take(1);
+    for (int l = 0; l < 3; l++) d->Np[l] = take(1);
+    for (int l = 0; l < 6; l++) d->tau[l] = take(1);
+    d->b = take(3);
+    d->lvset = take(1);
+    d->dinv = take(1);
+    d->flag = dmalloc<uint8_t>(sv, n, "flags");
+    d->gid = dmalloc<int>(sv, n, "ghost map");
+    d->red_partials = dmalloc<double>(sv, 8 * 4096, "reduction partials");
+    d->red_counter = dmalloc<unsigned int>(sv, 1, "reduction counter");
+    d->maxdiv_d = dmalloc<double>(sv, 1, "max div");
+    if (!d->flag || !d->gid || !d->red_partials || !d->red_counter || !d->maxdiv_d) return false;
+    if (!cuda_check(sv, cudaMallocHost(&d->maxdiv_h, sizeof(double)), "pinned scalar")) return false;
+    return true;
+}
+
+// Level set and flags (src/ibm3d_setup.c:1081-1254) on the GPU.
+bool build_levelset(IBMSolver *sv) {
+    ibm3d_device *d = sv->dev;
+    const long long n = d->g.ncell;
+    if (!sv->poly) {
+        std::vector<double> h(n, 0.5);
+        cudaMemcpyAsync(d->lvset, h.data(), sizeof(double) * n, cudaMemcpyHostToDevice, d->s);
+        std::vector<uint8_t> f(n, FLUID);
+        cudaMemcpyAsync(d->flag, f.data(), n, cudaMemcpyHostToDevice, d->s);
+        cudaStreamSynchronize(d->s);
+        return true;
+    }
+    CptModel m;
+    build_cpt_model(sv->poly, 15, m);
+    int nfb = 0;
+    if (gpu_cpt(d->s, m, sv->Nx + 4, sv->Ny + 4, sv->Nz + 4, d->ax[0].c, d->ax[1].c, d->ax[2].c, d->lvset, 15, &nfb) != 0) {
+        set_status(sv, IBM3D_ECUDA, "level-set kernels failed");
+        return false;
+    }
+    d->cpt_fallback = nfb;
+    gpu_flags(d->s, d->g, d->lvset, d->flag);
+    return cuda_check(sv, cudaStreamSynchronize(d->s), "flags");
+}
+
+// Ghost stencils (GPU), dependency levels and operator tables (host).
+bool build_ghosts(IBMSolver *sv) {
+    ibm3d_device *d = sv->dev;
+    const Grid &g = d->g;
+    const long long n = g.ncell;
+    std::vector<uint8_t> fl(n);
+    cudaMemcpyAsync(fl.data(), d->flag, n, cudaMemcpyDeviceToHost, d->s);
+    cudaStreamSynchronize(d->s);
+    d->gcell_lex.clear();
+    for (int i = 0; i < sv->Nx; i++)
+        for (int j = 0; j < sv->Ny; j++)
+            for (int k = 0; k < sv->Nz; k++) {
+                const long long P = cidx(g, i, j, k);
+                if (fl[P] == GHOST) d->gcell_lex.push_back((int)P);
+            }
+    const int ng = (int)d->gcell_lex.size();
+    d->nghost = ng;
+    d->gst.assign(ng, GhostStencil{});
+    std::vector<int> hgid(n, -1);
+    if (ng > 0) {
+        int *gc = nullptr;
+        GhostStencil *gs = nullptr;
+        cudaMalloc(&gc, sizeof(int) * ng);
+        cudaMalloc(&gs, sizeof(GhostStencil) * ng);
+        cudaMemcpyAsync(gc, d->gcell_lex.data(), sizeof(int) * ng, cudaMemcpyHostToDevice, d->s);
+        const int rc = gpu_ghost_stencils(d->s, g, d->ax[0].c, d->ax[1].c, d->ax[2].c, d->lvset, d->flag, gc, ng, gs);
+        cudaMemcpyAsync(d->gst.data(), gs, sizeof(GhostStencil) * ng, cudaMemcpyDeviceToHost, d->s);
+        cudaStreamSynchronize(d->s);
+        cudaFree(gc);
+        cudaFree(gs);
+        if (rc != 0) {
+            set_status(sv, IBM3D_ECUDA, "ghost stencil kernel failed");
+            return false;
+        }
+        for (int q = 0; q < ng; q++)
+            if (!d->gst[q].ok) {
+                int i, j, k;
+                cijk(g, d->gcell_lex[q], i, j, k);
+                set_status(sv, IBM3D_EGEOM, "mirror point of ghost cell (%d,%d,%d) lies outside the grid", i, j, k);
+                return false;
+            }
+        // Lexicographic ghost id of each ghost cell.
+        std::vector<int> lexid(n, -1);
+        for (int q = 0; q < ng; q++) lexid[d->gcell_lex[q]] = q;
+        // Dependency level: 1 + max level of lower-index ghosts in the stencil.
+        std::vector<int> level(ng, 0);
+        int nlev = 1;
+        for (int q = 0; q < ng; q++) {
+            int lv = 0;
+            for (int e = 0; e < 8; e++) {
+                const int c = d->gst[q].cell[e];
+                if (c < 0) continue;
+                const int h = lexid[c];
+                if (h >= 0 && h < q) lv = std::max(lv, level[h] + 1);
+            }
+            level[q] = lv;
+            nlev = std::max(nlev, lv + 1);
+        }
+        // Level-major order.
+        std::vector<int> order(ng);
+        for (int q = 0; q < ng; q++) order[q] = q;
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return level[a] < level[b]; });
+        std::vector<int> newid(ng);
+        for (int q = 0; q < ng; q++) newid[order[q]] = q;
+        std::vector<int> lstart(nlev + 1, 0);
+        for (int q = 0; q < ng; q++) lstart[level[q] + 1]++;
+        for (int l = 0; l < nlev; l++) lstart[l + 1] += lstart[l];
+        std::vector<int> cell(ng), ref(8 * ng), gidx(8 * ng);
+        std::vector<int8_t> kind(8 * ng);
+        std::vector<double> w(8 * ng), wself(ng);
+        for (int t = 0; t < ng; t++) {
+            const int q = order[t];
+            const GhostStencil &st = d->gst[q];
+            cell[t] = d->gcell_lex[q];
+            wself[t] = st.wself;
+            hgid[cell[t]] = t;
+            for (int e = 0; e < 8; e++) {
+                const int c = st.cell[e];
+                w[8 * t + e] = st.w[e];
+                gidx[8 * t + e] = c;
+                if (c < 0) {
+                    kind[8 * t + e] = GK_SKIP;
+                    ref[8 * t + e] = 0;
+                } else if (lexid[c] > q) {
+                    kind[8 * t + e] = GK_OLD;
+                    ref[8 * t + e] = newid[lexid[c]];
+                } else {
+                    kind[8 * t + e] = GK_ARRAY;
+                    ref[8 * t + e] = c;
+                }
+            }
+        }
+        d->nlevels = nlev;
+        // Device copies: ints [cell | ref | gidx | level_start], doubles [w | wself | old(4*ng) | gw].
+        d->g_mem = dmalloc<int>(sv, (size_t)ng * 17 + nlev + 1, "ghost tables");
+        d->g_dmem = dmalloc<double>(sv, (size_t)ng * (8 + 1 + 4), "ghost weights");
+        d->g_kind = dmalloc<int8_t>(sv, (size_t)ng * 8, "ghost kinds");
+        if (!d->g_mem || !d->g_dmem || !d->g_kind) return false;
+        int *im = d->g_mem;
+        cudaMemcpyAsync(im, cell.data(), sizeof(int) * ng, cudaMemcpyHostToDevice, d->s);
+        cudaMemcpyAsync(im + ng, ref.data(), sizeof(int) * 8 * ng, cudaMemcpyHostToDevice, d->s);
+        cudaMemcpyAsync(im + 9 * ng, gidx.data(), sizeof(int) * 8 * ng, cudaMemcpyHostToDevice, d->s);
+        cudaMemcpyAsync(im + 17 * ng, lstart.data(), sizeof(int) * (nlev + 1), cudaMemcpyHostToDevice, d->s);
+        double *dm = d->g_dmem;
+        cudaMemcpyAsync(dm, w.data(), sizeof(double) * 8 * ng, cudaMemcpyHostToDevice, d->s);
+        cudaMemcpyAsync(dm + 8 * ng, wself.data(), sizeof(double) * ng, cudaMemcpyHostToDevice, d->s);
+        cudaMemcpyAsync(d->g_kind, kind.data(), 8 * ng, cudaMemcpyHostToDevice, d->s);
+        d->gargs = GhostArgs{ng, nlev, im + 17 * ng, im, im + ng, d->g_kind, dm, dm + 8 * ng, dm + 9 * ng};
+        d->g_gidx = im + 9 * ng;
+        d->g_gw = dm;
+        d->g_gwself = dm + 8 * ng;
+    }
+    cudaMemcpyAsync(d->gid, hgid.data(), sizeof(int) * n, cudaMemcpyHostToDevice, d->s);
+    return cuda_check(sv, cudaStreamSynchronize(d->s), "ghost tables");
+}
+
+// 1/coeffsum of fluid rows and the host p_coeffsum (src/ibm3d_setup.c:1641-1649).
+void build_coeffsum(IBMSolver *sv) {
+    ibm3d_device *d = sv->dev;
+    const long long n = d->g.ncell;
+    std::vector<uint8_t> fl(n);
+    cudaMemcpyAsync(fl.data(), d->flag, n, cudaMemcpyDeviceToHost, d->s);
+    cudaStreamSynchronize(d->s);
+    std::vector<double> dinv(n, 0.0);
+    std::fill(sv->p_coeffsum, sv->p_coeffsum + n, 0.0);
+    bool singular = true;
+    for (int f = 0; f < 6; f++)
+        if (sv->bc[f].type == BC_PRESSURE || sv->bc[f].type == BC_VELOCITY_PERIODIC) singular = false;
+    for (int i = 0; i < sv->Nx; i++)
+        for (int j = 0; j < sv->Ny; j++)
+            for (int k = 0; k < sv->Nz; k++) {
+                const long long P = cidx(d->g, i, j, k);
+                if (singular && i == 0 && j == 0 && k == 0) continue;
+                if (fl[P] != FLUID) continue;
+                const double cs = sv->ky_N[j + 2] + sv->kx_E[i + 2] + sv->ky_S[j + 2] + sv->kx_W[i + 2] +
+                                  sv->kz_D[k + 2] + sv->kz_U[k + 2];
+                sv->p_coeffsum[P] = cs;
+                dinv[P] = 1.0 / cs;
+            }
+    for (long long P = 0; P < n; P++) sv->flag[P] = fl[P];
+    cudaMemcpyAsync(d->dinv, dinv.data(), sizeof(double) * n, cudaMemcpyHostToDevice, d->s);
+    cudaStreamSynchronize(d->s);
+}
+
+void swap3(double *a[3], double *b[3]) {
+    for (int l = 0; l < 3; l++) std::swap(a[l], b[l]);
+}
+
+ConvArgs conv_args(ibm3d_device *d) {
+    ConvArgs a{};
+    for (int l = 0; l < 3; l++) {
+        a.u[l] = d->u[l];
+        a.U[l] = d->U[l];
+        a.Np[l] = d->Np[l];
+        a.N[l] = d->N[l];
+        a.b[l] = d->b + l * d->g.ncell;
+    }
+    for (int t = 0; t < 6; t++) a.tau[t] = d->tau[t];
+    a.p = d->p;
+    return a;
+}
+
+void calc_tau(IBMSolver *sv) {
+    ibm3d_device *d = sv->dev;
+    if (!d->les) return;
+    TauArgs t{};
+    for (int q = 0; q < 6; q++) t.tau[q] = d->tau[q];
+    const double *u[3] = {d->u[0], d->u[1], d->u[2]};
+    launch_smagorinsky(d->s, d->g, d->ax[0], d->ax[1], d->ax[2], d->flag, d->lvset, u, t, sv->turb_model.Cs);
+}
+
+void fill_outer(IBMSolver *sv) {
+    ibm3d_device *d = sv->dev;
+    launch_fill_outer(d->s, d->g, d->bc, d->u, d->p);
+}
+
+void ghost_update(IBMSolver *sv, bool solids) {
+    ibm3d_device *d = sv->dev;
+    if (solids) launch_solid_nan(d->s, d->g, d->flag, d->u, d->p);
+    launch_ghost_update(d->s, d->gargs, d->u, d->p);
+}
+
+// One fractional step (src/ibm3d_fracstep.c:60-74).
+void one_step(IBMSolver *sv) {
+    ibm3d_device *d = sv->dev;
+    Prof &pf = d->prof;
+    const double f[3] = {sv->ext_force.const_f1, sv->ext_force.const_f2, sv->ext_force.const_f3};
+    const OpCtx ctx = op_ctx(d);
+
+    int t = pf.begin("tau");
+    calc_tau(sv);
+    pf.end(t);
+    t = pf.begin("conv_rhs");
+    launch_conv_rhs(d->s, d->g, d->ax[0], d->ax[1], d->ax[2], d->bc, d->flag, conv_args(d), sv->dt, f, d->les);
+    pf.end(t);
+
+    SolveParams pm;
+    pm.tol = sv->tol;
+    pm.maxit = 200;
+    pm.Re = sv->Re;
+    pm.prof = &pf;
+    t = pf.begin("mom_solve");
+    int rc = bicgstab(d->s, ctx, OP_MOM, d->kmom, d->b, d->ustar, pm, nullptr, d->rep_mom);
+    pf.end(t);
+    if (rc == 1) {
+        for (int l = 0; l < 3; l++)
+            if (d->rep_mom.relres[l] >= sv->tol) fprintf(stderr, "warning: u%d_star did not converge\n", l + 1);
+    } else if (rc == 2) {
+        set_status(sv, IBM3D_EBREAKDOWN, "breakdown in the momentum solve");
+    }
+
+    UstarArgs ua{};
+    for (int l = 0; l < 3; l++) {
+        ua.us[l] = d->ustar + l * d->g.ncell;
+        ua.Us[l] = d->Us[l];
+    }
+    ua.p = d->p;
+    ua.b = d->b;
+    t = pf.begin("ustar_prhs");
+    launch_ustar_prhs(d->s, d->g, d->ax[0], d->ax[1], d->ax[2], d->bc, d->flag, ua, sv->dt, sv->Re);
+    pf.end(t);
+
+    SolveParams pp = pm;
+    pp.maxit = 1000;
+    pp.divtol = d->divtol;
+    const bool use_mg = sv->precond_type == PRECOND_AMG || sv->linear_solver_type == SOLVER_AMG;
+    t = pf.begin("p_solve");
+    rc = bicgstab(d->s, ctx, OP_PRES, d->kpres, d->b, d->pp, pp, use_mg ? d->mg : nullptr, d->rep_p);
+    pf.end(t);
+    if (rc == 1) fprintf(stderr, "warning: p_prime did not converge\n");
+    else if (rc == 2) set_status(sv, IBM3D_EBREAKDOWN, "breakdown in the pressure solve");
+
+    NextArgs na{};
+    for (int l = 0; l < 3; l++) {
+        na.us[l] = d->ustar + l * d->g.ncell;
+        na.Us[l] = d->Us[l];
+        na.un[l] = d->un[l];
+        na.Un[l] = d->Un[l];
+    }
+    na.p = d->p;
+    na.pp = d->pp;
+    na.pn = d->pn;
+    t = pf.begin("update_next");
+    launch_update_next(d->s, d->g, d->ax[0], d->ax[1], d->ax[2], d->bc, d->flag, na, sv->dt, d->red_partials,
+                       d->red_counter, d->maxdiv_d, kUpdateBlocks);
+    pf.end(t);
+    swap3(d->u, d->un);
+    swap3(d->U, d->Un);
+    std::swap(d->p, d->pn);
+    swap3(d->N, d->Np);
+}
+
+void print_row(IBMSolver *sv, int i, long elapsed_ms) {
+    ibm3d_device *d = sv->dev;
+    if (sv->iter % 10 == 1 || i == 1) {
+        printf("\n  iter       u1 res       u2 res       u3 res        p res       time\n");
+        printf("---------------------------------------------------------------------\n");
+    }
+    long hour = elapsed_ms / 3600000, min = elapsed_ms / 60000 % 60;
+    long sec = elapsed_ms / 1000 % 60 + (elapsed_ms % 1000 > 500);
+    if (sec >= 60) { sec -= 60; min += 1; }
+    if (min >= 60) { min -= 60; hour += 1; }
+    printf("%6d   %10.4e   %10.4e   %10.4e   %10.4e   %02ld:%02ld:%02ld\n", sv->iter, d->rep_mom.relres[0],
+           d->rep_mom.relres[1], d->rep_mom.relres[2], d->rep_p.relres[0], hour, min, sec);
+}
+
+bool check_ready(IBMSolver *sv, const char *fn) {
+    if (!sv || !sv->dev || !sv->dev->assembled) {
+        set_status(sv, IBM3D_EARG, "%s called before IBMSolver_assemble", fn);
+        return false;
+    }
+    return true;
+}
+
+void upload_state(IBMSolver *sv, const double *u1, const double *u2, const double *u3, const double *p) {
+    ibm3d_device *d = sv->dev;
+    const size_t b = sizeof(double) * d->g.ncell;
+    cudaMemcpyAsync(d->u[0], u1, b, cudaMemcpyHostToDevice, d->s);
+    cudaMemcpyAsync(d->u[1], u2, b, cudaMemcpyHostToDevice, d->s);
+    cudaMemcpyAsync(d->u[2], u3, b, cudaMemcpyHostToDevice, d->s);
+    cudaMemcpyAsync(d->p, p, b, cudaMemcpyHostToDevice, d->s);
+    cuda_check(sv, cudaStreamSynchronize(d->s), "state upload");
+    sv->iter = 0;
+    sv->time = 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+// ------------------------------------------------------------ setup ---
+IBMSolver *IBMSolver_new(const int num_process, const int rank, const int Px, const int Py, const int Pz) {
+    IBMSolver *s = (IBMSolver *)calloc(1, sizeof(IBMSolver));
+    s->dev = new ibm3d_device();
+    if (const char *e = getenv("IBM3D_NO_ABORT")) s->dev->abort_on_error = atoi(e) == 0;
+    if (rank < 0 || rank > num_process) {
+        set_status(s, IBM3D_EARG, "Invalid rank: %d", rank);
+        return s;
+    }
+    s->num_process = num_process;
+    s->rank = rank;
+    // One GPU holds the whole domain: the decomposition collapses to 1x1x1.
+    (void)Px; (void)Py; (void)Pz;
+    s->Px = s->Py = s->Pz = 1;
+    s->ri = s->rj = s->rk = 0;
+    s->ext_force.val_type = VAL_CONST;
+    s->turb_model.type = TURBMODEL_NONE;
+    s->linear_solver_type = SOLVER_BiCGSTAB;
+    s->precond_type = PRECOND_AMG;
+    s->tol = 1e-6;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        set_status(s, IBM3D_ECUDA, "no CUDA device available: the GB300 path has no CPU fallback");
+        return s;
+    }
+    cudaGetDevice(&s->dev->dev_id);
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, s->dev->dev_id) == cudaSuccess)
+        snprintf(s->dev->dev_name, sizeof s->dev->dev_name, "%s (sm_%d%d)", prop.name, prop.major, prop.minor);
+    cuda_check(s, cudaStreamCreateWithFlags(&s->dev->s, cudaStreamNonBlocking), "stream");
+    s->dev->prof.s = s->dev->s;
+    return s;
+}
+
+void IBMSolver_destroy(IBMSolver *s) {
+    if (!s) return;
+    if (s->dev) {
+        release_device(s->dev);
+        delete s->dev;
+    }
+    free(s->dx); free(s->dy); free(s->dz);
+    free(s->xc); free(s->yc); free(s->zc);
+    free(s->kx_W); free(s->kx_E); free(s->ky_S); free(s->ky_N); free(s->kz_D); free(s->kz_U);
+    free(s->flag); free(s->lvset); free(s->p_coeffsum);
+    free(s->u1); free(s->u2); free(s->u3); free(s->p);
+    free(s);
+}
+
+void IBMSolver_set_grid(IBMSolver *s, const int Nx, const int Ny, const int Nz, const double *xf, const double *yf,
+                        const double *zf) {
+    if (Nx < 2 || Ny < 2 || Nz < 2) {
+        set_status(s, IBM3D_EARG, "grid must have at least 2 cells per axis (got %d x %d x %d)", Nx, Ny, Nz);
+        return;
+    }
+    s->Nx_global = s->Nx = Nx;
+    s->Ny_global = s->Ny = Ny;
+    s->Nz_global = s->Nz = Nz;
+    auto alloc1 = [](int n) { return (double *)calloc(n + 4, sizeof(double)); };
+    s->dx = alloc1(Nx); s->xc = alloc1(Nx); s->kx_W = alloc1(Nx); s->kx_E = alloc1(Nx);
+    s->dy = alloc1(Ny); s->yc = alloc1(Ny); s->ky_S = alloc1(Ny); s->ky_N = alloc1(Ny);
+    s->dz = alloc1(Nz); s->zc = alloc1(Nz); s->kz_D = alloc1(Nz); s->kz_U = alloc1(Nz);
+    for (int i = 0; i < Nx; i++) {
+        s->dx[i + 2] = xf[i + 1] - xf[i];
+        s->xc[i + 2] = (xf[i + 1] + xf[i]) / 2;
+    }
+    for (int j = 0; j < Ny; j++) {
+        s->dy[j + 2] = yf[j + 1] - yf[j];
+        s->yc[j + 2] = (yf[j + 1] + yf[j]) / 2;
+    }
+    for (int k = 0; k < Nz; k++) {
+        s->dz[k + 2] = zf[k + 1] - zf[k];
+        s->zc[k + 2] = (zf[k + 1] + zf[k]) / 2;
+    }
+    s->xmin = xf[0]; s->xmax = xf[Nx];
+    s->ymin = yf[0]; s->ymax = yf[Ny];
+    s->zmin = zf[0]; s->zmax = zf[Nz];
+    const size_t n = (size_t)ncell_of(s);
+    s->flag = (int *)calloc(n, sizeof(int));
+    s->lvset = (double *)calloc(n, sizeof(double));
+    s->p_coeffsum = (double *)calloc(n, sizeof(double));
+    s->u1 = (double *)calloc(n, sizeof(double));
+    s->u2 = (double *)calloc(n, sizeof(double));
+    s->u3 = (double *)calloc(n, sizeof(double));
+    s->p = (double *)calloc(n, sizeof(double));
+}
+
+void IBMSolver_set_params(IBMSolver *s, const double Re, const double dt) {
+    s->Re = Re;
+    s->dt = dt;
+}
+
+void IBMSolver_set_ext_force(IBMSolver *s, IBMSolverValType val_type, ...) {
+    va_list ap;
+    va_start(ap, val_type);
+    s->ext_force.val_type = val_type;
+    if (val_type == VAL_CONST) {
+        s->ext_force.const_f1 = va_arg(ap, double);
+        s->ext_force.const_f2 = va_arg(ap, double);
+        s->ext_force.const_f3 = va_arg(ap, double);
+    } else {
+        s->ext_force.func_f1 = va_arg(ap, IBMSolverForceFunc);
+        s->ext_force.func_f2 = va_arg(ap, IBMSolverForceFunc);
+        s->ext_force.func_f3 = va_arg(ap, IBMSolverForceFunc);
+    }
+    va_end(ap);
+}
+
+void IBMSolver_set_turb_model(IBMSolver *s, IBMSolverTurbModelType type, ...) {
+    va_list ap;
+    va_start(ap, type);
+    s->turb_model.type = type;
+    if (type == TURBMODEL_SMAGORINSKY) s->turb_model.Cs = va_arg(ap, double);
+    else if (type != TURBMODEL_NONE) set_status(s, IBM3D_EUNSUPPORTED, "turbulence model %d is not implemented", (int)type);
+    va_end(ap);
+}
+
+static void set_bc_impl(IBMSolver *s, int direction, IBMSolverBCType type, IBMSolverValType vt, double u1, double u2,
+                        double u3, double pv, IBMSolverBCValFunc f1, IBMSolverBCValFunc f2, IBMSolverBCValFunc f3,
+                        IBMSolverBCValFunc fp) {
+    for (int i = 0; i < 6; i++) {
+        if (!(direction & (1 << i))) continue;
+        s->bc[i].type = type;
+        s->bc[i].val_type = vt;
+        if (vt == VAL_CONST) {
+            s->bc[i].const_u1 = u1;
+            s->bc[i].const_u2 = u2;
+            s->bc[i].const_u3 = u3;
+            s->bc[i].const_p = pv;
+        } else {
+            s->bc[i].func_u1 = f1;
+            s->bc[i].func_u2 = f2;
+            s->bc[i].func_u3 = f3;
+            s->bc[i].func_p = fp;
+        }
+    }
+}
+
+void IBMSolver_set_bc(IBMSolver *s, IBMSolverDirection direction, IBMSolverBCType type, ...) {
+    IBMSolverValType vt = VAL_CONST;
+    double u1 = kNaN, u2 = kNaN, u3 = kNaN, pv = kNaN;
+    IBMSolverBCValFunc f1 = nullptr, f2 = nullptr, f3 = nullptr, fp = nullptr;
+    va_list ap;
+    va_start(ap, type);
+    switch (type) {
+    case BC_VELOCITY_COMPONENT:
+        vt = (IBMSolverValType)va_arg(ap, int);
+        if (vt == VAL_CONST) {
+            u1 = va_arg(ap, double);
+            u2 = va_arg(ap, double);
+            u3 = va_arg(ap, double);
+        } else {
+            f1 = va_arg(ap, IBMSolverBCValFunc);
+            f2 = va_arg(ap, IBMSolverBCValFunc);
+            f3 = va_arg(ap, IBMSolverBCValFunc);
+        }
+        break;
+    case BC_PRESSURE:
+    case BC_VELOCITY_PERIODIC:
+        vt = (IBMSolverValType)va_arg(ap, int);
+        if (vt == VAL_CONST) pv = va_arg(ap, double);
+        else fp = va_arg(ap, IBMSolverBCValFunc);
+        break;
+    case BC_STATIONARY_WALL:
+        type = BC_VELOCITY_COMPONENT;
+        u1 = u2 = u3 = 0;
+        break;
+    case BC_SYMMETRIC:
+        type = BC_FREE_SLIP_WALL;
+        break;
+    default:;
+    }
+    va_end(ap);
+    set_bc_impl(s, direction, type, vt, u1, u2, u3, pv, f1, f2, f3, fp);
+}
+
+void IBMSolver_set_obstacle(IBMSolver *s, Polyhedron *poly) { s->poly = poly; }
+
+void IBMSolver_set_linear_solver(IBMSolver *s, IBMSolverLinearSolverType type, IBMSolverPrecondType precond,
+                                 const double tol) {
+    if (type == SOLVER_AMG && precond != PRECOND_NONE) {
+        set_status(s, IBM3D_EARG, "Cannot use preconditioner with BoomerAMG solver");
+        return;
+    }
+    s->linear_solver_type = type;
+    s->precond_type = precond;
+    s->tol = tol;
+}
+
+void IBMSolver_set_autosave(IBMSolver *s, const char *filename, int period) {
+    s->autosave_filename = filename;
+    s->autosave_period = period;
+}
+
+// src/ibm3d_setup.c:499-639
+void IBMSolver_assemble(IBMSolver *s) {
+    ibm3d_device *d = s->dev;
+    if (!d || !d->s) {
+        set_status(s, IBM3D_ECUDA, "no GPU stream: the solver was not created on a CUDA device");
+        return;
+    }
+    if (!s->dx) {
+        set_status(s, IBM3D_EARG, "IBMSolver_set_grid must be called before IBMSolver_assemble");
+        return;
+    }
+    if (isperiodic(s->bc[0].type) != isperiodic(s->bc[2].type) || isperiodic(s->bc[1].type) != isperiodic(s->bc[3].type) ||
+        isperiodic(s->bc[4].type) != isperiodic(s->bc[5].type)) {
+        set_status(s, IBM3D_EARG, "Inconsistent periodic boundary condition");
+        return;
+    }
+    if (s->ext_force.val_type != VAL_CONST) {
+        set_status(s, IBM3D_EUNSUPPORTED, "VAL_FUNC body forces are not supported on the GPU path");
+        return;
+    }
+    for (int f = 0; f < 6; f++)
+        if (s->bc[f].val_type != VAL_CONST) {
+            set_status(s, IBM3D_EUNSUPPORTED, "VAL_FUNC boundary values are not supported on the GPU path");
+            return;
+        }
+    if (s->turb_model.type != TURBMODEL_NONE && s->turb_model.type != TURBMODEL_SMAGORINSKY) {
+        set_status(s, IBM3D_EUNSUPPORTED, "turbulence model %d is not implemented", (int)s->turb_model.type);
+        return;
+    }
+    host_metrics(s);
+    Grid &g = d->g;
+    g.nx = s->Nx;
+    g.ny = s->Ny;
+    g.nz = s->Nz;
+    g.sy = s->Nz + 4;
+    g.sx = (long long)(s->Ny + 4) * g.sy;
+    g.ncell = (long long)(s->Nx + 4) * g.sx;
+    release_device(d);
+    d->s = nullptr;
+    cuda_check(s, cudaStreamCreateWithFlags(&d->s, cudaStreamNonBlocking), "stream");
+    d->prof.s = d->s;
+    for (int f = 0; f < 6; f++) make_bcface(s, f, d->bc.f[f]);
+    d->bc.p_singular = 1;
+    for (int f = 0; f < 6; f++)
+        if (s->bc[f].type == BC_PRESSURE || s->bc[f].type == BC_VELOCITY_PERIODIC) d->bc.p_singular = 0;
+    d->les = s->turb_model.type == TURBMODEL_SMAGORINSKY;
+    if (!upload_axes(s) || !alloc_fields(s)) return;
+    if (!build_levelset(s)) return;
+    if (!build_ghosts(s)) return;
+    build_coeffsum(s);
+    cudaMemcpyAsync(s->lvset, d->lvset, sizeof(double) * g.ncell, cudaMemcpyDeviceToHost, d->s);
+    if (d->kmom.allocate(g.ncell, 3, false) != 0 || d->kpres.allocate(g.ncell, 1, true) != 0) {
+        set_status(s, IBM3D_ECUDA, "Krylov workspace allocation failed");
+        return;
+    }
+    d->mg = new GMG();
+    GMGConfig mc;
+    if (d->mg->setup(d->s, op_ctx(d), d->nghost ? d->gargs.cell : nullptr, d->nghost, s->Re, s->dt, mc) != 0) {
+        set_status(s, IBM3D_ECUDA, "multigrid setup failed");
+        return;
+    }
+    if (!cuda_check(s, cudaStreamSynchronize(d->s), "assemble")) return;
+    d->assembled = true;
+    d->status = IBM3D_OK;
+}
+
+// src/utils.c:111-171, on the host from the assembled level set.
+void IBMSolver_ghost_interp(IBMSolver *s, const int i, const int j, const int k, int idx[][3], double coeff[]) {
+    const int Ny = s->Ny, Nz = s->Nz;
+    auto L = [&](int a, int b, int c) { return s->lvset[(long long)(Ny + 4) * (Nz + 4) * (a + 2) + (Nz + 4) * (b + 2) + c + 2]; };
+    const double *xc = s->xc, *yc = s->yc, *zc = s->zc;
+    const double nx = (L(i + 1, j, k) - L(i - 1, j, k)) / (xc[i + 3] - xc[i + 1]);
+    const double ny = (L(i, j + 1, k) - L(i, j - 1, k)) / (yc[j + 3] - yc[j + 1]);
+    const double nz = (L(i, j, k + 1) - L(i, j, k - 1)) / (zc[k + 3] - zc[k + 1]);
+    const double c = -2 * L(i, j, k);
+    const Vector m = Vector_lincom(1, Vector{xc[i + 2], yc[j + 2], zc[k + 2]}, c, Vector{nx, ny, nz});
+    auto ub = [](int len, const double *arr, double val) {
+        int l = 0, h = len;
+        while (l < h) {
+            const int mid = l + (h - l) / 2;
+            if (val >= arr[mid]) l = mid + 1;
+            else h = mid;
+        }
+        return l;
+    };
+    const int im = ub(s->Nx + 4, xc, m.x) - 3, jm = ub(s->Ny + 4, yc, m.y) - 3, km = ub(s->Nz + 4, zc, m.z) - 3;
+    for (int l = 0; l < 8; l++) {
+        idx[l][0] = im + !!(l & 4);
+        idx[l][1] = jm + !!(l & 2);
+        idx[l][2] = km + !!(l & 1);
+    }
+    const double xl = xc[im + 2], xu = xc[im + 3], yl = yc[jm + 2], yu = yc[jm + 3], zl = zc[km + 2], zu = zc[km + 3];
+    const double vol = (xu - xl) * (yu - yl) * (zu - zl);
+    coeff[0] = (xu - m.x) * (yu - m.y) * (zu - m.z) / vol;
+    coeff[1] = (xu - m.x) * (yu - m.y) * (m.z - zl) / vol;
+    coeff[2] = (xu - m.x) * (m.y - yl) * (zu - m.z) / vol;
+    coeff[3] = (xu - m.x) * (m.y - yl) * (m.z - zl) / vol;
+    coeff[4] = (m.x - xl) * (yu - m.y) * (zu - m.z) / vol;
+    coeff[5] = (m.x - xl) * (yu - m.y) * (m.z - zl) / vol;
+    coeff[6] = (m.x - xl) * (m.y - yl) * (zu - m.z) / vol;
+    coeff[7] = (m.x - xl) * (m.y - yl) * (m.z - zl) / vol;
+}
+
+// ------------------------------------------------------------- init ---
+// src/ibm3d_init.c:15-37
+void IBMSolver_init_flow_const(IBMSolver *s, const double u1, const double u2, const double u3, const double p) {
+    if (!check_ready(s, "IBMSolver_init_flow_const")) return;
+    const size_t n = (size_t)ncell_of(s);
+    std::fill(s->u1, s->u1 + n, u1);
+    std::fill(s->u2, s->u2 + n, u2);
+    std::fill(s->u3, s->u3 + n, u3);
+    std::fill(s->p, s->p + n, p);
+    upload_state(s, s->u1, s->u2, s->u3, s->p);
+}
+
+// src/ibm3d_init.c:237-262
+void IBMSolver_init_flow_func(IBMSolver *s, IBMSolverInitFunc f1, IBMSolverInitFunc f2, IBMSolverInitFunc f3,
+                              IBMSolverInitFunc fp) {
+    if (!check_ready(s, "IBMSolver_init_flow_func")) return;
+    for (int i = -2; i < s->Nx + 2; i++)
+        for (int j = -2; j < s->Ny + 2; j++)
+            for (int k = -2; k < s->Nz + 2; k++) {
+                const long long P = cidx(s->dev->g, i, j, k);
+                const double x = s->xc[i + 2], y = s->yc[j + 2], z = s->zc[k + 2];
+                s->u1[P] = f1(x, y, z);
+                s->u2[P] = f2(x, y, z);
+                s->u3[P] = f3(x, y, z);
+                s->p[P] = fp(x, y, z);
+            }
+    upload_state(s, s->u1, s->u2, s->u3, s->p);
+}
+
+void IBMSolver_init_flow_array(IBMSolver *s, const double *u1, const double *u2, const double *u3, const double *p) {
+    if (!check_ready(s, "IBMSolver_init_flow_array")) return;
+    upload_state(s, u1, u2, u3, p);
+}
+
+// ----------------------------------------------------------- export ---
+struct StateHeader {
+    char magic[8];
+    int nx, ny, nz, iter;
+    double time;
+};
+
+void IBMSolver_export_result(IBMSolver *s, const char *name) {
+    if (!check_ready(s, "IBMSolver_export_result")) return;
+    IBMSolver_sync_host(s);
+    std::string path = std::string(name) + ".ibm3d";
+    FILE *f = fopen(path.c_str(), "wb");
+    if (!f) {
+        set_status(s, IBM3D_EARG, "cannot open file \"%s\"", path.c_str());
+        return;
+    }
+    StateHeader h{};
+    memcpy(h.magic, "IBM3DST1", 8);
+    h.nx = s->Nx; h.ny = s->Ny; h.nz = s->Nz; h.iter = s->iter; h.time = s->time;
+    const size_t n = (size_t)ncell_of(s);
+    fwrite(&h, sizeof h, 1, f);
+    fwrite(s->u1, sizeof(double), n, f);
+    fwrite(s->u2, sizeof(double), n, f);
+    fwrite(s->u3, sizeof(double), n, f);
+    fwrite(s->p, sizeof(double), n, f);
+    fclose(f);
+}
+
+// src/ibm3d_init.c:45-224 (reads the state export_result writes).
+void IBMSolver_init_flow_file(IBMSolver *s, const char *name) {
+    if (!check_ready(s, "IBMSolver_init_flow_file")) return;
+    std::string path = std::string(name) + ".ibm3d";
+    FILE *f = fopen(path.c_str(), "rb");
+    if (!f) {
+        set_status(s, IBM3D_EARG, "cannot open file \"%s\"", path.c_str());
+        return;
+    }
+    StateHeader h{};
+    const size_t n = (size_t)ncell_of(s);
+    bool ok = fread(&h, sizeof h, 1, f) == 1 && memcmp(h.magic, "IBM3DST1", 8) == 0 && h.nx == s->Nx &&
+              h.ny == s->Ny && h.nz == s->Nz;
+    ok = ok && fread(s->u1, sizeof(double), n, f) == n && fread(s->u2, sizeof(double), n, f) == n &&
+         fread(s->u3, sizeof(double), n, f) == n && fread(s->p, sizeof(double), n, f) == n;
+    fclose(f);
+    if (!ok) {
+        set_status(s, IBM3D_EARG, "\"%s\" is not a state file of this grid", path.c_str());
+        return;
+    }
+    upload_state(s, s->u1, s->u2, s->u3, s->p);
+    s->iter = h.iter;
+    s->time = h.time;
+}
+
+void IBMSolver_export_lvset_flag(IBMSolver *s, const char *name) {
+    if (!check_ready(s, "IBMSolver_export_lvset_flag")) return;
+    std::string path = std::string(name) + ".lvset_flag";
+    FILE *f = fopen(path.c_str(), "wb");
+    if (!f) {
+        set_status(s, IBM3D_EARG, "cannot open file \"%s\"", path.c_str());
+        return;
+    }
+    const size_t n = (size_t)ncell_of(s);
+    fwrite(s->lvset, sizeof(double), n, f);
+    fwrite(s->flag, sizeof(int), n, f);
+    fclose(f);
+}
+
+void IBMSolver_export_intermediate(IBMSolver *s, const char *name) {
+    if (!check_ready(s, "IBMSolver_export_intermediate")) return;
+    std::string path = std::string(name) + ".intermediate";
+    FILE *f = fopen(path.c_str(), "wb");
+    if (!f) {
+        set_status(s, IBM3D_EARG, "cannot open file \"%s\"", path.c_str());
+        return;
+    }
+    const size_t n = (size_t)ncell_of(s);
+    std::vector<double> h(n);
+    const int which[7] = {IBM3D_F_USTAR1, IBM3D_F_USTAR2, IBM3D_F_USTAR3, IBM3D_F_PPRIME, IBM3D_F_U1, IBM3D_F_U2, IBM3D_F_U3};
+    for (int w : which) {
+        IBMSolver_get_field(s, w, h.data());
+        fwrite(h.data(), sizeof(double), n, f);
+    }
+    fclose(f);
+}
+
+// -------------------------------------------------------------- turb ---
+void IBMSolver_calc_tau_r(IBMSolver *s) {
+    if (!check_ready(s, "IBMSolver_calc_tau_r")) return;
+    calc_tau(s);
+    cuda_check(s, cudaStreamSynchronize(s->dev->s), "calc_tau_r");
+}
+
+// ---------------------------------------------------------- iterate ---
+// src/ibm3d_fracstep.c:38-115
+void IBMSolver_iterate(IBMSolver *s, int num_time_steps, bool verbose) {
+    if (!check_ready(s, "IBMSolver_iterate")) return;
+    ibm3d_device *d = s->dev;
+    const double start_time = s->time;
+    d->status = IBM3D_OK;
+    fill_outer(s);
+    launch_interp_stag(d->s, d->g, d->ax[0], d->ax[1], d->ax[2], d->u, d->U);
+    ghost_update(s, true);
+    {
+        const double f[3] = {s->ext_force.const_f1, s->ext_force.const_f2, s->ext_force.const_f3};
+        launch_conv_rhs(d->s, d->g, d->ax[0], d->ax[1], d->ax[2], d->bc, d->flag, conv_args(d), s->dt, f, 0);
+        swap3(d->N, d->Np);
+    }
+    struct timespec t0, t1;
+    clock_gettime(CLOCK_REALTIME, &t0);
+    for (int i = 1; i <= num_time_steps; i++) {
+        one_step(s);
+        s->iter++;
+        s->time = start_time + s->dt * i;
+        int t = d->prof.begin("fill_outer");
+        fill_outer(s);
+        d->prof.end(t);
+        t = d->prof.begin("ghost_update");
+        ghost_update(s, false);
+        d->prof.end(t);
+        cudaMemcpyAsync(d->maxdiv_h, d->maxdiv_d, sizeof(double), cudaMemcpyDeviceToHost, d->s);
+        if (!cuda_check(s, cudaStreamSynchronize(d->s), "time step")) return;
+        d->max_div = *d->maxdiv_h;
+        d->prof.flush();
+        if (verbose && s->rank == 0) {
+            clock_gettime(CLOCK_REALTIME, &t1);
+            const long el = (t1.tv_sec * 1000 + t1.tv_nsec / 1000000) - (t0.tv_sec * 1000 + t0.tv_nsec / 1000000);
+            print_row(s, i, el);
+        }
+        if (s->autosave_period > 0 && s->iter % s->autosave_period == 0) {
+            if (s->rank == 0) printf("\nAutosave...\n\n");
+            char fn[1024];
+            snprintf(fn, sizeof fn, "%s-%05d", s->autosave_filename, s->iter);
+            IBMSolver_export_result(s, fn);
+        }
+    }
+}
+
+// ------------------------------------------------------- extensions ---
+int IBMSolver_last_status(const IBMSolver *s) { return s && s->dev ? s->dev->status : IBM3D_EARG; }
+
+const char *IBMSolver_status_string(int st) {
+    switch (st) {
+    case IBM3D_OK: return "ok";
+    case IBM3D_ENOCONV: return "Krylov solve did not converge";
+    case IBM3D_EBREAKDOWN: return "BiCGSTAB breakdown";
+    case IBM3D_ECUDA: return "CUDA error";
+    case IBM3D_EARG: return "invalid argument";
+    case IBM3D_EGEOM: return "ghost-cell mirror point outside the grid";
+    case IBM3D_EUNSUPPORTED: return "unsupported on the GPU path";
+    }
+    return "unknown";
+}
+
+void IBMSolver_set_bc_const(IBMSolver *s, IBMSolverDirection dir, IBMSolverBCType type, double u1, double u2,
+                            double u3, double p) {
+    switch (type) {
+    case BC_VELOCITY_COMPONENT:
+        set_bc_impl(s, dir, type, VAL_CONST, u1, u2, u3, kNaN, nullptr, nullptr, nullptr, nullptr);
+        break;
+    case BC_PRESSURE:
+    case BC_VELOCITY_PERIODIC:
+        set_bc_impl(s, dir, type, VAL_CONST, kNaN, kNaN, kNaN, p, nullptr, nullptr, nullptr, nullptr);
+        break;
+    case BC_STATIONARY_WALL:
+        set_bc_impl(s, dir, BC_VELOCITY_COMPONENT, VAL_CONST, 0, 0, 0, kNaN, nullptr, nullptr, nullptr, nullptr);
+        break;
+    case BC_SYMMETRIC:
+        set_bc_impl(s, dir, BC_FREE_SLIP_WALL, VAL_CONST, kNaN, kNaN, kNaN, kNaN, nullptr, nullptr, nullptr, nullptr);
+        break;
+    default:
+        set_bc_impl(s, dir, type, VAL_CONST, kNaN, kNaN, kNaN, kNaN, nullptr, nullptr, nullptr, nullptr);
+    }
+}
+
+void IBMSolver_set_ext_force_const(IBMSolver *s, double f1, double f2, double f3) {
+    s->ext_force.val_type = VAL_CONST;
+    s->ext_force.const_f1 = f1;
+    s->ext_force.const_f2 = f2;
+    s->ext_force.const_f3 = f3;
+}
+
+void IBMSolver_set_smagorinsky(IBMSolver *s, double Cs) {
+    s->turb_model.type = TURBMODEL_SMAGORINSKY;
+    s->turb_model.Cs = Cs;
+}
+
+void IBMSolver_set_div_tol(IBMSolver *s, double div_tol) { s->dev->divtol = div_tol; }
+
+void IBMSolver_set_precision(IBMSolver *s, int mode) {
+    if (mode != IBM3D_FP64) {
+        set_status(s, IBM3D_EUNSUPPORTED, "precision mode %d is not available", mode);
+        return;
+    }
+    s->dev->precision = mode;
+}
+
+void IBMSolver_get_field(IBMSolver *s, int field, double *out) {
+    if (!check_ready(s, "IBMSolver_get_field")) return;
+    ibm3d_device *d = s->dev;
+    const Grid &g = d->g;
+    const size_t n = g.ncell;
+    const double *src = nullptr;
+    int face = -1;
+    switch (field) {
+    case IBM3D_F_U1: src = d->u[0]; break;
+    case IBM3D_F_U2: src = d->u[1]; break;
+    case IBM3D_F_U3: src = d->u[2]; break;
+    case IBM3D_F_P: src = d->p; break;
+    case IBM3D_F_FACE_U1: src = d->U[0]; face = 0; break;
+    case IBM3D_F_FACE_U2: src = d->U[1]; face = 1; break;
+    case IBM3D_F_FACE_U3: src = d->U[2]; face = 2; break;
+    case IBM3D_F_USTAR1: src = d->ustar; break;
+    case IBM3D_F_USTAR2: src = d->ustar + n; break;
+    case IBM3D_F_USTAR3: src = d->ustar + 2 * n; break;
+    case IBM3D_F_FACE_USTAR1: src = d->Us[0]; face = 0; break;
+    case IBM3D_F_FACE_USTAR2: src = d->Us[1]; face = 1; break;
+    case IBM3D_F_FACE_USTAR3: src = d->Us[2]; face = 2; break;
+    case IBM3D_F_PPRIME: src = d->pp; break;
+    // After a step N and N_prev are swapped: N_prev holds the last step's N.
+    case IBM3D_F_N1: src = d->Np[0]; break;
+    case IBM3D_F_N2: src = d->Np[1]; break;
+    case IBM3D_F_N3: src = d->Np[2]; break;
+    case IBM3D_F_LVSET: src = d->lvset; break;
+    case IBM3D_F_COEFFSUM:
+        memcpy(out, s->p_coeffsum, sizeof(double) * n);
+        return;
+    default:
+        if (field >= IBM3D_F_TAU11 && field <= IBM3D_F_TAU33) {
+            src = d->tau[field - IBM3D_F_TAU11];
+            break;
+        }
+        set_status(s, IBM3D_EARG, "unknown field %d", field);
+        return;
+    }
+    std::vector<double> h(n);
+    cudaMemcpyAsync(h.data(), src, sizeof(double) * n, cudaMemcpyDeviceToHost, d->s);
+    if (!cuda_check(s, cudaStreamSynchronize(d->s), "get_field")) return;
+    if (face < 0) {
+        memcpy(out, h.data(), sizeof(double) * n);
+        return;
+    }
+    const int Nx = s->Nx, Ny = s->Ny, Nz = s->Nz;
+    size_t q = 0;
+    if (face == 0) {
+        for (int i = 0; i <= Nx; i++)
+            for (int j = -2; j < Ny + 2; j++)
+                for (int k = -2; k < Nz + 2; k++) out[q++] = h[cidx(g, i, j, k)];
+    } else if (face == 1) {
+        for (int i = -2; i < Nx + 2; i++)
+            for (int j = 0; j <= Ny; j++)
+                for (int k = -2; k < Nz + 2; k++) out[q++] = h[cidx(g, i, j, k)];
+    } else {
+        for (int i = -2; i < Nx + 2; i++)
+            for (int j = -2; j < Ny + 2; j++)
+                for (int k = 0; k <= Nz; k++) out[q++] = h[cidx(g, i, j, k)];
+    }
+}
+
+void IBMSolver_get_flag(IBMSolver *s, int *out) {
+    if (!check_ready(s, "IBMSolver_get_flag")) return;
+    memcpy(out, s->flag, sizeof(int) * (size_t)ncell_of(s));
+}
+
+void IBMSolver_sync_host(IBMSolver *s) {
+    if (!check_ready(s, "IBMSolver_sync_host")) return;
+    IBMSolver_get_field(s, IBM3D_F_U1, s->u1);
+    IBMSolver_get_field(s, IBM3D_F_U2, s->u2);
+    IBMSolver_get_field(s, IBM3D_F_U3, s->u3);
+    IBMSolver_get_field(s, IBM3D_F_P, s->p);
+}
+
+int IBMSolver_num_ghost(IBMSolver *s) { return s && s->dev ? s->dev->nghost : 0; }
+
+int IBMSolver_num_ghost_levels(IBMSolver *s) { return s && s->dev ? s->dev->nlevels : 0; }
+
+void IBMSolver_get_ghost_stencils(IBMSolver *s, int *ijk, int *idx, double *coeff) {
+    if (!check_ready(s, "IBMSolver_get_ghost_stencils")) return;
+    ibm3d_device *d = s->dev;
+    for (int q = 0; q < d->nghost; q++) {
+        int i, j, k;
+        cijk(d->g, d->gcell_lex[q], i, j, k);
+        ijk[3 * q] = i;
+        ijk[3 * q + 1] = j;
+        ijk[3 * q + 2] = k;
+        const GhostStencil &st = d->gst[q];
+        for (int l = 0; l < 8; l++) {
+            idx[24 * q + 3 * l] = st.im + !!(l & 4);
+            idx[24 * q + 3 * l + 1] = st.jm + !!(l & 2);
+            idx[24 * q + 3 * l + 2] = st.km + !!(l & 1);
+            coeff[8 * q + l] = st.raw[l];
+        }
+    }
+}
+
+void IBMSolver_get_stats(const IBMSolver *s, IBMSolverStats *out) {
+    const ibm3d_device *d = s->dev;
+    memset(out, 0, sizeof *out);
+    out->iter = s->iter;
+    out->time = s->time;
+    for (int l = 0; l < 3; l++) {
+        out->iters_u[l] = d->rep_mom.iters[l];
+        out->res_u[l] = d->rep_mom.relres[l];
+    }
+    out->iters_p = d->rep_p.iters[0];
+    out->res_p = d->rep_p.relres[0];
+    out->max_div = d->max_div;
+    out->mg_levels = d->mg ? d->mg->nlevels() : 0;
+    out->cpt_fallback = d->cpt_fallback;
+}
+
+double IBMSolver_time_iterate(IBMSolver *s, int nsteps) {
+    if (!check_ready(s, "IBMSolver_time_iterate")) return -1;
+    ibm3d_device *d = s->dev;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaStreamSynchronize(d->s);
+    cudaEventRecord(a, d->s);
+    IBMSolver_iterate(s, nsteps, false);
+    cudaEventRecord(b, d->s);
+    cudaEventSynchronize(b);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return ms;
+}
+
+void IBMSolver_set_profiling(IBMSolver *s, int on) {
+    s->dev->prof.reset();
+    s->dev->prof.on = on != 0;
+}
+
+int IBMSolver_get_profile(IBMSolver *s, int max, char names[][32], int *launches, double *total_ms) {
+    ibm3d_device *d = s->dev;
+    d->prof.flush();
+    int q = 0;
+    for (auto &kv : d->prof.total) {
+        if (q >= max) break;
+        snprintf(names[q], 32, "%s", kv.first.c_str());
+        launches[q] = (int)kv.second.first;
+        total_ms[q] = kv.second.second;
+        q++;
+    }
+    return q;
+}
+
+const char *IBMSolver_device_name(IBMSolver *s) { return s && s->dev ? s->dev->dev_name : ""; }
+
+// Polyhedron_cpt (src/geo3d.c:436-704) on the GPU for an arbitrary grid.
+void Polyhedron_cpt(const Polyhedron *const poly, const int nx, const int ny, const int nz, const double *x,
+                    const double *y, const double *z, double *f, const double maxd) {
+    CptModel m;
+    build_cpt_model(poly, maxd, m);
+    double *dx = nullptr, *dy = nullptr, *dz = nullptr, *df = nullptr;
+    const size_t n = (size_t)nx * ny * nz;
+    cudaStream_t s;
+    if (cudaStreamCreate(&s) != cudaSuccess || cudaMalloc(&dx, sizeof(double) * nx) != cudaSuccess ||
+        cudaMalloc(&dy, sizeof(double) * ny) != cudaSuccess || cudaMalloc(&dz, sizeof(double) * nz) != cudaSuccess ||
+        cudaMalloc(&df, sizeof(double) * n) != cudaSuccess) {
+        fprintf(stderr, "error: Polyhedron_cpt needs a CUDA device\n");
+        std::exit(255);
+    }
+    cudaMemcpyAsync(dx, x, sizeof(double) * nx, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(dy, y, sizeof(double) * ny, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(dz, z, sizeof(double) * nz, cudaMemcpyHostToDevice, s);
+    const int rc = gpu_cpt(s, m, nx, ny, nz, dx, dy, dz, df, maxd, nullptr);
+    cudaMemcpyAsync(f, df, sizeof(double) * n, cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    cudaFree(dx); cudaFree(dy); cudaFree(dz); cudaFree(df);
+    cudaStreamDestroy(s);
+    if (rc != 0) {
+        fprintf(stderr, "error: Polyhedron_cpt kernels failed\n");
+        std::exit(255);
+    }
+}
+
+}  // extern "C"

@@ -1,0 +1,107 @@
+/*
+ * ibm3d-gb300 extensions to the reference C ABI.
+ *
+ * None of these exist in the reference; they are additive and never change
+ * the behaviour of the reference entry points.  They serve callers that
+ * cannot use C varargs (FFI layers), expose per-step solver statistics and
+ * device timing, and let a host hand fields to the GPU and read them back.
+ */
+#ifndef IBM3D_GB300_H
+#define IBM3D_GB300_H
+
+#include "ibm3d.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status of the last call on a solver: 0 ok, otherwise an IBM3D_E* code. */
+enum {
+    IBM3D_OK = 0,
+    IBM3D_ENOCONV = 1,      /* a Krylov solve hit its iteration cap (warning, as in the reference) */
+    IBM3D_EBREAKDOWN = 2,   /* BiCGSTAB breakdown */
+    IBM3D_ECUDA = 3,        /* CUDA error or no usable GPU */
+    IBM3D_EARG = 4,         /* invalid argument or call order */
+    IBM3D_EGEOM = 5,        /* ghost-cell mirror point outside the grid */
+    IBM3D_EUNSUPPORTED = 6  /* feature not available on the GPU path */
+};
+int IBMSolver_last_status(const IBMSolver *);
+const char *IBMSolver_status_string(int status);
+
+/* Non-variadic forms of set_bc / set_ext_force / set_turb_model (same
+   semantics as the VAL_CONST variadic calls). */
+void IBMSolver_set_bc_const(IBMSolver *, IBMSolverDirection, IBMSolverBCType,
+                            double u1, double u2, double u3, double p);
+void IBMSolver_set_ext_force_const(IBMSolver *, double f1, double f2, double f3);
+void IBMSolver_set_smagorinsky(IBMSolver *, double Cs);
+
+/* Pressure-solve stopping rule.  div_tol > 0: stop once the projected face
+   velocity satisfies max|div U^{n+1}| <= div_tol on fluid cells; 0 (the
+   default) keeps the reference's ||r||/||b|| < tol rule. */
+void IBMSolver_set_div_tol(IBMSolver *, double div_tol);
+
+/* Arithmetic of the step: IBM3D_FP64 (default, the plain FP64 step). */
+enum { IBM3D_FP64 = 0 };
+void IBMSolver_set_precision(IBMSolver *, int mode);
+
+/* Initial state from host arrays in the padded (N+4)^3 layout, k fastest
+   (u1, u2, u3, p).  Sets iter = 0 and time = 0 like init_flow_const. */
+void IBMSolver_init_flow_array(IBMSolver *, const double *u1, const double *u2, const double *u3, const double *p);
+
+/* Field read-back in the reference's layouts.  Cell fields: (Nx+4)(Ny+4)(Nz+4);
+   U1: (Nx+1)(Ny+4)(Nz+4); U2: (Nx+4)(Ny+1)(Nz+4); U3: (Nx+4)(Ny+4)(Nz+1). */
+enum {
+    IBM3D_F_U1 = 0, IBM3D_F_U2, IBM3D_F_U3, IBM3D_F_P,
+    IBM3D_F_FACE_U1, IBM3D_F_FACE_U2, IBM3D_F_FACE_U3,
+    IBM3D_F_USTAR1, IBM3D_F_USTAR2, IBM3D_F_USTAR3,
+    IBM3D_F_FACE_USTAR1, IBM3D_F_FACE_USTAR2, IBM3D_F_FACE_USTAR3,
+    IBM3D_F_PPRIME, IBM3D_F_N1, IBM3D_F_N2, IBM3D_F_N3,
+    IBM3D_F_LVSET, IBM3D_F_COEFFSUM,
+    IBM3D_F_TAU11, IBM3D_F_TAU12, IBM3D_F_TAU13, IBM3D_F_TAU22, IBM3D_F_TAU23, IBM3D_F_TAU33,
+    IBM3D_F_COUNT
+};
+void IBMSolver_get_field(IBMSolver *, int field, double *out);
+void IBMSolver_get_flag(IBMSolver *, int *out);
+/* Copies u1, u2, u3, p into the struct's host mirrors. */
+void IBMSolver_sync_host(IBMSolver *);
+
+/* Ghost cells, in lexicographic (i, j, k) order.  For each ghost: its
+   (i, j, k), the 8 stencil cells and raw trilinear weights exactly as
+   IBMSolver_ghost_interp returns them (computed on the GPU). */
+int IBMSolver_num_ghost(IBMSolver *);
+void IBMSolver_get_ghost_stencils(IBMSolver *, int *ijk, int *interp_idx, double *interp_coeff);
+/* Dependency levels of the in-place ghost update. */
+int IBMSolver_num_ghost_levels(IBMSolver *);
+
+typedef struct {
+    int iter;               /* solver->iter after the step */
+    double time;
+    int iters_u[3];         /* BiCGSTAB iterations, momentum components */
+    int iters_p;            /* BiCGSTAB iterations, pressure */
+    double res_u[3];        /* final relative residual norms */
+    double res_p;
+    double max_div;         /* max |div U^{n+1}| over fluid cells (pinned cell excluded) */
+    int mg_levels;          /* pressure multigrid levels (incl. the fine grid) */
+    int cpt_fallback;       /* level-set points settled by the full extrusion scan */
+} IBMSolverStats;
+void IBMSolver_get_stats(const IBMSolver *, IBMSolverStats *);
+
+/* Device timing: runs IBMSolver_iterate(nsteps) bracketed by CUDA events on
+   the solver's stream and returns the elapsed device milliseconds. */
+double IBMSolver_time_iterate(IBMSolver *, int nsteps);
+
+/* Per-stage device time accumulated while profiling is on (CUDA events
+   around each stage of each step).  Stage names: conv_rhs, tau, mom_solve,
+   ustar_prhs, p_solve, update_next, fill_outer, ghost_update; plus the
+   individual Krylov kernels spmv_mom, spmv_p, mg_vcycle. */
+void IBMSolver_set_profiling(IBMSolver *, int on);
+int IBMSolver_get_profile(IBMSolver *, int max, char names[][32], int *launches, double *total_ms);
+
+/* Device name of the solver's GPU (for logs). */
+const char *IBMSolver_device_name(IBMSolver *);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

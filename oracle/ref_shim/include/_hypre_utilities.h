@@ -1,0 +1,2 @@
+/* Forwarding header of the hypre stand-in (see HYPRE.h). Test infrastructure. */
+#include "HYPRE.h"
