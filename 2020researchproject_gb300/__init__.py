@@ -107,6 +107,9 @@ def load_library(path: str = LIB_PATH):
         "IBMSolver_set_profiling": (None, [vp, i]),
         "IBMSolver_get_profile": (i, [vp, i, vp, ip, dp]),
         "IBMSolver_device_name": (ctypes.c_char_p, [vp]),
+        "IBMSolver_kernel_launches": (ctypes.c_longlong, []),
+        "IBMSolver_host_register": (i, [vp, ctypes.c_size_t]),
+        "IBMSolver_host_unregister": (i, [vp]),
         "Polyhedron_new": (vp, []),
         "Polyhedron_destroy": (None, [vp]),
         "Polyhedron_read_stl": (None, [vp, vp]),
@@ -122,6 +125,20 @@ def load_library(path: str = LIB_PATH):
 
 def _ptr(a: np.ndarray):
     return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def kernel_launches() -> int:
+    """Kernels the library has launched since it was loaded."""
+    return int(load_library().IBMSolver_kernel_launches())
+
+
+def pin(a: np.ndarray) -> bool:
+    """Page-lock a numpy array's memory for direct host<->device DMA."""
+    return load_library().IBMSolver_host_register(a.ctypes.data_as(ctypes.c_void_p), a.nbytes) == 0
+
+
+def unpin(a: np.ndarray) -> None:
+    load_library().IBMSolver_host_unregister(a.ctypes.data_as(ctypes.c_void_p))
 
 
 class Polyhedron:
@@ -258,6 +275,13 @@ class IBMSolver:
 
     def get_field(self, name):
         out = np.empty(self._field_shape(name), dtype=np.float64)
+        self._lib.IBMSolver_get_field(self._s, FIELDS.index(name), _ptr(out))
+        self._check("get_field")
+        return out
+
+    def get_field_into(self, name, out):
+        """Read a field into a caller-owned C-contiguous float64 array."""
+        assert out.flags.c_contiguous and out.dtype == np.float64 and out.shape == self._field_shape(name)
         self._lib.IBMSolver_get_field(self._s, FIELDS.index(name), _ptr(out))
         self._check("get_field")
         return out

@@ -8,6 +8,9 @@
 
 namespace ibm {
 
+// Number of kernels this library has launched (for per-step launch counts).
+void note_launches(int n);
+
 struct ConvArgs {
     const double *u[3];
     const double *U[3];

@@ -377,6 +377,7 @@ k_apply(const OpCtx ctx, const int op, const int comp, const long long n, const 
 
 void apply_operator(cudaStream_t st, const OpCtx &ctx, int op, int comp, const double *x, double *y) {
     k_apply<<<KBLOCKS, KTHREADS, 0, st>>>(ctx, op, comp, ctx.g.ncell, x, y);
+    note_launches(1);
 }
 
 // -------------------------------------------------------------- driver --
@@ -442,6 +443,7 @@ int bicgstab(cudaStream_t st, const OpCtx &ctx, int op, KrylovWork &w, const dou
     const long long n = w.n;
     const int nc = w.nc;
     k_bicg_init<<<KBLOCKS, KTHREADS, 0, st>>>(n, nc, b, x, w.r, w.r0, w.p, w.v, w.scal, w.partials, w.counter);
+    note_launches(1);
     const double two_re = 2 * prm.Re;
     int it = 0;
     auto fetch = [&]() {
@@ -452,6 +454,7 @@ int bicgstab(cudaStream_t st, const OpCtx &ctx, int op, KrylovWork &w, const dou
     while (!all_in(w.scal_h, nc, KS_DONE, KS_BREAKDOWN, KS_DONE) && it < prm.maxit) {
         it++;
         k_bicg_p<<<KBLOCKS, KTHREADS, 0, st>>>(n, nc, w.r, w.p, w.v, w.scal);
+        note_launches(1);
         int tm = -1;
         if (M) {
             tm = prof_begin(prm.prof, "mg_vcycle");
@@ -460,14 +463,17 @@ int bicgstab(cudaStream_t st, const OpCtx &ctx, int op, KrylovWork &w, const dou
         }
         tm = prof_begin(prm.prof, op == OP_MOM ? "spmv_mom" : "spmv_p");
         k_bicg_spmv_v<<<KBLOCKS, KTHREADS, 0, st>>>(ctx, op, n, nc, w.ph, w.v, w.r0, w.scal, w.partials, w.counter);
+        note_launches(1);
         prof_end(prm.prof, tm);
         k_bicg_s<<<KBLOCKS, KTHREADS, 0, st>>>(ctx, n, nc, w.r, w.v, w.s, w.scal, prm.tol, prm.divtol, two_re,
                                              w.partials, w.counter);
+        note_launches(1);
         if (prm.sync_half) {
             fetch();
             if (all_in(w.scal_h, nc, KS_HALF, KS_DONE, KS_BREAKDOWN)) {
                 k_bicg_xr<<<KBLOCKS, KTHREADS, 0, st>>>(ctx, n, nc, x, w.r, w.r0, w.ph, w.sh, w.s, w.t, w.scal,
                                                       prm.tol, prm.divtol, two_re, w.partials, w.counter);
+                note_launches(1);
                 fetch();
                 break;
             }
@@ -479,9 +485,11 @@ int bicgstab(cudaStream_t st, const OpCtx &ctx, int op, KrylovWork &w, const dou
         }
         tm = prof_begin(prm.prof, op == OP_MOM ? "spmv_mom" : "spmv_p");
         k_bicg_spmv_t<<<KBLOCKS, KTHREADS, 0, st>>>(ctx, op, n, nc, w.sh, w.t, w.s, w.scal, w.partials, w.counter);
+        note_launches(1);
         prof_end(prm.prof, tm);
         k_bicg_xr<<<KBLOCKS, KTHREADS, 0, st>>>(ctx, n, nc, x, w.r, w.r0, w.ph, w.sh, w.s, w.t, w.scal, prm.tol,
                                               prm.divtol, two_re, w.partials, w.counter);
+        note_launches(1);
         fetch();
     }
     int status = 0;

@@ -480,11 +480,15 @@ void GMG::smooth0(cudaStream_t s, const double *r, double *z, int sweeps) {
     for (int it = 0; it < sweeps; it++) {
         for (int col = 0; col < (seam ? 4 : 2); col++)
             k_mg0_color<<<nblk(n, 256), 256, 0, s>>>(ctx_, r, z, col, per);
+            note_launches(1);
         if (nghost_ > 0) {
             k_mg0_ghost<<<nblk(nghost_, 128), 128, 0, s>>>(ctx_, r, z, ghost_cell_, nghost_, ghost_tmp_);
+            note_launches(1);
             k_mg0_ghost_scatter<<<nblk(nghost_, 128), 128, 0, s>>>(ghost_cell_, nghost_, ghost_tmp_, z);
+            note_launches(1);
         }
         k_mg0_outer<<<nblk(nouter_, 256), 256, 0, s>>>(ctx_, r, z, outer_, nouter_);
+        note_launches(1);
     }
 }
 
@@ -498,6 +502,7 @@ void GMG::apply(cudaStream_t s, const double *r, double *z) {
     Per3 per{{per_[0], per_[1], per_[2]}};
     smooth0(s, r, z, cfg_.nu_pre);
     k_mg0_restrict<<<nblk(levels_[0].n, 256), 256, 0, s>>>(ctx_, r, z, levels_[0]);
+    note_launches(1);
     const int nl = (int)levels_.size();
     for (int l = 0; l < tail_; l++) {
         MGLevel<double> &L = levels_[l];
@@ -505,15 +510,19 @@ void GMG::apply(cudaStream_t s, const double *r, double *z) {
         for (int it = 0; it < cfg_.nu_pre; it++)
             for (int col = 0; col < 4; col++) k_mgc_color<<<nblk(L.n, 256), 256, 0, s>>>(L, col, per);
         k_mgc_restrict<<<nblk(levels_[l + 1].n, 256), 256, 0, s>>>(L, levels_[l + 1], per);
+        note_launches(1);
     }
     k_mg_tail<<<1, 1024, 0, s>>>(dlevels_, tail_, nl, cfg_.nu_pre, cfg_.nu_post, cfg_.coarse_sweeps, per);
+    note_launches(1);
     for (int l = tail_ - 1; l >= 0; l--) {
         MGLevel<double> &L = levels_[l];
         k_mgc_prolong<<<nblk(L.n, 256), 256, 0, s>>>(levels_[l + 1], L);
+        note_launches(1);
         for (int it = 0; it < cfg_.nu_post; it++)
             for (int col = 0; col < 4; col++) k_mgc_color<<<nblk(L.n, 256), 256, 0, s>>>(L, col, per);
     }
     k_mg0_prolong<<<nblk((long long)g.nx * g.ny * g.nz, 256), 256, 0, s>>>(ctx_, z, levels_[0]);
+    note_launches(1);
     smooth0(s, r, z, cfg_.nu_post);
 }
 

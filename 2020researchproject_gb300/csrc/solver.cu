@@ -27,6 +27,13 @@
 
 using namespace ibm;
 
+#include <atomic>
+
+namespace ibm {
+static std::atomic<long long> g_launches{0};
+void note_launches(int n) { g_launches += n; }
+}  // namespace ibm
+
 struct ibm3d_device {
     cudaStream_t s = nullptr;
     Grid g{};
@@ -1206,13 +1213,14 @@ void IBMSolver_get_field(IBMSolver *s, int field, double *out) {
         set_status(s, IBM3D_EARG, "unknown field %d", field);
         return;
     }
+    if (face < 0) {
+        cudaMemcpyAsync(out, src, sizeof(double) * n, cudaMemcpyDeviceToHost, d->s);
+        cuda_check(s, cudaStreamSynchronize(d->s), "get_field");
+        return;
+    }
     std::vector<double> h(n);
     cudaMemcpyAsync(h.data(), src, sizeof(double) * n, cudaMemcpyDeviceToHost, d->s);
     if (!cuda_check(s, cudaStreamSynchronize(d->s), "get_field")) return;
-    if (face < 0) {
-        memcpy(out, h.data(), sizeof(double) * n);
-        return;
-    }
     const int Nx = s->Nx, Ny = s->Ny, Nz = s->Nz;
     size_t q = 0;
     if (face == 0) {
@@ -1318,6 +1326,14 @@ int IBMSolver_get_profile(IBMSolver *s, int max, char names[][32], int *launches
     }
     return q;
 }
+
+long long IBMSolver_kernel_launches(void) { return ibm::g_launches.load(); }
+
+int IBMSolver_host_register(void *ptr, size_t bytes) {
+    return cudaHostRegister(ptr, bytes, cudaHostRegisterDefault) == cudaSuccess ? 0 : -1;
+}
+
+int IBMSolver_host_unregister(void *ptr) { return cudaHostUnregister(ptr) == cudaSuccess ? 0 : -1; }
 
 const char *IBMSolver_device_name(IBMSolver *s) { return s && s->dev ? s->dev->dev_name : ""; }
 

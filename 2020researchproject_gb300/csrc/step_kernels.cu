@@ -93,6 +93,7 @@ void launch_conv_rhs(cudaStream_t s, const Grid &g, const Axis &ax, const Axis &
                      const BCSet &bc, const uint8_t *flag, const ConvArgs &a, double dt, const double f[3],
                      int les) {
     k_conv_rhs<<<grid_for(g.ncell, 256), 256, 0, s>>>(g, ax, ay, az, bc, flag, a, dt, f[0], f[1], f[2], les);
+    note_launches(1);
 }
 
 // ------------------------------------------------------------------------
@@ -139,6 +140,7 @@ void launch_smagorinsky(cudaStream_t s, const Grid &g, const Axis &ax, const Axi
                         double cs) {
     const long long n = (long long)g.nx * g.ny * g.nz;
     k_smagorinsky<<<grid_for(n, 256), 256, 0, s>>>(g, ax, ay, az, flag, lvset, u[0], u[1], u[2], t, cs);
+    note_launches(1);
 }
 
 // ------------------------------------------------------------------------
@@ -206,6 +208,7 @@ k_ustar_prhs(const Grid g, const Axis ax, const Axis ay, const Axis az, const BC
 void launch_ustar_prhs(cudaStream_t s, const Grid &g, const Axis &ax, const Axis &ay, const Axis &az,
                        const BCSet &bc, const uint8_t *flag, const UstarArgs &a, double dt, double Re) {
     k_ustar_prhs<<<grid_for(g.ncell, 256), 256, 0, s>>>(g, ax, ay, az, bc, flag, a, dt, Re);
+    note_launches(1);
 }
 
 // ------------------------------------------------------------------------
@@ -270,6 +273,7 @@ void launch_update_next(cudaStream_t s, const Grid &g, const Axis &ax, const Axi
                         const BCSet &bc, const uint8_t *flag, const NextArgs &a, double dt, double *partials,
                         unsigned int *counter, double *maxdiv_out, int nblocks) {
     k_update_next<<<nblocks, 256, 0, s>>>(g, ax, ay, az, bc, flag, a, dt, partials, counter, maxdiv_out);
+    note_launches(1);
 }
 
 // ------------------------------------------------------------------------
@@ -377,6 +381,7 @@ void launch_fill_outer(cudaStream_t s, const Grid &g, const BCSet &bc, double *c
     k_fill_outer<<<grid_for(nx, 128), 128, 0, s>>>(g, bc, 0, u[0], u[1], u[2], p);
     k_fill_outer<<<grid_for(ny, 128), 128, 0, s>>>(g, bc, 1, u[0], u[1], u[2], p);
     k_fill_outer<<<grid_for(nz, 128), 128, 0, s>>>(g, bc, 2, u[0], u[1], u[2], p);
+    note_launches(3);
 }
 
 // ------------------------------------------------------------------------
@@ -400,6 +405,7 @@ k_interp_stag(const Grid g, const Axis ax, const Axis ay, const Axis az, const d
 void launch_interp_stag(cudaStream_t s, const Grid &g, const Axis &ax, const Axis &ay, const Axis &az,
                         const double *const u[3], double *const U[3]) {
     k_interp_stag<<<grid_for(g.ncell, 256), 256, 0, s>>>(g, ax, ay, az, u[0], u[1], u[2], U[0], U[1], U[2]);
+    note_launches(1);
 }
 
 // ------------------------------------------------------------------------
@@ -457,6 +463,7 @@ k_ghost_update(GhostArgs a, double *u0, double *u1, double *u2, double *p) {
 void launch_ghost_update(cudaStream_t s, const GhostArgs &a, double *const u[3], double *p) {
     if (a.nghost == 0) return;
     k_ghost_update<<<1, 1024, 0, s>>>(a, u[0], u[1], u[2], p);
+    note_launches(1);
 }
 
 // Interior solid cells -> NaN (the SOLID branch of update_ghost).
@@ -477,6 +484,7 @@ __global__ void k_solid_nan(const Grid g, const uint8_t *__restrict__ flag, doub
 void launch_solid_nan(cudaStream_t s, const Grid &g, const uint8_t *flag, double *const u[3], double *p) {
     const long long n = (long long)g.nx * g.ny * g.nz;
     k_solid_nan<<<grid_for(n, 256), 256, 0, s>>>(g, flag, u[0], u[1], u[2], p);
+    note_launches(1);
 }
 
 }  // namespace ibm

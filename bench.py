@@ -1,0 +1,324 @@
+#!/usr/bin/env python
+"""Benchmark of the immersed-boundary fractional step on GB300.
+
+Workload: flow past a sphere, 192x128x128 cells (3,145,728 interior cells),
+body-clustered grid on [-5,15]x[-5,5]^2, 20480-triangle icosphere r = 0.5,
+Re 300, dt 5e-3, uniform inflow, pressure outlet, free-slip sides; the
+pressure solve runs to max|div U^{n+1}| <= 1e-8 on fluid cells every step,
+momentum to the reference drivers' relative tolerance 1e-6.  Synthetic,
+seeded inputs (the reference has no public dataset).
+
+Metric: Mcell-steps/s = interior cells x steps / seconds.
+  value : device time (CUDA events on the solver's stream) of K steps with
+          the state resident in HBM (the step's working set, >1 GB, is far
+          larger than the 129 MB L2, so nothing is served from cache).
+  e2e   : the same K steps through the C ABI with HOST buffers: every step
+          uploads u1, u2, u3, p from pinned host memory
+          (IBMSolver_init_flow_array), runs IBMSolver_iterate(1) and reads
+          the four fields back (IBMSolver_get_field); host wall clock.
+Default run: N=1, K=10 timed steps after W=3 warm-up steps.
+
+--impl reference runs the CPU restatement of the reference time step
+(oracle/, OpenMP on every host core) on the same workload and metric.
+Under torchrun (N>1) every rank advances its own replica of the case (the
+single-case path does not shard); value is the total over ranks divided by
+the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+DIV_TOL = 1e-8
+MOM_TOL = 1e-6
+# Algorithmic bytes per padded cell of one pressure SpMV launch (FP64):
+# read x, write y, read the dot-product partner (r0 or s), read 1/coeffsum,
+# read the flag byte.
+SPMV_P_BYTES_PER_CELL = 8 + 8 + 8 + 8 + 1
+
+
+def _dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def _barrier_max(value, world):
+    """Barrier + max over ranks (gloo; the path has no data collective)."""
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    if not dist.is_initialized():
+        dist.init_process_group("gloo")
+    t = torch.tensor([value], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        if not dist.is_initialized():
+            dist.init_process_group("gloo")
+        dist.barrier()
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.QUERY, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in open(self.path):
+                t = [x.strip() for x in line.split(",")]
+                if len(t) >= 9:
+                    rows.append(t)
+        finally:
+            os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[q] for r in rows for q in range(4) if r[5 + q].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peak_gbs():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def traffic_per_launch(kernel):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary
+    (profiles/roofline_traffic.txt: '<kernel> <workload> <bytes>'), or None."""
+    path = os.path.join(ROOT, "profiles", "roofline_traffic.txt")
+    try:
+        for line in open(path):
+            t = line.split()
+            if len(t) >= 3 and not line.startswith("#") and t[0] == kernel:
+                return float(t[2])
+    except OSError:
+        pass
+    return None
+
+
+def oracle_case(case, lvset, threads, div_tol=DIV_TOL, tol=MOM_TOL):
+    c = {k: v for k, v in case.items() if k not in ("stl", "init", "name")}
+    c.update(lvset=lvset, threads=threads, div_tol=div_tol, tol=tol)
+    return c
+
+
+def cpu_level_set(case):
+    """Level set for the oracle when no GPU set-up is at hand: the CPU
+    oracle's own closest-point transform (reference algorithm)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+    c = {k: v for k, v in case.items() if k not in ("init", "name")}
+    c.update(threads=os.cpu_count() or 1)
+    return orc.Oracle(c).get("lvset")
+
+
+def run_cpu(case, lvset, steps, warmup, threads, sample_budget_s=None):
+    """Time the CPU oracle on the workload; returns (cells*steps/s, steps, secs)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+    wl = importlib.import_module("2020researchproject_gb300.workloads")
+    o = orc.Oracle(oracle_case(case, lvset, threads))
+    o.init(*wl.initial_state(case))
+    if warmup:
+        o.iterate(warmup)
+    ncell = (len(case["xf"]) - 1) * (len(case["yf"]) - 1) * (len(case["zf"]) - 1)
+    done, t0 = 0, time.perf_counter()
+    while done < steps:
+        o.iterate(1)
+        done += 1
+        if sample_budget_s is not None and time.perf_counter() - t0 > sample_budget_s:
+            break
+    secs = time.perf_counter() - t0
+    return ncell * done / secs / 1e6, done, secs, o.stats()
+
+
+def bench_reference(args):
+    world, rank, local = _dist()
+    if rank != 0:
+        return 0
+    wl = importlib.import_module("2020researchproject_gb300.workloads")
+    case = wl.sphere()
+    threads = os.cpu_count() or 1
+    lvset = cpu_level_set(case) if not args.lvset_from_gpu else None
+    if lvset is None:
+        ibm = importlib.import_module("2020researchproject_gb300")
+        lvset = wl.build_solver(ibm, case).get_field("lvset")
+    value, done, secs, st = run_cpu(case, lvset, args.steps, args.warmup, threads)
+    line = {
+        "metric": "Mcell-steps/s", "value": round(value, 4), "unit": "Mcell-steps/s", "impl": "reference",
+        "n_gpus": args.gpus, "steps": done, "warmup": args.warmup, "ms_per_step": round(secs / done * 1e3, 2),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": case["name"], "cells": 192 * 128 * 128, "triangles": 20480, "div_tol": DIV_TOL},
+        "cpu_baseline": {"value": round(value, 4), "unit": "Mcell-steps/s", "cores": threads, "kind": "port",
+                         "sample": f"{done} full fractional steps of the {case['name']} workload"},
+        "e2e": {"value": round(value, 4), "unit": "Mcell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "oracle_stats": st,
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def bench_gb300(args):
+    world, rank, local = _dist()
+    if world > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    ibm = importlib.import_module("2020researchproject_gb300")
+    wl = importlib.import_module("2020researchproject_gb300.workloads")
+    case = wl.sphere()
+    ncell = (len(case["xf"]) - 1) * (len(case["yf"]) - 1) * (len(case["zf"]) - 1)
+    t0 = time.perf_counter()
+    s = wl.build_solver(ibm, case, tol=MOM_TOL, div_tol=DIV_TOL)
+    setup_s = time.perf_counter() - t0
+    u0 = wl.initial_state(case)
+    s.init_flow_array(*u0)
+    s.iterate(args.warmup)
+
+    # --- device-timed region: K steps, state resident in HBM.
+    _barrier(world)
+    l0 = ibm.kernel_launches()
+    print(f"[bench] setup {setup_s:.2f} s; timed region starts after {l0} kernel launches", file=sys.stderr)
+    with ClockSampler(0 if world > 1 else int(os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0] or 0)) as clk:
+        ms = s.time_iterate(args.steps)
+    launches = ibm.kernel_launches() - l0
+    ms = _barrier_max(ms, world)
+    st = s.stats()
+    value = world * ncell * args.steps / (ms / 1e3) / 1e6
+
+    # --- stage profile (CUDA events per stage / per Krylov kernel).
+    s.set_profiling(True)
+    s.iterate(2)
+    prof = s.profile()
+    s.set_profiling(False)
+    peak, peak_src = measured_peak_gbs()
+    padded = (len(case["xf"]) + 3) * (len(case["yf"]) + 3) * (len(case["zf"]) + 3)
+    n_spmv, t_spmv = prof.get("spmv_p", (0, 0.0))
+    roof = None
+    if n_spmv:
+        bytes_per_launch = SPMV_P_BYTES_PER_CELL * padded
+        ach = bytes_per_launch / (t_spmv / n_spmv / 1e3) / 1e9
+        tr = traffic_per_launch("k_bicg_spmv_p")
+        roof = {"bound": "hbm", "kernel": "pressure SpMV (k_bicg_spmv_v/_t, OP_PRES)", "achieved": round(ach, 1),
+                "peak": peak, "unit": "GB/s", "frac": round(ach / peak, 4), "peak_source": peak_src,
+                "traffic": tr, "bytes_per_launch": bytes_per_launch,
+                "avg_launch_us": round(t_spmv / n_spmv * 1e3, 2)}
+
+    # --- end to end through the C ABI with pinned host buffers.
+    fields = ["u1", "u2", "u3", "p"]
+    host = [s.get_field(f) for f in fields]
+    outs = [np.empty_like(h) for h in host]
+    pinned = all(ibm.pin(a) for a in host + outs)
+    _barrier(world)
+    t1 = time.perf_counter()
+    for _ in range(args.steps):
+        s.init_flow_array(*host)
+        s.iterate(1)
+        for q, f in enumerate(fields):
+            s.get_field_into(f, outs[q])
+        host, outs = outs, host
+    e2e_s = _barrier_max(time.perf_counter() - t1, world)
+    e2e = world * ncell * args.steps / e2e_s / 1e6
+    bytes_io = 4 * host[0].nbytes
+
+    line = {
+        "metric": "Mcell-steps/s", "value": round(value, 3), "unit": "Mcell-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": case["name"], "cells": ncell, "triangles": 20480, "Re": case["re"],
+                   "dt": case["dt"], "div_tol": DIV_TOL, "momentum_tol": MOM_TOL, "parallelism": f"replicas{world}",
+                   "l2": "working set > L2 (no flush needed)", "setup_s": round(setup_s, 2),
+                   "device": s.device_name()},
+        "e2e": {"value": round(e2e, 3), "unit": "Mcell-steps/s", "h2d_bytes_per_step": bytes_io,
+                "d2h_bytes_per_step": bytes_io, "pinned": pinned},
+        "roofline": roof,
+        "gpu_launches": int(launches),
+        "launches_before_timed": int(l0),
+        "clocks": clk.summary(),
+        "solver": {"iters_p": st["iters_p"], "iters_u": st["iters_u"], "max_div": st["max_div"],
+                   "mg_levels": st["mg_levels"]},
+        "profile_ms": {k: [v[0], round(v[1], 3)] for k, v in sorted(prof.items())},
+    }
+    if rank == 0 and world == 1 and not args.no_cpu:
+        lv = s.get_field("lvset")
+        cv, done, secs, _ = run_cpu(case, lv, steps=2, warmup=0, threads=os.cpu_count() or 1, sample_budget_s=25)
+        line["cpu_baseline"] = {"value": round(cv, 4), "unit": "Mcell-steps/s", "cores": os.cpu_count() or 1,
+                                "kind": "port",
+                                "sample": f"{done} fractional steps of the same {case['name']} workload "
+                                          f"({secs:.1f} s), CPU restatement of the reference step"}
+    if rank == 0:
+        print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--lvset-from-gpu", action="store_true",
+                    help="reference arm: take the level set from the GPU set-up instead of the CPU transform")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        return bench_reference(args)
+    return bench_gb300(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

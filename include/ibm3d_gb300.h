@@ -9,6 +9,8 @@
 #ifndef IBM3D_GB300_H
 #define IBM3D_GB300_H
 
+#include <stddef.h>
+
 #include "ibm3d.h"
 
 #ifdef __cplusplus
@@ -96,6 +98,15 @@ double IBMSolver_time_iterate(IBMSolver *, int nsteps);
    individual Krylov kernels spmv_mom, spmv_p, mg_vcycle. */
 void IBMSolver_set_profiling(IBMSolver *, int on);
 int IBMSolver_get_profile(IBMSolver *, int max, char names[][32], int *launches, double *total_ms);
+
+/* Kernels this library has launched since load (all solvers). */
+long long IBMSolver_kernel_launches(void);
+
+/* Page-lock / release caller-owned host memory so that the field uploads
+   (IBMSolver_init_flow_array) and read-backs (IBMSolver_get_field) it is
+   used for run as direct DMA.  0 on success. */
+int IBMSolver_host_register(void *ptr, size_t bytes);
+int IBMSolver_host_unregister(void *ptr);
 
 /* Device name of the solver's GPU (for logs). */
 const char *IBMSolver_device_name(IBMSolver *);

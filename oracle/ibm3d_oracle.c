@@ -378,9 +378,11 @@ static void update_f(CptGrid *G, int i, int j, int k, double dist, int sgn) {
 }
 
 /* FaceExtrusion_cpt (src/geo3d.c:871-938). */
-static void face_cpt(CptGrid *G, const V3 p[6], int sgn) {
+static void face_cpt(CptGrid *G, const V3 p[6], int sgn, int ilo, int ihi) {
     int b[6];
     box_of(G, p, 6, b);
+    if (b[0] < ilo) b[0] = ilo;
+    if (b[1] > ihi) b[1] = ihi;
     Plane pl[5] = {plane3(p[0], p[2], p[1]), plane3(p[3], p[4], p[5]), plane3(p[0], p[1], p[4]),
                    plane3(p[1], p[2], p[5]), plane3(p[0], p[3], p[5])};
     double nn = vnorm((V3){pl[0].a, pl[0].b, pl[0].c});
@@ -396,9 +398,11 @@ static void face_cpt(CptGrid *G, const V3 p[6], int sgn) {
 }
 
 /* EdgeExtrusion_cpt (src/geo3d.c:811-869). */
-static void edge_cpt(CptGrid *G, const V3 p[6], int sgn) {
+static void edge_cpt(CptGrid *G, const V3 p[6], int sgn, int ilo, int ihi) {
     int b[6];
     box_of(G, p, 6, b);
+    if (b[0] < ilo) b[0] = ilo;
+    if (b[1] > ihi) b[1] = ihi;
     Plane pl[5] = {plane3(p[0], p[4], p[2]), plane3(p[1], p[3], p[5]), plane3(p[0], p[2], p[3]),
                    plane3(p[2], p[4], p[5]), plane3(p[0], p[1], p[5])};
     V3 ab = vsub(p[1], p[0]);
@@ -417,11 +421,29 @@ static void edge_cpt(CptGrid *G, const V3 p[6], int sgn) {
             }
 }
 
-/* VertexExtrusion_cpt (src/geo3d.c:784-809). */
-static void vertex_cpt(CptGrid *G, V3 v, V3 axis, double ang, double rad, int sgn) {
+/* VertexExtrusion_cpt (src/geo3d.c:784-809).  The reference scans the box
+   vertex +- radius; points outside the cone's own bounding box (widened by
+   a margin far above rounding) fail its angle test, so the scan is limited
+   to that box without changing any result.  i is restricted to [ilo, ihi). */
+static void vertex_cpt(CptGrid *G, V3 v, V3 axis, double ang, double rad, int sgn, int ilo, int ihi) {
     int b[6] = {lower_bound_(G->nx, G->x, v.x - rad), upper_bound_(G->nx, G->x, v.x + rad),
                 lower_bound_(G->ny, G->y, v.y - rad), upper_bound_(G->ny, G->y, v.y + rad),
                 lower_bound_(G->nz, G->z, v.z - rad), upper_bound_(G->nz, G->z, v.z + rad)};
+    const double la = vnorm(axis), comp[3] = {axis.x / la, axis.y / la, axis.z / la}, vc[3] = {v.x, v.y, v.z};
+    const double *ga[3] = {G->x, G->y, G->z};
+    const int gn[3] = {G->nx, G->ny, G->nz};
+    for (int d = 0; d < 3; d++) {
+        double c = comp[d] < -1 ? -1 : comp[d] > 1 ? 1 : comp[d];
+        double al = acos(c), th = ang + 1e-6;
+        double hi = al - th <= 0 ? 1.0 : cos(al - th), lo = al + th >= 3.141592653589793 ? -1.0 : cos(al + th);
+        double m = 1e-6 * (1 + rad);
+        double bl = vc[d] + rad * (lo < 0 ? lo : 0) - m, bh = vc[d] + rad * (hi > 0 ? hi : 0) + m;
+        int tl = lower_bound_(gn[d], ga[d], bl), th2 = upper_bound_(gn[d], ga[d], bh);
+        if (tl > b[2 * d]) b[2 * d] = tl;
+        if (th2 < b[2 * d + 1]) b[2 * d + 1] = th2;
+    }
+    if (b[0] < ilo) b[0] = ilo;
+    if (b[1] > ihi) b[1] = ihi;
     for (int i = b[0]; i < b[1]; i++)
         for (int j = b[2]; j < b[3]; j++)
             for (int k = b[4]; k < b[5]; k++) {
@@ -436,18 +458,24 @@ static void cpt(const Poly *P, CptGrid *G, double maxd) {
     const double PI = 3.141592653589793;
     long n = (long)G->nx * G->ny * G->nz;
     for (long q = 0; q < n; q++) G->f[q] = NAN;
+    /* Every thread replays the whole extrusion sequence on its own slab of
+       i, so each grid point sees the reference's update order. */
+#pragma omp parallel
+    {
+    const int T = omp_get_num_threads(), tid = omp_get_thread_num();
+    const int ilo = (int)((long)G->nx * tid / T), ihi = (int)((long)G->nx * (tid + 1) / T);
     for (int i = 0; i < P->nf; i++) {
         V3 p[6];
         for (int j = 0; j < 3; j++) {
             p[j] = P->vc[P->fv[i][j]];
             p[j + 3] = vlin(1, p[j], maxd, P->fn[i]);
         }
-        face_cpt(G, p, 1);
+        face_cpt(G, p, 1, ilo, ihi);
         for (int j = 0; j < 3; j++) {
             p[j] = P->vc[P->fv[i][(3 - j) % 3]];
             p[j + 3] = vlin(1, p[j], -maxd, P->fn[i]);
         }
-        face_cpt(G, p, -1);
+        face_cpt(G, p, -1, ilo, ihi);
     }
     for (int i = 0; i < P->ne; i++) {
         V3 p[6];
@@ -482,7 +510,7 @@ static void cpt(const Poly *P, CptGrid *G, double maxd) {
             p[3] = vlin(1, p[1], s, wl[w]);
             p[4] = vlin(1, p[0], s, wr[w]);
             p[5] = vlin(1, p[1], s, wr[w]);
-            edge_cpt(G, p, sgn);
+            edge_cpt(G, p, sgn, ilo, ihi);
         }
     }
     for (int i = 0; i < P->nv; i++) {
@@ -515,8 +543,9 @@ static void cpt(const Poly *P, CptGrid *G, double maxd) {
             if (d < 0) concave = 0;
         }
         free(adj);
-        if (!concave) vertex_cpt(G, vx, axis, cone, maxd, 1);
-        if (!convex) vertex_cpt(G, vx, (V3){-axis.x, -axis.y, -axis.z}, cone, maxd, -1);
+        if (!concave) vertex_cpt(G, vx, axis, cone, maxd, 1, ilo, ihi);
+        if (!convex) vertex_cpt(G, vx, (V3){-axis.x, -axis.y, -axis.z}, cone, maxd, -1, ilo, ihi);
+    }
     }
     /* Fill (src/geo3d.c:643-703). */
     for (int i = 0; i < G->nx; i++)
