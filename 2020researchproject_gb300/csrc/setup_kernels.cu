@@ -448,3 +448,117 @@ int gpu_ghost_stencils(cudaStream_t s, const Grid &g, const double *xc, const do
 }
 
 }  // namespace ibm
+
+// ---------------------------------------------------------------------------
+// Allocation-free closest-point transform.
+//
+// Some callers cannot call cudaMalloc at the moment they need a level set:
+// hosts whose framework allocator (PyTorch's caching allocator, a serving
+// process with a fixed per-job budget) already owns the device memory so a
+// raw cudaMalloc can fail or fragment it, and latency-bound loops that must
+// not pay for an allocation.  Polyhedron_cpt_noalloc serves them: it runs the same kernels
+// as Polyhedron_cpt, but every device buffer - the grid coordinates, the
+// output, the extrusion list, the BVH and the fallback list - is carved out
+// of one file-scope device array of CPT_NOALLOC_BYTES (32 MiB), which every
+// GPU that loads this library holds until the process exits.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+namespace ibm {
+constexpr size_t CPT_NOALLOC_BYTES = 32u << 20;
+static __device__ __align__(256) unsigned char g_cpt_noalloc_scratch[CPT_NOALLOC_BYTES];
+}  // namespace ibm
+
+namespace {
+// Device address of the scratch array, looked up once per device.
+constexpr int kMaxDevices = 64;
+unsigned char *g_noalloc_ptr[kMaxDevices] = {nullptr};
+std::mutex g_noalloc_mutex;
+
+unsigned char *noalloc_scratch(int dev) {
+    if (dev < 0 || dev >= kMaxDevices) return nullptr;
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, ibm::g_cpt_noalloc_scratch);
+        if (e != cudaSuccess) {
+            fprintf(stderr, "error: Polyhedron_cpt_noalloc: cudaGetSymbolAddress failed: %s\n", cudaGetErrorString(e));
+            return nullptr;
+        }
+        g_noalloc_ptr[dev] = (unsigned char *)p;
+    }
+    return g_noalloc_ptr[dev];
+}
+}  // namespace
+
+extern "C" int Polyhedron_cpt_noalloc(const Polyhedron *const poly, const int nx, const int ny, const int nz,
+                                      const double *x, const double *y, const double *z, double *f,
+                                      const double maxd) {
+    using namespace ibm;
+    CptModel m;
+    build_cpt_model(poly, maxd, m);
+    const long long n = (long long)nx * ny * nz;
+    // Layout of the scratch array, each piece 256-byte aligned.
+    size_t off = 0;
+    auto place = [&](size_t bytes) {
+        const size_t at = off;
+        off += (bytes + 255) & ~(size_t)255;
+        return at;
+    };
+    const size_t o_x = place(sizeof(double) * nx), o_y = place(sizeof(double) * ny), o_z = place(sizeof(double) * nz);
+    const size_t o_f = place(sizeof(double) * n);
+    const size_t o_feat = place(sizeof(CptFeature) * m.features.size());
+    const size_t o_tfs = place(sizeof(int) * m.tri_feat_start.size());
+    const size_t o_tf = place(sizeof(int) * m.tri_feats.size());
+    const size_t o_txyz = place(sizeof(float) * m.tri_xyz.size());
+    const size_t o_node = place(sizeof(BVHNode) * m.nodes.size());
+    const size_t o_fb = place(sizeof(int) * n);
+    const size_t o_cnt = place(sizeof(int));
+    if (off > CPT_NOALLOC_BYTES) {
+        fprintf(stderr,
+                "error: Polyhedron_cpt_noalloc: a %d x %d x %d grid with %zu extrusions needs %zu bytes of "
+                "scratch, more than the %zu-byte static buffer; use Polyhedron_cpt\n",
+                nx, ny, nz, m.features.size(), off, CPT_NOALLOC_BYTES);
+        return -1;
+    }
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return -1;
+    unsigned char *base = noalloc_scratch(dev);
+    if (!base) return -1;
+    const cudaStream_t s = 0;
+    auto up = [&](size_t o, const void *src, size_t bytes) {
+        if (bytes) cudaMemcpyAsync(base + o, src, bytes, cudaMemcpyHostToDevice, s);
+    };
+    up(o_x, x, sizeof(double) * nx);
+    up(o_y, y, sizeof(double) * ny);
+    up(o_z, z, sizeof(double) * nz);
+    up(o_feat, m.features.data(), sizeof(CptFeature) * m.features.size());
+    up(o_tfs, m.tri_feat_start.data(), sizeof(int) * m.tri_feat_start.size());
+    up(o_tf, m.tri_feats.data(), sizeof(int) * m.tri_feats.size());
+    up(o_txyz, m.tri_xyz.data(), sizeof(float) * m.tri_xyz.size());
+    up(o_node, m.nodes.data(), sizeof(BVHNode) * m.nodes.size());
+    // The array keeps the previous call's contents: the fallback counter
+    // must start at zero every call.
+    cudaMemsetAsync(base + o_cnt, 0, sizeof(int), s);
+    CptDev d{};
+    d.feat = (const CptFeature *)(base + o_feat);
+    d.nfeat = (int)m.features.size();
+    d.tfs = (const int *)(base + o_tfs);
+    d.tf = (const int *)(base + o_tf);
+    d.txyz = (const float *)(base + o_txyz);
+    d.node = (const BVHNode *)(base + o_node);
+    d.nnode = (int)m.nodes.size();
+    const double *dx = (const double *)(base + o_x), *dy = (const double *)(base + o_y), *dz = (const double *)(base + o_z);
+    double *df = (double *)(base + o_f);
+    int *fb_list = (int *)(base + o_fb), *fb_count = (int *)(base + o_cnt);
+    k_cpt<<<nblk(n, 128), 128, 0, s>>>(d, nx, ny, nz, dx, dy, dz, df, maxd, fb_list, fb_count);
+    int nfb = 0;
+    cudaMemcpyAsync(&nfb, fb_count, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return -1;
+    if (nfb > 0) k_cpt_fallback<<<nfb < 4096 ? nfb : 4096, 256, 0, s>>>(d, nx, ny, nz, dx, dy, dz, df, fb_list, nfb);
+    k_cpt_fill<<<nblk((long long)nx * ny, 128), 128, 0, s>>>(df, nx, ny, nz, 2, maxd);
+    k_cpt_fill<<<nblk((long long)nx * nz, 128), 128, 0, s>>>(df, nx, ny, nz, 1, maxd);
+    k_cpt_fill<<<nblk((long long)ny * nz, 128), 128, 0, s>>>(df, nx, ny, nz, 0, maxd);
+    cudaMemcpyAsync(f, df, sizeof(double) * n, cudaMemcpyDeviceToHost, s);
+    return cudaStreamSynchronize(s) == cudaSuccess ? 0 : -1;
+}

@@ -55,6 +55,27 @@ void Polyhedron_cpt(
     const double maxd
 );
 
+/* No counterpart in the reference.  Same contract as Polyhedron_cpt (host
+   arrays in and out) for callers that must not allocate device memory at
+   this point - hosts whose framework allocator already owns the GPU memory,
+   loops that cannot pay for an allocation.  It calls no cudaMalloc/cudaFree:
+   all device buffers come from one static 32 MiB device array that every
+   GPU loading the library holds until exit.  Returns 0, or -1 (with a
+   message) when the grid, output and extrusion list need more than 32 MiB
+   or on a CUDA error.  The array keeps the previous call's contents; the
+   one value that must start at zero, the count of points left to the
+   fallback scan, is cleared by every call.  The first call on a device
+   looks up the array's address (setup), so make that first call before any
+   stream capture.  Calls share the array: calls that overlap on the GPU
+   (other threads, other streams) race. */
+int Polyhedron_cpt_noalloc(
+    const Polyhedron *const poly,
+    const int nx, const int ny, const int nz,
+    const double *x, const double *y, const double *z,
+    double *f,
+    const double maxd
+);
+
 #ifdef __cplusplus
 }
 #endif
