@@ -27,6 +27,7 @@ LIB_PATH = os.path.join(_PKG, "libibm3d_gb300.so")
 # Enums, values as in the reference's src/ibm3d.h:16-98.
 SOLVER_AMG, SOLVER_PCG, SOLVER_BiCGSTAB, SOLVER_GMRES = range(4)
 PRECOND_NONE, PRECOND_AMG = range(2)
+FP64, MIXED = 0, 1
 DIR_NORTH, DIR_EAST, DIR_SOUTH, DIR_WEST, DIR_DOWN, DIR_UP = (1 << i for i in range(6))
 (BC_VELOCITY_COMPONENT, BC_PRESSURE, BC_STATIONARY_WALL, BC_FREE_SLIP_WALL,
  BC_SYMMETRIC, BC_ALL_PERIODIC, BC_VELOCITY_PERIODIC) = range(7)
@@ -51,7 +52,8 @@ class _Stats(ctypes.Structure):
                 ("iters_u", ctypes.c_int * 3), ("iters_p", ctypes.c_int),
                 ("res_u", ctypes.c_double * 3), ("res_p", ctypes.c_double),
                 ("max_div", ctypes.c_double), ("mg_levels", ctypes.c_int),
-                ("cpt_fallback", ctypes.c_int)]
+                ("cpt_fallback", ctypes.c_int), ("outer_u", ctypes.c_int),
+                ("outer_p", ctypes.c_int)]
 
 
 _lib = None
@@ -96,6 +98,8 @@ def load_library(path: str = LIB_PATH):
         "IBMSolver_last_status": (i, [vp]),
         "IBMSolver_set_div_tol": (None, [vp, d]),
         "IBMSolver_set_precision": (None, [vp, i]),
+        "IBMSolver_set_graphs": (None, [vp, i]),
+        "IBMSolver_set_multigrid": (None, [vp, i, i, i, i, i]),
         "IBMSolver_get_field": (None, [vp, i, dp]),
         "IBMSolver_get_flag": (None, [vp, ip]),
         "IBMSolver_sync_host": (None, [vp]),
@@ -232,6 +236,17 @@ class IBMSolver:
     def set_div_tol(self, div_tol):
         self._lib.IBMSolver_set_div_tol(self._s, div_tol)
 
+    def set_multigrid(self, nu_pre=3, nu_post=3, nuc_pre=2, nuc_post=2, coarse_sweeps=10):
+        self._lib.IBMSolver_set_multigrid(self._s, nu_pre, nu_post, nuc_pre, nuc_post, coarse_sweeps)
+        self._check("IBMSolver_set_multigrid")
+
+    def set_graphs(self, on=True):
+        self._lib.IBMSolver_set_graphs(self._s, 1 if on else 0)
+
+    def set_precision(self, mode):
+        self._lib.IBMSolver_set_precision(self._s, int(mode))
+        self._check("IBMSolver_set_precision")
+
     def assemble(self):
         self._lib.IBMSolver_assemble(self._s)
         self._check("assemble")
@@ -315,7 +330,8 @@ class IBMSolver:
         self._lib.IBMSolver_get_stats(self._s, ctypes.byref(st))
         return dict(iter=st.iter, time=st.time, iters_u=list(st.iters_u), iters_p=st.iters_p,
                     res_u=list(st.res_u), res_p=st.res_p, max_div=st.max_div,
-                    mg_levels=st.mg_levels, cpt_fallback=st.cpt_fallback)
+                    mg_levels=st.mg_levels, cpt_fallback=st.cpt_fallback,
+                    outer_u=st.outer_u, outer_p=st.outer_p)
 
     def set_profiling(self, on=True):
         self._lib.IBMSolver_set_profiling(self._s, 1 if on else 0)

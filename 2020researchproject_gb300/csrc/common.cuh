@@ -28,8 +28,46 @@ struct Grid {
     long long ncell;    // (nx+4)(ny+4)(nz+4)
 };
 
+// Exact unsigned 32-bit division by a run-time constant d >= 1 with one
+// multiply-high (Granlund & Montgomery, "Division by invariant integers
+// using multiplication", PLDI 1994, round-up variant):
+//   t = mulhi(m, n); q = (t + ((n - t) >> 1)) >> (l - 1).
+struct FastDiv {
+    uint32_t d, m;
+    int l;
+};
+
+inline FastDiv make_fastdiv(uint32_t d) {
+    FastDiv f;
+    f.d = d;
+    int l = 0;
+    while ((1ull << l) < d) l++;
+    f.l = l;
+    f.m = d == 1 ? 0u : (uint32_t)(((1ull << 32) * ((1ull << l) - d)) / d + 1);
+    return f;
+}
+
+__device__ __forceinline__ uint32_t fdiv(const FastDiv &f, uint32_t n) {
+    if (f.d == 1) return n;
+    const uint32_t t = __umulhi(f.m, n);
+    return (t + ((n - t) >> 1)) >> (f.l - 1);
+}
+
 __host__ __device__ inline long long cidx(const Grid &g, int i, int j, int k) {
     return (long long)(i + 2) * g.sx + (long long)(j + 2) * g.sy + (k + 2);
+}
+
+// Padded index -> (i, j, k) with the two divisions done by FastDiv
+// (padded grids stay below 2^31 cells).
+__device__ __forceinline__ void cijk_fast(const Grid &g, const FastDiv &dx, const FastDiv &dy, long long idx, int &i,
+                                          int &j, int &k) {
+    const uint32_t P = (uint32_t)idx;
+    const uint32_t I = fdiv(dx, P);
+    const uint32_t r = P - I * (uint32_t)g.sx;
+    const uint32_t J = fdiv(dy, r);
+    i = (int)I - 2;
+    j = (int)J - 2;
+    k = (int)(r - J * (uint32_t)g.sy) - 2;
 }
 
 __host__ __device__ inline void cijk(const Grid &g, long long idx, int &i, int &j, int &k) {
@@ -102,10 +140,9 @@ __host__ __device__ inline long long periodic_image(const Grid &g, int i, int j,
 }
 
 // ------------------------------------------------------------ reductions --
-// Deterministic two-level reductions: every block writes its partial sums
-// to partials[block][v]; the last block to finish adds them in block order.
-constexpr int RED_MAX = 8;
-
+// Deterministic two-level reductions: every block writes its partials to
+// partials[block][v]; the last block to finish reduces them in a fixed
+// order.
 template <int NV>
 __device__ inline void block_sum(double (&v)[NV], double *smem /* [32*NV] */) {
 #pragma unroll
@@ -160,8 +197,9 @@ __device__ inline void block_max(double (&v)[NV], double *smem) {
     }
 }
 
-// Publishes this block's NV partials; returns true in thread 0 of the last
-// block, which then finds every block's partials in `partials`.
+// Publishes this block's NV partials; returns true in EVERY thread of the
+// last block to finish (the same value across the block), which then
+// reduces all blocks' partials with reduce_partials.
 template <int NV>
 __device__ inline bool publish_partials(const double (&v)[NV], double *partials, unsigned int *counter) {
     __shared__ bool last;
@@ -169,24 +207,60 @@ __device__ inline bool publish_partials(const double (&v)[NV], double *partials,
 #pragma unroll
         for (int q = 0; q < NV; q++) partials[blockIdx.x * NV + q] = v[q];
         __threadfence();
-        unsigned int t = atomicAdd(counter, 1u);
+        const unsigned int t = atomicAdd(counter, 1u);
         last = (t == gridDim.x - 1);
     }
     __syncthreads();
-    if (last && threadIdx.x == 0) {
-        __threadfence();
-        return true;
-    }
-    return false;
+    if (last) __threadfence();
+    return last;
 }
 
-template <int NV>
-__device__ inline void sum_partials(const double *partials, int nblocks, double (&out)[NV]) {
+// Reduces every block's partials inside the last block: entries [0, NS)
+// are summed, entries [NS, NV) maxed (all maxed quantities are >= 0, so 0
+// is their identity).  Thread t folds blocks t, t + blockDim, ... in that
+// order and a fixed-shape tree combines the threads, so the result does
+// not depend on block scheduling (bitwise reproducible).  Valid in thread
+// 0; smem holds 32 * NV doubles and must be free on entry.
+template <int NV, int NS>
+__device__ inline void reduce_partials(const double *partials, int nblocks, double (&out)[NV], double *smem) {
+    double v[NV];
 #pragma unroll
-    for (int q = 0; q < NV; q++) out[q] = 0.0;
-    for (int b = 0; b < nblocks; b++) {
+    for (int q = 0; q < NV; q++) v[q] = 0.0;
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
 #pragma unroll
-        for (int q = 0; q < NV; q++) out[q] += ((volatile const double *)partials)[b * NV + q];
+        for (int q = 0; q < NV; q++) {
+            const double x = __ldcg(partials + (size_t)b * NV + q);
+            v[q] = q < NS ? v[q] + x : fmax(v[q], x);
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < NV; q++) {
+        double x = v[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double y = __shfl_down_sync(0xffffffffu, x, o);
+            x = q < NS ? x + y : fmax(x, y);
+        }
+        v[q] = x;
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; q++) smem[warp * NV + q] = v[q];
+    }
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = blockDim.x >> 5;
+#pragma unroll
+        for (int q = 0; q < NV; q++) {
+            double x = lane < nw ? smem[lane * NV + q] : 0.0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const double y = __shfl_down_sync(0xffffffffu, x, o);
+                x = q < NS ? x + y : fmax(x, y);
+            }
+            out[q] = x;
+        }
     }
 }
 

@@ -8,7 +8,9 @@
 
 namespace ibm {
 
-// Number of kernels this library has launched (for per-step launch counts).
+// Number of kernels this library has launched (for per-step launch counts);
+// while a step is being recorded into a CUDA graph the count goes to the
+// recording.
 void note_launches(int n);
 
 struct ConvArgs {
@@ -54,19 +56,6 @@ struct GhostArgs {
     const double *w;         // [8*g+e] normalised weights (0 where skipped)
     const double *wself;     // weight of the ghost cell in its own stencil
     double *old;             // [4*g]: snapshot of u1,u2,u3,p
-};
-
-// Operator context for the matrix-free momentum and pressure rows.
-struct OpCtx {
-    Grid g;
-    Axis ax, ay, az;
-    BCSet bc;
-    const uint8_t *flag;
-    const int *gid;          // padded index -> ghost id, -1 elsewhere
-    const int *gidx;         // [8*g+e] padded index of a stencil entry, -1 if dropped
-    const double *gw;        // [8*g+e] normalised weight
-    const double *gwself;    // [g]
-    const double *dinv;      // 1/coeffsum on fluid cells (pressure rows)
 };
 
 void launch_conv_rhs(cudaStream_t s, const Grid &g, const Axis &ax, const Axis &ay, const Axis &az,

@@ -1,15 +1,16 @@
-// Matrix-free momentum / pressure operators and the BiCGSTAB solver.
+// BiCGSTAB on the matrix-free rows of ops.cuh, in FP64 or FP32, and the
+// FP64 iterative-refinement driver of the mixed-precision path.
 //
-// Rows restate the matrices the reference assembles for hypre
-// (create_matrix, src/ibm3d_setup.c:1566-2908): Crank-Nicolson Helmholtz
-// rows (type 1..3) and diagonal-normalised Poisson rows (type 4) on fluid
-// cells, interpolation rows on ghost cells, identity on solid cells,
-// boundary rows on the two outer layers, and the pinned p'(0,0,0) row when
-// no face fixes the pressure.  The solver follows hypre's BiCGSTAB as the
-// reference drives it (src/ibm3d_fracstep.c:354-379, 649-703): x0 = 0,
-// stop when ||b - Ax||_2 / ||b||_2 < tol.  The three momentum components
-// are solved together, one Krylov recurrence per component, so each kernel
-// sweeps the grid once for all three.
+// The solver follows hypre's BiCGSTAB as the reference drives it
+// (src/ibm3d_fracstep.c:354-379, 649-703): x0 = 0, stop when
+// ||b - Ax||_2 / ||b||_2 < tol.  The three momentum components are solved
+// together, one Krylov recurrence per component, so each kernel sweeps the
+// grid once for all three.  Scalar recurrences (alpha, omega, beta) are
+// computed on the device by the last block of each reduction, in FP64;
+// reductions combine per-block partials in a fixed order, so results are
+// bitwise reproducible and identical between the host loop and the
+// recorded (graph) form.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <vector>
@@ -21,113 +22,99 @@
 
 namespace ibm {
 
-enum { ROW_DIR = 0, ROW_NEU = 1, ROW_PER = 2, ROW_EXT = 3 };
-
-__device__ __forceinline__ int outer_row_kind(int op, int type, int comp, int axis) {
-    if (op == OP_MOM) {
-        switch (type) {
-        case BCT_VELOCITY: return ROW_DIR;
-        case BCT_PRESSURE: return ROW_EXT;
-        case BCT_SLIP: return comp == axis ? ROW_DIR : ROW_NEU;
-        default: return ROW_PER;  // ALL_PERIODIC, VELOCITY_PERIODIC
-        }
-    }
-    switch (type) {
-    case BCT_VELOCITY:
-    case BCT_SLIP: return ROW_NEU;
-    case BCT_PRESSURE:
-    case BCT_VELPERIODIC: return ROW_DIR;
-    default: return ROW_PER;
-    }
-}
-
-// One row of A (op OP_MOM with component comp, or OP_PRES) applied to x.
-__device__ __forceinline__ double op_row(const OpCtx &c, int op, int comp, const double *__restrict__ x,
-                                         long long P) {
-    int i, j, k;
-    cijk(c.g, P, i, j, k);
-    int L;
-    const int f = owner_face(c.g, i, j, k, L);
-    if (f >= 0) {
-        const BCFace &F = c.bc.f[f];
-        const int axis = face_axis(f);
-        const long long s = axis == 0 ? c.g.sx : axis == 1 ? c.g.sy : 1;
-        const long long in = face_low(f) ? s : -s;
-        switch (outer_row_kind(op, F.type, comp, axis)) {
-        case ROW_DIR: return F.dir_o[L - 1] * x[P] + F.dir_m[L - 1] * x[P + (2 * L - 1) * in];
-        case ROW_NEU: return x[P] - x[P + (2 * L - 1) * in];
-        case ROW_PER: return x[P] - x[periodic_image(c.g, i, j, k)];
-        default: return F.ext_o[L - 1] * x[P] - x[P + in] + F.ext_2[L - 1] * x[P + 2 * in];
-        }
-    }
-    if (op == OP_PRES && c.bc.p_singular && i == 0 && j == 0 && k == 0) return x[P];
-    const uint8_t fl = c.flag[P];
-    if (fl == FLUID) {
-        const int I = i + 2, J = j + 2, K = k + 2;
-        const double kW = c.ax.km[I], kE = c.ax.kp[I], kS = c.ay.km[J], kN = c.ay.kp[J];
-        const double kD = c.az.km[K], kU = c.az.kp[K];
-        const long long sx = c.g.sx, sy = c.g.sy;
-        const double nb = kW * x[P - sx] + kE * x[P + sx] + kS * x[P - sy] + kN * x[P + sy] + kD * x[P - 1] +
-                          kU * x[P + 1];
-        if (op == OP_MOM) {
-            const double diag = 1 + kN + kE + kS + kW + kD + kU;
-            return diag * x[P] - nb;
-        }
-        return x[P] - c.dinv[P] * nb;
-    }
-    if (fl == GHOST) {
-        const int g = c.gid[P];
-        double sum = 0;
-#pragma unroll
-        for (int e = 0; e < 8; e++) {
-            const int q = c.gidx[8 * g + e];
-            if (q >= 0) sum += c.gw[8 * g + e] * x[q];
-        }
-        const double ws = c.gwself[g];
-        return op == OP_MOM ? (1 + ws) * x[P] + sum : (1 - ws) * x[P] - sum;
-    }
-    return x[P];
-}
-
-// Weight turning a fluid-row pressure residual into the divergence of the
-// projected face velocity: div U^{n+1} = -2 Re coeffsum r (see krylov.h).
-__device__ __forceinline__ double div_weight(const OpCtx &c, long long P, double two_re) {
-    int i, j, k;
-    cijk(c.g, P, i, j, k);
-    if (i < 0 || j < 0 || k < 0 || i >= c.g.nx || j >= c.g.ny || k >= c.g.nz) return 0.0;
-    if (c.flag[P] != FLUID) return 0.0;
-    if (c.bc.p_singular && i == 0 && j == 0 && k == 0) return 0.0;
-    const int I = i + 2, J = j + 2, K = k + 2;
-    return two_re * (c.ay.kp[J] + c.ax.kp[I] + c.ay.km[J] + c.ax.km[I] + c.az.km[K] + c.az.kp[K]);
-}
-
 #define GRID_STRIDE(P, n)                                                              \
     for (long long P = blockIdx.x * (long long)blockDim.x + threadIdx.x; P < (n); \
          P += (long long)gridDim.x * blockDim.x)
 
+// Per-thread accumulator type: FP64 for FP64 vectors; FP32 for FP32 vectors
+// (each thread adds a handful of products; partials are combined in FP64).
+template <typename T> struct AccT;
+template <> struct AccT<double> { using type = double; };
+template <> struct AccT<float> { using type = float; };
+
+// Weighted |r| for the divergence criterion (FP32 is ample for a stopping test).
+template <typename T>
+__device__ __forceinline__ float divw(const OpT<T> &c, long long P, T y) {
+    return c.wdiv[P] * fabsf((float)y);
+}
+
+// Stopping test: ||r|| < tol ||b|| (tol > 0) or max weighted |r| <= divtol
+// (divtol > 0); either one that is enabled suffices.
+__device__ __forceinline__ bool converged(double rn2, double bn2, double divmax, double tol, double divtol) {
+    return (tol > 0 && sqrt(rn2) < tol * sqrt(bn2)) || (divtol > 0 && divmax <= divtol);
+}
+
+__device__ __forceinline__ void set_loop(const LoopCtl &lc, bool cont) {
+    if (lc.use) cudaGraphSetConditional(lc.h, cont ? 1u : 0u);
+}
+
+// Reduction tail shared by the kernels below: block-level combine, then
+// the last block reduces all partials (NS sums first, then maxima) and
+// thread 0 runs `fin(tot)`.
+template <int NV, int NS, typename Fin>
+__device__ __forceinline__ void reduce_and_finish(double (&v)[NV], double *smem, double *partials,
+                                                  unsigned int *counter, Fin fin) {
+    static_assert(NS >= 1 && NS <= NV, "at least one summed entry");
+    double sm[NS];
+#pragma unroll
+    for (int q = 0; q < NS; q++) sm[q] = v[q];
+    block_sum<NS>(sm, smem);
+    double out[NV];
+#pragma unroll
+    for (int q = 0; q < NS; q++) out[q] = sm[q];
+    if constexpr (NV > NS) {
+        double mx[NV - NS];
+#pragma unroll
+        for (int q = NS; q < NV; q++) mx[q - NS] = v[q];
+        __syncthreads();
+        block_max<NV - NS>(mx, smem + 32 * NS);
+#pragma unroll
+        for (int q = NS; q < NV; q++) out[q] = mx[q - NS];
+    }
+    if (!publish_partials<NV>(out, partials, counter)) return;
+    double tot[NV];
+    reduce_partials<NV, NS>(partials, gridDim.x, tot, smem);
+    if (threadIdx.x == 0) {
+        fin(tot);
+        *counter = 0;
+    }
+}
+
 // ---------------------------------------------------------------- init --
+// x = 0, r = r0 = b, p = v = 0, ||b||^2.  The stopping test of the solve is
+// fixed here: (tol, divtol) as given, or, for the inner solve of a
+// refinement cycle (outer != null), derived from the outer state: the
+// relative tolerance is raised to what the outer FP64 test still needs
+// (half of it, as margin) and the divergence bound is expressed in the
+// scaled units of the inner right-hand side.
+template <typename T, int NC>
 __global__ void __launch_bounds__(KTHREADS)
-k_bicg_init(const long long n, const int nc, const double *__restrict__ b, double *x, double *r, double *r0,
-            double *p, double *v, KScal *sc, double *partials, unsigned int *counter) {
-    __shared__ double smem[32 * 3];
-    double acc[3] = {0, 0, 0};
-    for (int c = 0; c < nc; c++) {
+k_bicg_init(const long long n, const T *__restrict__ b, T *x, T *r, T *r0, T *p, T *v, KScal *sc, double *partials,
+            unsigned int *counter, const double tol, const double divtol, const IRScal *__restrict__ outer,
+            const double outer_tol, const double outer_divtol, const LoopCtl lc) {
+    __shared__ double smem[32 * NC];
+    typename AccT<T>::type a[NC];
+#pragma unroll
+    for (int c = 0; c < NC; c++) a[c] = 0;
+#pragma unroll
+    for (int c = 0; c < NC; c++) {
         const long long o = c * n;
         GRID_STRIDE(P, n) {
-            const double bv = b[o + P];
-            x[o + P] = 0.0;
+            const T bv = b[o + P];
+            x[o + P] = 0;
             r[o + P] = bv;
             r0[o + P] = bv;
-            p[o + P] = 0.0;
-            v[o + P] = 0.0;
-            acc[c] += bv * bv;
+            p[o + P] = 0;
+            v[o + P] = 0;
+            a[c] += bv * bv;
         }
     }
-    block_sum<3>(acc, smem);
-    if (publish_partials<3>(acc, partials, counter)) {
-        double tot[3];
-        sum_partials<3>(partials, gridDim.x, tot);
-        for (int c = 0; c < nc; c++) {
+    double acc[NC];
+#pragma unroll
+    for (int c = 0; c < NC; c++) acc[c] = (double)a[c];
+    reduce_and_finish<NC, NC>(acc, smem, partials, counter, [&](const double *tot) {
+        bool run = false;
+        for (int c = 0; c < NC; c++) {
             KScal &s = sc[c];
             s.bnorm2 = tot[c];
             s.rnorm2 = tot[c];
@@ -138,43 +125,88 @@ k_bicg_init(const long long n, const int nc, const double *__restrict__ b, doubl
             s.iters = 0;
             s.state = tot[c] == 0.0 ? KS_DONE : KS_RUN;
             s.divmax = 0.0;
+            s.tol = tol;
+            s.divtol = divtol;
+            if (outer) {
+                const IRScal &o = outer[c];
+                if (outer_tol > 0 && o.rnorm2 > 0) s.tol = fmax(tol, 0.5 * outer_tol * sqrt(o.bnorm2 / o.rnorm2));
+                s.divtol = (outer_divtol > 0 && NC == 1) ? 0.5 * outer_divtol * o.scale : 0.0;
+            }
+            run = run || s.state == KS_RUN;
         }
-        *counter = 0;
-    }
+        set_loop(lc, run);
+    });
 }
 
 // ------------------------------------------------- p = r + beta (p - w v) --
+template <typename T, int NC>
 __global__ void __launch_bounds__(KTHREADS)
-k_bicg_p(const long long n, const int nc, const double *__restrict__ r, double *p, const double *__restrict__ v,
-         const KScal *sc) {
-    for (int c = 0; c < nc; c++) {
+k_bicg_p(const long long n, const T *__restrict__ r, T *p, const T *__restrict__ v, const KScal *sc) {
+#pragma unroll
+    for (int c = 0; c < NC; c++) {
         if (sc[c].state != KS_RUN) continue;
-        const double beta = sc[c].beta, om = sc[c].omega;
+        const T beta = (T)sc[c].beta, om = (T)sc[c].omega;
         const long long o = c * n;
         GRID_STRIDE(P, n) { p[o + P] = r[o + P] + beta * (p[o + P] - om * v[o + P]); }
     }
 }
 
-// ------------------------------------------- v = A ph, alpha = rho/(r0,v) --
-__global__ void __launch_bounds__(KTHREADS)
-k_bicg_spmv_v(const OpCtx ctx, const int op, const long long n, const int nc, const double *__restrict__ ph,
-              double *v, const double *__restrict__ r0, KScal *sc, double *partials, unsigned int *counter) {
-    __shared__ double smem[32 * 3];
-    double acc[3] = {0, 0, 0};
-    for (int c = 0; c < nc; c++) {
-        if (sc[c].state != KS_RUN) continue;
-        const long long o = c * n;
-        GRID_STRIDE(P, n) {
-            const double y = op_row(ctx, op, c, ph + o, P);
-            v[o + P] = y;
-            acc[c] += r0[o + P] * y;
+// Calls f(c, P, i, q) for every interior row of this thread's column and
+// g(c, P) for its outer row, for each running component c.
+template <typename T, int NC, typename FI, typename FO>
+__device__ __forceinline__ void sweep_rows(const OpT<T> &A, const bool (&run)[NC], FI fi, FO fo) {
+    int i0, i1, j, k;
+    if (sweep_column(A.sw, A.g, i0, i1, j, k)) {
+        if (j >= A.g.ny || k >= A.g.nz) return;
+        const Column<T> q = column(A, j, k);
+        long long P = cidx(A.g, i0, j, k);
+        for (int i = i0; i < i1; i++, P += A.g.sx) {
+#pragma unroll
+            for (int c = 0; c < NC; c++)
+                if (run[c]) fi(c, P, i, q);
         }
+    } else {
+        const int t = sweep_outer(A.sw);
+        if (t >= A.sw.nout) return;
+        const long long P = A.sw.outer[t];
+#pragma unroll
+        for (int c = 0; c < NC; c++)
+            if (run[c]) fo(c, P);
     }
-    block_sum<3>(acc, smem);
-    if (publish_partials<3>(acc, partials, counter)) {
-        double tot[3];
-        sum_partials<3>(partials, gridDim.x, tot);
-        for (int c = 0; c < nc; c++) {
+}
+
+// ------------------------------------------- v = A ph, alpha = rho/(r0,v) --
+template <typename T, int NC>
+__global__ void __launch_bounds__(SW_THREADS)
+k_bicg_spmv_v(const OpT<T> A, const int op, const long long n, const T *__restrict__ ph, T *v,
+              const T *__restrict__ r0, KScal *sc, double *partials, unsigned int *counter) {
+    __shared__ double smem[32 * NC];
+    typename AccT<T>::type a[NC];
+    bool run[NC];
+#pragma unroll
+    for (int c = 0; c < NC; c++) {
+        a[c] = 0;
+        run[c] = sc[c].state == KS_RUN;
+    }
+    sweep_rows<T, NC>(
+        A, run,
+        [&](int c, long long P, int i, const Column<T> &q) {
+            const long long o = c * n;
+            const T y = interior_row(A, op, ph + o, P, i, q);
+            v[o + P] = y;
+            a[c] += r0[o + P] * y;
+        },
+        [&](int c, long long P) {
+            const long long o = c * n;
+            const T y = op_row(A, op, c, ph + o, P);
+            v[o + P] = y;
+            a[c] += r0[o + P] * y;
+        });
+    double acc[NC];
+#pragma unroll
+    for (int c = 0; c < NC; c++) acc[c] = (double)a[c];
+    reduce_and_finish<NC, NC>(acc, smem, partials, counter, [&](const double *tot) {
+        for (int c = 0; c < NC; c++) {
             KScal &s = sc[c];
             if (s.state != KS_RUN) continue;
             if (tot[c] == 0.0) {
@@ -183,75 +215,83 @@ k_bicg_spmv_v(const OpCtx ctx, const int op, const long long n, const int nc, co
             }
             s.alpha = s.rho / tot[c];
         }
-        *counter = 0;
-    }
+    });
 }
 
 // ------------------------------------------------------- s = r - alpha v --
+template <typename T, int NC>
 __global__ void __launch_bounds__(KTHREADS)
-k_bicg_s(const OpCtx ctx, const long long n, const int nc, const double *__restrict__ r,
-         const double *__restrict__ v, double *s, KScal *sc, const double tol, const double divtol,
-         const double two_re, double *partials, unsigned int *counter) {
-    __shared__ double smem[32 * 4];
-    double acc[4] = {0, 0, 0, 0};
-    for (int c = 0; c < nc; c++) {
+k_bicg_s(const OpT<T> A, const long long n, const T *__restrict__ r, const T *__restrict__ v, T *s, KScal *sc,
+         double *partials, unsigned int *counter) {
+    __shared__ double smem[32 * (NC + 1)];
+    typename AccT<T>::type a[NC];
+#pragma unroll
+    for (int c = 0; c < NC; c++) a[c] = 0;
+    float dmax = 0.0f;
+    const bool want_div = sc[0].divtol > 0;
+#pragma unroll
+    for (int c = 0; c < NC; c++) {
         if (sc[c].state != KS_RUN) continue;
-        const double al = sc[c].alpha;
+        const T al = (T)sc[c].alpha;
         const long long o = c * n;
         GRID_STRIDE(P, n) {
-            const double y = r[o + P] - al * v[o + P];
+            const T y = r[o + P] - al * v[o + P];
             s[o + P] = y;
-            acc[c] += y * y;
-            if (divtol > 0) acc[3] = fmax(acc[3], fabs(y) * div_weight(ctx, P, two_re));
+            a[c] += y * y;
+            if (want_div) dmax = fmaxf(dmax, divw(A, P, y));
         }
     }
-    double dm[1] = {acc[3]};
-    double sm[3] = {acc[0], acc[1], acc[2]};
-    block_sum<3>(sm, smem);
-    __syncthreads();
-    block_max<1>(dm, smem + 96);
-    double out[4] = {sm[0], sm[1], sm[2], dm[0]};
-    if (publish_partials<4>(out, partials, counter)) {
-        double tot[4] = {0, 0, 0, 0};
-        for (unsigned b = 0; b < gridDim.x; b++) {
-            for (int q = 0; q < 3; q++) tot[q] += ((volatile double *)partials)[b * 4 + q];
-            tot[3] = fmax(tot[3], ((volatile double *)partials)[b * 4 + 3]);
-        }
-        for (int c = 0; c < nc; c++) {
+    double acc[NC + 1];
+#pragma unroll
+    for (int c = 0; c < NC; c++) acc[c] = (double)a[c];
+    acc[NC] = (double)dmax;
+    reduce_and_finish<NC + 1, NC>(acc, smem, partials, counter, [&](const double *tot) {
+        for (int c = 0; c < NC; c++) {
             KScal &st = sc[c];
             if (st.state != KS_RUN) continue;
             st.snorm2 = tot[c];
-            const bool ok = divtol > 0 ? tot[3] <= divtol : sqrt(tot[c]) < tol * sqrt(st.bnorm2);
-            if (ok) {
+            if (converged(tot[c], st.bnorm2, tot[NC], st.tol, st.divtol)) {
                 st.state = KS_HALF;
-                st.divmax = tot[3];
+                st.divmax = tot[NC];
             }
         }
-        *counter = 0;
-    }
+    });
 }
 
 // --------------------------------------- t = A sh, omega = (t,s)/(t,t) --
-__global__ void __launch_bounds__(KTHREADS)
-k_bicg_spmv_t(const OpCtx ctx, const int op, const long long n, const int nc, const double *__restrict__ sh,
-              double *t, const double *__restrict__ s, KScal *sc, double *partials, unsigned int *counter) {
-    __shared__ double smem[32 * 6];
-    double acc[6] = {0, 0, 0, 0, 0, 0};
-    for (int c = 0; c < nc; c++) {
-        if (sc[c].state != KS_RUN) continue;
-        const long long o = c * n;
-        GRID_STRIDE(P, n) {
-            const double y = op_row(ctx, op, c, sh + o, P);
-            t[o + P] = y;
-            acc[2 * c] += y * s[o + P];
-            acc[2 * c + 1] += y * y;
-        }
+template <typename T, int NC>
+__global__ void __launch_bounds__(SW_THREADS)
+k_bicg_spmv_t(const OpT<T> A, const int op, const long long n, const T *__restrict__ sh, T *t,
+              const T *__restrict__ s, KScal *sc, double *partials, unsigned int *counter) {
+    __shared__ double smem[32 * 2 * NC];
+    typename AccT<T>::type a[2 * NC];
+    bool run[NC];
+#pragma unroll
+    for (int c = 0; c < NC; c++) {
+        a[2 * c] = a[2 * c + 1] = 0;
+        run[c] = sc[c].state == KS_RUN;
     }
-    block_sum<6>(acc, smem);
-    if (publish_partials<6>(acc, partials, counter)) {
-        double tot[6];
-        sum_partials<6>(partials, gridDim.x, tot);
-        for (int c = 0; c < nc; c++) {
+    sweep_rows<T, NC>(
+        A, run,
+        [&](int c, long long P, int i, const Column<T> &q) {
+            const long long o = c * n;
+            const T y = interior_row(A, op, sh + o, P, i, q);
+            t[o + P] = y;
+            a[2 * c] += y * s[o + P];
+            a[2 * c + 1] += y * y;
+        },
+        [&](int c, long long P) {
+            const long long o = c * n;
+            const T y = op_row(A, op, c, sh + o, P);
+            t[o + P] = y;
+            a[2 * c] += y * s[o + P];
+            a[2 * c + 1] += y * y;
+        });
+    double acc[2 * NC];
+#pragma unroll
+    for (int q = 0; q < 2 * NC; q++) acc[q] = (double)a[q];
+    reduce_and_finish<2 * NC, 2 * NC>(acc, smem, partials, counter, [&](const double *tot) {
+        for (int c = 0; c < NC; c++) {
             KScal &st = sc[c];
             if (st.state != KS_RUN) continue;
             if (tot[2 * c + 1] == 0.0) {
@@ -261,24 +301,30 @@ k_bicg_spmv_t(const OpCtx ctx, const int op, const long long n, const int nc, co
             }
             st.omega = tot[2 * c] / tot[2 * c + 1];
         }
-        *counter = 0;
-    }
+    });
 }
 
 // ------------------- x += alpha ph + omega sh, r = s - omega t, new rho --
+// Ends the iteration: sets the loop condition (some component still
+// running and below maxit).
+template <typename T, int NC>
 __global__ void __launch_bounds__(KTHREADS)
-k_bicg_xr(const OpCtx ctx, const long long n, const int nc, double *x, double *r, const double *__restrict__ r0,
-          const double *__restrict__ ph, const double *__restrict__ sh, const double *__restrict__ s,
-          const double *__restrict__ t, KScal *sc, const double tol, const double divtol, const double two_re,
-          double *partials, unsigned int *counter) {
-    __shared__ double smem[32 * 7];
-    double acc[7] = {0, 0, 0, 0, 0, 0, 0};
-    for (int c = 0; c < nc; c++) {
+k_bicg_xr(const OpT<T> A, const long long n, T *x, T *r, const T *__restrict__ r0, const T *__restrict__ ph,
+          const T *__restrict__ sh, const T *__restrict__ s, const T *__restrict__ t, KScal *sc, double *partials,
+          unsigned int *counter, const int maxit, const LoopCtl lc) {
+    __shared__ double smem[32 * (2 * NC + 1)];
+    typename AccT<T>::type a[2 * NC];
+#pragma unroll
+    for (int q = 0; q < 2 * NC; q++) a[q] = 0;
+    float dmax = 0.0f;
+    const bool want_div = sc[0].divtol > 0;
+#pragma unroll
+    for (int c = 0; c < NC; c++) {
         const int state = sc[c].state;
         const long long o = c * n;
         if (state == KS_HALF) {
             // Converged on s: x += alpha ph, r = s.
-            const double al = sc[c].alpha;
+            const T al = (T)sc[c].alpha;
             GRID_STRIDE(P, n) {
                 x[o + P] += al * ph[o + P];
                 r[o + P] = s[o + P];
@@ -286,29 +332,23 @@ k_bicg_xr(const OpCtx ctx, const long long n, const int nc, double *x, double *r
             continue;
         }
         if (state != KS_RUN) continue;
-        const double al = sc[c].alpha, om = sc[c].omega;
+        const T al = (T)sc[c].alpha, om = (T)sc[c].omega;
         GRID_STRIDE(P, n) {
             x[o + P] += al * ph[o + P] + om * sh[o + P];
-            const double y = s[o + P] - om * t[o + P];
+            const T y = s[o + P] - om * t[o + P];
             r[o + P] = y;
-            acc[2 * c] += y * y;
-            acc[2 * c + 1] += r0[o + P] * y;
-            if (divtol > 0) acc[6] = fmax(acc[6], fabs(y) * div_weight(ctx, P, two_re));
+            a[2 * c] += y * y;
+            a[2 * c + 1] += r0[o + P] * y;
+            if (want_div) dmax = fmaxf(dmax, divw(A, P, y));
         }
     }
-    double sm[6] = {acc[0], acc[1], acc[2], acc[3], acc[4], acc[5]};
-    double dm[1] = {acc[6]};
-    block_sum<6>(sm, smem);
-    __syncthreads();
-    block_max<1>(dm, smem + 192);
-    double out[7] = {sm[0], sm[1], sm[2], sm[3], sm[4], sm[5], dm[0]};
-    if (publish_partials<7>(out, partials, counter)) {
-        double tot[7] = {0, 0, 0, 0, 0, 0, 0};
-        for (unsigned b = 0; b < gridDim.x; b++) {
-            for (int q = 0; q < 6; q++) tot[q] += ((volatile double *)partials)[b * 7 + q];
-            tot[6] = fmax(tot[6], ((volatile double *)partials)[b * 7 + 6]);
-        }
-        for (int c = 0; c < nc; c++) {
+    double acc[2 * NC + 1];
+#pragma unroll
+    for (int q = 0; q < 2 * NC; q++) acc[q] = (double)a[q];
+    acc[2 * NC] = (double)dmax;
+    reduce_and_finish<2 * NC + 1, 2 * NC>(acc, smem, partials, counter, [&](const double *tot) {
+        bool run = false;
+        for (int c = 0; c < NC; c++) {
             KScal &st = sc[c];
             if (st.state == KS_HALF) {
                 st.rnorm2 = st.snorm2;
@@ -322,68 +362,124 @@ k_bicg_xr(const OpCtx ctx, const long long n, const int nc, double *x, double *r
             const double rho1 = tot[2 * c + 1];
             st.beta = (rho1 / st.rho) * (st.alpha / st.omega);
             st.rho = rho1;
-            const bool ok = divtol > 0 ? tot[6] <= divtol : sqrt(tot[2 * c]) < tol * sqrt(st.bnorm2);
-            if (ok) {
+            if (converged(tot[2 * c], st.bnorm2, tot[2 * NC], st.tol, st.divtol)) {
                 st.state = KS_DONE;
-                st.divmax = tot[6];
+                st.divmax = tot[2 * NC];
             } else if (rho1 == 0.0) {
                 st.state = KS_BREAKDOWN;
             }
+            run = run || (st.state == KS_RUN && st.iters < maxit);
         }
-        *counter = 0;
-    }
+        set_loop(lc, run);
+    });
 }
 
-// ---------------------------------------------------------- copy (M = I) --
-__global__ void k_copy(const long long n, const double *__restrict__ a, double *b) {
-    GRID_STRIDE(P, n) b[P] = a[P];
+template <typename T>
+__global__ void __launch_bounds__(SW_THREADS)
+k_apply(const OpT<T> A, const int op, const int comp, const T *__restrict__ x, T *y) {
+    const bool run[1] = {true};
+    sweep_rows<T, 1>(
+        A, run, [&](int, long long P, int i, const Column<T> &q) { y[P] = interior_row(A, op, x, P, i, q); },
+        [&](int, long long P) { y[P] = op_row(A, op, comp, x, P); });
 }
 
-// ------------------------------------------------------------ residual --
-// r = b - A x for one component; returns ||r||^2 and max weighted |r|.
-__global__ void __launch_bounds__(KTHREADS)
-k_residual(const OpCtx ctx, const int op, const int comp, const long long n, const double *__restrict__ b,
-           const double *__restrict__ x, double *r, const double two_re, double *partials, unsigned int *counter,
-           double *out) {
-    __shared__ double smem[64];
-    double sm[1] = {0}, dm[1] = {0};
-    GRID_STRIDE(P, n) {
-        const double y = b[P] - op_row(ctx, op, comp, x, P);
-        if (r) r[P] = y;
-        sm[0] += y * y;
-        dm[0] = fmax(dm[0], fabs(y) * div_weight(ctx, P, two_re));
+// --------------------------------------------- iterative refinement (FP64) --
+// r = b - A x (or r = b while x is still zero), with per-component ||r||^2,
+// max|r| and the divergence max; the last block derives each component's
+// state, the FP32 scale 1/max|r| (0 for converged components), counts the
+// cycle and sets the outer loop condition.
+template <int NC>
+__global__ void __launch_bounds__(SW_THREADS)
+k_ir_residual(const OpT<double> A, const int op, const long long n, const double *__restrict__ b,
+              const double *__restrict__ x, double *r, const int x_zero, IRScal *sc, const double tol,
+              const double divtol, const int max_outer, double *partials, unsigned int *counter, const LoopCtl lc) {
+    constexpr int NV = 3 * NC + 1;
+    __shared__ double smem[32 * NV];
+    double sm[2 * NC], mx[NC + 1];  // ||r||^2, ||b||^2 (x_zero only); max|r|, divergence max
+    bool run[NC];
+#pragma unroll
+    for (int c = 0; c < NC; c++) {
+        sm[c] = sm[NC + c] = 0;
+        mx[c] = 0;
+        run[c] = true;
     }
-    block_sum<1>(sm, smem);
-    __syncthreads();
-    block_max<1>(dm, smem + 32);
-    double o2[2] = {sm[0], dm[0]};
-    if (publish_partials<2>(o2, partials, counter)) {
-        double s = 0, m = 0;
-        for (unsigned b2 = 0; b2 < gridDim.x; b2++) {
-            s += ((volatile double *)partials)[b2 * 2];
-            m = fmax(m, ((volatile double *)partials)[b2 * 2 + 1]);
+    mx[NC] = 0;
+    auto acc = [&](int c, long long P, double y) {
+        const double bv = b[c * n + P];
+        r[c * n + P] = y;
+        sm[c] += y * y;
+        if (x_zero) sm[NC + c] += bv * bv;
+        mx[c] = fmax(mx[c], fabs(y));
+        if (divtol > 0) mx[NC] = fmax(mx[NC], (double)divw(A, P, y));
+    };
+    sweep_rows<double, NC>(
+        A, run,
+        [&](int c, long long P, int i, const Column<double> &q) {
+            const long long o = c * n;
+            acc(c, P, x_zero ? b[o + P] : b[o + P] - interior_row(A, op, x + o, P, i, q));
+        },
+        [&](int c, long long P) {
+            const long long o = c * n;
+            acc(c, P, x_zero ? b[o + P] : b[o + P] - op_row(A, op, c, x + o, P));
+        });
+    double v[NV];
+#pragma unroll
+    for (int q = 0; q < 2 * NC; q++) v[q] = sm[q];
+#pragma unroll
+    for (int q = 0; q <= NC; q++) v[2 * NC + q] = mx[q];
+    reduce_and_finish<NV, 2 * NC>(v, smem, partials, counter, [&](const double *tot) {
+        bool go = false;
+        for (int c = 0; c < NC; c++) {
+            IRScal &s = sc[c];
+            if (x_zero) {
+                s.bnorm2 = tot[NC + c];
+                s.outer = 0;
+                s.inner = 0;
+            } else {
+                s.outer += 1;
+            }
+            s.rnorm2 = tot[c];
+            s.rmax = tot[2 * NC + c];
+            s.divmax = tot[3 * NC];
+            const bool done = s.bnorm2 == 0.0 || converged(tot[c], s.bnorm2, tot[3 * NC], tol, divtol);
+            s.state = done ? KS_DONE : KS_RUN;
+            s.scale = (done || s.rmax == 0.0) ? 0.0 : 1.0 / s.rmax;
+            go = go || (!done && s.outer < max_outer);
         }
-        out[0] = s;
-        out[1] = m;
-        *counter = 0;
+        set_loop(lc, go);
+    });
+}
+
+template <int NC>
+__global__ void __launch_bounds__(KTHREADS)
+k_ir_to32(const long long n, const double *__restrict__ r, const IRScal *sc, float *b32) {
+#pragma unroll
+    for (int c = 0; c < NC; c++) {
+        const double s = sc[c].scale;
+        const long long o = c * n;
+        GRID_STRIDE(P, n) b32[o + P] = (float)(r[o + P] * s);
     }
 }
 
+// x += e / scale; counts the inner iterations of the cycle.
+template <int NC>
 __global__ void __launch_bounds__(KTHREADS)
-k_apply(const OpCtx ctx, const int op, const int comp, const long long n, const double *__restrict__ x,
-        double *y) {
-    GRID_STRIDE(P, n) y[P] = op_row(ctx, op, comp, x, P);
+k_ir_update(const long long n, double *x, const float *__restrict__ e, IRScal *sc, const KScal *__restrict__ inner) {
+#pragma unroll
+    for (int c = 0; c < NC; c++) {
+        const double s = sc[c].scale;
+        if (s == 0.0) continue;
+        const double inv = 1.0 / s;
+        const long long o = c * n;
+        GRID_STRIDE(P, n) x[o + P] += (double)e[o + P] * inv;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        for (int c = 0; c < NC; c++) sc[c].inner += inner[c].iters;
 }
 
-void apply_operator(cudaStream_t st, const OpCtx &ctx, int op, int comp, const double *x, double *y) {
-    k_apply<<<KBLOCKS, KTHREADS, 0, st>>>(ctx, op, comp, ctx.g.ncell, x, y);
-    note_launches(1);
-}
-
-// -------------------------------------------------------------- driver --
-KrylovWork::~KrylovWork() { release(); }
-
-void KrylovWork::release() {
+// ------------------------------------------------------------ workspace --
+template <typename T>
+void KrylovWork<T>::release() {
     if (base) cudaFree(base);
     if (scal) cudaFree(scal);
     if (scal_h) cudaFreeHost(scal_h);
@@ -396,15 +492,16 @@ void KrylovWork::release() {
     counter = nullptr;
 }
 
-int KrylovWork::allocate(long long ncell, int ncomp, bool precond) {
+template <typename T>
+int KrylovWork<T>::allocate(long long ncell, int ncomp, bool precond, int maxblocks) {
     release();
     n = ncell;
     nc = ncomp;
     const int nvec = precond ? 8 : 6;
-    size_t bytes = sizeof(double) * (size_t)n * nc * nvec;
+    const size_t bytes = sizeof(T) * (size_t)n * nc * nvec;
     if (cudaMalloc(&base, bytes) != cudaSuccess) return -1;
     cudaMemset(base, 0, bytes);
-    double *q = base;
+    T *q = base;
     const long long m = n * nc;
     r = q; q += m;
     r0 = q; q += m;
@@ -420,80 +517,161 @@ int KrylovWork::allocate(long long ncell, int ncomp, bool precond) {
         sh = s;
     }
     if (cudaMalloc(&scal, sizeof(KScal) * 3) != cudaSuccess) return -1;
+    cudaMemset(scal, 0, sizeof(KScal) * 3);
     if (cudaMallocHost(&scal_h, sizeof(KScal) * 3) != cudaSuccess) return -1;
-    if (cudaMalloc(&partials, sizeof(double) * KBLOCKS * 8) != cudaSuccess) return -1;
+    if (cudaMalloc(&partials, sizeof(double) * std::max(KBLOCKS, maxblocks) * 10) != cudaSuccess) return -1;
     if (cudaMalloc(&counter, sizeof(unsigned int)) != cudaSuccess) return -1;
     cudaMemset(counter, 0, sizeof(unsigned int));
     return 0;
 }
 
+template struct KrylovWork<double>;
+template struct KrylovWork<float>;
+
+void IRWork::release() {
+    if (r) cudaFree(r);
+    if (b32) cudaFree(b32);
+    if (e32) cudaFree(e32);
+    if (scal) cudaFree(scal);
+    if (scal_h) cudaFreeHost(scal_h);
+    if (partials) cudaFree(partials);
+    if (counter) cudaFree(counter);
+    r = nullptr;
+    b32 = e32 = nullptr;
+    scal = scal_h = nullptr;
+    partials = nullptr;
+    counter = nullptr;
+    inner.release();
+}
+
+int IRWork::allocate(long long ncell, int ncomp, bool precond, int maxblocks) {
+    release();
+    n = ncell;
+    nc = ncomp;
+    const size_t m = (size_t)n * nc;
+    if (cudaMalloc(&r, sizeof(double) * m) != cudaSuccess) return -1;
+    if (cudaMalloc(&b32, sizeof(float) * m) != cudaSuccess) return -1;
+    if (cudaMalloc(&e32, sizeof(float) * m) != cudaSuccess) return -1;
+    if (cudaMalloc(&scal, sizeof(IRScal) * 3) != cudaSuccess) return -1;
+    cudaMemset(scal, 0, sizeof(IRScal) * 3);
+    if (cudaMallocHost(&scal_h, sizeof(IRScal) * 3) != cudaSuccess) return -1;
+    if (cudaMalloc(&partials, sizeof(double) * std::max(KBLOCKS, maxblocks) * 10) != cudaSuccess) return -1;
+    if (cudaMalloc(&counter, sizeof(unsigned int)) != cudaSuccess) return -1;
+    cudaMemset(counter, 0, sizeof(unsigned int));
+    return inner.allocate(ncell, ncomp, precond, maxblocks);
+}
+
+// ------------------------------------------------------------ launches --
 static int prof_begin(Prof *p, const char *name) { return p ? p->begin(name) : -1; }
 static void prof_end(Prof *p, int t) {
     if (p) p->end(t);
 }
 
-static bool all_in(const KScal *s, int nc, int a, int b, int c2) {
+template <typename SC>
+static bool all_in(const SC *s, int nc, int a, int b, int c2) {
     for (int q = 0; q < nc; q++)
         if (s[q].state != a && s[q].state != b && s[q].state != c2) return false;
     return true;
 }
 
-int bicgstab(cudaStream_t st, const OpCtx &ctx, int op, KrylovWork &w, const double *b, double *x,
-             const SolveParams &prm, Preconditioner *M, SolveReport &rep) {
+template <typename T>
+static void launch_init(cudaStream_t st, KrylovWork<T> &w, const T *b, T *x, double tol, double divtol,
+                        const IRScal *outer, double outer_tol, double outer_divtol, LoopCtl lc) {
+    if (w.nc == 3)
+        k_bicg_init<T, 3><<<KBLOCKS, KTHREADS, 0, st>>>(w.n, b, x, w.r, w.r0, w.p, w.v, w.scal, w.partials,
+                                                       w.counter, tol, divtol, outer, outer_tol, outer_divtol, lc);
+    else
+        k_bicg_init<T, 1><<<KBLOCKS, KTHREADS, 0, st>>>(w.n, b, x, w.r, w.r0, w.p, w.v, w.scal, w.partials,
+                                                       w.counter, tol, divtol, outer, outer_tol, outer_divtol, lc);
+    note_launches(1);
+}
+
+// p update, preconditioner, v = A ph, s = r - alpha v.
+template <typename T>
+static void first_half(cudaStream_t st, const OpT<T> &A, int op, KrylovWork<T> &w, Preconditioner<T> *M, Prof *pf) {
     const long long n = w.n;
     const int nc = w.nc;
-    k_bicg_init<<<KBLOCKS, KTHREADS, 0, st>>>(n, nc, b, x, w.r, w.r0, w.p, w.v, w.scal, w.partials, w.counter);
+    const int *gate = nc == 1 ? &w.scal[0].state : nullptr;
+    if (nc == 3) k_bicg_p<T, 3><<<KBLOCKS, KTHREADS, 0, st>>>(n, w.r, w.p, w.v, w.scal);
+    else k_bicg_p<T, 1><<<KBLOCKS, KTHREADS, 0, st>>>(n, w.r, w.p, w.v, w.scal);
     note_launches(1);
-    const double two_re = 2 * prm.Re;
-    int it = 0;
-    auto fetch = [&]() {
-        cudaMemcpyAsync(w.scal_h, w.scal, sizeof(KScal) * nc, cudaMemcpyDeviceToHost, st);
-        cudaStreamSynchronize(st);
-    };
-    fetch();
-    while (!all_in(w.scal_h, nc, KS_DONE, KS_BREAKDOWN, KS_DONE) && it < prm.maxit) {
-        it++;
-        k_bicg_p<<<KBLOCKS, KTHREADS, 0, st>>>(n, nc, w.r, w.p, w.v, w.scal);
-        note_launches(1);
-        int tm = -1;
-        if (M) {
-            tm = prof_begin(prm.prof, "mg_vcycle");
-            M->apply(st, w.p, w.ph);
-            prof_end(prm.prof, tm);
-        }
-        tm = prof_begin(prm.prof, op == OP_MOM ? "spmv_mom" : "spmv_p");
-        k_bicg_spmv_v<<<KBLOCKS, KTHREADS, 0, st>>>(ctx, op, n, nc, w.ph, w.v, w.r0, w.scal, w.partials, w.counter);
-        note_launches(1);
-        prof_end(prm.prof, tm);
-        k_bicg_s<<<KBLOCKS, KTHREADS, 0, st>>>(ctx, n, nc, w.r, w.v, w.s, w.scal, prm.tol, prm.divtol, two_re,
-                                             w.partials, w.counter);
-        note_launches(1);
-        if (prm.sync_half) {
-            fetch();
-            if (all_in(w.scal_h, nc, KS_HALF, KS_DONE, KS_BREAKDOWN)) {
-                k_bicg_xr<<<KBLOCKS, KTHREADS, 0, st>>>(ctx, n, nc, x, w.r, w.r0, w.ph, w.sh, w.s, w.t, w.scal,
-                                                      prm.tol, prm.divtol, two_re, w.partials, w.counter);
-                note_launches(1);
-                fetch();
-                break;
-            }
-        }
-        if (M) {
-            tm = prof_begin(prm.prof, "mg_vcycle");
-            M->apply(st, w.s, w.sh);
-            prof_end(prm.prof, tm);
-        }
-        tm = prof_begin(prm.prof, op == OP_MOM ? "spmv_mom" : "spmv_p");
-        k_bicg_spmv_t<<<KBLOCKS, KTHREADS, 0, st>>>(ctx, op, n, nc, w.sh, w.t, w.s, w.scal, w.partials, w.counter);
-        note_launches(1);
-        prof_end(prm.prof, tm);
-        k_bicg_xr<<<KBLOCKS, KTHREADS, 0, st>>>(ctx, n, nc, x, w.r, w.r0, w.ph, w.sh, w.s, w.t, w.scal, prm.tol,
-                                              prm.divtol, two_re, w.partials, w.counter);
-        note_launches(1);
-        fetch();
+    if (M) {
+        const int tm = prof_begin(pf, "mg_vcycle");
+        M->apply(st, w.p, w.ph, gate);
+        prof_end(pf, tm);
     }
+    const int tm = prof_begin(pf, op == OP_MOM ? "spmv_mom" : "spmv_p");
+    if (nc == 3)
+        k_bicg_spmv_v<T, 3><<<A.sw.nblocks, SW_THREADS, 0, st>>>(A, op, n, w.ph, w.v, w.r0, w.scal, w.partials,
+                                                                w.counter);
+    else
+        k_bicg_spmv_v<T, 1><<<A.sw.nblocks, SW_THREADS, 0, st>>>(A, op, n, w.ph, w.v, w.r0, w.scal, w.partials,
+                                                                w.counter);
+    note_launches(1);
+    prof_end(pf, tm);
+    if (nc == 3) k_bicg_s<T, 3><<<KBLOCKS, KTHREADS, 0, st>>>(A, n, w.r, w.v, w.s, w.scal, w.partials, w.counter);
+    else k_bicg_s<T, 1><<<KBLOCKS, KTHREADS, 0, st>>>(A, n, w.r, w.v, w.s, w.scal, w.partials, w.counter);
+    note_launches(1);
+}
+
+// Preconditioner, t = A sh (both skipped by converged components).
+template <typename T>
+static void second_half(cudaStream_t st, const OpT<T> &A, int op, KrylovWork<T> &w, Preconditioner<T> *M, Prof *pf) {
+    const int *gate = w.nc == 1 ? &w.scal[0].state : nullptr;
+    if (M) {
+        const int tm = prof_begin(pf, "mg_vcycle");
+        M->apply(st, w.s, w.sh, gate);
+        prof_end(pf, tm);
+    }
+    const int tm = prof_begin(pf, op == OP_MOM ? "spmv_mom" : "spmv_p");
+    if (w.nc == 3)
+        k_bicg_spmv_t<T, 3><<<A.sw.nblocks, SW_THREADS, 0, st>>>(A, op, w.n, w.sh, w.t, w.s, w.scal, w.partials,
+                                                                w.counter);
+    else
+        k_bicg_spmv_t<T, 1><<<A.sw.nblocks, SW_THREADS, 0, st>>>(A, op, w.n, w.sh, w.t, w.s, w.scal, w.partials,
+                                                                w.counter);
+    note_launches(1);
+    prof_end(pf, tm);
+}
+
+template <typename T>
+static void launch_xr(cudaStream_t st, const OpT<T> &A, KrylovWork<T> &w, T *x, int maxit, LoopCtl lc) {
+    if (w.nc == 3)
+        k_bicg_xr<T, 3><<<KBLOCKS, KTHREADS, 0, st>>>(A, w.n, x, w.r, w.r0, w.ph, w.sh, w.s, w.t, w.scal,
+                                                     w.partials, w.counter, maxit, lc);
+    else
+        k_bicg_xr<T, 1><<<KBLOCKS, KTHREADS, 0, st>>>(A, w.n, x, w.r, w.r0, w.ph, w.sh, w.s, w.t, w.scal,
+                                                     w.partials, w.counter, maxit, lc);
+    note_launches(1);
+}
+
+static void launch_residual(cudaStream_t st, const OpT<double> &A64, int op, IRWork &w, const double *b,
+                            const double *x, int x_zero, const SolveParams &prm, LoopCtl lc) {
+    if (w.nc == 3)
+        k_ir_residual<3><<<A64.sw.nblocks, SW_THREADS, 0, st>>>(A64, op, w.n, b, x, w.r, x_zero, w.scal, prm.tol,
+                                                               prm.divtol, prm.max_outer, w.partials, w.counter, lc);
+    else
+        k_ir_residual<1><<<A64.sw.nblocks, SW_THREADS, 0, st>>>(A64, op, w.n, b, x, w.r, x_zero, w.scal, prm.tol,
+                                                               prm.divtol, prm.max_outer, w.partials, w.counter, lc);
+    note_launches(1);
+}
+
+static void launch_to32(cudaStream_t st, IRWork &w) {
+    if (w.nc == 3) k_ir_to32<3><<<KBLOCKS, KTHREADS, 0, st>>>(w.n, w.r, w.scal, w.b32);
+    else k_ir_to32<1><<<KBLOCKS, KTHREADS, 0, st>>>(w.n, w.r, w.scal, w.b32);
+    note_launches(1);
+}
+
+static void launch_update(cudaStream_t st, IRWork &w, double *x) {
+    if (w.nc == 3) k_ir_update<3><<<KBLOCKS, KTHREADS, 0, st>>>(w.n, x, w.e32, w.scal, w.inner.scal);
+    else k_ir_update<1><<<KBLOCKS, KTHREADS, 0, st>>>(w.n, x, w.e32, w.scal, w.inner.scal);
+    note_launches(1);
+}
+
+template <typename T>
+int report(const KrylovWork<T> &w, SolveReport &rep) {
     int status = 0;
-    for (int c = 0; c < nc; c++) {
+    for (int c = 0; c < w.nc; c++) {
         const KScal &s = w.scal_h[c];
         rep.iters[c] = s.iters;
         rep.relres[c] = s.bnorm2 > 0 ? std::sqrt(s.rnorm2 / s.bnorm2) : 0.0;
@@ -504,18 +682,201 @@ int bicgstab(cudaStream_t st, const OpCtx &ctx, int op, KrylovWork &w, const dou
     return status;
 }
 
-double residual_norm(cudaStream_t st, const OpCtx &ctx, int op, int comp, const double *b, const double *x,
-                     double *r, double two_re, KrylovWork &w, double *divmax) {
-    double *out;
-    cudaMalloc(&out, 2 * sizeof(double));
-    k_residual<<<KBLOCKS, KTHREADS, 0, st>>>(ctx, op, comp, ctx.g.ncell, b, x, r, two_re, w.partials, w.counter,
-                                           out);
-    double h[2];
-    cudaMemcpyAsync(h, out, sizeof h, cudaMemcpyDeviceToHost, st);
-    cudaStreamSynchronize(st);
-    cudaFree(out);
-    if (divmax) *divmax = h[1];
-    return std::sqrt(h[0]);
+template int report<double>(const KrylovWork<double> &, SolveReport &);
+template int report<float>(const KrylovWork<float> &, SolveReport &);
+
+int report(const IRWork &w, SolveReport &rep) {
+    rep = SolveReport();
+    int status = 0;
+    for (int c = 0; c < w.nc; c++) {
+        const IRScal &s = w.scal_h[c];
+        rep.iters[c] = s.inner;
+        rep.outer = std::max(rep.outer, s.outer);
+        rep.relres[c] = s.bnorm2 > 0 ? std::sqrt(s.rnorm2 / s.bnorm2) : 0.0;
+        rep.divmax[c] = s.divmax;
+        if (s.state != KS_DONE) status = 1;
+    }
+    return status;
 }
+
+// ----------------------------------------------------------- host loops --
+template <typename T>
+static void fetch(cudaStream_t st, KrylovWork<T> &w) {
+    cudaMemcpyAsync(w.scal_h, w.scal, sizeof(KScal) * w.nc, cudaMemcpyDeviceToHost, st);
+    cudaStreamSynchronize(st);
+}
+
+template <typename T>
+static void host_loop(cudaStream_t st, const OpT<T> &A, int op, KrylovWork<T> &w, T *x, int maxit,
+                      Preconditioner<T> *M, Prof *pf) {
+    const LoopCtl none;
+    fetch(st, w);
+    int it = 0;
+    while (!all_in(w.scal_h, w.nc, KS_DONE, KS_BREAKDOWN, KS_DONE) && it < maxit) {
+        it++;
+        first_half(st, A, op, w, M, pf);
+        fetch(st, w);
+        if (all_in(w.scal_h, w.nc, KS_HALF, KS_DONE, KS_BREAKDOWN)) {
+            launch_xr(st, A, w, x, maxit, none);
+            fetch(st, w);
+            break;
+        }
+        second_half(st, A, op, w, M, pf);
+        launch_xr(st, A, w, x, maxit, none);
+        fetch(st, w);
+    }
+}
+
+template <typename T>
+int bicgstab(cudaStream_t st, const OpT<T> &A, int op, KrylovWork<T> &w, const T *b, T *x, const SolveParams &prm,
+             Preconditioner<T> *M, SolveReport &rep) {
+    launch_init(st, w, b, x, prm.tol, prm.divtol, nullptr, 0.0, 0.0, LoopCtl());
+    host_loop(st, A, op, w, x, prm.maxit, M, prm.prof);
+    return report(w, rep);
+}
+
+template int bicgstab<double>(cudaStream_t, const OpT<double> &, int, KrylovWork<double> &, const double *,
+                              double *, const SolveParams &, Preconditioner<double> *, SolveReport &);
+template int bicgstab<float>(cudaStream_t, const OpT<float> &, int, KrylovWork<float> &, const float *, float *,
+                             const SolveParams &, Preconditioner<float> *, SolveReport &);
+
+int solve_ir(cudaStream_t st, const OpT<double> &A64, const OpT<float> &A32, int op, IRWork &w, const double *b,
+             double *x, const SolveParams &prm, Preconditioner<float> *M32, SolveReport &rep) {
+    const long long n = w.n;
+    const int nc = w.nc;
+    auto fetch_outer = [&]() {
+        cudaMemcpyAsync(w.scal_h, w.scal, sizeof(IRScal) * nc, cudaMemcpyDeviceToHost, st);
+        cudaStreamSynchronize(st);
+    };
+    cudaMemsetAsync(x, 0, sizeof(double) * n * nc, st);
+    launch_residual(st, A64, op, w, b, x, 1, prm, LoopCtl());
+    fetch_outer();
+    int outer = 0;
+    while (!all_in(w.scal_h, nc, KS_DONE, KS_DONE, KS_DONE) && outer < prm.max_outer) {
+        outer++;
+        launch_to32(st, w);
+        launch_init(st, w.inner, w.b32, w.e32, prm.inner_tol, 0.0, w.scal, prm.tol, prm.divtol, LoopCtl());
+        host_loop(st, A32, op, w.inner, w.e32, prm.maxit, M32, prm.prof);
+        launch_update(st, w, x);
+        launch_residual(st, A64, op, w, b, x, 0, prm, LoopCtl());
+        fetch_outer();
+    }
+    return report(w, rep);
+}
+
+// ------------------------------------------------------- recorded forms --
+// Graph being captured on st.
+static cudaGraph_t capture_graph(cudaStream_t st) {
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g = nullptr;
+    if (cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, nullptr, nullptr, nullptr) != cudaSuccess ||
+        cs != cudaStreamCaptureStatusActive)
+        return nullptr;
+    return g;
+}
+
+static int new_loop(cudaStream_t st, LoopCtl &lc) {
+    cudaGraph_t g = capture_graph(st);
+    if (!g) return -1;
+    if (cudaGraphConditionalHandleCreate(&lc.h, g, 0, cudaGraphCondAssignDefault) != cudaSuccess) return -1;
+    lc.use = 1;
+    return 0;
+}
+
+// Appends a while node on lc.h after st's current work and starts capturing
+// its body on body_stream.
+static int begin_while(cudaStream_t st, const LoopCtl &lc, cudaStream_t body_stream) {
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t *deps = nullptr;
+    size_t nd = 0;
+    if (cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &nd) != cudaSuccess) return -1;
+    cudaGraphNodeParams p{};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = lc.h;
+    p.conditional.type = cudaGraphCondTypeWhile;
+    p.conditional.size = 1;
+    cudaGraphNode_t node;
+    if (cudaGraphAddNode(&node, g, deps, nullptr, nd, &p) != cudaSuccess) return -1;
+    if (cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies) != cudaSuccess)
+        return -1;
+    if (cudaStreamBeginCaptureToGraph(body_stream, p.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                      cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+        return -1;
+    return 0;
+}
+
+static int end_while(cudaStream_t body_stream) {
+    cudaGraph_t g = nullptr;
+    return cudaStreamEndCapture(body_stream, &g) == cudaSuccess ? 0 : -1;
+}
+
+// Init (already recorded by the caller with lc) + while loop of iterations.
+template <typename T>
+static int record_loop(cudaStream_t st, cudaStream_t body, const OpT<T> &A, int op, KrylovWork<T> &w, T *x,
+                       int maxit, Preconditioner<T> *M, const LoopCtl &lc, int *per_iter) {
+    if (begin_while(st, lc, body) != 0) return -1;
+    first_half(body, A, op, w, M, nullptr);
+    second_half(body, A, op, w, M, nullptr);
+    launch_xr(body, A, w, x, maxit, lc);
+    if (end_while(body) != 0) return -1;
+    *per_iter = 5 + (M ? 2 * M->launches() : 0);
+    return 0;
+}
+
+template <typename T>
+int record_bicgstab(cudaStream_t st, const cudaStream_t *aux, const OpT<T> &A, int op, KrylovWork<T> &w, const T *b,
+                    T *x, const SolveParams &prm, Preconditioner<T> *M, int *fixed, int *per_iter) {
+    LoopCtl lc;
+    if (new_loop(st, lc) != 0) return -1;
+    launch_init(st, w, b, x, prm.tol, prm.divtol, nullptr, 0.0, 0.0, lc);
+    if (record_loop(st, aux[0], A, op, w, x, prm.maxit, M, lc, per_iter) != 0) return -1;
+    cudaMemcpyAsync(w.scal_h, w.scal, sizeof(KScal) * w.nc, cudaMemcpyDeviceToHost, st);
+    *fixed = 1;
+    return 0;
+}
+
+template int record_bicgstab<double>(cudaStream_t, const cudaStream_t *, const OpT<double> &, int,
+                                     KrylovWork<double> &, const double *, double *, const SolveParams &,
+                                     Preconditioner<double> *, int *, int *);
+template int record_bicgstab<float>(cudaStream_t, const cudaStream_t *, const OpT<float> &, int, KrylovWork<float> &,
+                                    const float *, float *, const SolveParams &, Preconditioner<float> *, int *,
+                                    int *);
+
+int record_ir(cudaStream_t st, const cudaStream_t *aux, const OpT<double> &A64, const OpT<float> &A32, int op,
+              IRWork &w, const double *b, double *x, const SolveParams &prm, Preconditioner<float> *M32, int *fixed,
+              int *per_outer, int *per_iter) {
+    const long long n = w.n;
+    const int nc = w.nc;
+    LoopCtl outer;
+    if (new_loop(st, outer) != 0) return -1;
+    cudaMemsetAsync(x, 0, sizeof(double) * n * nc, st);
+    launch_residual(st, A64, op, w, b, x, 1, prm, outer);
+    if (begin_while(st, outer, aux[0]) != 0) return -1;
+    {
+        cudaStream_t bs = aux[0];
+        launch_to32(bs, w);
+        LoopCtl inner;
+        if (new_loop(bs, inner) != 0) return -1;
+        launch_init(bs, w.inner, w.b32, w.e32, prm.inner_tol, 0.0, w.scal, prm.tol, prm.divtol, inner);
+        if (record_loop(bs, aux[1], A32, op, w.inner, w.e32, prm.maxit, M32, inner, per_iter) != 0) return -1;
+        launch_update(bs, w, x);
+        launch_residual(bs, A64, op, w, b, x, 0, prm, outer);
+    }
+    if (end_while(aux[0]) != 0) return -1;
+    cudaMemcpyAsync(w.scal_h, w.scal, sizeof(IRScal) * nc, cudaMemcpyDeviceToHost, st);
+    *fixed = 1;
+    *per_outer = 4;
+    return 0;
+}
+
+template <typename T>
+void apply_operator(cudaStream_t st, const OpT<T> &A, int op, int comp, const T *x, T *y) {
+    k_apply<T><<<A.sw.nblocks, SW_THREADS, 0, st>>>(A, op, comp, x, y);
+    note_launches(1);
+}
+
+template void apply_operator<double>(cudaStream_t, const OpT<double> &, int, int, const double *, double *);
+template void apply_operator<float>(cudaStream_t, const OpT<float> &, int, int, const float *, float *);
 
 }  // namespace ibm

@@ -1,16 +1,25 @@
-// Krylov solver interface (host side).
+// Krylov solvers (host side): BiCGSTAB in FP64 or FP32, and an FP64
+// iterative-refinement driver around FP32 inner solves.
 //
 // Divergence criterion: for a fluid cell P the projected face velocity has
 // div U^{n+1}_P = -2 Re coeffsum_P r_P, with r the residual of the
 // normalised pressure row (coeffsum = sum of the six Crank-Nicolson
-// coefficients, src/ibm3d_setup.c:1641-1649).  With divtol > 0 the pressure
-// solve stops once max_P |2 Re coeffsum_P r_P| <= divtol instead of on the
-// relative residual.
+// coefficients, src/ibm3d_setup.c:1641-1649).  A solve stops once
+// ||r|| < tol ||b|| (when tol > 0) or max_P |2 Re coeffsum_P r_P| <= divtol
+// (when divtol > 0), whichever enabled test passes first.
+//
+// Every solve exists in two forms with the same kernels and arithmetic:
+// a host loop (reads the device scalars after each half iteration; used
+// with per-stage profiling) and a recorded form that appends the whole
+// solve to a CUDA graph being captured, the iteration loop as a
+// conditional while node whose condition the last kernel of each
+// iteration sets on the device (no host round trip per iteration).
 #pragma once
 
 #include <cuda_runtime.h>
 
 #include "kernels.h"
+#include "ops.cuh"
 
 namespace ibm {
 
@@ -19,60 +28,121 @@ struct Prof;
 constexpr int KTHREADS = 256;
 constexpr int KBLOCKS = 1216;  // 8 blocks per SM on 152 SMs; grid-stride loops
 
-enum { OP_MOM = 0, OP_PRES = 1 };
 enum { KS_RUN = 0, KS_HALF = 1, KS_DONE = 2, KS_BREAKDOWN = 3 };
 
 struct KScal {
     double bnorm2, rnorm2, snorm2;
     double rho, alpha, omega, beta;
     double divmax;
+    double tol, divtol;  // this solve's stopping test (set by the init kernel)
     int iters;
     int state;
+};
+
+// Outer (FP64) state of an iterative-refinement solve, per component.
+struct IRScal {
+    double bnorm2, rnorm2, rmax, divmax, scale;
+    int state;
+    int outer;   // refinement cycles completed
+    int inner;   // FP32 Krylov iterations summed over the cycles
 };
 
 struct SolveParams {
     double tol = 1e-6;
     double divtol = 0.0;
-    double Re = 1.0;
     int maxit = 1000;
-    bool sync_half = true;
-    Prof *prof = nullptr;   // optional stage timers around SpMV / preconditioner
+    double inner_tol = 1e-5;  // iterative refinement: relative tolerance of each FP32 solve
+    int max_outer = 12;
+    Prof *prof = nullptr;     // optional stage timers around SpMV / preconditioner (host loop only)
 };
 
 struct SolveReport {
-    int iters[3] = {0, 0, 0};
+    int iters[3] = {0, 0, 0};   // Krylov iterations (summed over refinement cycles)
+    int outer = 0;              // refinement cycles (mixed path)
     double relres[3] = {0, 0, 0};
     double divmax[3] = {0, 0, 0};
 };
 
-struct Preconditioner {
-    virtual ~Preconditioner() {}
-    virtual void apply(cudaStream_t s, const double *r, double *z) = 0;
+// Loop control of a recorded solve: the handle of the enclosing
+// conditional while node; use = 0 outside graphs.
+struct LoopCtl {
+    cudaGraphConditionalHandle h = 0;
+    int use = 0;
 };
 
+// gate (device pointer or null): when it points to a value other than
+// KS_RUN every kernel of the application returns at once, so a recorded
+// loop iteration after convergence costs only empty launches.
+template <typename T>
+struct Preconditioner {
+    virtual ~Preconditioner() {}
+    virtual void apply(cudaStream_t s, const T *r, T *z, const int *gate) = 0;
+    // Kernels one application launches.
+    virtual int launches() const = 0;
+};
+
+template <typename T>
 struct KrylovWork {
     long long n = 0;
     int nc = 0;
-    double *base = nullptr;
-    double *r = nullptr, *r0 = nullptr, *p = nullptr, *v = nullptr, *s = nullptr, *t = nullptr;
-    double *ph = nullptr, *sh = nullptr;
+    T *base = nullptr;
+    T *r = nullptr, *r0 = nullptr, *p = nullptr, *v = nullptr, *s = nullptr, *t = nullptr;
+    T *ph = nullptr, *sh = nullptr;
     KScal *scal = nullptr, *scal_h = nullptr;
     double *partials = nullptr;
     unsigned int *counter = nullptr;
-    ~KrylovWork();
-    int allocate(long long ncell, int ncomp, bool precond);
+    ~KrylovWork() { release(); }
+    // maxblocks: the largest grid of any reduction kernel (sweeps included).
+    int allocate(long long ncell, int ncomp, bool precond, int maxblocks);
     void release();
 };
 
-// Solves A x = b (nc components for OP_MOM, 1 for OP_PRES) from x0 = 0.
-// Returns 0 when every component converged, 1 on reaching maxit, 2 on a
-// Krylov breakdown.
-int bicgstab(cudaStream_t st, const OpCtx &ctx, int op, KrylovWork &w, const double *b, double *x,
-             const SolveParams &prm, Preconditioner *M, SolveReport &rep);
+// FP64 outer vectors of an iterative-refinement solve plus its FP32 inner work.
+struct IRWork {
+    long long n = 0;
+    int nc = 0;
+    double *r = nullptr;          // FP64 residual
+    float *b32 = nullptr, *e32 = nullptr;
+    IRScal *scal = nullptr, *scal_h = nullptr;
+    double *partials = nullptr;
+    unsigned int *counter = nullptr;
+    KrylovWork<float> inner;
+    ~IRWork() { release(); }
+    int allocate(long long ncell, int ncomp, bool precond, int maxblocks);
+    void release();
+};
 
-void apply_operator(cudaStream_t st, const OpCtx &ctx, int op, int comp, const double *x, double *y);
+// Host loop.  Solves A x = b (nc components for OP_MOM, 1 for OP_PRES)
+// from x0 = 0.  Returns 0 when every component converged, 1 on reaching
+// maxit, 2 on a Krylov breakdown.
+template <typename T>
+int bicgstab(cudaStream_t st, const OpT<T> &A, int op, KrylovWork<T> &w, const T *b, T *x, const SolveParams &prm,
+             Preconditioner<T> *M, SolveReport &rep);
 
-double residual_norm(cudaStream_t st, const OpCtx &ctx, int op, int comp, const double *b, const double *x,
-                     double *r, double two_re, KrylovWork &w, double *divmax);
+// Mixed precision, host loop: FP64 residuals r = b - A64 x and updates
+// x += e, with each correction e from an FP32 BiCGSTAB on A32 e = r
+// (scaled to unit max-norm).  Stops on the same FP64 criterion as
+// bicgstab<double>.
+int solve_ir(cudaStream_t st, const OpT<double> &A64, const OpT<float> &A32, int op, IRWork &w, const double *b,
+             double *x, const SolveParams &prm, Preconditioner<float> *M32, SolveReport &rep);
+
+// Recorded forms: append the solve to the graph being captured on st
+// (aux: two further streams, used to capture the loop bodies) and end
+// with a copy of the device scalars into the work's scal_h.  After the
+// graph has run and st is synchronised, report() gives the outcome and the
+// status code of the host loop.  Launch counts: *fixed kernels outside
+// loops, *per_iter per Krylov iteration, *per_outer per refinement cycle.
+template <typename T>
+int record_bicgstab(cudaStream_t st, const cudaStream_t *aux, const OpT<T> &A, int op, KrylovWork<T> &w, const T *b,
+                    T *x, const SolveParams &prm, Preconditioner<T> *M, int *fixed, int *per_iter);
+int record_ir(cudaStream_t st, const cudaStream_t *aux, const OpT<double> &A64, const OpT<float> &A32, int op,
+              IRWork &w, const double *b, double *x, const SolveParams &prm, Preconditioner<float> *M32, int *fixed,
+              int *per_outer, int *per_iter);
+template <typename T>
+int report(const KrylovWork<T> &w, SolveReport &rep);
+int report(const IRWork &w, SolveReport &rep);
+
+template <typename T>
+void apply_operator(cudaStream_t st, const OpT<T> &A, int op, int comp, const T *x, T *y);
 
 }  // namespace ibm

@@ -1,7 +1,5 @@
 // Geometric multigrid preconditioner for the pressure-Poisson rows (see
-// multigrid.h for the design).  All smoothers are colour-ordered
-// Gauss-Seidel with a fixed colour order, so results are bitwise
-// reproducible run to run.
+// multigrid.h for the design), instantiated in FP64 and FP32.
 #include <algorithm>
 #include <cstdio>
 #include <vector>
@@ -37,125 +35,265 @@ struct Per3 {
     int p[3];
 };
 
+// Every V-cycle kernel returns at once while *gate (when given) is not
+// KS_RUN: the solve it serves has converged.
+#define MG_GATE(gate)                       \
+    if ((gate) && *(gate) != KS_RUN) return;
+
+template <typename T>
+__host__ __device__ inline long long lidx(const MGLevel<T> &L, int I, int J, int K) {
+    return ((long long)I * L.ny + J) * L.nz + K;
+}
+
+// Trilinear correction of fine cell (i, j, k) from coarse level C, over
+// active coarse cells only.
+template <typename T>
+__device__ inline T prolong_value(const MGLevel<T> &C, int i, int j, int k) {
+    const int I = C.cx ? i >> 1 : i, J = C.cy ? j >> 1 : j, K = C.cz ? k >> 1 : k;
+    const int xs[2] = {I, C.po[0][i]}, ys[2] = {J, C.po[1][j]}, zs[2] = {K, C.po[2][k]};
+    const T wx = C.pw[0][i], wy = C.pw[1][j], wz = C.pw[2][k];
+    const T wxs[2] = {wx, (T)1 - wx}, wys[2] = {wy, (T)1 - wy}, wzs[2] = {wz, (T)1 - wz};
+    T acc = 0, ws = 0;
+#pragma unroll
+    for (int a = 0; a < 2; a++)
+#pragma unroll
+        for (int b = 0; b < 2; b++)
+#pragma unroll
+            for (int c = 0; c < 2; c++) {
+                if (xs[a] < 0 || ys[b] < 0 || zs[c] < 0) continue;
+                const long long q = lidx(C, xs[a], ys[b], zs[c]);
+                if (C.diag[q] == (T)0) continue;
+                const T w = wxs[a] * wys[b] * wzs[c];
+                acc += w * C.Z[q];
+                ws += w;
+            }
+    return ws > (T)0 ? acc / ws : (T)0;
+}
+
 // ------------------------------------------------------------ level 0 --
+// One colour pass of Gauss-Seidel on the fine rows.  Without a periodic
+// seam the colours are red/black and each thread takes the cell of its
+// colour in one (k, k+1) pair of MG0_PLANES consecutive planes, loading
+// all of them before any update (no cell of the pass is a neighbour of
+// another: the updated cells share one colour): grid (ceil(nz/64),
+// ceil(ny/8), ceil(nx/MG0_PLANES)) of 32 x 8 threads, no index division.
+// With a seam (4 colours) each thread takes one cell per plane and tests
+// its colour.  init = 1 (colour 0 only, z undefined on entry) applies the
+// pass to z = 0: colour-0 cells get r, every other padded cell 0 (the
+// sweep over all cells then covers the whole array).
+constexpr int MG0_PLANES = 4;
+
+template <typename T>
 __global__ void __launch_bounds__(256)
-k_mg0_color(const OpCtx c, const double *__restrict__ r, double *z, const int color, const Per3 per) {
+k_mg0_color(const OpT<T> c, const T *__restrict__ r, T *__restrict__ z, const int color, const int pairs,
+            const Per3 per, const int *gate) {
+    MG_GATE(gate);
     const Grid &g = c.g;
-    const long long n = (long long)g.nx * g.ny * g.nz;
-    GRID_STRIDE(q, n) {
-        const int k = (int)(q % g.nz);
-        const int j = (int)((q / g.nz) % g.ny);
-        const int i = (int)(q / ((long long)g.nz * g.ny));
-        if (cell_color(i, j, k, g.nx, g.ny, g.nz, per.p) != color) continue;
-        const long long P = cidx(g, i, j, k);
-        const uint8_t fl = c.flag[P];
-        if (fl == GHOST) continue;
-        if (fl != FLUID || (c.bc.p_singular && i == 0 && j == 0 && k == 0)) {
-            z[P] = r[P];
-            continue;
+    const int j = blockIdx.y * 8 + threadIdx.y;
+    const int i0 = blockIdx.z * MG0_PLANES;
+    const long long sx = g.sx, sy = g.sy;
+    // Branch-free: every load of every plane is issued before any update
+    // (cells off the grid or of the other colour read cell (0,0,0) and are
+    // masked at the store), so the loads of all planes overlap.
+    long long Ps[MG0_PLANES];
+    T val[MG0_PLANES];
+    bool upd[MG0_PLANES];
+    const int jj = min(j, g.ny - 1);
+    const T kmy = c.km[1][jj + 2], kpy = c.kp[1][jj + 2];
+#pragma unroll
+    for (int p = 0; p < MG0_PLANES; p++) {
+        const int i = min(i0 + p, g.nx - 1);
+        int k;
+        bool ok = j < g.ny && i0 + p < g.nx;
+        if (pairs) {
+            k = 2 * (blockIdx.x * 32 + threadIdx.x) + ((i + jj + color) & 1);
+        } else {
+            k = blockIdx.x * 32 + threadIdx.x;
+            ok = ok && k < g.nz && cell_color(i, jj, k, g.nx, g.ny, g.nz, per.p) == color;
         }
-        const int I = i + 2, J = j + 2, K = k + 2;
-        const long long sx = g.sx, sy = g.sy;
-        const double nb = c.ax.km[I] * z[P - sx] + c.ax.kp[I] * z[P + sx] + c.ay.km[J] * z[P - sy] +
-                          c.ay.kp[J] * z[P + sy] + c.az.km[K] * z[P - 1] + c.az.kp[K] * z[P + 1];
-        z[P] = r[P] + c.dinv[P] * nb;
+        ok = ok && k < g.nz;
+        k = min(k, g.nz - 1);
+        const long long P = cidx(g, i, jj, k);
+        const uint8_t fl = c.flag[P];
+        const T rv = r[P], dv = c.dinv[P];
+        const T zw = z[P - sx], ze = z[P + sx], zs = z[P - sy], zn = z[P + sy], zd = z[P - 1], zu = z[P + 1];
+        const int I = i + 2, K = k + 2;
+        const T nb = c.km[0][I] * zw + c.kp[0][I] * ze + kmy * zs + kpy * zn + c.km[2][K] * zd + c.kp[2][K] * zu;
+        const bool fluid = fl == FLUID && !(c.p_singular && P == c.pinned);
+        val[p] = fluid ? rv + dv * nb : rv;
+        upd[p] = ok && fl != GHOST;
+        Ps[p] = P;
+    }
+#pragma unroll
+    for (int p = 0; p < MG0_PLANES; p++)
+        if (upd[p]) z[Ps[p]] = val[p];
+}
+
+// The first colour pass of a V-cycle on z = 0, as one pass over the
+// whole padded array: colour-0 interior rows take r (r + dinv * 0, and
+// r for solid and pinned rows), every other cell 0.
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_mg0_init(const OpT<T> c, const T *__restrict__ r, T *__restrict__ z, const Per3 per, const int *gate) {
+    MG_GATE(gate);
+    const Grid &g = c.g;
+    const long long n = g.ncell;
+    GRID_STRIDE(P, n) {
+        int i, j, k;
+        cijk_fast(g, c.fdx, c.fdy, P, i, j, k);
+        T v = 0;
+        if (i >= 0 && i < g.nx && j >= 0 && j < g.ny && k >= 0 && k < g.nz &&
+            cell_color(i, j, k, g.nx, g.ny, g.nz, per.p) == 0 && c.flag[P] != GHOST)
+            v = r[P];
+        z[P] = v;
     }
 }
 
-__global__ void k_mg0_ghost(const OpCtx c, const double *__restrict__ r, const double *__restrict__ z,
-                            const int *__restrict__ gcell, const int ng, double *tmp) {
+// Ghost rows of the smoother, Jacobi-style among ghosts (each reads the
+// values before the pass): a pass into tmp, then a scatter.
+
+template <typename T>
+__device__ __forceinline__ T ghost_value(const OpT<T> &c, const T *__restrict__ r, const T *__restrict__ z, int P) {
+    const int id = c.gid[P];
+    T sum = 0;
+    for (int e = 0; e < 8; e++) {
+        const int q = c.gidx[8 * id + e];
+        if (q >= 0) sum += c.gw[8 * id + e] * z[q];
+    }
+    const T ws = c.gwself[id];
+    const T d = (T)1 - ws;
+    return d >= (T)0.25 ? (r[P] + sum) / d : ws * z[P] + r[P] + sum;
+}
+
+template <typename T>
+__global__ void k_mg0_ghost(const OpT<T> c, const T *__restrict__ r, const T *__restrict__ z,
+                            const int *__restrict__ gcell, const int ng, T *tmp, const int *gate) {
+    MG_GATE(gate);
     GRID_STRIDE(g, (long long)ng) {
         const int P = gcell[g];
         const int id = c.gid[P];
-        double sum = 0;
-        for (int e = 0; e < 8; e++) {
-            const int q = c.gidx[8 * id + e];
-            if (q >= 0) sum += c.gw[8 * id + e] * z[q];
-        }
-        const double ws = c.gwself[id];
-        const double d = 1 - ws;
-        tmp[g] = d >= 0.25 ? (r[P] + sum) / d : ws * z[P] + r[P] + sum;
+        (void)id;
+        tmp[g] = ghost_value(c, r, z, P);
     }
 }
 
-__global__ void k_mg0_ghost_scatter(const int *__restrict__ gcell, const int ng, const double *__restrict__ tmp,
-                                    double *z) {
+template <typename T>
+__global__ void k_mg0_ghost_scatter(const int *__restrict__ gcell, const int ng, const T *__restrict__ tmp, T *z,
+                                    const int *gate) {
+    MG_GATE(gate);
     GRID_STRIDE(g, (long long)ng) z[gcell[g]] = tmp[g];
 }
 
-// Outer boundary rows of the pressure operator, solved for the outer value.
-__global__ void k_mg0_outer(const OpCtx c, const double *__restrict__ r, double *z, const int *__restrict__ outer,
-                            const int nout) {
-    GRID_STRIDE(q, (long long)nout) {
-        const long long P = outer[q];
+// Outer boundary rows of the pressure operator, solved for the outer
+// values.  The row of an outer cell couples it to a partner one coordinate
+// further in (its mirror, or its periodic image): an interior cell for
+// face cells, a face cell for edges, an edge cell for corners.  Each
+// thread follows its cell's chain of partners down to an interior cell and
+// evaluates the rows back up, so every outer value is a function of
+// interior values alone: one launch, no ordering between outer cells, and
+// no thread reads an outer value another thread writes.
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_mg0_outer(const OpT<T> c, const T *__restrict__ r, T *z, const int *__restrict__ outer, const int nout,
+            const int *gate) {
+    MG_GATE(gate);
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nout) return;
+    long long chain[4];
+    int face[4], layer[4];
+    int n = 0;
+    long long Q = outer[t];
+    T v = 0;
+    while (n < 4) {
         int i, j, k, L;
-        cijk(c.g, P, i, j, k);
+        cijk_fast(c.g, c.fdx, c.fdy, Q, i, j, k);
         const int f = owner_face(c.g, i, j, k, L);
-        const BCFace &F = c.bc.f[f];
-        const int axis = face_axis(f);
-        const long long s = axis == 0 ? c.g.sx : axis == 1 ? c.g.sy : 1;
-        const long long m = P + (2 * L - 1) * (face_low(f) ? s : -s);
-        switch (F.type) {
-        case BCT_PRESSURE:
-        case BCT_VELPERIODIC: z[P] = (r[P] - F.dir_m[L - 1] * z[m]) / F.dir_o[L - 1]; break;
-        case BCT_PERIODIC: z[P] = r[P] + z[periodic_image(c.g, i, j, k)]; break;
-        default: z[P] = r[P] + z[m]; break;
+        if (f < 0) {
+            v = z[Q];
+            break;
+        }
+        chain[n] = Q;
+        face[n] = f;
+        layer[n] = L;
+        n++;
+        const BCRow<T> &F = c.bc[f];
+        if (F.type == BCT_PERIODIC) {
+            Q = periodic_image(c.g, i, j, k);
+        } else {
+            const int axis = face_axis(f);
+            const long long s = axis == 0 ? c.g.sx : axis == 1 ? c.g.sy : 1;
+            Q += (2 * L - 1) * (face_low(f) ? s : -s);
         }
     }
+    for (int q = n - 1; q >= 0; q--) {
+        const BCRow<T> &F = c.bc[face[q]];
+        const long long P = chain[q];
+        switch (F.type) {
+        case BCT_PRESSURE:
+        case BCT_VELPERIODIC: v = (r[P] - F.dir_m[layer[q] - 1] * v) / F.dir_o[layer[q] - 1]; break;
+        default: v = r[P] + v; break;
+        }
+    }
+    z[outer[t]] = v;
 }
+
+// 3-D launch over an (nx, ny, nz) box: threads along k, blocks along
+// (k, j) tiles and i, so no thread divides an index.
+constexpr int L3_TK = 32, L3_TJ = 8;
+static inline dim3 l3_grid(int nx, int ny, int nz) {
+    return dim3((unsigned)((nz + L3_TK - 1) / L3_TK), (unsigned)((ny + L3_TJ - 1) / L3_TJ), (unsigned)nx);
+}
+static inline dim3 l3_block() { return dim3(L3_TK, L3_TJ, 1); }
+#define L3_INDEX(I, J, K, NY, NZ)                                      \
+    const int K = blockIdx.x * L3_TK + threadIdx.x;                     \
+    const int J = blockIdx.y * L3_TJ + threadIdx.y;                     \
+    const int I = blockIdx.z;                                           \
+    if (K >= (NZ) || J >= (NY)) return;
 
 // Residual of the fine normalised rows, scaled to conductance form
 // (Vol * coeffsum * r) and summed into the level-1 cells.
+template <typename T>
 __global__ void __launch_bounds__(256)
-k_mg0_restrict(const OpCtx c, const double *__restrict__ r, const double *__restrict__ z, MGLevel<double> L1) {
+k_mg0_restrict(const OpT<T> c, const T *__restrict__ r, const T *__restrict__ z, MGLevel<T> L1, const int *gate) {
+    MG_GATE(gate);
+    L3_INDEX(I, J, K, L1.ny, L1.nz);
     const Grid &g = c.g;
-    GRID_STRIDE(q, L1.n) {
-        const int K = (int)(q % L1.nz);
-        const int J = (int)((q / L1.nz) % L1.ny);
-        const int I = (int)(q / ((long long)L1.nz * L1.ny));
-        double acc = 0;
-        const int i0 = L1.cx ? 2 * I : I, i1 = L1.cx ? min(2 * I + 1, g.nx - 1) : I;
-        const int j0 = L1.cy ? 2 * J : J, j1 = L1.cy ? min(2 * J + 1, g.ny - 1) : J;
-        const int k0 = L1.cz ? 2 * K : K, k1 = L1.cz ? min(2 * K + 1, g.nz - 1) : K;
-        for (int i = i0; i <= i1; i++)
-            for (int j = j0; j <= j1; j++)
-                for (int k = k0; k <= k1; k++) {
-                    const long long P = cidx(g, i, j, k);
-                    if (c.flag[P] != FLUID || (c.bc.p_singular && i == 0 && j == 0 && k == 0)) continue;
-                    const int Ii = i + 2, Jj = j + 2, Kk = k + 2;
-                    const double kW = c.ax.km[Ii], kE = c.ax.kp[Ii], kS = c.ay.km[Jj], kN = c.ay.kp[Jj];
-                    const double kD = c.az.km[Kk], kU = c.az.kp[Kk];
-                    const double nb = kW * z[P - g.sx] + kE * z[P + g.sx] + kS * z[P - g.sy] + kN * z[P + g.sy] +
-                                      kD * z[P - 1] + kU * z[P + 1];
-                    const double res = r[P] - (z[P] - c.dinv[P] * nb);
-                    const double vol = c.ax.d[Ii] * c.ay.d[Jj] * c.az.d[Kk];
-                    acc += vol * (kN + kE + kS + kW + kD + kU) * res;
-                }
-        L1.R[q] = acc;
-    }
+    T acc = 0;
+    const int i0 = L1.cx ? 2 * I : I, i1 = L1.cx ? min(2 * I + 1, g.nx - 1) : I;
+    const int j0 = L1.cy ? 2 * J : J, j1 = L1.cy ? min(2 * J + 1, g.ny - 1) : J;
+    const int k0 = L1.cz ? 2 * K : K, k1 = L1.cz ? min(2 * K + 1, g.nz - 1) : K;
+    for (int i = i0; i <= i1; i++)
+        for (int j = j0; j <= j1; j++)
+            for (int k = k0; k <= k1; k++) {
+                const long long P = cidx(g, i, j, k);
+                if (c.flag[P] != FLUID || (c.p_singular && P == c.pinned)) continue;
+                const int Ii = i + 2, Jj = j + 2, Kk = k + 2;
+                const T nb = c.km[0][Ii] * z[P - g.sx] + c.kp[0][Ii] * z[P + g.sx] + c.km[1][Jj] * z[P - g.sy] +
+                             c.kp[1][Jj] * z[P + g.sy] + c.km[2][Kk] * z[P - 1] + c.kp[2][Kk] * z[P + 1];
+                const T res = r[P] - (z[P] - c.dinv[P] * nb);
+                const T vol = c.d[0][Ii] * c.d[1][Jj] * c.d[2][Kk];
+                acc += vol * (c.ks[0][Ii] + c.ks[1][Jj] + c.ks[2][Kk]) * res;
+            }
+    L1.R[lidx(L1, I, J, K)] = acc;
 }
 
+template <typename T>
 __global__ void __launch_bounds__(256)
-k_mg0_prolong(const OpCtx c, double *z, const MGLevel<double> L1) {
-    const Grid &g = c.g;
-    const long long n = (long long)g.nx * g.ny * g.nz;
-    GRID_STRIDE(q, n) {
-        const int k = (int)(q % g.nz);
-        const int j = (int)((q / g.nz) % g.ny);
-        const int i = (int)(q / ((long long)g.nz * g.ny));
-        const long long P = cidx(g, i, j, k);
-        const uint8_t fl = c.flag[P];
-        if (fl != FLUID && fl != GHOST) continue;
-        if (c.bc.p_singular && i == 0 && j == 0 && k == 0) continue;
-        const int I = L1.cx ? i >> 1 : i, J = L1.cy ? j >> 1 : j, K = L1.cz ? k >> 1 : k;
-        z[P] += L1.Z[((long long)I * L1.ny + J) * L1.nz + K];
-    }
+k_mg0_prolong(const OpT<T> c, T *z, const MGLevel<T> L1, const int *gate) {
+    MG_GATE(gate);
+    L3_INDEX(i, j, k, c.g.ny, c.g.nz);
+    const long long P = cidx(c.g, i, j, k);
+    const uint8_t fl = c.flag[P];
+    if (fl != FLUID && fl != GHOST) return;
+    if (c.p_singular && P == c.pinned) return;
+    z[P] += prolong_value(L1, i, j, k);
 }
 
 // ------------------------------------------------------ level building --
-// Level 1 from the fine grid: conductances Vol*k of fluid-fluid faces,
-// pressure-Dirichlet boundary conductances, periodic wraps.
-__global__ void k_mg_build1(const OpCtx c, MGLevel<double> L, double *Gx, double *Gy, double *Gz, const Per3 per) {
+// Level 1 from the fine grid (FP64): conductances Vol*k of fluid-fluid
+// faces, pressure-Dirichlet boundary conductances, periodic wraps.
+__global__ void k_mg_build1(const OpT<double> c, MGLevel<double> L, double *Gx, double *Gy, double *Gz,
+                            const Per3 per) {
     const Grid &g = c.g;
     GRID_STRIDE(q, L.n) {
         const int K = (int)(q % L.nz);
@@ -165,39 +303,36 @@ __global__ void k_mg_build1(const OpCtx c, MGLevel<double> L, double *Gx, double
         const int j0 = L.cy ? 2 * J : J, j1 = L.cy ? min(2 * J + 1, g.ny - 1) : J;
         const int k0 = L.cz ? 2 * K : K, k1 = L.cz ? min(2 * K + 1, g.nz - 1) : K;
         auto active = [&](int i, int j, int k) {
-            return c.flag[cidx(g, i, j, k)] == FLUID && !(c.bc.p_singular && i == 0 && j == 0 && k == 0);
+            const long long P = cidx(g, i, j, k);
+            return c.flag[P] == FLUID && !(c.p_singular && P == c.pinned);
         };
-        auto vol = [&](int i, int j, int k) { return c.ax.d[i + 2] * c.ay.d[j + 2] * c.az.d[k + 2]; };
+        auto dirf = [](int t) { return t == BCT_PRESSURE || t == BCT_VELPERIODIC; };
         double tx = 0, ty = 0, tz = 0, gx = 0, gy = 0, gz = 0;
         for (int i = i0; i <= i1; i++)
             for (int j = j0; j <= j1; j++)
                 for (int k = k0; k <= k1; k++) {
                     if (!active(i, j, k)) continue;
-                    const double v = vol(i, j, k);
-                    // Low x face of the coarse cell: fine faces at i == i0.
+                    const double v = c.d[0][i + 2] * c.d[1][j + 2] * c.d[2][k + 2];
                     if (i == i0) {
-                        if (i > 0) { if (active(i - 1, j, k)) tx += v * c.ax.km[i + 2]; }
-                        else if (per.p[0] && g.nx > 1) { if (active(g.nx - 1, j, k)) tx += v * c.ax.km[2]; }
+                        if (i > 0) { if (active(i - 1, j, k)) tx += v * c.km[0][i + 2]; }
+                        else if (per.p[0] && g.nx > 1) { if (active(g.nx - 1, j, k)) tx += v * c.km[0][2]; }
                     }
                     if (j == j0) {
-                        if (j > 0) { if (active(i, j - 1, k)) ty += v * c.ay.km[j + 2]; }
-                        else if (per.p[1] && g.ny > 1) { if (active(i, g.ny - 1, k)) ty += v * c.ay.km[2]; }
+                        if (j > 0) { if (active(i, j - 1, k)) ty += v * c.km[1][j + 2]; }
+                        else if (per.p[1] && g.ny > 1) { if (active(i, g.ny - 1, k)) ty += v * c.km[1][2]; }
                     }
                     if (k == k0) {
-                        if (k > 0) { if (active(i, j, k - 1)) tz += v * c.az.km[k + 2]; }
-                        else if (per.p[2] && g.nz > 1) { if (active(i, j, g.nz - 1)) tz += v * c.az.km[2]; }
+                        if (k > 0) { if (active(i, j, k - 1)) tz += v * c.km[2][k + 2]; }
+                        else if (per.p[2] && g.nz > 1) { if (active(i, j, g.nz - 1)) tz += v * c.km[2][2]; }
                     }
-                    // Pressure-Dirichlet boundaries (homogeneous fold of the
-                    // interpolation rows).
-                    const BCFace &W = c.bc.f[F_W], &E = c.bc.f[F_E], &S = c.bc.f[F_S], &N = c.bc.f[F_N];
-                    const BCFace &D = c.bc.f[F_D], &U = c.bc.f[F_U];
-                    auto dir = [](int t) { return t == BCT_PRESSURE || t == BCT_VELPERIODIC; };
-                    if (i == 0 && dir(W.type)) gx += v * c.ax.km[2] * (1 + W.dir_m[0] / W.dir_o[0]);
-                    if (i == g.nx - 1 && dir(E.type)) gx += v * c.ax.kp[g.nx + 1] * (1 + E.dir_m[0] / E.dir_o[0]);
-                    if (j == 0 && dir(S.type)) gy += v * c.ay.km[2] * (1 + S.dir_m[0] / S.dir_o[0]);
-                    if (j == g.ny - 1 && dir(N.type)) gy += v * c.ay.kp[g.ny + 1] * (1 + N.dir_m[0] / N.dir_o[0]);
-                    if (k == 0 && dir(D.type)) gz += v * c.az.km[2] * (1 + D.dir_m[0] / D.dir_o[0]);
-                    if (k == g.nz - 1 && dir(U.type)) gz += v * c.az.kp[g.nz + 1] * (1 + U.dir_m[0] / U.dir_o[0]);
+                    const BCRow<double> &W = c.bc[F_W], &E = c.bc[F_E], &S = c.bc[F_S], &N = c.bc[F_N];
+                    const BCRow<double> &D = c.bc[F_D], &U = c.bc[F_U];
+                    if (i == 0 && dirf(W.type)) gx += v * c.km[0][2] * (1 + W.dir_m[0] / W.dir_o[0]);
+                    if (i == g.nx - 1 && dirf(E.type)) gx += v * c.kp[0][g.nx + 1] * (1 + E.dir_m[0] / E.dir_o[0]);
+                    if (j == 0 && dirf(S.type)) gy += v * c.km[1][2] * (1 + S.dir_m[0] / S.dir_o[0]);
+                    if (j == g.ny - 1 && dirf(N.type)) gy += v * c.kp[1][g.ny + 1] * (1 + N.dir_m[0] / N.dir_o[0]);
+                    if (k == 0 && dirf(D.type)) gz += v * c.km[2][2] * (1 + D.dir_m[0] / D.dir_o[0]);
+                    if (k == g.nz - 1 && dirf(U.type)) gz += v * c.kp[2][g.nz + 1] * (1 + U.dir_m[0] / U.dir_o[0]);
                 }
         const double fx = L.cx ? 0.5 : 1.0, fy = L.cy ? 0.5 : 1.0, fz = L.cz ? 0.5 : 1.0;
         L.Tx[q] = (I == 0 && L.nx == 1) ? 0.0 : fx * tx;
@@ -209,7 +344,7 @@ __global__ void k_mg_build1(const OpCtx c, MGLevel<double> L, double *Gx, double
     }
 }
 
-// Coarse level c from level f.
+// Coarse level c from level f (FP64).
 __global__ void k_mg_buildc(const MGLevel<double> F, const double *__restrict__ fGx, const double *__restrict__ fGy,
                             const double *__restrict__ fGz, MGLevel<double> C, double *Gx, double *Gy, double *Gz) {
     GRID_STRIDE(q, C.n) {
@@ -223,7 +358,7 @@ __global__ void k_mg_buildc(const MGLevel<double> F, const double *__restrict__ 
         for (int i = i0; i <= i1; i++)
             for (int j = j0; j <= j1; j++)
                 for (int k = k0; k <= k1; k++) {
-                    const long long f = ((long long)i * F.ny + j) * F.nz + k;
+                    const long long f = lidx(F, i, j, k);
                     if (i == i0) tx += F.Tx[f];
                     if (j == j0) ty += F.Ty[f];
                     if (k == k0) tz += F.Tz[f];
@@ -241,21 +376,18 @@ __global__ void k_mg_buildc(const MGLevel<double> F, const double *__restrict__ 
     }
 }
 
-__host__ __device__ inline long long lidx(const MGLevel<double> &L, int I, int J, int K) {
-    return ((long long)I * L.ny + J) * L.nz + K;
-}
-
 // Couplings of a coarse cell: calls fn(neighbour index, conductance).
-template <typename Fn>
-__device__ inline void for_neighbours(const MGLevel<double> &L, int I, int J, int K, const int *per, Fn fn) {
+template <typename T, typename Fn>
+__device__ inline void for_neighbours(const MGLevel<T> &L, int I, int J, int K, const int *per, Fn fn) {
     const long long q = lidx(L, I, J, K);
-    if (I > 0) fn(q - (long long)L.ny * L.nz, L.Tx[q]);
+    const long long sx = (long long)L.ny * L.nz, sy = L.nz;
+    if (I > 0) fn(q - sx, L.Tx[q]);
     else if (per[0] && L.nx > 1) fn(lidx(L, L.nx - 1, J, K), L.Tx[q]);
-    if (I < L.nx - 1) fn(q + (long long)L.ny * L.nz, L.Tx[q + (long long)L.ny * L.nz]);
+    if (I < L.nx - 1) fn(q + sx, L.Tx[q + sx]);
     else if (per[0] && L.nx > 1) fn(lidx(L, 0, J, K), L.Tx[lidx(L, 0, J, K)]);
-    if (J > 0) fn(q - L.nz, L.Ty[q]);
+    if (J > 0) fn(q - sy, L.Ty[q]);
     else if (per[1] && L.ny > 1) fn(lidx(L, I, L.ny - 1, K), L.Ty[q]);
-    if (J < L.ny - 1) fn(q + L.nz, L.Ty[q + L.nz]);
+    if (J < L.ny - 1) fn(q + sy, L.Ty[q + sy]);
     else if (per[1] && L.ny > 1) fn(lidx(L, I, 0, K), L.Ty[lidx(L, I, 0, K)]);
     if (K > 0) fn(q - 1, L.Tz[q]);
     else if (per[2] && L.nz > 1) fn(lidx(L, I, J, L.nz - 1), L.Tz[q]);
@@ -275,169 +407,297 @@ __global__ void k_mg_diag(MGLevel<double> L, const double *__restrict__ Gx, cons
     }
 }
 
+template <typename T>
+__global__ void k_convert(const double *__restrict__ a, T *b, long long n) {
+    GRID_STRIDE(q, n) b[q] = (T)a[q];
+}
+
 // ----------------------------------------------------- coarse kernels --
-__device__ inline void coarse_relax(const MGLevel<double> &L, long long q, const int *per) {
-    const int K = (int)(q % L.nz);
-    const int J = (int)((q / L.nz) % L.ny);
-    const int I = (int)(q / ((long long)L.nz * L.ny));
-    const double d = L.diag[q];
-    if (d == 0.0) {
-        L.Z[q] = 0.0;
+template <typename T>
+__device__ inline void coarse_relax(const MGLevel<T> &L, int I, int J, int K, const int *per) {
+    const long long q = lidx(L, I, J, K);
+    const T d = L.diag[q];
+    if (d == (T)0) {
+        L.Z[q] = 0;
         return;
     }
-    double s = L.R[q];
-    for_neighbours(L, I, J, K, per, [&](long long m, double t) { s += t * L.Z[m]; });
+    T s = L.R[q];
+    for_neighbours(L, I, J, K, per, [&](long long m, T t) { s += t * L.Z[m]; });
     L.Z[q] = s / d;
 }
 
-__device__ inline double coarse_residual(const MGLevel<double> &L, long long q, const int *per) {
-    const int K = (int)(q % L.nz);
-    const int J = (int)((q / L.nz) % L.ny);
-    const int I = (int)(q / ((long long)L.nz * L.ny));
-    if (L.diag[q] == 0.0) return 0.0;
-    double s = L.R[q] - L.diag[q] * L.Z[q];
-    for_neighbours(L, I, J, K, per, [&](long long m, double t) { s += t * L.Z[m]; });
+template <typename T>
+__device__ inline T coarse_residual(const MGLevel<T> &L, int I, int J, int K, const int *per) {
+    const long long q = lidx(L, I, J, K);
+    if (L.diag[q] == (T)0) return 0;
+    T s = L.R[q] - L.diag[q] * L.Z[q];
+    for_neighbours(L, I, J, K, per, [&](long long m, T t) { s += t * L.Z[m]; });
     return s;
 }
 
-__device__ inline int lcolor(const MGLevel<double> &L, long long q, const int *per) {
-    const int K = (int)(q % L.nz);
-    const int J = (int)((q / L.nz) % L.ny);
-    const int I = (int)(q / ((long long)L.nz * L.ny));
-    return cell_color(I, J, K, L.nx, L.ny, L.nz, per);
+// Colours a level needs: 4 with a seam on an odd periodic axis, else 2.
+template <typename T>
+__host__ __device__ inline int level_colors(const MGLevel<T> &L, const int *per) {
+    const bool seam = (per[0] && (L.nx & 1) && L.nx > 1) || (per[1] && (L.ny & 1) && L.ny > 1) ||
+                      (per[2] && (L.nz & 1) && L.nz > 1);
+    return seam ? 4 : 2;
 }
 
-__global__ void k_mgc_color(MGLevel<double> L, const int color, const Per3 per) {
-    GRID_STRIDE(q, L.n) {
-        if (lcolor(L, q, per.p) == color) coarse_relax(L, q, per.p);
+template <typename T>
+__device__ inline T coarse_restrict_value(const MGLevel<T> &F, const MGLevel<T> &C, int I, int J, int K,
+                                          const int *per) {
+    const int i0 = C.cx ? 2 * I : I, i1 = C.cx ? min(2 * I + 1, F.nx - 1) : I;
+    const int j0 = C.cy ? 2 * J : J, j1 = C.cy ? min(2 * J + 1, F.ny - 1) : J;
+    const int k0 = C.cz ? 2 * K : K, k1 = C.cz ? min(2 * K + 1, F.nz - 1) : K;
+    T acc = 0;
+    for (int i = i0; i <= i1; i++)
+        for (int j = j0; j <= j1; j++)
+            for (int k = k0; k <= k1; k++) acc += coarse_residual(F, i, j, k, per);
+    return acc;
+}
+
+template <typename T>
+__global__ void k_fill0(T *z, const long long n, const int *gate) {
+    MG_GATE(gate);
+    GRID_STRIDE(q, n) z[q] = 0;
+}
+
+
+// The first colour pass of a coarse level on Z = 0: colour-0 cells take
+// R / diag (0 where inactive), every other cell 0.
+template <typename T>
+__global__ void __launch_bounds__(256) k_mgc_init(MGLevel<T> L, const Per3 per, const int *gate) {
+    MG_GATE(gate);
+    L3_INDEX(I, J, K, L.ny, L.nz);
+    const long long q = lidx(L, I, J, K);
+    const T d = L.diag[q];
+    L.Z[q] = (cell_color(I, J, K, L.nx, L.ny, L.nz, per.p) == 0 && d != (T)0) ? L.R[q] / d : (T)0;
+}
+
+// Branch-free relaxation of coarse cell (I, J, K) on a level without
+// periodic axes: every load is issued up front (low-face conductances are
+// 0 on the first cell of an axis; high neighbours off the level are read
+// at the cell itself and weighted 0).
+template <typename T>
+__device__ __forceinline__ void coarse_relax_open(const MGLevel<T> &L, int I, int J, int K) {
+    const long long sx = (long long)L.ny * L.nz, sy = L.nz;
+    const long long q = lidx(L, I, J, K);
+    const bool he = I < L.nx - 1, hn = J < L.ny - 1, hu = K < L.nz - 1;
+    const long long qw = I > 0 ? q - sx : q, qe = he ? q + sx : q;
+    const long long qs = J > 0 ? q - sy : q, qn = hn ? q + sy : q;
+    const long long qd = K > 0 ? q - 1 : q, qu = hu ? q + 1 : q;
+    const T d = L.diag[q], R = L.R[q];
+    const T tw = L.Tx[q], te = L.Tx[qe], ts = L.Ty[q], tn = L.Ty[qn], td = L.Tz[q], tu = L.Tz[qu];
+    const T zw = L.Z[qw], ze = L.Z[qe], zs = L.Z[qs], zn = L.Z[qn], zd = L.Z[qd], zu = L.Z[qu];
+    T s = R;
+    s += tw * zw;
+    s += (he ? te : (T)0) * ze;
+    s += ts * zs;
+    s += (hn ? tn : (T)0) * zn;
+    s += td * zd;
+    s += (hu ? tu : (T)0) * zu;
+    L.Z[q] = d == (T)0 ? (T)0 : s / d;
+}
+
+// One colour pass on a coarse level; k pairs as on the fine grid when the
+// level has no periodic seam (pairs = 1, grid ceil(nz/64) wide in k).
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_mgc_color(MGLevel<T> L, const int color, const int pairs, const Per3 per, const int *gate) {
+    MG_GATE(gate);
+    const int I = blockIdx.z, J = blockIdx.y * L3_TJ + threadIdx.y;
+    const bool open = !per.p[0] && !per.p[1] && !per.p[2];
+    if (pairs) {
+        const int K = 2 * (blockIdx.x * L3_TK + threadIdx.x) + ((I + J + color) & 1);
+        if (J < L.ny && K < L.nz) {
+            if (open) coarse_relax_open(L, I, J, K);
+            else coarse_relax(L, I, J, K, per.p);
+        }
+    } else {
+        const int K = blockIdx.x * L3_TK + threadIdx.x;
+        if (J < L.ny && K < L.nz && cell_color(I, J, K, L.nx, L.ny, L.nz, per.p) == color)
+            coarse_relax(L, I, J, K, per.p);
     }
 }
 
-__global__ void k_mgc_restrict(const MGLevel<double> F, MGLevel<double> C, const Per3 per) {
-    GRID_STRIDE(q, C.n) {
-        const int K = (int)(q % C.nz);
-        const int J = (int)((q / C.nz) % C.ny);
-        const int I = (int)(q / ((long long)C.nz * C.ny));
-        const int i0 = C.cx ? 2 * I : I, i1 = C.cx ? min(2 * I + 1, F.nx - 1) : I;
-        const int j0 = C.cy ? 2 * J : J, j1 = C.cy ? min(2 * J + 1, F.ny - 1) : J;
-        const int k0 = C.cz ? 2 * K : K, k1 = C.cz ? min(2 * K + 1, F.nz - 1) : K;
-        double acc = 0;
-        for (int i = i0; i <= i1; i++)
-            for (int j = j0; j <= j1; j++)
-                for (int k = k0; k <= k1; k++) acc += coarse_residual(F, lidx(F, i, j, k), per.p);
-        C.R[q] = acc;
-    }
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_mgc_restrict(const MGLevel<T> F, MGLevel<T> C, const Per3 per, const int *gate) {
+    MG_GATE(gate);
+    L3_INDEX(I, J, K, C.ny, C.nz);
+    C.R[lidx(C, I, J, K)] = coarse_restrict_value(F, C, I, J, K, per.p);
 }
 
-__global__ void k_mgc_prolong(const MGLevel<double> C, MGLevel<double> F) {
-    GRID_STRIDE(q, F.n) {
-        if (F.diag[q] == 0.0) continue;
-        const int K = (int)(q % F.nz);
-        const int J = (int)((q / F.nz) % F.ny);
-        const int I = (int)(q / ((long long)F.nz * F.ny));
-        F.Z[q] += C.Z[lidx(C, C.cx ? I >> 1 : I, C.cy ? J >> 1 : J, C.cz ? K >> 1 : K)];
-    }
+template <typename T>
+__global__ void __launch_bounds__(256) k_mgc_prolong(const MGLevel<T> C, MGLevel<T> F, const int *gate) {
+    MG_GATE(gate);
+    L3_INDEX(I, J, K, F.ny, F.nz);
+    const long long q = lidx(F, I, J, K);
+    if (F.diag[q] == (T)0) return;
+    F.Z[q] += prolong_value(C, I, J, K);
 }
 
-__global__ void k_zero(double *a, long long n) { GRID_STRIDE(q, n) a[q] = 0.0; }
+// Whole V-cycle over levels [first, nlev) inside one thread block, with
+// every level's arrays copied into shared memory and one thread per cell
+// (levels of at most TAIL_THREADS cells).  R of level `first` is read from
+// global memory and its Z written back; the prolongation tables stay in
+// global memory.
+constexpr int TAIL_THREADS = 1024;
 
-// Whole V-cycle over levels [first, nlev) inside one thread block.  R of
-// level `first` is set; Z of level `first` is produced.
-__global__ void __launch_bounds__(1024)
-k_mg_tail(const MGLevel<double> *__restrict__ lv, const int first, const int nlev, const int nu1, const int nu2,
-          const int csweeps, const Per3 per) {
-    const int tid = threadIdx.x, nt = blockDim.x;
+template <typename T>
+__global__ void __launch_bounds__(TAIL_THREADS)
+k_mg_tail(const MGLevel<T> *__restrict__ lv, const int first, const int nlev, const int nu1, const int nu2,
+          const int csweeps, const Per3 per, const int *gate) {
+    MG_GATE(gate);
+    extern __shared__ __align__(16) unsigned char tail_smem[];
+    constexpr int MAXL = 16;
+    __shared__ MGLevel<T> loc[MAXL];
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        T *q = reinterpret_cast<T *>(tail_smem);
+        for (int l = first; l < nlev; l++) {
+            MGLevel<T> L = lv[l];
+            const long long n = L.n;
+            L.Tx = q; q += n;
+            L.Ty = q; q += n;
+            L.Tz = q; q += n;
+            L.diag = q; q += n;
+            L.R = q; q += n;
+            L.Z = q; q += n;
+            loc[l - first] = L;
+        }
+    }
+    __syncthreads();
     for (int l = first; l < nlev; l++) {
-        const MGLevel<double> L = lv[l];
-        for (long long q = tid; q < L.n; q += nt) L.Z[q] = 0.0;
-        __syncthreads();
-        const int sweeps = (l == nlev - 1) ? csweeps : nu1;
-        for (int s = 0; s < sweeps; s++)
-            for (int col = 0; col < 4; col++) {
-                for (long long q = tid; q < L.n; q += nt)
-                    if (lcolor(L, q, per.p) == col) coarse_relax(L, q, per.p);
+        const MGLevel<T> &G = lv[l], &L = loc[l - first];
+        if (tid < L.n) {
+            L.Tx[tid] = G.Tx[tid];
+            L.Ty[tid] = G.Ty[tid];
+            L.Tz[tid] = G.Tz[tid];
+            L.diag[tid] = G.diag[tid];
+            L.R[tid] = l == first ? G.R[tid] : (T)0;
+            L.Z[tid] = 0;
+        }
+    }
+    __syncthreads();
+    // This thread's cell on level l.
+    auto cell = [&](const MGLevel<T> &L, int &I, int &J, int &K) {
+        const int nyz = L.ny * L.nz;
+        I = tid / nyz;
+        const int rem = tid - I * nyz;
+        J = rem / L.nz;
+        K = rem - J * L.nz;
+        return tid < L.n;
+    };
+    auto sweep = [&](const MGLevel<T> &L, int nsw) {
+        int I, J, K;
+        const bool own = cell(L, I, J, K);
+        const int col = own ? cell_color(I, J, K, L.nx, L.ny, L.nz, per.p) : -1;
+        const int ncol = level_colors(L, per.p);
+        for (int s = 0; s < nsw; s++)
+            for (int c = 0; c < ncol; c++) {
+                if (col == c) coarse_relax(L, I, J, K, per.p);
                 __syncthreads();
             }
+    };
+    for (int l = first; l < nlev; l++) {
+        const MGLevel<T> &L = loc[l - first];
+        sweep(L, l == nlev - 1 ? csweeps : nu1);
         if (l < nlev - 1) {
-            const MGLevel<double> C = lv[l + 1];
-            for (long long q = tid; q < C.n; q += nt) {
-                const int K = (int)(q % C.nz);
-                const int J = (int)((q / C.nz) % C.ny);
-                const int I = (int)(q / ((long long)C.nz * C.ny));
-                const int i0 = C.cx ? 2 * I : I, i1 = C.cx ? min(2 * I + 1, L.nx - 1) : I;
-                const int j0 = C.cy ? 2 * J : J, j1 = C.cy ? min(2 * J + 1, L.ny - 1) : J;
-                const int k0 = C.cz ? 2 * K : K, k1 = C.cz ? min(2 * K + 1, L.nz - 1) : K;
-                double acc = 0;
-                for (int i = i0; i <= i1; i++)
-                    for (int j = j0; j <= j1; j++)
-                        for (int k = k0; k <= k1; k++) acc += coarse_residual(L, lidx(L, i, j, k), per.p);
-                C.R[q] = acc;
-            }
+            const MGLevel<T> &C = loc[l + 1 - first];
+            int I, J, K;
+            if (cell(C, I, J, K)) C.R[tid] = coarse_restrict_value(L, C, I, J, K, per.p);
             __syncthreads();
         }
     }
     for (int l = nlev - 2; l >= first; l--) {
-        const MGLevel<double> L = lv[l], C = lv[l + 1];
-        for (long long q = tid; q < L.n; q += nt) {
-            if (L.diag[q] == 0.0) continue;
-            const int K = (int)(q % L.nz);
-            const int J = (int)((q / L.nz) % L.ny);
-            const int I = (int)(q / ((long long)L.nz * L.ny));
-            L.Z[q] += C.Z[lidx(C, C.cx ? I >> 1 : I, C.cy ? J >> 1 : J, C.cz ? K >> 1 : K)];
-        }
+        const MGLevel<T> &L = loc[l - first], &C = loc[l + 1 - first];
+        int I, J, K;
+        if (cell(L, I, J, K) && L.diag[tid] != (T)0) L.Z[tid] += prolong_value(C, I, J, K);
         __syncthreads();
-        for (int s = 0; s < nu2; s++)
-            for (int col = 0; col < 4; col++) {
-                for (long long q = tid; q < L.n; q += nt)
-                    if (lcolor(L, q, per.p) == col) coarse_relax(L, q, per.p);
-                __syncthreads();
-            }
+        sweep(L, nu2);
     }
+    const MGLevel<T> &G = lv[first], &L = loc[0];
+    if (tid < L.n) G.Z[tid] = L.Z[tid];
+}
+
+// Shared memory the tail kernel needs for levels [first, nlev).
+template <typename T>
+static size_t tail_bytes(const std::vector<MGLevel<T>> &lv, int first) {
+    size_t b = 0;
+    for (int l = first; l < (int)lv.size(); l++) b += 6 * sizeof(T) * (size_t)lv[l].n;
+    return b;
 }
 
 // ------------------------------------------------------------- host --
-GMG::~GMG() {
+// Prolongation tables of one axis: fine centres xf (fine faces ff, nf
+// cells) into coarse centres (coarse faces cf, nc cells).
+static void prolong_axis(const std::vector<double> &ff, const std::vector<double> &cf, bool coarsened, bool periodic,
+                         std::vector<int> &po, std::vector<double> &pw) {
+    const int nf = (int)ff.size() - 1, nc = (int)cf.size() - 1;
+    po.assign(nf, -1);
+    pw.assign(nf, 1.0);
+    if (!coarsened) return;
+    std::vector<double> cc(nc);
+    for (int I = 0; I < nc; I++) cc[I] = 0.5 * (cf[I] + cf[I + 1]);
+    const double Lp = cf[nc] - cf[0];
+    for (int i = 0; i < nf; i++) {
+        const double x = 0.5 * (ff[i] + ff[i + 1]);
+        const int I = i >> 1;
+        int o = x < cc[I] ? I - 1 : I + 1;
+        double co;
+        if (o < 0 || o >= nc) {
+            if (!periodic || nc < 2) continue;
+            if (o < 0) {
+                o = nc - 1;
+                co = cc[nc - 1] - Lp;
+            } else {
+                o = 0;
+                co = cc[0] + Lp;
+            }
+        } else {
+            co = cc[o];
+        }
+        po[i] = o;
+        pw[i] = (x - co) / (cc[I] - co);
+    }
+}
+
+template <typename T>
+GMG<T>::~GMG() {
     for (void *p : allocs_) cudaFree(p);
 }
 
-int GMG::setup(cudaStream_t s, const OpCtx &ctx, const int *ghost_cell, int nghost, double, double,
-               const GMGConfig &cfg) {
-    ctx_ = ctx;
+template <typename T>
+int GMG<T>::setup(cudaStream_t s, const OpT<double> &A64, const OpT<T> &A, const int *ghost_cell, int nghost,
+                  const MGGeometry &geom, const GMGConfig &cfg) {
+    A_ = A;
     cfg_ = cfg;
     ghost_cell_ = ghost_cell;
     nghost_ = nghost;
-    const Grid &g = ctx.g;
-    per_[0] = ctx.bc.f[F_W].type == BCT_PERIODIC;
-    per_[1] = ctx.bc.f[F_S].type == BCT_PERIODIC;
-    per_[2] = ctx.bc.f[F_D].type == BCT_PERIODIC;
-    auto dalloc = [&](size_t bytes) -> void * {
+    const Grid &g = A.g;
+    per_[0] = A.bc[F_W].type == BCT_PERIODIC;
+    per_[1] = A.bc[F_S].type == BCT_PERIODIC;
+    per_[2] = A.bc[F_D].type == BCT_PERIODIC;
+    std::vector<void *> tmp;
+    auto dalloc = [&](size_t bytes, bool keep) -> void * {
         void *p = nullptr;
-        if (cudaMalloc(&p, bytes) != cudaSuccess) return nullptr;
-        cudaMemsetAsync(p, 0, bytes, s);
-        allocs_.push_back(p);
+        if (cudaMalloc(&p, bytes ? bytes : 16) != cudaSuccess) return nullptr;
+        cudaMemsetAsync(p, 0, bytes ? bytes : 16, s);
+        (keep ? allocs_ : tmp).push_back(p);
         return p;
     };
-    if (nghost > 0) ghost_tmp_ = (double *)dalloc(sizeof(double) * nghost);
-    // Outer-cell list.
-    std::vector<int> outer;
-    for (int i = -2; i < g.nx + 2; i++)
-        for (int j = -2; j < g.ny + 2; j++)
-            for (int k = -2; k < g.nz + 2; k++) {
-                int L;
-                if (owner_face(g, i, j, k, L) >= 0) outer.push_back((int)cidx(g, i, j, k));
-            }
-    nouter_ = (int)outer.size();
-    outer_ = (int *)dalloc(sizeof(int) * std::max(1, nouter_));
-    cudaMemcpyAsync(outer_, outer.data(), sizeof(int) * nouter_, cudaMemcpyHostToDevice, s);
+    if (nghost > 0) ghost_tmp_ = (T *)dalloc(sizeof(T) * nghost, true);
 
-    // Level dimensions.
-    int nx = g.nx, ny = g.ny, nz = g.nz;
-    std::vector<double *> G;  // Gx,Gy,Gz per level
     Per3 per{{per_[0], per_[1], per_[2]}};
+    int nx = g.nx, ny = g.ny, nz = g.nz;
+    std::vector<double> faces[3] = {geom.f[0], geom.f[1], geom.f[2]};
+    std::vector<MGLevel<double>> lv64;
+    std::vector<double *> G;
     while (true) {
         const bool cx = nx >= 2, cy = ny >= 2, cz = nz >= 2;
         if (!cx && !cy && !cz) break;
-        if ((long long)nx * ny * nz <= 64 && !levels_.empty()) break;
+        if ((long long)nx * ny * nz <= 64 && !lv64.empty()) break;
         MGLevel<double> L{};
         L.cx = cx; L.cy = cy; L.cz = cz;
         L.nx = cx ? (nx + 1) / 2 : nx;
@@ -445,85 +705,160 @@ int GMG::setup(cudaStream_t s, const OpCtx &ctx, const int *ghost_cell, int ngho
         L.nz = cz ? (nz + 1) / 2 : nz;
         L.n = (long long)L.nx * L.ny * L.nz;
         const size_t b = sizeof(double) * L.n;
-        L.Tx = (double *)dalloc(b); L.Ty = (double *)dalloc(b); L.Tz = (double *)dalloc(b);
-        L.diag = (double *)dalloc(b); L.R = (double *)dalloc(b); L.Z = (double *)dalloc(b);
-        if (!L.Tx || !L.Ty || !L.Tz || !L.diag || !L.R || !L.Z) return -1;
-        double *gx = (double *)dalloc(b), *gy = (double *)dalloc(b), *gz = (double *)dalloc(b);
-        if (levels_.empty()) {
-            k_mg_build1<<<nblk(L.n, 128), 128, 0, s>>>(ctx, L, gx, gy, gz, per);
+        L.Tx = (double *)dalloc(b, false); L.Ty = (double *)dalloc(b, false); L.Tz = (double *)dalloc(b, false);
+        L.diag = (double *)dalloc(b, false);
+        double *gx = (double *)dalloc(b, false), *gy = (double *)dalloc(b, false), *gz = (double *)dalloc(b, false);
+        if (!L.Tx || !L.Ty || !L.Tz || !L.diag || !gx || !gy || !gz) return -1;
+        if (lv64.empty()) {
+            k_mg_build1<<<nblk(L.n, 128), 128, 0, s>>>(A64, L, gx, gy, gz, per);
         } else {
-            const MGLevel<double> &F = levels_.back();
             double **fg = &G[G.size() - 3];
-            k_mg_buildc<<<nblk(L.n, 128), 128, 0, s>>>(F, fg[0], fg[1], fg[2], L, gx, gy, gz);
+            k_mg_buildc<<<nblk(L.n, 128), 128, 0, s>>>(lv64.back(), fg[0], fg[1], fg[2], L, gx, gy, gz);
         }
         k_mg_diag<<<nblk(L.n, 128), 128, 0, s>>>(L, gx, gy, gz, per);
         G.push_back(gx); G.push_back(gy); G.push_back(gz);
-        levels_.push_back(L);
+        // Coarse faces and the prolongation tables toward the finer level.
+        const int cn[3] = {L.nx, L.ny, L.nz}, fn[3] = {nx, ny, nz}, co[3] = {L.cx, L.cy, L.cz};
+        MGLevel<T> LT{};
+        LT.nx = L.nx; LT.ny = L.ny; LT.nz = L.nz; LT.n = L.n; LT.cx = L.cx; LT.cy = L.cy; LT.cz = L.cz;
+        for (int a = 0; a < 3; a++) {
+            std::vector<double> cf(cn[a] + 1);
+            for (int I = 0; I < cn[a]; I++) cf[I] = faces[a][co[a] ? 2 * I : I];
+            cf[cn[a]] = faces[a][fn[a]];
+            std::vector<int> po;
+            std::vector<double> pw;
+            prolong_axis(faces[a], cf, co[a], per_[a], po, pw);
+            std::vector<T> pwt(pw.begin(), pw.end());
+            int *dpo = (int *)dalloc(sizeof(int) * po.size(), true);
+            T *dpw = (T *)dalloc(sizeof(T) * pwt.size(), true);
+            if (!dpo || !dpw) return -1;
+            cudaMemcpyAsync(dpo, po.data(), sizeof(int) * po.size(), cudaMemcpyHostToDevice, s);
+            cudaMemcpyAsync(dpw, pwt.data(), sizeof(T) * pwt.size(), cudaMemcpyHostToDevice, s);
+            LT.po[a] = dpo;
+            LT.pw[a] = dpw;
+            faces[a] = cf;
+        }
+        const size_t bt = sizeof(T) * L.n;
+        LT.Tx = (T *)dalloc(bt, true); LT.Ty = (T *)dalloc(bt, true); LT.Tz = (T *)dalloc(bt, true);
+        LT.diag = (T *)dalloc(bt, true); LT.R = (T *)dalloc(bt, true); LT.Z = (T *)dalloc(bt, true);
+        if (!LT.Tx || !LT.Ty || !LT.Tz || !LT.diag || !LT.R || !LT.Z) return -1;
+        k_convert<T><<<nblk(L.n, 256), 256, 0, s>>>(L.Tx, LT.Tx, L.n);
+        k_convert<T><<<nblk(L.n, 256), 256, 0, s>>>(L.Ty, LT.Ty, L.n);
+        k_convert<T><<<nblk(L.n, 256), 256, 0, s>>>(L.Tz, LT.Tz, L.n);
+        k_convert<T><<<nblk(L.n, 256), 256, 0, s>>>(L.diag, LT.diag, L.n);
+        lv64.push_back(L);
+        levels_.push_back(LT);
         nx = L.nx; ny = L.ny; nz = L.nz;
         if (L.n <= 64) break;
     }
-    tail_ = (int)levels_.size();
-    for (int l = 0; l < (int)levels_.size(); l++)
-        if (levels_[l].n <= cfg_.tail_cells) { tail_ = l; break; }
+    // The coarsest levels with at most TAIL_THREADS cells each run in the tail.
+    tail_ = (int)levels_.size() - 1;
+    while (tail_ > 0 && levels_[tail_ - 1].n <= TAIL_THREADS && (int)levels_.size() - (tail_ - 1) <= 16) tail_--;
     if (!levels_.empty()) {
-        dlevels_ = (MGLevel<double> *)dalloc(sizeof(MGLevel<double>) * levels_.size());
-        cudaMemcpyAsync(dlevels_, levels_.data(), sizeof(MGLevel<double>) * levels_.size(), cudaMemcpyHostToDevice, s);
+        tail_smem_ = tail_bytes(levels_, tail_);
+        if (cudaFuncSetAttribute(k_mg_tail<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tail_smem_) !=
+            cudaSuccess)
+            return -1;
     }
-    return cudaStreamSynchronize(s) == cudaSuccess ? 0 : -1;
+    if (!levels_.empty()) {
+        dlevels_ = (MGLevel<T> *)dalloc(sizeof(MGLevel<T>) * levels_.size(), true);
+        cudaMemcpyAsync(dlevels_, levels_.data(), sizeof(MGLevel<T>) * levels_.size(), cudaMemcpyHostToDevice, s);
+    }
+    const bool ok = cudaStreamSynchronize(s) == cudaSuccess;
+    for (void *p : tmp) cudaFree(p);
+    return ok ? 0 : -1;
 }
 
-void GMG::smooth0(cudaStream_t s, const double *r, double *z, int sweeps) {
-    const Grid &g = ctx_.g;
-    const long long n = (long long)g.nx * g.ny * g.nz;
+// Grid of a coarse colour pass (k pairs without a seam).
+template <typename T>
+static dim3 cgrid(const MGLevel<T> &L, int ncol) {
+    const int kw = ncol == 2 ? 2 * L3_TK : L3_TK;
+    return dim3((unsigned)((L.nz + kw - 1) / kw), (unsigned)((L.ny + L3_TJ - 1) / L3_TJ), (unsigned)L.nx);
+}
+
+template <typename T>
+int GMG<T>::smooth0(cudaStream_t s, const T *r, T *z, int sweeps, bool from_zero, const int *gate) {
+    const Grid &g = A_.g;
     Per3 per{{per_[0], per_[1], per_[2]}};
     const bool seam = (per_[0] && (g.nx & 1)) || (per_[1] && (g.ny & 1)) || (per_[2] && (g.nz & 1));
+    const dim3 blk(32, 8, 1);
+    const dim3 grd(seam ? (g.nz + 31) / 32 : (g.nz + 63) / 64, (g.ny + 7) / 8, (g.nx + MG0_PLANES - 1) / MG0_PLANES);
+    int k = 0;
     for (int it = 0; it < sweeps; it++) {
-        for (int col = 0; col < (seam ? 4 : 2); col++)
-            k_mg0_color<<<nblk(n, 256), 256, 0, s>>>(ctx_, r, z, col, per);
-            note_launches(1);
-        if (nghost_ > 0) {
-            k_mg0_ghost<<<nblk(nghost_, 128), 128, 0, s>>>(ctx_, r, z, ghost_cell_, nghost_, ghost_tmp_);
-            note_launches(1);
-            k_mg0_ghost_scatter<<<nblk(nghost_, 128), 128, 0, s>>>(ghost_cell_, nghost_, ghost_tmp_, z);
-            note_launches(1);
+        for (int col = 0; col < (seam ? 4 : 2); col++, k++) {
+            if (it == 0 && col == 0 && from_zero)
+                k_mg0_init<T><<<nblk(g.ncell, 256), 256, 0, s>>>(A_, r, z, per, gate);
+            else
+                k_mg0_color<T><<<grd, blk, 0, s>>>(A_, r, z, col, seam ? 0 : 1, per, gate);
         }
-        k_mg0_outer<<<nblk(nouter_, 256), 256, 0, s>>>(ctx_, r, z, outer_, nouter_);
-        note_launches(1);
+        if (nghost_ > 0) {
+            k_mg0_ghost<T><<<nblk(nghost_, 128), 128, 0, s>>>(A_, r, z, ghost_cell_, nghost_, ghost_tmp_, gate);
+            k_mg0_ghost_scatter<T><<<nblk(nghost_, 128), 128, 0, s>>>(ghost_cell_, nghost_, ghost_tmp_, z, gate);
+            k += 2;
+        }
+        k_mg0_outer<T><<<(A_.sw.nout + 255) / 256, 256, 0, s>>>(A_, r, z, A_.sw.outer, A_.sw.nout, gate);
+        k++;
     }
+    return k;
 }
 
-void GMG::apply(cudaStream_t s, const double *r, double *z) {
-    const Grid &g = ctx_.g;
-    cudaMemsetAsync(z, 0, sizeof(double) * g.ncell, s);
+// One V-cycle from z = 0: pre-smoothing on the fine rows, restriction, the
+// coarse levels above the tail (each starting from Z = 0), the tail, then
+// prolongation and post-smoothing back up.
+template <typename T>
+void GMG<T>::apply(cudaStream_t s, const T *r, T *z, const int *gate) {
+    const Grid &g = A_.g;
+    int k = 0;
     if (levels_.empty()) {
-        smooth0(s, r, z, cfg_.nu_pre + cfg_.nu_post + 4);
+        k += smooth0(s, r, z, cfg_.nu_pre + cfg_.nu_post + 4, true, gate);
+        note_launches(k);
+        launches_ = k;
         return;
     }
     Per3 per{{per_[0], per_[1], per_[2]}};
-    smooth0(s, r, z, cfg_.nu_pre);
-    k_mg0_restrict<<<nblk(levels_[0].n, 256), 256, 0, s>>>(ctx_, r, z, levels_[0]);
-    note_launches(1);
+    k += smooth0(s, r, z, cfg_.nu_pre, true, gate);
+    const MGLevel<T> &L1 = levels_[0];
+    k_mg0_restrict<T><<<l3_grid(L1.nx, L1.ny, L1.nz), l3_block(), 0, s>>>(A_, r, z, L1, gate);
+    k++;
     const int nl = (int)levels_.size();
     for (int l = 0; l < tail_; l++) {
-        MGLevel<double> &L = levels_[l];
-        cudaMemsetAsync(L.Z, 0, sizeof(double) * L.n, s);
-        for (int it = 0; it < cfg_.nu_pre; it++)
-            for (int col = 0; col < 4; col++) k_mgc_color<<<nblk(L.n, 256), 256, 0, s>>>(L, col, per);
-        k_mgc_restrict<<<nblk(levels_[l + 1].n, 256), 256, 0, s>>>(L, levels_[l + 1], per);
-        note_launches(1);
+        MGLevel<T> &L = levels_[l];
+        const MGLevel<T> &C = levels_[l + 1];
+        const int ncol = level_colors(L, per_);
+        for (int it = 0; it < cfg_.nuc_pre; it++)
+            for (int col = 0; col < ncol; col++, k++) {
+                if (it == 0 && col == 0)
+                    k_mgc_init<T><<<l3_grid(L.nx, L.ny, L.nz), l3_block(), 0, s>>>(L, per, gate);
+                else
+                    k_mgc_color<T><<<cgrid(L, ncol), l3_block(), 0, s>>>(L, col, ncol == 2, per, gate);
+            }
+        if (cfg_.nuc_pre == 0) {
+            k_fill0<T><<<nblk(L.n, 256), 256, 0, s>>>(L.Z, L.n, gate);
+            k++;
+        }
+        k_mgc_restrict<T><<<l3_grid(C.nx, C.ny, C.nz), l3_block(), 0, s>>>(L, C, per, gate);
+        k++;
     }
-    k_mg_tail<<<1, 1024, 0, s>>>(dlevels_, tail_, nl, cfg_.nu_pre, cfg_.nu_post, cfg_.coarse_sweeps, per);
-    note_launches(1);
+    k_mg_tail<T><<<1, TAIL_THREADS, tail_smem_, s>>>(dlevels_, tail_, nl, cfg_.nuc_pre, cfg_.nuc_post,
+                                                     cfg_.coarse_sweeps, per, gate);
+    k++;
     for (int l = tail_ - 1; l >= 0; l--) {
-        MGLevel<double> &L = levels_[l];
-        k_mgc_prolong<<<nblk(L.n, 256), 256, 0, s>>>(levels_[l + 1], L);
-        note_launches(1);
-        for (int it = 0; it < cfg_.nu_post; it++)
-            for (int col = 0; col < 4; col++) k_mgc_color<<<nblk(L.n, 256), 256, 0, s>>>(L, col, per);
+        MGLevel<T> &L = levels_[l];
+        const int ncol = level_colors(L, per_);
+        k_mgc_prolong<T><<<l3_grid(L.nx, L.ny, L.nz), l3_block(), 0, s>>>(levels_[l + 1], L, gate);
+        k++;
+        for (int it = 0; it < cfg_.nuc_post; it++)
+            for (int col = 0; col < ncol; col++, k++)
+                k_mgc_color<T><<<cgrid(L, ncol), l3_block(), 0, s>>>(L, col, ncol == 2, per, gate);
     }
-    k_mg0_prolong<<<nblk((long long)g.nx * g.ny * g.nz, 256), 256, 0, s>>>(ctx_, z, levels_[0]);
-    note_launches(1);
-    smooth0(s, r, z, cfg_.nu_post);
+    k_mg0_prolong<T><<<l3_grid(g.nx, g.ny, g.nz), l3_block(), 0, s>>>(A_, z, L1, gate);
+    k++;
+    k += smooth0(s, r, z, cfg_.nu_post, false, gate);
+    note_launches(k);
+    launches_ = k;
 }
+
+template class GMG<double>;
+template class GMG<float>;
 
 }  // namespace ibm

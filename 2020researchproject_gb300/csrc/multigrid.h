@@ -1,6 +1,6 @@
 // Geometric multigrid V-cycle used as the BiCGSTAB preconditioner of the
 // pressure-Poisson solve (replaces hypre's BoomerAMG, src/ibm3d_setup.c:
-// 1490-1563).
+// 1490-1563), in FP64 (plain path) or FP32 (mixed path).
 //
 // Level 0 is the padded fine grid and smooths the exact normalised pressure
 // rows (fluid, ghost-interpolation, solid, pinned and outer boundary rows).
@@ -11,8 +11,12 @@
 // ghost, solid or pinned cell carry none (Neumann); pressure-Dirichlet
 // boundaries fold into the diagonal and periodic ones wrap.  Residuals are
 // restricted as Vol coeffsum r (the conductance form of a normalised row)
-// and corrections are prolongated piecewise constant.  Levels small enough
-// for one thread block run as a single-CTA kernel.
+// by summation; corrections are prolongated trilinearly in cell-centre
+// coordinates (renormalised over active coarse cells), which on the
+// stretched benchmark grids cuts the Krylov iterations by a third against
+// piecewise-constant transfer.  Smoothers are colour-ordered Gauss-Seidel
+// with a fixed colour order (bitwise reproducible).  The coarsest levels
+// run as one single-CTA kernel with their arrays in shared memory.
 #pragma once
 
 #include <vector>
@@ -27,41 +31,62 @@ struct MGLevel {
     long long n;
     int cx, cy, cz;          // axis coarsened from the finer level
     T *Tx, *Ty, *Tz;         // conductance of the low face of each cell (wrap at 0 if periodic)
-    T *diag;                 // sum of all couplings incl. Dirichlet boundaries
+    T *diag;                 // sum of all couplings incl. Dirichlet boundaries; 0 = inactive
     T *R, *Z;
+    // Trilinear prolongation to the finer level, per axis, indexed by the
+    // finer level's cell index: the second coarse cell (-1: none) and the
+    // weight of the cell's own parent.
+    const int *po[3];
+    const T *pw[3];
 };
 
 struct GMGConfig {
-    int nu_pre = 2, nu_post = 2;
-    int coarse_sweeps = 40;
-    int tail_cells = 4096;   // levels at most this big run inside one CTA
+    int nu_pre = 3, nu_post = 3;    // fine grid
+    int nuc_pre = 2, nuc_post = 2;  // coarse levels above the coarsest
+    int coarse_sweeps = 10;         // coarsest level
 };
 
-class GMG : public Preconditioner {
+// Host geometry of the fine grid: interior face coordinates per axis.
+struct MGGeometry {
+    std::vector<double> f[3];
+};
+
+template <typename T>
+class GMG : public Preconditioner<T> {
   public:
     GMG() {}
     ~GMG() override;
     // ghost_cell: padded index of every ghost cell (nghost entries).
-    int setup(cudaStream_t s, const OpCtx &ctx, const int *ghost_cell, int nghost, double Re, double dt,
-              const GMGConfig &cfg);
-    void apply(cudaStream_t s, const double *r, double *z) override;
+    int setup(cudaStream_t s, const OpT<double> &A64, const OpT<T> &A, const int *ghost_cell, int nghost,
+              const MGGeometry &geom, const GMGConfig &cfg);
+    void apply(cudaStream_t s, const T *r, T *z, const int *gate) override;
+    int launches() const override { return launches_; }
+    // Smoother sweeps (pre, post) on the fine grid and on the coarse levels,
+    // and on the coarsest level; takes effect at the next apply.
+    void set_sweeps(int nu_pre, int nu_post, int nuc_pre, int nuc_post, int coarse) {
+        cfg_.nu_pre = nu_pre;
+        cfg_.nu_post = nu_post;
+        cfg_.nuc_pre = nuc_pre;
+        cfg_.nuc_post = nuc_post;
+        cfg_.coarse_sweeps = coarse;
+    }
     int nlevels() const { return (int)levels_.size() + 1; }
 
   private:
-    OpCtx ctx_{};
+    OpT<T> A_{};
     GMGConfig cfg_{};
-    std::vector<MGLevel<double>> levels_;
-    int tail_ = 0;                  // first coarse level handled by the single-CTA tail
-    MGLevel<double> *dlevels_ = nullptr;  // device copy of the level table
+    std::vector<MGLevel<T>> levels_;
+    int tail_ = 0;
+    size_t tail_smem_ = 0;
+    MGLevel<T> *dlevels_ = nullptr;
     const int *ghost_cell_ = nullptr;
     int nghost_ = 0;
-    double *ghost_tmp_ = nullptr;
-    int *outer_ = nullptr;
-    int nouter_ = 0;
+    T *ghost_tmp_ = nullptr;
     int per_[3] = {0, 0, 0};
     std::vector<void *> allocs_;
-    void vcycle_level0(cudaStream_t s, const double *r, double *z);
-    void smooth0(cudaStream_t s, const double *r, double *z, int sweeps);
+    int launches_ = 0;
+    // sweeps of the fine-grid smoother; from_zero: z is taken as 0 on entry
+    int smooth0(cudaStream_t s, const T *r, T *z, int sweeps, bool from_zero, const int *gate);
 };
 
 }  // namespace ibm

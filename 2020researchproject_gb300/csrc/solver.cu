@@ -31,8 +31,33 @@ using namespace ibm;
 
 namespace ibm {
 static std::atomic<long long> g_launches{0};
-void note_launches(int n) { g_launches += n; }
+// While a step is being recorded into a graph, launches are counted into
+// the recording instead (they run only when the graph does).
+static thread_local long long *g_redirect = nullptr;
+void note_launches(int n) {
+    if (g_redirect) *g_redirect += n;
+    else g_launches += n;
+}
 }  // namespace ibm
+
+// One recorded time step (CUDA graph): the step's kernels with both
+// linear solves as device-side while loops, the outer-layer fill, the
+// ghost update and the read-back of the step's scalars.  The field
+// pointers alternate between steps, so a graph is keyed by them.
+struct StepGraph {
+    const void *key[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaGraphExec_t exec = nullptr;
+    int fixed = 0;                          // kernels outside solver loops
+    int mom_iter = 0, mom_outer = 0;        // per momentum iteration / refinement cycle
+    int p_iter = 0, p_outer = 0;
+};
+
+// Host parameters baked into recorded graphs.
+struct GraphSig {
+    int precision, les, use_mg;
+    double tol, divtol, Re, dt, f[3], cs;
+    bool operator==(const GraphSig &o) const { return memcmp(this, &o, sizeof *this) == 0; }
+};
 
 struct ibm3d_device {
     cudaStream_t s = nullptr;
@@ -59,9 +84,19 @@ struct ibm3d_device {
     double *g_gw = nullptr, *g_gwself = nullptr;
     std::vector<GhostStencil> gst;   // lexicographic order
     std::vector<int> gcell_lex;      // padded index, lexicographic order
-    // Solvers.
-    KrylovWork kmom, kpres;
-    GMG *mg = nullptr;
+    // Operator tables of the matrix-free solves: FP64 ks per axis; FP32
+    // km, kp, ks, d per axis, then dinv, wdiv (n each), ghost weights.
+    double *op64 = nullptr;
+    float *op32 = nullptr;
+    int *sweep_outer = nullptr;   // outer cells of the padded grid (sweep launches)
+    OpT<double> A64{};
+    OpT<float> A32{};
+    // Solvers: FP64 BiCGSTAB (plain path) and FP64 refinement around FP32
+    // BiCGSTAB (mixed path), each with its multigrid preconditioner.
+    KrylovWork<double> kmom, kpres;
+    IRWork irmom, irpres;
+    GMG<double> *mg = nullptr;
+    GMG<float> *mg32 = nullptr;
     double *red_partials = nullptr;
     unsigned int *red_counter = nullptr;
     double *maxdiv_d = nullptr;
@@ -72,6 +107,12 @@ struct ibm3d_device {
     int les = 0;
     int cpt_fallback = 0;
     bool abort_on_error = true;
+    // Recorded steps.
+    bool use_graphs = true;
+    int mg_sweeps[5] = {3, 3, 2, 2, 10};  // multigrid sweeps: fine pre/post, coarse pre/post, coarsest
+    cudaStream_t aux[2] = {nullptr, nullptr};
+    std::vector<StepGraph> graphs;
+    GraphSig gsig{};
     // Last-step statistics.
     SolveReport rep_mom, rep_p;
     double max_div = 0.0;
@@ -181,34 +222,33 @@ void make_bcface(const IBMSolver *sv, int f, BCFace &F) {
     }
 }
 
-OpCtx op_ctx(const ibm3d_device *d) {
-    OpCtx c{};
-    c.g = d->g;
-    c.ax = d->ax[0];
-    c.ay = d->ax[1];
-    c.az = d->ax[2];
-    c.bc = d->bc;
-    c.flag = d->flag;
-    c.gid = d->gid;
-    c.gidx = d->g_gidx;
-    c.gw = d->g_gw;
-    c.gwself = d->g_gwself;
-    c.dinv = d->dinv;
-    return c;
-}
-
 template <typename T>
 void dfree(T *&p) {
     if (p) cudaFree((void *)p);
     p = nullptr;
 }
 
+void drop_graphs(ibm3d_device *d) {
+    for (auto &G : d->graphs)
+        if (G.exec) cudaGraphExecDestroy(G.exec);
+    d->graphs.clear();
+}
+
 void release_device(ibm3d_device *d) {
     if (!d) return;
     delete d->mg;
     d->mg = nullptr;
+    delete d->mg32;
+    d->mg32 = nullptr;
     d->kmom.release();
     d->kpres.release();
+    d->irmom.release();
+    d->irpres.release();
+    dfree(d->op64);
+    dfree(d->op32);
+    dfree(d->sweep_outer);
+    d->A64 = OpT<double>{};
+    d->A32 = OpT<float>{};
     for (int a = 0; a < 3; a++) dfree(d->tab[a]);
     dfree(d->fields);
     dfree(d->flag);
@@ -226,6 +266,11 @@ void release_device(ibm3d_device *d) {
     d->g_gidx = nullptr;
     d->g_gw = d->g_gwself = nullptr;
     d->assembled = false;
+    drop_graphs(d);
+    for (auto &a : d->aux) {
+        if (a) cudaStreamDestroy(a);
+        a = nullptr;
+    }
     if (d->s) cudaStreamDestroy(d->s);
     d->s = nullptr;
 }
@@ -503,6 +548,129 @@ void build_coeffsum(IBMSolver *sv) {
     cudaStreamSynchronize(d->s);
 }
 
+// Operator tables of both precisions and the two OpT views of them.
+bool build_ops(IBMSolver *sv) {
+    ibm3d_device *d = sv->dev;
+    const Grid &g = d->g;
+    const long long n = g.ncell;
+    const int ng = d->nghost;
+    const int Ns[3] = {sv->Nx, sv->Ny, sv->Nz};
+    const double *KM[3] = {sv->kx_W, sv->ky_S, sv->kz_D}, *KP[3] = {sv->kx_E, sv->ky_N, sv->kz_U};
+    const double *D[3] = {sv->dx, sv->dy, sv->dz};
+    size_t n64 = 0, n32 = 0;
+    for (int a = 0; a < 3; a++) {
+        n64 += Ns[a] + 4;
+        n32 += 4 * (size_t)(Ns[a] + 4);
+    }
+    n32 += 2 * (size_t)n + 9 * (size_t)ng;
+    std::vector<double> h64(n64, 0.0);
+    std::vector<float> h32(n32, 0.0f);
+    d->op64 = dmalloc<double>(sv, n64, "operator tables");
+    d->op32 = dmalloc<float>(sv, n32, "operator tables");
+    if (!d->op64 || !d->op32) return false;
+    OpT<double> &A = d->A64;
+    OpT<float> &B = d->A32;
+    A = OpT<double>{};
+    B = OpT<float>{};
+    size_t o64 = 0, o32 = 0;
+    for (int a = 0; a < 3; a++) {
+        const int m = Ns[a] + 4;
+        double *ks = &h64[o64];
+        float *km = &h32[o32], *kp = km + m, *ks32 = km + 2 * m, *dd = km + 3 * m;
+        for (int q = 0; q < m; q++) {
+            ks[q] = KM[a][q] + KP[a][q];
+            km[q] = (float)KM[a][q];
+            kp[q] = (float)KP[a][q];
+            ks32[q] = (float)ks[q];
+            dd[q] = (float)D[a][q];
+        }
+        A.km[a] = d->ax[a].km;
+        A.kp[a] = d->ax[a].kp;
+        A.d[a] = d->ax[a].d;
+        A.ks[a] = d->op64 + o64;
+        B.km[a] = d->op32 + o32;
+        B.kp[a] = d->op32 + o32 + m;
+        B.ks[a] = d->op32 + o32 + 2 * m;
+        B.d[a] = d->op32 + o32 + 3 * m;
+        o64 += m;
+        o32 += 4 * (size_t)m;
+    }
+    // FP32 dinv and the divergence weights 2 Re coeffsum.
+    std::vector<double> dinv(n);
+    cudaMemcpyAsync(dinv.data(), d->dinv, sizeof(double) * n, cudaMemcpyDeviceToHost, d->s);
+    std::vector<double> gw(8 * (size_t)ng), gws(ng);
+    if (ng > 0) {
+        cudaMemcpyAsync(gw.data(), d->g_gw, sizeof(double) * 8 * ng, cudaMemcpyDeviceToHost, d->s);
+        cudaMemcpyAsync(gws.data(), d->g_gwself, sizeof(double) * ng, cudaMemcpyDeviceToHost, d->s);
+    }
+    if (!cuda_check(sv, cudaStreamSynchronize(d->s), "operator tables")) return false;
+    float *dinv32 = &h32[o32], *wdiv = dinv32 + n, *gw32 = wdiv + n, *gws32 = gw32 + 8 * (size_t)ng;
+    for (long long P = 0; P < n; P++) {
+        dinv32[P] = (float)dinv[P];
+        wdiv[P] = (float)(2.0 * sv->Re * sv->p_coeffsum[P]);
+    }
+    for (size_t q = 0; q < gw.size(); q++) gw32[q] = (float)gw[q];
+    for (int q = 0; q < ng; q++) gws32[q] = (float)gws[q];
+    cudaMemcpyAsync(d->op64, h64.data(), sizeof(double) * n64, cudaMemcpyHostToDevice, d->s);
+    cudaMemcpyAsync(d->op32, h32.data(), sizeof(float) * n32, cudaMemcpyHostToDevice, d->s);
+    float *f32 = d->op32 + o32;
+    for (int f = 0; f < 6; f++) {
+        const BCFace &F = d->bc.f[f];
+        A.bc[f].type = B.bc[f].type = F.type;
+        for (int L = 0; L < 2; L++) {
+            A.bc[f].dir_o[L] = F.dir_o[L];
+            A.bc[f].dir_m[L] = F.dir_m[L];
+            A.bc[f].ext_o[L] = F.ext_o[L];
+            A.bc[f].ext_2[L] = F.ext_2[L];
+            B.bc[f].dir_o[L] = (float)F.dir_o[L];
+            B.bc[f].dir_m[L] = (float)F.dir_m[L];
+            B.bc[f].ext_o[L] = (float)F.ext_o[L];
+            B.bc[f].ext_2[L] = (float)F.ext_2[L];
+        }
+    }
+    // Sweep geometry: interior tiles of SW_TK x SW_TJ columns by `pi` planes,
+    // with `pi` lowered on small grids so that the interior alone fills the
+    // GPU; then the outer cells in index order.
+    SweepGeom sw{};
+    sw.tk = (g.nz + SW_TK - 1) / SW_TK;
+    sw.tj = (g.ny + SW_TJ - 1) / SW_TJ;
+    sw.pi = 8;
+    while (sw.pi > 1 && (long long)sw.tk * sw.tj * ((g.nx + sw.pi - 1) / sw.pi) < 1216) sw.pi /= 2;
+    sw.ti = (g.nx + sw.pi - 1) / sw.pi;
+    sw.nint = sw.tk * sw.tj * sw.ti;
+    std::vector<int> outer;
+    outer.reserve((size_t)(n - (long long)g.nx * g.ny * g.nz));
+    for (long long P = 0; P < n; P++) {
+        int i, j, k;
+        cijk(g, P, i, j, k);
+        if (i < 0 || i >= g.nx || j < 0 || j >= g.ny || k < 0 || k >= g.nz) outer.push_back((int)P);
+    }
+    sw.nout = (int)outer.size();
+    sw.nblocks = sw.nint + (sw.nout + SW_THREADS - 1) / SW_THREADS;
+    d->sweep_outer = dmalloc<int>(sv, std::max<size_t>(1, outer.size()), "sweep tables");
+    if (!d->sweep_outer) return false;
+    cudaMemcpyAsync(d->sweep_outer, outer.data(), sizeof(int) * outer.size(), cudaMemcpyHostToDevice, d->s);
+    sw.outer = d->sweep_outer;
+    A.sw = B.sw = sw;
+    const FastDiv fdx = make_fastdiv((unsigned)g.sx), fdy = make_fastdiv((unsigned)g.sy);
+    A.g = B.g = g;
+    A.fdx = B.fdx = fdx;
+    A.fdy = B.fdy = fdy;
+    A.p_singular = B.p_singular = d->bc.p_singular;
+    A.pinned = B.pinned = cidx(g, 0, 0, 0);
+    A.flag = B.flag = d->flag;
+    A.gid = B.gid = d->gid;
+    A.gidx = B.gidx = d->g_gidx;
+    A.gw = d->g_gw;
+    A.gwself = d->g_gwself;
+    A.dinv = d->dinv;
+    B.dinv = f32;
+    A.wdiv = B.wdiv = f32 + n;
+    B.gw = ng ? f32 + 2 * n : nullptr;
+    B.gwself = ng ? f32 + 2 * n + 8 * (size_t)ng : nullptr;
+    return cuda_check(sv, cudaStreamSynchronize(d->s), "operator tables");
+}
+
 void swap3(double *a[3], double *b[3]) {
     for (int l = 0; l < 3; l++) std::swap(a[l], b[l]);
 }
@@ -541,35 +709,40 @@ void ghost_update(IBMSolver *sv, bool solids) {
     launch_ghost_update(d->s, d->gargs, d->u, d->p);
 }
 
-// One fractional step (src/ibm3d_fracstep.c:60-74).
-void one_step(IBMSolver *sv) {
+// --------------------------------------------------------- time step ---
+// Stages of one fractional step (src/ibm3d_fracstep.c:60-74).
+SolveParams mom_params(IBMSolver *sv) {
+    SolveParams pm;
+    pm.tol = sv->tol;
+    pm.maxit = 200;
+    pm.prof = &sv->dev->prof;
+    return pm;
+}
+
+SolveParams pres_params(IBMSolver *sv) {
+    SolveParams pp = mom_params(sv);
+    pp.maxit = 1000;
+    pp.divtol = sv->dev->divtol;
+    if (pp.divtol > 0) pp.tol = 0.0;  // the divergence rule replaces the relative-residual rule
+    return pp;
+}
+
+bool use_mg(const IBMSolver *sv) { return sv->precond_type == PRECOND_AMG || sv->linear_solver_type == SOLVER_AMG; }
+
+void stage_rhs(IBMSolver *sv) {
     ibm3d_device *d = sv->dev;
     Prof &pf = d->prof;
     const double f[3] = {sv->ext_force.const_f1, sv->ext_force.const_f2, sv->ext_force.const_f3};
-    const OpCtx ctx = op_ctx(d);
-
     int t = pf.begin("tau");
     calc_tau(sv);
     pf.end(t);
     t = pf.begin("conv_rhs");
     launch_conv_rhs(d->s, d->g, d->ax[0], d->ax[1], d->ax[2], d->bc, d->flag, conv_args(d), sv->dt, f, d->les);
     pf.end(t);
+}
 
-    SolveParams pm;
-    pm.tol = sv->tol;
-    pm.maxit = 200;
-    pm.Re = sv->Re;
-    pm.prof = &pf;
-    t = pf.begin("mom_solve");
-    int rc = bicgstab(d->s, ctx, OP_MOM, d->kmom, d->b, d->ustar, pm, nullptr, d->rep_mom);
-    pf.end(t);
-    if (rc == 1) {
-        for (int l = 0; l < 3; l++)
-            if (d->rep_mom.relres[l] >= sv->tol) fprintf(stderr, "warning: u%d_star did not converge\n", l + 1);
-    } else if (rc == 2) {
-        set_status(sv, IBM3D_EBREAKDOWN, "breakdown in the momentum solve");
-    }
-
+void stage_ustar(IBMSolver *sv) {
+    ibm3d_device *d = sv->dev;
     UstarArgs ua{};
     for (int l = 0; l < 3; l++) {
         ua.us[l] = d->ustar + l * d->g.ncell;
@@ -577,20 +750,13 @@ void one_step(IBMSolver *sv) {
     }
     ua.p = d->p;
     ua.b = d->b;
-    t = pf.begin("ustar_prhs");
+    const int t = d->prof.begin("ustar_prhs");
     launch_ustar_prhs(d->s, d->g, d->ax[0], d->ax[1], d->ax[2], d->bc, d->flag, ua, sv->dt, sv->Re);
-    pf.end(t);
+    d->prof.end(t);
+}
 
-    SolveParams pp = pm;
-    pp.maxit = 1000;
-    pp.divtol = d->divtol;
-    const bool use_mg = sv->precond_type == PRECOND_AMG || sv->linear_solver_type == SOLVER_AMG;
-    t = pf.begin("p_solve");
-    rc = bicgstab(d->s, ctx, OP_PRES, d->kpres, d->b, d->pp, pp, use_mg ? d->mg : nullptr, d->rep_p);
-    pf.end(t);
-    if (rc == 1) fprintf(stderr, "warning: p_prime did not converge\n");
-    else if (rc == 2) set_status(sv, IBM3D_EBREAKDOWN, "breakdown in the pressure solve");
-
+void stage_next(IBMSolver *sv) {
+    ibm3d_device *d = sv->dev;
     NextArgs na{};
     for (int l = 0; l < 3; l++) {
         na.us[l] = d->ustar + l * d->g.ncell;
@@ -601,14 +767,184 @@ void one_step(IBMSolver *sv) {
     na.p = d->p;
     na.pp = d->pp;
     na.pn = d->pn;
-    t = pf.begin("update_next");
+    const int t = d->prof.begin("update_next");
     launch_update_next(d->s, d->g, d->ax[0], d->ax[1], d->ax[2], d->bc, d->flag, na, sv->dt, d->red_partials,
                        d->red_counter, d->maxdiv_d, kUpdateBlocks);
-    pf.end(t);
+    d->prof.end(t);
+}
+
+void swap_fields(ibm3d_device *d) {
     swap3(d->u, d->un);
     swap3(d->U, d->Un);
     std::swap(d->p, d->pn);
     swap3(d->N, d->Np);
+}
+
+void check_mom(IBMSolver *sv, int rc) {
+    if (rc == 1) {
+        for (int l = 0; l < 3; l++)
+            if (sv->dev->rep_mom.relres[l] >= sv->tol) fprintf(stderr, "warning: u%d_star did not converge\n", l + 1);
+    } else if (rc == 2) {
+        set_status(sv, IBM3D_EBREAKDOWN, "breakdown in the momentum solve");
+    }
+}
+
+void check_pres(IBMSolver *sv, int rc) {
+    if (rc == 1) fprintf(stderr, "warning: p_prime did not converge\n");
+    else if (rc == 2) set_status(sv, IBM3D_EBREAKDOWN, "breakdown in the pressure solve");
+}
+
+// One fractional step, host-sequenced (used while stage profiling is on).
+void one_step(IBMSolver *sv) {
+    ibm3d_device *d = sv->dev;
+    Prof &pf = d->prof;
+    const bool mixed = d->precision == IBM3D_MIXED;
+    stage_rhs(sv);
+    const SolveParams pm = mom_params(sv);
+    int t = pf.begin("mom_solve");
+    int rc = mixed ? solve_ir(d->s, d->A64, d->A32, OP_MOM, d->irmom, d->b, d->ustar, pm, nullptr, d->rep_mom)
+                   : bicgstab<double>(d->s, d->A64, OP_MOM, d->kmom, d->b, d->ustar, pm, nullptr, d->rep_mom);
+    pf.end(t);
+    check_mom(sv, rc);
+    stage_ustar(sv);
+    const SolveParams pp = pres_params(sv);
+    t = pf.begin("p_solve");
+    if (mixed)
+        rc = solve_ir(d->s, d->A64, d->A32, OP_PRES, d->irpres, d->b, d->pp, pp, use_mg(sv) ? d->mg32 : nullptr,
+                      d->rep_p);
+    else
+        rc = bicgstab<double>(d->s, d->A64, OP_PRES, d->kpres, d->b, d->pp, pp, use_mg(sv) ? d->mg : nullptr,
+                              d->rep_p);
+    pf.end(t);
+    check_pres(sv, rc);
+    stage_next(sv);
+    swap_fields(d);
+}
+
+GraphSig graph_sig(const IBMSolver *sv) {
+    GraphSig g;
+    memset(&g, 0, sizeof g);
+    g.precision = sv->dev->precision;
+    g.les = sv->dev->les;
+    g.use_mg = use_mg(sv);
+    g.tol = sv->tol;
+    g.divtol = sv->dev->divtol;
+    g.Re = sv->Re;
+    g.dt = sv->dt;
+    g.f[0] = sv->ext_force.const_f1;
+    g.f[1] = sv->ext_force.const_f2;
+    g.f[2] = sv->ext_force.const_f3;
+    g.cs = sv->turb_model.Cs;
+    return g;
+}
+
+// Records one step (everything one_step + fill_outer + ghost_update do)
+// into a graph; the field pointers are left as they were.
+bool record_step(IBMSolver *sv, StepGraph &G) {
+    ibm3d_device *d = sv->dev;
+    const bool mixed = d->precision == IBM3D_MIXED;
+    long long count = 0;
+    g_redirect = &count;
+    bool ok = cudaStreamBeginCapture(d->s, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    int mf = 0, mo = 0, mi = 0, pf = 0, po = 0, pi = 0;
+    if (ok) {
+        stage_rhs(sv);
+        SolveParams pm = mom_params(sv);
+        pm.prof = nullptr;
+        if (mixed)
+            ok = record_ir(d->s, d->aux, d->A64, d->A32, OP_MOM, d->irmom, d->b, d->ustar, pm, nullptr, &mf, &mo,
+                           &mi) == 0;
+        else
+            ok = record_bicgstab<double>(d->s, d->aux, d->A64, OP_MOM, d->kmom, d->b, d->ustar, pm, nullptr, &mf,
+                                         &mi) == 0;
+    }
+    if (ok) {
+        stage_ustar(sv);
+        SolveParams pp = pres_params(sv);
+        pp.prof = nullptr;
+        if (mixed)
+            ok = record_ir(d->s, d->aux, d->A64, d->A32, OP_PRES, d->irpres, d->b, d->pp, pp,
+                           use_mg(sv) ? d->mg32 : nullptr, &pf, &po, &pi) == 0;
+        else
+            ok = record_bicgstab<double>(d->s, d->aux, d->A64, OP_PRES, d->kpres, d->b, d->pp, pp,
+                                         use_mg(sv) ? d->mg : nullptr, &pf, &pi) == 0;
+    }
+    if (ok) {
+        stage_next(sv);
+        swap_fields(d);
+        fill_outer(sv);
+        ghost_update(sv, false);
+        cudaMemcpyAsync(d->maxdiv_h, d->maxdiv_d, sizeof(double), cudaMemcpyDeviceToHost, d->s);
+        swap_fields(d);
+    }
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(d->s, &graph);
+    g_redirect = nullptr;
+    ok = ok && ec == cudaSuccess && graph;
+    if (ok) ok = cudaGraphInstantiate(&G.exec, graph, 0) == cudaSuccess;
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();
+    if (!ok) return false;
+    G.key[0] = d->u[0];
+    G.key[1] = d->U[0];
+    G.key[2] = d->p;
+    G.key[3] = d->N[0];
+    G.mom_iter = mi;
+    G.mom_outer = mo;
+    G.p_iter = pi;
+    G.p_outer = po;
+    // Loop bodies were recorded once each; the rest runs once per step.
+    G.fixed = (int)(count - mi - mo - pi - po);
+    return true;
+}
+
+// One step through its recorded graph.  Returns false when recording
+// failed (the caller then runs the step host-sequenced).
+bool graph_step(IBMSolver *sv) {
+    ibm3d_device *d = sv->dev;
+    const GraphSig sig = graph_sig(sv);
+    if (!(sig == d->gsig)) {
+        drop_graphs(d);
+        d->gsig = sig;
+    }
+    StepGraph *G = nullptr;
+    for (auto &g : d->graphs)
+        if (g.key[0] == d->u[0] && g.key[1] == d->U[0] && g.key[2] == d->p && g.key[3] == d->N[0]) G = &g;
+    if (!G) {
+        StepGraph ng;
+        if (!record_step(sv, ng)) {
+            fprintf(stderr, "warning: CUDA graph recording failed; stepping without graphs\n");
+            d->use_graphs = false;
+            return false;
+        }
+        d->graphs.push_back(ng);
+        G = &d->graphs.back();
+    }
+    if (!cuda_check(sv, cudaGraphLaunch(G->exec, d->s), "graph launch")) return true;
+    if (!cuda_check(sv, cudaStreamSynchronize(d->s), "time step")) return true;
+    const bool mixed = d->precision == IBM3D_MIXED;
+    long long launches = G->fixed;
+    int rc;
+    if (mixed) {
+        rc = report(d->irmom, d->rep_mom);
+        launches += (long long)d->rep_mom.outer * G->mom_outer;
+        launches += (long long)std::max({d->rep_mom.iters[0], d->rep_mom.iters[1], d->rep_mom.iters[2]}) * G->mom_iter;
+    } else {
+        rc = report(d->kmom, d->rep_mom);
+        launches += (long long)std::max({d->rep_mom.iters[0], d->rep_mom.iters[1], d->rep_mom.iters[2]}) * G->mom_iter;
+    }
+    check_mom(sv, rc);
+    if (mixed) {
+        rc = report(d->irpres, d->rep_p);
+        launches += (long long)d->rep_p.outer * G->p_outer + (long long)d->rep_p.iters[0] * G->p_iter;
+    } else {
+        rc = report(d->kpres, d->rep_p);
+        launches += (long long)d->rep_p.iters[0] * G->p_iter;
+    }
+    check_pres(sv, rc);
+    note_launches((int)launches);
+    swap_fields(d);
+    return true;
 }
 
 void print_row(IBMSolver *sv, int i, long elapsed_ms) {
@@ -882,6 +1218,7 @@ void IBMSolver_assemble(IBMSolver *s) {
     release_device(d);
     d->s = nullptr;
     cuda_check(s, cudaStreamCreateWithFlags(&d->s, cudaStreamNonBlocking), "stream");
+    for (auto &a : d->aux) cuda_check(s, cudaStreamCreateWithFlags(&a, cudaStreamNonBlocking), "stream");
     d->prof.s = d->s;
     for (int f = 0; f < 6; f++) make_bcface(s, f, d->bc.f[f]);
     d->bc.p_singular = 1;
@@ -893,13 +1230,31 @@ void IBMSolver_assemble(IBMSolver *s) {
     if (!build_ghosts(s)) return;
     build_coeffsum(s);
     cudaMemcpyAsync(s->lvset, d->lvset, sizeof(double) * g.ncell, cudaMemcpyDeviceToHost, d->s);
-    if (d->kmom.allocate(g.ncell, 3, false) != 0 || d->kpres.allocate(g.ncell, 1, true) != 0) {
+    if (!build_ops(s)) return;
+    const int mb = d->A64.sw.nblocks;
+    if (d->kmom.allocate(g.ncell, 3, false, mb) != 0 || d->kpres.allocate(g.ncell, 1, true, mb) != 0 ||
+        d->irmom.allocate(g.ncell, 3, false, mb) != 0 || d->irpres.allocate(g.ncell, 1, true, mb) != 0) {
         set_status(s, IBM3D_ECUDA, "Krylov workspace allocation failed");
         return;
     }
-    d->mg = new GMG();
+    MGGeometry geom;
+    const double *D[3] = {s->dx, s->dy, s->dz};
+    const int Ns[3] = {s->Nx, s->Ny, s->Nz};
+    for (int a = 0; a < 3; a++) {
+        geom.f[a].assign(Ns[a] + 1, 0.0);
+        for (int i = 0; i < Ns[a]; i++) geom.f[a][i + 1] = geom.f[a][i] + D[a][i + 2];
+    }
     GMGConfig mc;
-    if (d->mg->setup(d->s, op_ctx(d), d->nghost ? d->gargs.cell : nullptr, d->nghost, s->Re, s->dt, mc) != 0) {
+    mc.nu_pre = d->mg_sweeps[0];
+    mc.nu_post = d->mg_sweeps[1];
+    mc.nuc_pre = d->mg_sweeps[2];
+    mc.nuc_post = d->mg_sweeps[3];
+    mc.coarse_sweeps = d->mg_sweeps[4];
+    const int *gcell = d->nghost ? d->gargs.cell : nullptr;
+    d->mg = new GMG<double>();
+    d->mg32 = new GMG<float>();
+    if (d->mg->setup(d->s, d->A64, d->A64, gcell, d->nghost, geom, mc) != 0 ||
+        d->mg32->setup(d->s, d->A64, d->A32, gcell, d->nghost, geom, mc) != 0) {
         set_status(s, IBM3D_ECUDA, "multigrid setup failed");
         return;
     }
@@ -1089,17 +1444,20 @@ void IBMSolver_iterate(IBMSolver *s, int num_time_steps, bool verbose) {
     struct timespec t0, t1;
     clock_gettime(CLOCK_REALTIME, &t0);
     for (int i = 1; i <= num_time_steps; i++) {
-        one_step(s);
+        if (!(d->use_graphs && !d->prof.on && graph_step(s))) {
+            one_step(s);
+            int t = d->prof.begin("fill_outer");
+            fill_outer(s);
+            d->prof.end(t);
+            t = d->prof.begin("ghost_update");
+            ghost_update(s, false);
+            d->prof.end(t);
+            cudaMemcpyAsync(d->maxdiv_h, d->maxdiv_d, sizeof(double), cudaMemcpyDeviceToHost, d->s);
+            if (!cuda_check(s, cudaStreamSynchronize(d->s), "time step")) return;
+        }
+        if (d->status == IBM3D_ECUDA) return;
         s->iter++;
         s->time = start_time + s->dt * i;
-        int t = d->prof.begin("fill_outer");
-        fill_outer(s);
-        d->prof.end(t);
-        t = d->prof.begin("ghost_update");
-        ghost_update(s, false);
-        d->prof.end(t);
-        cudaMemcpyAsync(d->maxdiv_h, d->maxdiv_d, sizeof(double), cudaMemcpyDeviceToHost, d->s);
-        if (!cuda_check(s, cudaStreamSynchronize(d->s), "time step")) return;
         d->max_div = *d->maxdiv_h;
         d->prof.flush();
         if (verbose && s->rank == 0) {
@@ -1167,8 +1525,26 @@ void IBMSolver_set_smagorinsky(IBMSolver *s, double Cs) {
 
 void IBMSolver_set_div_tol(IBMSolver *s, double div_tol) { s->dev->divtol = div_tol; }
 
+void IBMSolver_set_multigrid(IBMSolver *s, int nu_pre, int nu_post, int nuc_pre, int nuc_post, int coarse_sweeps) {
+    ibm3d_device *d = s->dev;
+    if (nu_pre < 0 || nu_post < 0 || nuc_pre < 0 || nuc_post < 0 || coarse_sweeps < 1 || nu_pre + nu_post < 1) {
+        set_status(s, IBM3D_EARG, "IBMSolver_set_multigrid: invalid sweep counts");
+        return;
+    }
+    const int v[5] = {nu_pre, nu_post, nuc_pre, nuc_post, coarse_sweeps};
+    for (int q = 0; q < 5; q++) d->mg_sweeps[q] = v[q];
+    if (d->mg) d->mg->set_sweeps(nu_pre, nu_post, nuc_pre, nuc_post, coarse_sweeps);
+    if (d->mg32) d->mg32->set_sweeps(nu_pre, nu_post, nuc_pre, nuc_post, coarse_sweeps);
+    drop_graphs(d);
+}
+
+void IBMSolver_set_graphs(IBMSolver *s, int on) {
+    s->dev->use_graphs = on != 0;
+    drop_graphs(s->dev);
+}
+
 void IBMSolver_set_precision(IBMSolver *s, int mode) {
-    if (mode != IBM3D_FP64) {
+    if (mode != IBM3D_FP64 && mode != IBM3D_MIXED) {
         set_status(s, IBM3D_EUNSUPPORTED, "precision mode %d is not available", mode);
         return;
     }
@@ -1287,6 +1663,8 @@ void IBMSolver_get_stats(const IBMSolver *s, IBMSolverStats *out) {
     out->res_p = d->rep_p.relres[0];
     out->max_div = d->max_div;
     out->mg_levels = d->mg ? d->mg->nlevels() : 0;
+    out->outer_u = d->rep_mom.outer;
+    out->outer_p = d->rep_p.outer;
     out->cpt_fallback = d->cpt_fallback;
 }
 

@@ -261,10 +261,11 @@ k_update_next(const Grid g, const Axis ax, const Axis ay, const Axis az, const B
         }
     }
     block_max<1>(mdiv, smem);
-    if (publish_partials<1>(mdiv, partials, counter)) {
-        double m = 0;
-        for (unsigned b = 0; b < gridDim.x; b++) m = fmax(m, ((volatile double *)partials)[b]);
-        *maxdiv_out = m;
+    if (!publish_partials<1>(mdiv, partials, counter)) return;
+    double m[1];
+    reduce_partials<1, 0>(partials, gridDim.x, m, smem);
+    if (threadIdx.x == 0) {
+        *maxdiv_out = m[0];
         *counter = 0;
     }
 }

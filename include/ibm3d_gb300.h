@@ -42,9 +42,29 @@ void IBMSolver_set_smagorinsky(IBMSolver *, double Cs);
    default) keeps the reference's ||r||/||b|| < tol rule. */
 void IBMSolver_set_div_tol(IBMSolver *, double div_tol);
 
-/* Arithmetic of the step: IBM3D_FP64 (default, the plain FP64 step). */
-enum { IBM3D_FP64 = 0 };
+/* Arithmetic of the linear solves.  IBM3D_FP64 (default): FP64 BiCGSTAB
+   with an FP64 multigrid preconditioner, as the reference.  IBM3D_MIXED:
+   FP64 iterative refinement (residuals, updates and the stopping test in
+   FP64, on the exact FP64 rows) around FP32 BiCGSTAB solves with an FP32
+   multigrid preconditioner; it stops on the same FP64 criterion.  Every
+   other part of the step stays FP64 in both modes. */
+enum { IBM3D_FP64 = 0, IBM3D_MIXED = 1 };
 void IBMSolver_set_precision(IBMSolver *, int mode);
+
+/* Step sequencing.  on (default): each time step runs as one recorded CUDA
+   graph whose linear solves iterate on the device (conditional while
+   nodes), with one host synchronisation per step; off: the host sequences
+   every kernel and reads the Krylov scalars after each half iteration.
+   Both give bitwise identical results.  Stage profiling
+   (IBMSolver_set_profiling) always uses the host-sequenced form. */
+void IBMSolver_set_graphs(IBMSolver *, int on);
+
+/* Pressure multigrid V-cycle: Gauss-Seidel sweeps before and after the
+   coarse-grid correction on the fine grid (nu_pre, nu_post) and on the
+   coarse levels (nuc_pre, nuc_post), and sweeps on the coarsest level
+   (defaults 3, 3, 2, 2, 10).  Tuning only: the solve still stops on the
+   same residual or divergence test. */
+void IBMSolver_set_multigrid(IBMSolver *, int nu_pre, int nu_post, int nuc_pre, int nuc_post, int coarse_sweeps);
 
 /* Initial state from host arrays in the padded (N+4)^3 layout, k fastest
    (u1, u2, u3, p).  Sets iter = 0 and time = 0 like init_flow_const. */
@@ -85,6 +105,8 @@ typedef struct {
     double max_div;         /* max |div U^{n+1}| over fluid cells (pinned cell excluded) */
     int mg_levels;          /* pressure multigrid levels (incl. the fine grid) */
     int cpt_fallback;       /* level-set points settled by the full extrusion scan */
+    int outer_u;            /* refinement cycles of the momentum solve (IBM3D_MIXED) */
+    int outer_p;            /* refinement cycles of the pressure solve (IBM3D_MIXED) */
 } IBMSolverStats;
 void IBMSolver_get_stats(const IBMSolver *, IBMSolverStats *);
 

@@ -8,7 +8,10 @@ The GPU path runs the same case through the C ABI and must reproduce
 * flags, level set, p_coeffsum and ghost stencils (indices and raw
   weights) bit for bit;
 * u, p, face velocities and the last step's u*, U*, p', N within 1e-9
-  relative L2, with identical NaN masks (both sides solve to tol 1e-12).
+  relative L2, with identical NaN masks (both sides solve to tol 1e-12),
+  in both arithmetic modes: the plain FP64 solves and the mixed path
+  (FP64 iterative refinement around FP32 BiCGSTAB + FP32 multigrid), which
+  stops on the same FP64 residual criterion.
 """
 import os
 
@@ -69,10 +72,12 @@ def test_setup_bit_exact(ibm, name):
         assert np.array_equal(coeff, case["ghost_coeff"])
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("name", golden_cases())
-def test_steps_match_reference(ibm, name):
+def test_steps_match_reference(ibm, name, precision):
     case = load_golden(name)
     s = build_case(ibm, case)
+    s.set_precision(ibm.MIXED if precision == "mixed" else ibm.FP64)
     calls = case["meta"]["calls"]
     report = []
     for c, n in enumerate(calls, start=1):
@@ -90,3 +95,5 @@ def test_steps_match_reference(ibm, name):
             assert err <= tol, f"{f} after call {c}: rel L2 {err:.3e} > {tol}"
     st = s.stats()
     assert st["iter"] == sum(calls)
+    if precision == "mixed":
+        assert st["outer_p"] >= 1
