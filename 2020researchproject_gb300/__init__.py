@@ -99,6 +99,7 @@ def load_library(path: str = LIB_PATH):
         "IBMSolver_set_div_tol": (None, [vp, d]),
         "IBMSolver_set_precision": (None, [vp, i]),
         "IBMSolver_set_graphs": (None, [vp, i]),
+        "IBMSolver_time_kernel": (ctypes.c_double, [vp, i, i, ctypes.POINTER(ctypes.c_double)]),
         "IBMSolver_set_multigrid": (None, [vp, i, i, i, i, i]),
         "IBMSolver_get_field": (None, [vp, i, dp]),
         "IBMSolver_get_flag": (None, [vp, ip]),
@@ -239,6 +240,15 @@ class IBMSolver:
     def set_multigrid(self, nu_pre=3, nu_post=3, nuc_pre=2, nuc_post=2, coarse_sweeps=10):
         self._lib.IBMSolver_set_multigrid(self._s, nu_pre, nu_post, nuc_pre, nuc_post, coarse_sweeps)
         self._check("IBMSolver_set_multigrid")
+
+    def time_kernel(self, which, reps=20):
+        """(avg ms per launch, algorithmic bytes per launch) of a hot kernel:
+        which = "mg_color" or "spmv_p"."""
+        b = ctypes.c_double(0.0)
+        code = {"mg_color": 0, "spmv_p": 1}[which]
+        ms = self._lib.IBMSolver_time_kernel(self._s, code, int(reps), ctypes.byref(b))
+        self._check("IBMSolver_time_kernel")
+        return ms, b.value
 
     def set_graphs(self, on=True):
         self._lib.IBMSolver_set_graphs(self._s, 1 if on else 0)

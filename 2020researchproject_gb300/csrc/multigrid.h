@@ -71,6 +71,11 @@ class GMG : public Preconditioner<T> {
         cfg_.coarse_sweeps = coarse;
     }
     int nlevels() const { return (int)levels_.size() + 1; }
+    // Average device time (ms) of one fine-grid colour pass over r, z
+    // (reps launches between CUDA events on s); bytes: its algorithmic
+    // bytes (z read once, r, 1/coeffsum, flag read and z written for the
+    // updated half of the interior cells).
+    float time_color(cudaStream_t s, const T *r, T *z, int reps, double *bytes);
 
   private:
     OpT<T> A_{};

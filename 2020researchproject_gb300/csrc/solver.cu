@@ -1686,6 +1686,44 @@ double IBMSolver_time_iterate(IBMSolver *s, int nsteps) {
     return ms;
 }
 
+double IBMSolver_time_kernel(IBMSolver *s, int which, int reps, double *bytes) {
+    if (!check_ready(s, "IBMSolver_time_kernel")) return -1;
+    ibm3d_device *d = s->dev;
+    const bool mixed = d->precision == IBM3D_MIXED;
+    double b = 0;
+    double ms = -1;
+    cudaStreamSynchronize(d->s);
+    if (which == IBM3D_K_MG_COLOR) {
+        // Scratch vectors of the pressure solve of the current precision.
+        ms = mixed ? d->mg32->time_color(d->s, d->irpres.inner.r, d->irpres.inner.s, reps, &b)
+                   : d->mg->time_color(d->s, d->kpres.r, d->kpres.s, reps, &b);
+    } else if (which == IBM3D_K_SPMV_P) {
+        cudaEvent_t e0, e1;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        cudaEventRecord(e0, d->s);
+        for (int q = 0; q < reps; q++) {
+            if (mixed) apply_operator<float>(d->s, d->A32, OP_PRES, 0, d->irpres.inner.r, d->irpres.inner.s);
+            else apply_operator<double>(d->s, d->A64, OP_PRES, 0, d->kpres.r, d->kpres.s);
+        }
+        cudaEventRecord(e1, d->s);
+        cudaEventSynchronize(e1);
+        float t = 0;
+        cudaEventElapsedTime(&t, e0, e1);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        ms = reps > 0 ? t / reps : 0;
+        const double w = mixed ? 4.0 : 8.0;
+        b = (double)d->g.ncell * (3 * w + 1);
+    } else {
+        set_status(s, IBM3D_EARG, "IBMSolver_time_kernel: unknown kernel %d", which);
+        return -1;
+    }
+    if (bytes) *bytes = b;
+    if (!cuda_check(s, cudaGetLastError(), "IBMSolver_time_kernel")) return -1;
+    return ms;
+}
+
 void IBMSolver_set_profiling(IBMSolver *s, int on) {
     s->dev->prof.reset();
     s->dev->prof.on = on != 0;

@@ -8,15 +8,23 @@ pressure solve runs to max|div U^{n+1}| <= 1e-8 on fluid cells every step,
 momentum to the reference drivers' relative tolerance 1e-6.  Synthetic,
 seeded inputs (the reference has no public dataset).
 
-Metric: Mcell-steps/s = interior cells x steps / seconds.
+Metric: Mcell-steps/s = interior cells x steps / seconds, for the
+mixed-precision step (FP32 Krylov/multigrid inner solves inside FP64
+iterative refinement, everything else FP64), with the plain FP64 step
+measured beside it on the same state ("fp64", "mixed_vs_fp64") and the
+velocity difference between the two after the run ("error_vs_fp64").
   value : device time (CUDA events on the solver's stream) of K steps with
           the state resident in HBM (the step's working set, >1 GB, is far
-          larger than the 129 MB L2, so nothing is served from cache).
+          larger than the 129 MB L2).  Each step is one recorded CUDA graph.
   e2e   : the same K steps through the C ABI with HOST buffers: every step
           uploads u1, u2, u3, p from pinned host memory
           (IBMSolver_init_flow_array), runs IBMSolver_iterate(1) and reads
           the four fields back (IBMSolver_get_field); host wall clock.
-Default run: N=1, K=10 timed steps after W=3 warm-up steps.
+  roofline: the dominant kernel (fine-grid colour pass of the pressure
+          multigrid) timed with CUDA events on the solver's stream, against
+          the measured HBM copy bandwidth.
+Default run: N=1, K=10 timed steps after W=3 warm-up steps;
+--precision fp64 makes the plain FP64 step the headline.
 
 --impl reference runs the CPU restatement of the reference time step
 (oracle/, OpenMP on every host core) on the same workload and metric.
@@ -43,10 +51,6 @@ sys.path.insert(0, ROOT)
 
 DIV_TOL = 1e-8
 MOM_TOL = 1e-6
-# Algorithmic bytes per padded cell of one pressure SpMV launch (FP64):
-# read x, write y, read the dot-product partner (r0 or s), read 1/coeffsum,
-# read the flag byte.
-SPMV_P_BYTES_PER_CELL = 8 + 8 + 8 + 8 + 1
 
 
 def _dist():
@@ -212,6 +216,57 @@ def bench_reference(args):
     return 0
 
 
+def _profiler_range(on):
+    """cudaProfilerStart/Stop around the headline timed region, so that
+    `ncu --profile-from-start off` captures exactly its launches (no effect
+    without a profiler)."""
+    import ctypes
+    for name in ("libcudart.so.13", "libcudart.so.12", "libcudart.so"):
+        try:
+            rt = ctypes.CDLL(name)
+        except OSError:
+            continue
+        (rt.cudaProfilerStart if on else rt.cudaProfilerStop)()
+        return
+
+
+def _timed_arm(ibm, wl, case, precision, args, world, u0, headline=False):
+    """Builds a solver for `case`, runs W warm-up steps and times K steps on
+    the device (CUDA events on the solver's stream), sampling clocks."""
+    t0 = time.perf_counter()
+    s = wl.build_solver(ibm, case, tol=MOM_TOL, div_tol=DIV_TOL)
+    s.set_precision(ibm.MIXED if precision == "mixed" else ibm.FP64)
+    if args.host_loop:
+        s.set_graphs(False)
+    setup_s = time.perf_counter() - t0
+    s.init_flow_array(*u0)
+    s.iterate(args.warmup)
+    _barrier(world)
+    l0 = ibm.kernel_launches()
+    gpu = 0 if world > 1 else int(os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0] or 0)
+    with ClockSampler(gpu) as clk:
+        if headline:
+            _profiler_range(True)
+        ms = s.time_iterate(args.steps)
+        if headline:
+            _profiler_range(False)
+    launches = ibm.kernel_launches() - l0
+    ms = _barrier_max(ms, world)
+    return {"solver": s, "ms": ms, "launches": launches, "launches_before": l0, "stats": s.stats(),
+            "clocks": clk.summary(), "setup_s": setup_s}
+
+
+def _vel_rel_l2(a, b):
+    """Relative L2 difference of two velocity fields (u1, u2, u3 stacked),
+    over cells finite in both."""
+    num = den = 0.0
+    for x, y in zip(a, b):
+        m = np.isfinite(x) & np.isfinite(y)
+        num += float(np.sum((x[m] - y[m]) ** 2))
+        den += float(np.sum(y[m] ** 2))
+    return (num / den) ** 0.5 if den > 0 else 0.0
+
+
 def bench_gb300(args):
     world, rank, local = _dist()
     if world > 1:
@@ -220,41 +275,51 @@ def bench_gb300(args):
     wl = importlib.import_module("2020researchproject_gb300.workloads")
     case = wl.sphere()
     ncell = (len(case["xf"]) - 1) * (len(case["yf"]) - 1) * (len(case["zf"]) - 1)
-    t0 = time.perf_counter()
-    s = wl.build_solver(ibm, case, tol=MOM_TOL, div_tol=DIV_TOL)
-    setup_s = time.perf_counter() - t0
     u0 = wl.initial_state(case)
-    s.init_flow_array(*u0)
-    s.iterate(args.warmup)
+    other = "fp64" if args.precision == "mixed" else "mixed"
 
-    # --- device-timed region: K steps, state resident in HBM.
-    _barrier(world)
-    l0 = ibm.kernel_launches()
-    print(f"[bench] setup {setup_s:.2f} s; timed region starts after {l0} kernel launches", file=sys.stderr)
-    with ClockSampler(0 if world > 1 else int(os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0] or 0)) as clk:
-        ms = s.time_iterate(args.steps)
-    launches = ibm.kernel_launches() - l0
-    ms = _barrier_max(ms, world)
-    st = s.stats()
-    value = world * ncell * args.steps / (ms / 1e3) / 1e6
+    # --- device-timed region of the headline arm, then of the other arm
+    # (same workload, same initial state, same step count).
+    head = _timed_arm(ibm, wl, case, args.precision, args, world, u0, headline=True)
+    print(f"[bench] {args.precision}: setup {head['setup_s']:.2f} s, {head['ms'] / args.steps:.2f} ms/step; timed "
+          f"region started after {head['launches_before']} kernel launches", file=sys.stderr)
+    s = head["solver"]
+    value = world * ncell * args.steps / (head["ms"] / 1e3) / 1e6
+    if args.profile_only:
+        if rank == 0:
+            print(json.dumps({"metric": "Mcell-steps/s", "value": round(value, 3), "unit": "Mcell-steps/s",
+                              "profile_only": True, "steps": args.steps, "warmup": args.warmup,
+                              "ms_per_step": round(head["ms"] / args.steps, 3),
+                              "gpu_launches": int(head["launches"]),
+                              "launches_before_timed": int(head["launches_before"])}))
+        return 0
+    sec = _timed_arm(ibm, wl, case, other, args, world, u0)
+    value2 = world * ncell * args.steps / (sec["ms"] / 1e3) / 1e6
+    vel = [s.get_field(f) for f in ("u1", "u2", "u3")]
+    vel2 = [sec["solver"].get_field(f) for f in ("u1", "u2", "u3")]
+    mixed_arm, fp64_arm = (head, sec) if args.precision == "mixed" else (sec, head)
+    err = _vel_rel_l2(vel, vel2)
+    del sec["solver"]
 
-    # --- stage profile (CUDA events per stage / per Krylov kernel).
+    # --- stage profile (host-sequenced step, CUDA events per stage).
     s.set_profiling(True)
     s.iterate(2)
     prof = s.profile()
     s.set_profiling(False)
+
+    # --- roofline of the dominant kernel: the fine-grid colour pass of the
+    # pressure multigrid (FP32 in the mixed step, FP64 in the plain one).
     peak, peak_src = measured_peak_gbs()
-    padded = (len(case["xf"]) + 3) * (len(case["yf"]) + 3) * (len(case["zf"]) + 3)
-    n_spmv, t_spmv = prof.get("spmv_p", (0, 0.0))
-    roof = None
-    if n_spmv:
-        bytes_per_launch = SPMV_P_BYTES_PER_CELL * padded
-        ach = bytes_per_launch / (t_spmv / n_spmv / 1e3) / 1e9
-        tr = traffic_per_launch("k_bicg_spmv_p")
-        roof = {"bound": "hbm", "kernel": "pressure SpMV (k_bicg_spmv_v/_t, OP_PRES)", "achieved": round(ach, 1),
-                "peak": peak, "unit": "GB/s", "frac": round(ach / peak, 4), "peak_source": peak_src,
-                "traffic": tr, "bytes_per_launch": bytes_per_launch,
-                "avg_launch_us": round(t_spmv / n_spmv * 1e3, 2)}
+    k_ms, k_bytes = s.time_kernel("mg_color", reps=50)
+    ach = k_bytes / (k_ms / 1e3) / 1e9
+    kname = "k_mg0_color_f32" if args.precision == "mixed" else "k_mg0_color_f64"
+    roof = {"bound": "hbm", "kernel": f"{kname} (fine-grid Gauss-Seidel colour pass, pressure multigrid)",
+            "achieved": round(ach, 1), "peak": peak, "unit": "GB/s", "frac": round(ach / peak, 4),
+            "peak_source": peak_src, "traffic": traffic_per_launch(kname),
+            "bytes_per_launch": k_bytes, "avg_launch_us": round(k_ms * 1e3, 2)}
+    sp_ms, sp_bytes = s.time_kernel("spmv_p", reps=50)
+    spmv = {"achieved_gbs": round(sp_bytes / (sp_ms / 1e3) / 1e9, 1), "avg_launch_us": round(sp_ms * 1e3, 2),
+            "bytes_per_launch": sp_bytes}
 
     # --- end to end through the C ABI with pinned host buffers.
     fields = ["u1", "u2", "u3", "p"]
@@ -273,22 +338,33 @@ def bench_gb300(args):
     e2e = world * ncell * args.steps / e2e_s / 1e6
     bytes_io = 4 * host[0].nbytes
 
+    st = head["stats"]
     line = {
         "metric": "Mcell-steps/s", "value": round(value, 3), "unit": "Mcell-steps/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(head["ms"] / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64" if args.precision == "mixed" else "f64", "data": "synthetic",
         "config": {"workload": case["name"], "cells": ncell, "triangles": 20480, "Re": case["re"],
-                   "dt": case["dt"], "div_tol": DIV_TOL, "momentum_tol": MOM_TOL, "parallelism": f"replicas{world}",
-                   "l2": "working set > L2 (no flush needed)", "setup_s": round(setup_s, 2),
-                   "device": s.device_name()},
+                   "dt": case["dt"], "div_tol": DIV_TOL, "momentum_tol": MOM_TOL, "precision": args.precision,
+                   "parallelism": f"replicas{world}", "l2": "working set > L2 (no flush needed)",
+                   "steps_as": "host loop" if args.host_loop else "CUDA graph per step",
+                   "setup_s": round(head["setup_s"], 2), "device": s.device_name()},
         "e2e": {"value": round(e2e, 3), "unit": "Mcell-steps/s", "h2d_bytes_per_step": bytes_io,
                 "d2h_bytes_per_step": bytes_io, "pinned": pinned},
         "roofline": roof,
-        "gpu_launches": int(launches),
-        "launches_before_timed": int(l0),
-        "clocks": clk.summary(),
-        "solver": {"iters_p": st["iters_p"], "iters_u": st["iters_u"], "max_div": st["max_div"],
-                   "mg_levels": st["mg_levels"]},
+        "spmv_p": spmv,
+        "gpu_launches": int(head["launches"]),
+        "launches_before_timed": int(head["launches_before"]),
+        "clocks": head["clocks"],
+        other: {"value": round(value2, 3), "ms_per_step": round(sec["ms"] / args.steps, 3),
+                "iters_p": sec["stats"]["iters_p"], "max_div": sec["stats"]["max_div"],
+                "gpu_launches": int(sec["launches"]), "clocks": sec["clocks"]},
+        "mixed_vs_fp64": round((mixed_arm["ms"] and fp64_arm["ms"] / mixed_arm["ms"]) or 0, 3),
+        "error_vs_fp64": {"velocity_rel_l2": err, "max_div_mixed": mixed_arm["stats"]["max_div"],
+                          "max_div_fp64": fp64_arm["stats"]["max_div"],
+                          "note": f"after {args.warmup + args.steps} steps from the same state"},
+        "solver": {"iters_p": st["iters_p"], "iters_u": st["iters_u"], "outer_p": st["outer_p"],
+                   "max_div": st["max_div"], "mg_levels": st["mg_levels"]},
         "profile_ms": {k: [v[0], round(v[1], 3)] for k, v in sorted(prof.items())},
     }
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -310,6 +386,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--host-loop", action="store_true",
+                    help="host-sequenced steps instead of recorded graphs (same kernels; for ncu launch lists, "
+                         "which do not list kernels inside graph loops)")
+    ap.add_argument("--profile-only", action="store_true",
+                    help="headline arm only (set-up, warm-up, timed region) for profiler runs")
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"],
+                    help="arithmetic of the headline arm (the other one is measured beside it)")
     ap.add_argument("--lvset-from-gpu", action="store_true",
                     help="reference arm: take the level set from the GPU set-up instead of the CPU transform")
     args = ap.parse_args()

@@ -114,6 +114,16 @@ void IBMSolver_get_stats(const IBMSolver *, IBMSolverStats *);
    the solver's stream and returns the elapsed device milliseconds. */
 double IBMSolver_time_iterate(IBMSolver *, int nsteps);
 
+/* Device time of one launch of a hot kernel on the solver's current data,
+   in the current precision: the average over reps launches between CUDA
+   events on the solver's stream (ms), and its algorithmic bytes per launch
+   in *bytes (for a roofline).  IBM3D_K_MG_COLOR: one colour pass of the
+   pressure multigrid's fine-grid smoother; IBM3D_K_SPMV_P: one pressure
+   operator application.  Both run on scratch vectors of the pressure
+   solve; the flow state is untouched. */
+enum { IBM3D_K_MG_COLOR = 0, IBM3D_K_SPMV_P = 1 };
+double IBMSolver_time_kernel(IBMSolver *, int which, int reps, double *bytes);
+
 /* Per-stage device time accumulated while profiling is on (CUDA events
    around each stage of each step).  Stage names: conv_rhs, tau, mom_solve,
    ustar_prhs, p_solve, update_next, fill_outer, ghost_update; plus the
