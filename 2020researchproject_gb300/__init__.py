@@ -100,7 +100,7 @@ def load_library(path: str = LIB_PATH):
         "IBMSolver_set_precision": (None, [vp, i]),
         "IBMSolver_set_graphs": (None, [vp, i]),
         "IBMSolver_time_kernel": (ctypes.c_double, [vp, i, i, ctypes.POINTER(ctypes.c_double)]),
-        "IBMSolver_set_multigrid": (None, [vp, i, i, i, i, i]),
+        "IBMSolver_set_multigrid": (None, [vp, i, i, i, i, i, ctypes.c_double]),
         "IBMSolver_get_field": (None, [vp, i, dp]),
         "IBMSolver_get_flag": (None, [vp, ip]),
         "IBMSolver_sync_host": (None, [vp]),
@@ -237,8 +237,8 @@ class IBMSolver:
     def set_div_tol(self, div_tol):
         self._lib.IBMSolver_set_div_tol(self._s, div_tol)
 
-    def set_multigrid(self, nu_pre=3, nu_post=3, nuc_pre=2, nuc_post=2, coarse_sweeps=10):
-        self._lib.IBMSolver_set_multigrid(self._s, nu_pre, nu_post, nuc_pre, nuc_post, coarse_sweeps)
+    def set_multigrid(self, nu_pre=5, nu_post=5, nuc_pre=1, nuc_post=1, coarse_sweeps=8, omega=1.0):
+        self._lib.IBMSolver_set_multigrid(self._s, nu_pre, nu_post, nuc_pre, nuc_post, coarse_sweeps, float(omega))
         self._check("IBMSolver_set_multigrid")
 
     def time_kernel(self, which, reps=20):

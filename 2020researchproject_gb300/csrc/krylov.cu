@@ -32,6 +32,24 @@ template <typename T> struct AccT;
 template <> struct AccT<double> { using type = double; };
 template <> struct AccT<float> { using type = float; };
 
+// 16-byte packs for the streaming vector kernels: with n % 4 == 0 every
+// vector (and every component of a 3-component vector) starts on a 16-byte
+// boundary, and a thread moves PW elements per load.
+template <typename T>
+struct alignas(16) Pack {
+    T v[16 / sizeof(T)];
+};
+template <typename T>
+constexpr int PW = 16 / sizeof(T);
+template <typename T>
+__device__ __forceinline__ Pack<T> ldp(const T *p, long long q) {
+    return reinterpret_cast<const Pack<T> *>(p)[q];
+}
+template <typename T>
+__device__ __forceinline__ void stp(T *p, long long q, const Pack<T> &x) {
+    reinterpret_cast<Pack<T> *>(p)[q] = x;
+}
+
 // Weighted |r| for the divergence criterion (FP32 is ample for a stopping test).
 template <typename T>
 __device__ __forceinline__ float divw(const OpT<T> &c, long long P, T y) {
@@ -139,15 +157,26 @@ k_bicg_init(const long long n, const T *__restrict__ b, T *x, T *r, T *r0, T *p,
 }
 
 // ------------------------------------------------- p = r + beta (p - w v) --
-template <typename T, int NC>
+template <typename T, int NC, bool VEC>
 __global__ void __launch_bounds__(KTHREADS)
-k_bicg_p(const long long n, const T *__restrict__ r, T *p, const T *__restrict__ v, const KScal *sc) {
+k_bicg_p(const long long n, const T *__restrict__ r, T *__restrict__ p, const T *__restrict__ v, const KScal *sc) {
 #pragma unroll
     for (int c = 0; c < NC; c++) {
         if (sc[c].state != KS_RUN) continue;
         const T beta = (T)sc[c].beta, om = (T)sc[c].omega;
         const long long o = c * n;
-        GRID_STRIDE(P, n) { p[o + P] = r[o + P] + beta * (p[o + P] - om * v[o + P]); }
+        if (VEC) {
+            const long long np = n / PW<T>, op = o / PW<T>;
+            GRID_STRIDE(q, np) {
+                const Pack<T> rr = ldp(r, op + q), vv = ldp(v, op + q);
+                Pack<T> pp = ldp(p, op + q);
+#pragma unroll
+                for (int l = 0; l < PW<T>; l++) pp.v[l] = rr.v[l] + beta * (pp.v[l] - om * vv.v[l]);
+                stp(p, op + q, pp);
+            }
+        } else {
+            GRID_STRIDE(P, n) { p[o + P] = r[o + P] + beta * (p[o + P] - om * v[o + P]); }
+        }
     }
 }
 
@@ -160,6 +189,7 @@ __device__ __forceinline__ void sweep_rows(const OpT<T> &A, const bool (&run)[NC
         if (j >= A.g.ny || k >= A.g.nz) return;
         const Column<T> q = column(A, j, k);
         long long P = cidx(A.g, i0, j, k);
+#pragma unroll 2
         for (int i = i0; i < i1; i++, P += A.g.sx) {
 #pragma unroll
             for (int c = 0; c < NC; c++)
@@ -178,7 +208,7 @@ __device__ __forceinline__ void sweep_rows(const OpT<T> &A, const bool (&run)[NC
 // ------------------------------------------- v = A ph, alpha = rho/(r0,v) --
 template <typename T, int NC>
 __global__ void __launch_bounds__(SW_THREADS)
-k_bicg_spmv_v(const OpT<T> A, const int op, const long long n, const T *__restrict__ ph, T *v,
+k_bicg_spmv_v(const OpT<T> A, const int op, const long long n, const T *__restrict__ ph, T *__restrict__ v,
               const T *__restrict__ r0, KScal *sc, double *partials, unsigned int *counter) {
     __shared__ double smem[32 * NC];
     typename AccT<T>::type a[NC];
@@ -219,10 +249,10 @@ k_bicg_spmv_v(const OpT<T> A, const int op, const long long n, const T *__restri
 }
 
 // ------------------------------------------------------- s = r - alpha v --
-template <typename T, int NC>
+template <typename T, int NC, bool VEC>
 __global__ void __launch_bounds__(KTHREADS)
-k_bicg_s(const OpT<T> A, const long long n, const T *__restrict__ r, const T *__restrict__ v, T *s, KScal *sc,
-         double *partials, unsigned int *counter) {
+k_bicg_s(const OpT<T> A, const long long n, const T *__restrict__ r, const T *__restrict__ v, T *__restrict__ s,
+         KScal *sc, double *partials, unsigned int *counter) {
     __shared__ double smem[32 * (NC + 1)];
     typename AccT<T>::type a[NC];
 #pragma unroll
@@ -234,11 +264,27 @@ k_bicg_s(const OpT<T> A, const long long n, const T *__restrict__ r, const T *__
         if (sc[c].state != KS_RUN) continue;
         const T al = (T)sc[c].alpha;
         const long long o = c * n;
-        GRID_STRIDE(P, n) {
-            const T y = r[o + P] - al * v[o + P];
-            s[o + P] = y;
-            a[c] += y * y;
-            if (want_div) dmax = fmaxf(dmax, divw(A, P, y));
+        if (VEC) {
+            const long long np = n / PW<T>, op = o / PW<T>;
+            GRID_STRIDE(q, np) {
+                const Pack<T> rr = ldp(r, op + q), vv = ldp(v, op + q);
+                Pack<T> ss;
+#pragma unroll
+                for (int l = 0; l < PW<T>; l++) {
+                    const T y = rr.v[l] - al * vv.v[l];
+                    ss.v[l] = y;
+                    a[c] += y * y;
+                    if (want_div) dmax = fmaxf(dmax, divw(A, q * PW<T> + l, y));
+                }
+                stp(s, op + q, ss);
+            }
+        } else {
+            GRID_STRIDE(P, n) {
+                const T y = r[o + P] - al * v[o + P];
+                s[o + P] = y;
+                a[c] += y * y;
+                if (want_div) dmax = fmaxf(dmax, divw(A, P, y));
+            }
         }
     }
     double acc[NC + 1];
@@ -261,7 +307,7 @@ k_bicg_s(const OpT<T> A, const long long n, const T *__restrict__ r, const T *__
 // --------------------------------------- t = A sh, omega = (t,s)/(t,t) --
 template <typename T, int NC>
 __global__ void __launch_bounds__(SW_THREADS)
-k_bicg_spmv_t(const OpT<T> A, const int op, const long long n, const T *__restrict__ sh, T *t,
+k_bicg_spmv_t(const OpT<T> A, const int op, const long long n, const T *__restrict__ sh, T *__restrict__ t,
               const T *__restrict__ s, KScal *sc, double *partials, unsigned int *counter) {
     __shared__ double smem[32 * 2 * NC];
     typename AccT<T>::type a[2 * NC];
@@ -307,11 +353,11 @@ k_bicg_spmv_t(const OpT<T> A, const int op, const long long n, const T *__restri
 // ------------------- x += alpha ph + omega sh, r = s - omega t, new rho --
 // Ends the iteration: sets the loop condition (some component still
 // running and below maxit).
-template <typename T, int NC>
+template <typename T, int NC, bool VEC>
 __global__ void __launch_bounds__(KTHREADS)
-k_bicg_xr(const OpT<T> A, const long long n, T *x, T *r, const T *__restrict__ r0, const T *__restrict__ ph,
-          const T *__restrict__ sh, const T *__restrict__ s, const T *__restrict__ t, KScal *sc, double *partials,
-          unsigned int *counter, const int maxit, const LoopCtl lc) {
+k_bicg_xr(const OpT<T> A, const long long n, T *__restrict__ x, T *__restrict__ r, const T *__restrict__ r0,
+          const T *__restrict__ ph, const T *__restrict__ sh, const T *__restrict__ s, const T *__restrict__ t,
+          KScal *sc, double *partials, unsigned int *counter, const int maxit, const LoopCtl lc) {
     __shared__ double smem[32 * (2 * NC + 1)];
     typename AccT<T>::type a[2 * NC];
 #pragma unroll
@@ -333,13 +379,34 @@ k_bicg_xr(const OpT<T> A, const long long n, T *x, T *r, const T *__restrict__ r
         }
         if (state != KS_RUN) continue;
         const T al = (T)sc[c].alpha, om = (T)sc[c].omega;
-        GRID_STRIDE(P, n) {
-            x[o + P] += al * ph[o + P] + om * sh[o + P];
-            const T y = s[o + P] - om * t[o + P];
-            r[o + P] = y;
-            a[2 * c] += y * y;
-            a[2 * c + 1] += r0[o + P] * y;
-            if (want_div) dmax = fmaxf(dmax, divw(A, P, y));
+        if (VEC) {
+            const long long np = n / PW<T>, op = o / PW<T>;
+            GRID_STRIDE(q, np) {
+                Pack<T> xx = ldp(x, op + q);
+                const Pack<T> pp = ldp(ph, op + q), ss = ldp(sh, op + q), s0 = ldp(s, op + q), tt = ldp(t, op + q),
+                              rr0 = ldp(r0, op + q);
+                Pack<T> rr;
+#pragma unroll
+                for (int l = 0; l < PW<T>; l++) {
+                    xx.v[l] += al * pp.v[l] + om * ss.v[l];
+                    const T y = s0.v[l] - om * tt.v[l];
+                    rr.v[l] = y;
+                    a[2 * c] += y * y;
+                    a[2 * c + 1] += rr0.v[l] * y;
+                    if (want_div) dmax = fmaxf(dmax, divw(A, q * PW<T> + l, y));
+                }
+                stp(x, op + q, xx);
+                stp(r, op + q, rr);
+            }
+        } else {
+            GRID_STRIDE(P, n) {
+                x[o + P] += al * ph[o + P] + om * sh[o + P];
+                const T y = s[o + P] - om * t[o + P];
+                r[o + P] = y;
+                a[2 * c] += y * y;
+                a[2 * c + 1] += r0[o + P] * y;
+                if (want_div) dmax = fmaxf(dmax, divw(A, P, y));
+            }
         }
     }
     double acc[2 * NC + 1];
@@ -592,8 +659,11 @@ static void first_half(cudaStream_t st, const OpT<T> &A, int op, KrylovWork<T> &
     const long long n = w.n;
     const int nc = w.nc;
     const int *gate = nc == 1 ? &w.scal[0].state : nullptr;
-    if (nc == 3) k_bicg_p<T, 3><<<KBLOCKS, KTHREADS, 0, st>>>(n, w.r, w.p, w.v, w.scal);
-    else k_bicg_p<T, 1><<<KBLOCKS, KTHREADS, 0, st>>>(n, w.r, w.p, w.v, w.scal);
+    const bool vec = n % 4 == 0;
+    if (nc == 3 && vec) k_bicg_p<T, 3, true><<<KBLOCKS, KTHREADS, 0, st>>>(n, w.r, w.p, w.v, w.scal);
+    else if (nc == 3) k_bicg_p<T, 3, false><<<KBLOCKS, KTHREADS, 0, st>>>(n, w.r, w.p, w.v, w.scal);
+    else if (vec) k_bicg_p<T, 1, true><<<KBLOCKS, KTHREADS, 0, st>>>(n, w.r, w.p, w.v, w.scal);
+    else k_bicg_p<T, 1, false><<<KBLOCKS, KTHREADS, 0, st>>>(n, w.r, w.p, w.v, w.scal);
     note_launches(1);
     if (M) {
         const int tm = prof_begin(pf, "mg_vcycle");
@@ -609,8 +679,10 @@ static void first_half(cudaStream_t st, const OpT<T> &A, int op, KrylovWork<T> &
                                                                 w.counter);
     note_launches(1);
     prof_end(pf, tm);
-    if (nc == 3) k_bicg_s<T, 3><<<KBLOCKS, KTHREADS, 0, st>>>(A, n, w.r, w.v, w.s, w.scal, w.partials, w.counter);
-    else k_bicg_s<T, 1><<<KBLOCKS, KTHREADS, 0, st>>>(A, n, w.r, w.v, w.s, w.scal, w.partials, w.counter);
+    if (nc == 3 && vec) k_bicg_s<T, 3, true><<<KBLOCKS, KTHREADS, 0, st>>>(A, n, w.r, w.v, w.s, w.scal, w.partials, w.counter);
+    else if (nc == 3) k_bicg_s<T, 3, false><<<KBLOCKS, KTHREADS, 0, st>>>(A, n, w.r, w.v, w.s, w.scal, w.partials, w.counter);
+    else if (vec) k_bicg_s<T, 1, true><<<KBLOCKS, KTHREADS, 0, st>>>(A, n, w.r, w.v, w.s, w.scal, w.partials, w.counter);
+    else k_bicg_s<T, 1, false><<<KBLOCKS, KTHREADS, 0, st>>>(A, n, w.r, w.v, w.s, w.scal, w.partials, w.counter);
     note_launches(1);
 }
 
@@ -636,12 +708,13 @@ static void second_half(cudaStream_t st, const OpT<T> &A, int op, KrylovWork<T> 
 
 template <typename T>
 static void launch_xr(cudaStream_t st, const OpT<T> &A, KrylovWork<T> &w, T *x, int maxit, LoopCtl lc) {
-    if (w.nc == 3)
-        k_bicg_xr<T, 3><<<KBLOCKS, KTHREADS, 0, st>>>(A, w.n, x, w.r, w.r0, w.ph, w.sh, w.s, w.t, w.scal,
-                                                     w.partials, w.counter, maxit, lc);
-    else
-        k_bicg_xr<T, 1><<<KBLOCKS, KTHREADS, 0, st>>>(A, w.n, x, w.r, w.r0, w.ph, w.sh, w.s, w.t, w.scal,
-                                                     w.partials, w.counter, maxit, lc);
+#define XR_ARGS A, w.n, x, w.r, w.r0, w.ph, w.sh, w.s, w.t, w.scal, w.partials, w.counter, maxit, lc
+    const bool vec = w.n % 4 == 0;
+    if (w.nc == 3 && vec) k_bicg_xr<T, 3, true><<<KBLOCKS, KTHREADS, 0, st>>>(XR_ARGS);
+    else if (w.nc == 3) k_bicg_xr<T, 3, false><<<KBLOCKS, KTHREADS, 0, st>>>(XR_ARGS);
+    else if (vec) k_bicg_xr<T, 1, true><<<KBLOCKS, KTHREADS, 0, st>>>(XR_ARGS);
+    else k_bicg_xr<T, 1, false><<<KBLOCKS, KTHREADS, 0, st>>>(XR_ARGS);
+#undef XR_ARGS
     note_launches(1);
 }
 

@@ -86,7 +86,7 @@ constexpr int MG0_PLANES = 4;
 template <typename T>
 __global__ void __launch_bounds__(256)
 k_mg0_color(const OpT<T> c, const T *__restrict__ r, T *__restrict__ z, const int color, const int pairs,
-            const Per3 per, const int *gate) {
+            const Per3 per, const T omega, const int *gate) {
     MG_GATE(gate);
     const Grid &g = c.g;
     const int j = blockIdx.y * 8 + threadIdx.y;
@@ -117,10 +117,12 @@ k_mg0_color(const OpT<T> c, const T *__restrict__ r, T *__restrict__ z, const in
         const uint8_t fl = c.flag[P];
         const T rv = r[P], dv = c.dinv[P];
         const T zw = z[P - sx], ze = z[P + sx], zs = z[P - sy], zn = z[P + sy], zd = z[P - 1], zu = z[P + 1];
+        const T zc = z[P];
         const int I = i + 2, K = k + 2;
         const T nb = c.km[0][I] * zw + c.kp[0][I] * ze + kmy * zs + kpy * zn + c.km[2][K] * zd + c.kp[2][K] * zu;
         const bool fluid = fl == FLUID && !(c.p_singular && P == c.pinned);
-        val[p] = fluid ? rv + dv * nb : rv;
+        const T gs = rv + dv * nb;
+        val[p] = fluid ? (omega == (T)1 ? gs : zc + omega * (gs - zc)) : rv;
         upd[p] = ok && fl != GHOST;
         Ps[p] = P;
     }
@@ -166,18 +168,6 @@ __device__ __forceinline__ T ghost_value(const OpT<T> &c, const T *__restrict__ 
 }
 
 template <typename T>
-__global__ void k_mg0_ghost(const OpT<T> c, const T *__restrict__ r, const T *__restrict__ z,
-                            const int *__restrict__ gcell, const int ng, T *tmp, const int *gate) {
-    MG_GATE(gate);
-    GRID_STRIDE(g, (long long)ng) {
-        const int P = gcell[g];
-        const int id = c.gid[P];
-        (void)id;
-        tmp[g] = ghost_value(c, r, z, P);
-    }
-}
-
-template <typename T>
 __global__ void k_mg0_ghost_scatter(const int *__restrict__ gcell, const int ng, const T *__restrict__ tmp, T *z,
                                     const int *gate) {
     MG_GATE(gate);
@@ -193,16 +183,11 @@ __global__ void k_mg0_ghost_scatter(const int *__restrict__ gcell, const int ng,
 // interior values alone: one launch, no ordering between outer cells, and
 // no thread reads an outer value another thread writes.
 template <typename T>
-__global__ void __launch_bounds__(256)
-k_mg0_outer(const OpT<T> c, const T *__restrict__ r, T *z, const int *__restrict__ outer, const int nout,
-            const int *gate) {
-    MG_GATE(gate);
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nout) return;
+__device__ __forceinline__ T outer_chain_value(const OpT<T> &c, const T *__restrict__ r, const T *z, long long P0) {
     long long chain[4];
     int face[4], layer[4];
     int n = 0;
-    long long Q = outer[t];
+    long long Q = P0;
     T v = 0;
     while (n < 4) {
         int i, j, k, L;
@@ -234,7 +219,27 @@ k_mg0_outer(const OpT<T> c, const T *__restrict__ r, T *z, const int *__restrict
         default: v = r[P] + v; break;
         }
     }
-    z[outer[t]] = v;
+    return v;
+}
+
+// The outer rows and the ghost rows of one smoother sweep in one launch:
+// blocks [0, gblocks) compute the ghost values into tmp (from z before the
+// pass, Jacobi-style), the others set the outer cells by chains; a chain
+// that ends on a ghost cell reads its value before the pass as well.  The
+// ghost values reach z in the following scatter launch.
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_mg0_outer(const OpT<T> c, const T *__restrict__ r, T *z, const int *__restrict__ outer, const int nout,
+            const int *__restrict__ gcell, const int ng, const int gblocks, T *tmp, const int *gate) {
+    MG_GATE(gate);
+    if ((int)blockIdx.x < gblocks) {
+        const int g = blockIdx.x * blockDim.x + threadIdx.x;
+        if (g < ng) tmp[g] = ghost_value(c, r, z, gcell[g]);
+        return;
+    }
+    const int t = (blockIdx.x - gblocks) * blockDim.x + threadIdx.x;
+    if (t >= nout) return;
+    z[outer[t]] = outer_chain_value(c, r, z, outer[t]);
 }
 
 // 3-D launch over an (nx, ny, nz) box: threads along k, blocks along
@@ -688,6 +693,19 @@ int GMG<T>::setup(cudaStream_t s, const OpT<double> &A64, const OpT<T> &A, const
         return p;
     };
     if (nghost > 0) ghost_tmp_ = (T *)dalloc(sizeof(T) * nghost, true);
+    // Does any ghost interpolation stencil reach an outer cell?  Then the
+    // ghost and outer rows of a sweep cannot share a launch.
+    ghost_reads_outer_ = false;
+    if (nghost > 0) {
+        std::vector<int> gidx(8 * (size_t)nghost);
+        cudaMemcpy(gidx.data(), A.gidx, sizeof(int) * gidx.size(), cudaMemcpyDeviceToHost);
+        for (int q : gidx) {
+            if (q < 0) continue;
+            int i, j, k;
+            cijk(g, q, i, j, k);
+            if (i < 0 || i >= g.nx || j < 0 || j >= g.ny || k < 0 || k >= g.nz) ghost_reads_outer_ = true;
+        }
+    }
 
     Per3 per{{per_[0], per_[1], per_[2]}};
     int nx = g.nx, ny = g.ny, nz = g.nz;
@@ -789,15 +807,25 @@ int GMG<T>::smooth0(cudaStream_t s, const T *r, T *z, int sweeps, bool from_zero
             if (it == 0 && col == 0 && from_zero)
                 k_mg0_init<T><<<nblk(g.ncell, 256), 256, 0, s>>>(A_, r, z, per, gate);
             else
-                k_mg0_color<T><<<grd, blk, 0, s>>>(A_, r, z, col, seam ? 0 : 1, per, gate);
+                k_mg0_color<T><<<grd, blk, 0, s>>>(A_, r, z, col, seam ? 0 : 1, per, (T)cfg_.omega, gate);
+        }
+        const int gb = (nghost_ + 255) / 256, ob = (A_.sw.nout + 255) / 256;
+        if (!ghost_reads_outer_) {
+            k_mg0_outer<T><<<gb + ob, 256, 0, s>>>(A_, r, z, A_.sw.outer, A_.sw.nout, ghost_cell_, nghost_, gb,
+                                                  ghost_tmp_, gate);
+            k++;
+        } else {  // a ghost stencil reaches an outer cell: ghosts first, outer rows after the scatter
+            k_mg0_outer<T><<<gb, 256, 0, s>>>(A_, r, z, A_.sw.outer, 0, ghost_cell_, nghost_, gb, ghost_tmp_, gate);
+            k++;
         }
         if (nghost_ > 0) {
-            k_mg0_ghost<T><<<nblk(nghost_, 128), 128, 0, s>>>(A_, r, z, ghost_cell_, nghost_, ghost_tmp_, gate);
             k_mg0_ghost_scatter<T><<<nblk(nghost_, 128), 128, 0, s>>>(ghost_cell_, nghost_, ghost_tmp_, z, gate);
-            k += 2;
+            k++;
         }
-        k_mg0_outer<T><<<(A_.sw.nout + 255) / 256, 256, 0, s>>>(A_, r, z, A_.sw.outer, A_.sw.nout, gate);
-        k++;
+        if (ghost_reads_outer_) {
+            k_mg0_outer<T><<<ob, 256, 0, s>>>(A_, r, z, A_.sw.outer, A_.sw.nout, ghost_cell_, 0, 0, ghost_tmp_, gate);
+            k++;
+        }
     }
     return k;
 }
@@ -871,7 +899,8 @@ float GMG<T>::time_color(cudaStream_t s, const T *r, T *z, int reps, double *byt
     cudaEventCreate(&a);
     cudaEventCreate(&b);
     cudaEventRecord(a, s);
-    for (int q = 0; q < reps; q++) k_mg0_color<T><<<grd, blk, 0, s>>>(A_, r, z, 1, seam ? 0 : 1, per, nullptr);
+    for (int q = 0; q < reps; q++)
+        k_mg0_color<T><<<grd, blk, 0, s>>>(A_, r, z, 1, seam ? 0 : 1, per, (T)cfg_.omega, nullptr);
     cudaEventRecord(b, s);
     cudaEventSynchronize(b);
     float ms = 0;

@@ -41,9 +41,10 @@ struct MGLevel {
 };
 
 struct GMGConfig {
-    int nu_pre = 3, nu_post = 3;    // fine grid
-    int nuc_pre = 2, nuc_post = 2;  // coarse levels above the coarsest
-    int coarse_sweeps = 10;         // coarsest level
+    int nu_pre = 5, nu_post = 5;    // fine grid
+    int nuc_pre = 1, nuc_post = 1;  // coarse levels above the coarsest
+    int coarse_sweeps = 8;          // coarsest level
+    double omega = 1.0;             // over-relaxation of the fine-grid fluid rows
 };
 
 // Host geometry of the fine grid: interior face coordinates per axis.
@@ -63,6 +64,7 @@ class GMG : public Preconditioner<T> {
     int launches() const override { return launches_; }
     // Smoother sweeps (pre, post) on the fine grid and on the coarse levels,
     // and on the coarsest level; takes effect at the next apply.
+    void set_omega(double w) { cfg_.omega = w; }
     void set_sweeps(int nu_pre, int nu_post, int nuc_pre, int nuc_post, int coarse) {
         cfg_.nu_pre = nu_pre;
         cfg_.nu_post = nu_post;
@@ -87,6 +89,7 @@ class GMG : public Preconditioner<T> {
     const int *ghost_cell_ = nullptr;
     int nghost_ = 0;
     T *ghost_tmp_ = nullptr;
+    bool ghost_reads_outer_ = false;
     int per_[3] = {0, 0, 0};
     std::vector<void *> allocs_;
     int launches_ = 0;

@@ -137,21 +137,23 @@ __device__ __forceinline__ Column<T> column(const OpT<T> &c, int j, int k) {
 }
 
 // Row of an interior cell (i, j, k) at padded index P: the same arithmetic
-// as op_row without the index decode and the outer-face test.
+// as op_row without the index decode and the outer-face test, and
+// branch-free for fluid, solid and pinned rows (every load issued up
+// front, the result selected); ghost rows, a few per thousand, branch.
 template <typename T>
 __device__ __forceinline__ T interior_row(const OpT<T> &c, int op, const T *__restrict__ x, long long P, int i,
                                           const Column<T> &q) {
-    if (op == OP_PRES && c.p_singular && P == c.pinned) return x[P];
     const uint8_t fl = c.flag[P];
-    if (fl == FLUID) {
-        const int I = i + 2;
-        const long long sx = c.g.sx, sy = c.g.sy;
-        const T nb = c.km[0][I] * x[P - sx] + c.kp[0][I] * x[P + sx] + q.kmy * x[P - sy] + q.kpy * x[P + sy] +
-                     q.kmz * x[P - 1] + q.kpz * x[P + 1];
-        if (op == OP_MOM) return ((T)1 + c.ks[0][I] + q.ksy + q.ksz) * x[P] - nb;
-        return x[P] - c.dinv[P] * nb;
-    }
-    if (fl == GHOST) {
+    const int I = i + 2;
+    const long long sx = c.g.sx, sy = c.g.sy;
+    const T xc = x[P], xw = x[P - sx], xe = x[P + sx], xs = x[P - sy], xn = x[P + sy], xd = x[P - 1], xu = x[P + 1];
+    const T nb = c.km[0][I] * xw + c.kp[0][I] * xe + q.kmy * xs + q.kpy * xn + q.kmz * xd + q.kpz * xu;
+    T y;
+    if (op == OP_MOM) y = ((T)1 + c.ks[0][I] + q.ksy + q.ksz) * xc - nb;
+    else y = xc - c.dinv[P] * nb;
+    const bool pinned = op == OP_PRES && c.p_singular && P == c.pinned;
+    if (fl != FLUID || pinned) y = xc;
+    if (fl == GHOST && !pinned) {
         const int g = c.gid[P];
         T sum = 0;
 #pragma unroll
@@ -160,9 +162,9 @@ __device__ __forceinline__ T interior_row(const OpT<T> &c, int op, const T *__re
             if (m >= 0) sum += c.gw[8 * g + e] * x[m];
         }
         const T ws = c.gwself[g];
-        return op == OP_MOM ? ((T)1 + ws) * x[P] + sum : ((T)1 - ws) * x[P] - sum;
+        y = op == OP_MOM ? ((T)1 + ws) * xc + sum : ((T)1 - ws) * xc - sum;
     }
-    return x[P];
+    return y;
 }
 
 // One row of A applied to x (op OP_MOM with component comp, or OP_PRES).

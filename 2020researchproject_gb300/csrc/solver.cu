@@ -109,7 +109,8 @@ struct ibm3d_device {
     bool abort_on_error = true;
     // Recorded steps.
     bool use_graphs = true;
-    int mg_sweeps[5] = {3, 3, 2, 2, 10};  // multigrid sweeps: fine pre/post, coarse pre/post, coarsest
+    int mg_sweeps[5] = {5, 5, 1, 1, 8};  // multigrid sweeps: fine pre/post, coarse pre/post, coarsest
+    double mg_omega = 1.0;               // over-relaxation of the fine-grid smoother
     cudaStream_t aux[2] = {nullptr, nullptr};
     std::vector<StepGraph> graphs;
     GraphSig gsig{};
@@ -1250,6 +1251,7 @@ void IBMSolver_assemble(IBMSolver *s) {
     mc.nuc_pre = d->mg_sweeps[2];
     mc.nuc_post = d->mg_sweeps[3];
     mc.coarse_sweeps = d->mg_sweeps[4];
+    mc.omega = d->mg_omega;
     const int *gcell = d->nghost ? d->gargs.cell : nullptr;
     d->mg = new GMG<double>();
     d->mg32 = new GMG<float>();
@@ -1525,16 +1527,25 @@ void IBMSolver_set_smagorinsky(IBMSolver *s, double Cs) {
 
 void IBMSolver_set_div_tol(IBMSolver *s, double div_tol) { s->dev->divtol = div_tol; }
 
-void IBMSolver_set_multigrid(IBMSolver *s, int nu_pre, int nu_post, int nuc_pre, int nuc_post, int coarse_sweeps) {
+void IBMSolver_set_multigrid(IBMSolver *s, int nu_pre, int nu_post, int nuc_pre, int nuc_post, int coarse_sweeps,
+                             double omega) {
     ibm3d_device *d = s->dev;
-    if (nu_pre < 0 || nu_post < 0 || nuc_pre < 0 || nuc_post < 0 || coarse_sweeps < 1 || nu_pre + nu_post < 1) {
-        set_status(s, IBM3D_EARG, "IBMSolver_set_multigrid: invalid sweep counts");
+    if (nu_pre < 0 || nu_post < 0 || nuc_pre < 0 || nuc_post < 0 || coarse_sweeps < 1 || nu_pre + nu_post < 1 ||
+        !(omega > 0.0 && omega < 2.0)) {
+        set_status(s, IBM3D_EARG, "IBMSolver_set_multigrid: invalid sweep counts or relaxation weight");
         return;
     }
     const int v[5] = {nu_pre, nu_post, nuc_pre, nuc_post, coarse_sweeps};
     for (int q = 0; q < 5; q++) d->mg_sweeps[q] = v[q];
-    if (d->mg) d->mg->set_sweeps(nu_pre, nu_post, nuc_pre, nuc_post, coarse_sweeps);
-    if (d->mg32) d->mg32->set_sweeps(nu_pre, nu_post, nuc_pre, nuc_post, coarse_sweeps);
+    d->mg_omega = omega;
+    if (d->mg) {
+        d->mg->set_sweeps(nu_pre, nu_post, nuc_pre, nuc_post, coarse_sweeps);
+        d->mg->set_omega(omega);
+    }
+    if (d->mg32) {
+        d->mg32->set_sweeps(nu_pre, nu_post, nuc_pre, nuc_post, coarse_sweeps);
+        d->mg32->set_omega(omega);
+    }
     drop_graphs(d);
 }
 
