@@ -115,6 +115,13 @@ def load_library(path: str = LIB_PATH):
         "IBMSolver_kernel_launches": (ctypes.c_longlong, []),
         "IBMSolver_host_register": (i, [vp, ctypes.c_size_t]),
         "IBMSolver_host_unregister": (i, [vp]),
+        "IBMBatch_new": (vp, []),
+        "IBMBatch_destroy": (None, [vp]),
+        "IBMBatch_add": (i, [vp, vp]),
+        "IBMBatch_remove": (i, [vp, vp]),
+        "IBMBatch_size": (i, [vp]),
+        "IBMBatch_iterate": (d, [vp, i]),
+        "IBMBatch_last_status": (i, [vp]),
         "Polyhedron_new": (vp, []),
         "Polyhedron_destroy": (None, [vp]),
         "Polyhedron_read_stl": (None, [vp, vp]),
@@ -355,3 +362,42 @@ class IBMSolver:
 
     def device_name(self):
         return self._lib.IBMSolver_device_name(self._s).decode()
+
+
+class Batch:
+    """Independent solvers advanced together, one CUDA graph launch per
+    batched step (IBMBatch_* of include/ibm3d_gb300.h).  Each member gets
+    exactly the results IBMSolver.iterate gives it alone."""
+
+    def __init__(self, solvers=()):
+        self._lib = load_library()
+        self._b = self._lib.IBMBatch_new()
+        self._members = []
+        for s in solvers:
+            self.add(s)
+
+    def add(self, solver):
+        if self._lib.IBMBatch_add(self._b, solver._s) != 0:
+            raise IBM3DError("IBMBatch_add failed (solver not assembled?)")
+        self._members.append(solver)
+
+    def remove(self, solver):
+        if self._lib.IBMBatch_remove(self._b, solver._s) != 0:
+            raise IBM3DError("IBMBatch_remove: not a member")
+        self._members.remove(solver)
+
+    def __len__(self):
+        return len(self._members)
+
+    def iterate(self, nsteps=1):
+        """Advances every member nsteps steps; returns device milliseconds."""
+        ms = self._lib.IBMBatch_iterate(self._b, int(nsteps))
+        st = self._lib.IBMBatch_last_status(self._b)
+        if ms < 0 or st not in (0, 1):
+            raise IBM3DError(f"IBMBatch_iterate: {STATUS.get(st, st)}")
+        return ms
+
+    def __del__(self):
+        if getattr(self, "_b", None):
+            self._lib.IBMBatch_destroy(self._b)
+            self._b = None

@@ -564,6 +564,7 @@ int KrylovWork<T>::allocate(long long ncell, int ncomp, bool precond, int maxblo
     release();
     n = ncell;
     nc = ncomp;
+    nblk = vector_blocks(ncell);
     const int nvec = precond ? 8 : 6;
     const size_t bytes = sizeof(T) * (size_t)n * nc * nvec;
     if (cudaMalloc(&base, bytes) != cudaSuccess) return -1;
@@ -586,7 +587,7 @@ int KrylovWork<T>::allocate(long long ncell, int ncomp, bool precond, int maxblo
     if (cudaMalloc(&scal, sizeof(KScal) * 3) != cudaSuccess) return -1;
     cudaMemset(scal, 0, sizeof(KScal) * 3);
     if (cudaMallocHost(&scal_h, sizeof(KScal) * 3) != cudaSuccess) return -1;
-    if (cudaMalloc(&partials, sizeof(double) * std::max(KBLOCKS, maxblocks) * 10) != cudaSuccess) return -1;
+    if (cudaMalloc(&partials, sizeof(double) * std::max(nblk, maxblocks) * 10) != cudaSuccess) return -1;
     if (cudaMalloc(&counter, sizeof(unsigned int)) != cudaSuccess) return -1;
     cudaMemset(counter, 0, sizeof(unsigned int));
     return 0;
@@ -615,6 +616,7 @@ int IRWork::allocate(long long ncell, int ncomp, bool precond, int maxblocks) {
     release();
     n = ncell;
     nc = ncomp;
+    nblk = vector_blocks(ncell);
     const size_t m = (size_t)n * nc;
     if (cudaMalloc(&r, sizeof(double) * m) != cudaSuccess) return -1;
     if (cudaMalloc(&b32, sizeof(float) * m) != cudaSuccess) return -1;
@@ -622,7 +624,7 @@ int IRWork::allocate(long long ncell, int ncomp, bool precond, int maxblocks) {
     if (cudaMalloc(&scal, sizeof(IRScal) * 3) != cudaSuccess) return -1;
     cudaMemset(scal, 0, sizeof(IRScal) * 3);
     if (cudaMallocHost(&scal_h, sizeof(IRScal) * 3) != cudaSuccess) return -1;
-    if (cudaMalloc(&partials, sizeof(double) * std::max(KBLOCKS, maxblocks) * 10) != cudaSuccess) return -1;
+    if (cudaMalloc(&partials, sizeof(double) * std::max(nblk, maxblocks) * 10) != cudaSuccess) return -1;
     if (cudaMalloc(&counter, sizeof(unsigned int)) != cudaSuccess) return -1;
     cudaMemset(counter, 0, sizeof(unsigned int));
     return inner.allocate(ncell, ncomp, precond, maxblocks);
@@ -645,10 +647,10 @@ template <typename T>
 static void launch_init(cudaStream_t st, KrylovWork<T> &w, const T *b, T *x, double tol, double divtol,
                         const IRScal *outer, double outer_tol, double outer_divtol, LoopCtl lc) {
     if (w.nc == 3)
-        k_bicg_init<T, 3><<<KBLOCKS, KTHREADS, 0, st>>>(w.n, b, x, w.r, w.r0, w.p, w.v, w.scal, w.partials,
+        k_bicg_init<T, 3><<<w.nblk, KTHREADS, 0, st>>>(w.n, b, x, w.r, w.r0, w.p, w.v, w.scal, w.partials,
                                                        w.counter, tol, divtol, outer, outer_tol, outer_divtol, lc);
     else
-        k_bicg_init<T, 1><<<KBLOCKS, KTHREADS, 0, st>>>(w.n, b, x, w.r, w.r0, w.p, w.v, w.scal, w.partials,
+        k_bicg_init<T, 1><<<w.nblk, KTHREADS, 0, st>>>(w.n, b, x, w.r, w.r0, w.p, w.v, w.scal, w.partials,
                                                        w.counter, tol, divtol, outer, outer_tol, outer_divtol, lc);
     note_launches(1);
 }
@@ -660,10 +662,10 @@ static void first_half(cudaStream_t st, const OpT<T> &A, int op, KrylovWork<T> &
     const int nc = w.nc;
     const int *gate = nc == 1 ? &w.scal[0].state : nullptr;
     const bool vec = n % 4 == 0;
-    if (nc == 3 && vec) k_bicg_p<T, 3, true><<<KBLOCKS, KTHREADS, 0, st>>>(n, w.r, w.p, w.v, w.scal);
-    else if (nc == 3) k_bicg_p<T, 3, false><<<KBLOCKS, KTHREADS, 0, st>>>(n, w.r, w.p, w.v, w.scal);
-    else if (vec) k_bicg_p<T, 1, true><<<KBLOCKS, KTHREADS, 0, st>>>(n, w.r, w.p, w.v, w.scal);
-    else k_bicg_p<T, 1, false><<<KBLOCKS, KTHREADS, 0, st>>>(n, w.r, w.p, w.v, w.scal);
+    if (nc == 3 && vec) k_bicg_p<T, 3, true><<<w.nblk, KTHREADS, 0, st>>>(n, w.r, w.p, w.v, w.scal);
+    else if (nc == 3) k_bicg_p<T, 3, false><<<w.nblk, KTHREADS, 0, st>>>(n, w.r, w.p, w.v, w.scal);
+    else if (vec) k_bicg_p<T, 1, true><<<w.nblk, KTHREADS, 0, st>>>(n, w.r, w.p, w.v, w.scal);
+    else k_bicg_p<T, 1, false><<<w.nblk, KTHREADS, 0, st>>>(n, w.r, w.p, w.v, w.scal);
     note_launches(1);
     if (M) {
         const int tm = prof_begin(pf, "mg_vcycle");
@@ -679,10 +681,10 @@ static void first_half(cudaStream_t st, const OpT<T> &A, int op, KrylovWork<T> &
                                                                 w.counter);
     note_launches(1);
     prof_end(pf, tm);
-    if (nc == 3 && vec) k_bicg_s<T, 3, true><<<KBLOCKS, KTHREADS, 0, st>>>(A, n, w.r, w.v, w.s, w.scal, w.partials, w.counter);
-    else if (nc == 3) k_bicg_s<T, 3, false><<<KBLOCKS, KTHREADS, 0, st>>>(A, n, w.r, w.v, w.s, w.scal, w.partials, w.counter);
-    else if (vec) k_bicg_s<T, 1, true><<<KBLOCKS, KTHREADS, 0, st>>>(A, n, w.r, w.v, w.s, w.scal, w.partials, w.counter);
-    else k_bicg_s<T, 1, false><<<KBLOCKS, KTHREADS, 0, st>>>(A, n, w.r, w.v, w.s, w.scal, w.partials, w.counter);
+    if (nc == 3 && vec) k_bicg_s<T, 3, true><<<w.nblk, KTHREADS, 0, st>>>(A, n, w.r, w.v, w.s, w.scal, w.partials, w.counter);
+    else if (nc == 3) k_bicg_s<T, 3, false><<<w.nblk, KTHREADS, 0, st>>>(A, n, w.r, w.v, w.s, w.scal, w.partials, w.counter);
+    else if (vec) k_bicg_s<T, 1, true><<<w.nblk, KTHREADS, 0, st>>>(A, n, w.r, w.v, w.s, w.scal, w.partials, w.counter);
+    else k_bicg_s<T, 1, false><<<w.nblk, KTHREADS, 0, st>>>(A, n, w.r, w.v, w.s, w.scal, w.partials, w.counter);
     note_launches(1);
 }
 
@@ -710,10 +712,10 @@ template <typename T>
 static void launch_xr(cudaStream_t st, const OpT<T> &A, KrylovWork<T> &w, T *x, int maxit, LoopCtl lc) {
 #define XR_ARGS A, w.n, x, w.r, w.r0, w.ph, w.sh, w.s, w.t, w.scal, w.partials, w.counter, maxit, lc
     const bool vec = w.n % 4 == 0;
-    if (w.nc == 3 && vec) k_bicg_xr<T, 3, true><<<KBLOCKS, KTHREADS, 0, st>>>(XR_ARGS);
-    else if (w.nc == 3) k_bicg_xr<T, 3, false><<<KBLOCKS, KTHREADS, 0, st>>>(XR_ARGS);
-    else if (vec) k_bicg_xr<T, 1, true><<<KBLOCKS, KTHREADS, 0, st>>>(XR_ARGS);
-    else k_bicg_xr<T, 1, false><<<KBLOCKS, KTHREADS, 0, st>>>(XR_ARGS);
+    if (w.nc == 3 && vec) k_bicg_xr<T, 3, true><<<w.nblk, KTHREADS, 0, st>>>(XR_ARGS);
+    else if (w.nc == 3) k_bicg_xr<T, 3, false><<<w.nblk, KTHREADS, 0, st>>>(XR_ARGS);
+    else if (vec) k_bicg_xr<T, 1, true><<<w.nblk, KTHREADS, 0, st>>>(XR_ARGS);
+    else k_bicg_xr<T, 1, false><<<w.nblk, KTHREADS, 0, st>>>(XR_ARGS);
 #undef XR_ARGS
     note_launches(1);
 }
@@ -730,14 +732,14 @@ static void launch_residual(cudaStream_t st, const OpT<double> &A64, int op, IRW
 }
 
 static void launch_to32(cudaStream_t st, IRWork &w) {
-    if (w.nc == 3) k_ir_to32<3><<<KBLOCKS, KTHREADS, 0, st>>>(w.n, w.r, w.scal, w.b32);
-    else k_ir_to32<1><<<KBLOCKS, KTHREADS, 0, st>>>(w.n, w.r, w.scal, w.b32);
+    if (w.nc == 3) k_ir_to32<3><<<w.nblk, KTHREADS, 0, st>>>(w.n, w.r, w.scal, w.b32);
+    else k_ir_to32<1><<<w.nblk, KTHREADS, 0, st>>>(w.n, w.r, w.scal, w.b32);
     note_launches(1);
 }
 
 static void launch_update(cudaStream_t st, IRWork &w, double *x) {
-    if (w.nc == 3) k_ir_update<3><<<KBLOCKS, KTHREADS, 0, st>>>(w.n, x, w.e32, w.scal, w.inner.scal);
-    else k_ir_update<1><<<KBLOCKS, KTHREADS, 0, st>>>(w.n, x, w.e32, w.scal, w.inner.scal);
+    if (w.nc == 3) k_ir_update<3><<<w.nblk, KTHREADS, 0, st>>>(w.n, x, w.e32, w.scal, w.inner.scal);
+    else k_ir_update<1><<<w.nblk, KTHREADS, 0, st>>>(w.n, x, w.e32, w.scal, w.inner.scal);
     note_launches(1);
 }
 

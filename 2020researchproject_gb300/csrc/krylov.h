@@ -28,6 +28,14 @@ struct Prof;
 constexpr int KTHREADS = 256;
 constexpr int KBLOCKS = 1216;  // 8 blocks per SM on 152 SMs; grid-stride loops
 
+// Blocks of the grid-stride vector kernels for a vector of n elements:
+// about 8 elements per thread, at most KBLOCKS, so that small cases
+// running side by side (batched steps) leave the GPU to each other.
+inline int vector_blocks(long long n) {
+    const long long b = (n + KTHREADS * 8 - 1) / (KTHREADS * 8);
+    return (int)(b < 1 ? 1 : b > KBLOCKS ? KBLOCKS : b);
+}
+
 enum { KS_RUN = 0, KS_HALF = 1, KS_DONE = 2, KS_BREAKDOWN = 3 };
 
 struct KScal {
@@ -85,6 +93,7 @@ template <typename T>
 struct KrylovWork {
     long long n = 0;
     int nc = 0;
+    int nblk = KBLOCKS;  // blocks of the vector kernels
     T *base = nullptr;
     T *r = nullptr, *r0 = nullptr, *p = nullptr, *v = nullptr, *s = nullptr, *t = nullptr;
     T *ph = nullptr, *sh = nullptr;
@@ -101,6 +110,7 @@ struct KrylovWork {
 struct IRWork {
     long long n = 0;
     int nc = 0;
+    int nblk = KBLOCKS;  // blocks of the vector kernels
     double *r = nullptr;          // FP64 residual
     float *b32 = nullptr, *e32 = nullptr;
     IRScal *scal = nullptr, *scal_h = nullptr;

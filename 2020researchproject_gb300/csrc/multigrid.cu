@@ -774,8 +774,13 @@ int GMG<T>::setup(cudaStream_t s, const OpT<double> &A64, const OpT<T> &A, const
     while (tail_ > 0 && levels_[tail_ - 1].n <= TAIL_THREADS && (int)levels_.size() - (tail_ - 1) <= 16) tail_--;
     if (!levels_.empty()) {
         tail_smem_ = tail_bytes(levels_, tail_);
-        if (cudaFuncSetAttribute(k_mg_tail<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tail_smem_) !=
-            cudaSuccess)
+        // The limit is a property of the kernel, shared by every solver in
+        // the process: only ever raise it.
+        cudaFuncAttributes fa{};
+        if (cudaFuncGetAttributes(&fa, k_mg_tail<T>) != cudaSuccess) return -1;
+        if ((size_t)fa.maxDynamicSharedSizeBytes < tail_smem_ &&
+            cudaFuncSetAttribute(k_mg_tail<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tail_smem_) !=
+                cudaSuccess)
             return -1;
     }
     if (!levels_.empty()) {

@@ -841,12 +841,14 @@ GraphSig graph_sig(const IBMSolver *sv) {
 
 // Records one step (everything one_step + fill_outer + ghost_update do)
 // into a graph; the field pointers are left as they were.
-bool record_step(IBMSolver *sv, StepGraph &G) {
+// Records one step onto d->s, which must be capturing (its own graph or a
+// batch graph it joined); fills G's keys and launch accounting.
+bool record_step_into(IBMSolver *sv, StepGraph &G) {
     ibm3d_device *d = sv->dev;
     const bool mixed = d->precision == IBM3D_MIXED;
     long long count = 0;
     g_redirect = &count;
-    bool ok = cudaStreamBeginCapture(d->s, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    bool ok = true;
     int mf = 0, mo = 0, mi = 0, pf = 0, po = 0, pi = 0;
     if (ok) {
         stage_rhs(sv);
@@ -878,13 +880,7 @@ bool record_step(IBMSolver *sv, StepGraph &G) {
         cudaMemcpyAsync(d->maxdiv_h, d->maxdiv_d, sizeof(double), cudaMemcpyDeviceToHost, d->s);
         swap_fields(d);
     }
-    cudaGraph_t graph = nullptr;
-    const cudaError_t ec = cudaStreamEndCapture(d->s, &graph);
     g_redirect = nullptr;
-    ok = ok && ec == cudaSuccess && graph;
-    if (ok) ok = cudaGraphInstantiate(&G.exec, graph, 0) == cudaSuccess;
-    if (graph) cudaGraphDestroy(graph);
-    cudaGetLastError();
     if (!ok) return false;
     G.key[0] = d->u[0];
     G.key[1] = d->U[0];
@@ -899,6 +895,64 @@ bool record_step(IBMSolver *sv, StepGraph &G) {
     return true;
 }
 
+// Ends any capture still open on the solver's aux streams (left by a
+// recording that failed half-way) and discards what it captured.
+void close_open_captures(ibm3d_device *d) {
+    for (cudaStream_t a : d->aux) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (a && cudaStreamIsCapturing(a, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
+            cudaGraph_t g = nullptr;
+            cudaStreamEndCapture(a, &g);
+        }
+    }
+    cudaGetLastError();
+}
+
+bool record_step(IBMSolver *sv, StepGraph &G) {
+    ibm3d_device *d = sv->dev;
+    bool ok = cudaStreamBeginCapture(d->s, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    if (ok) ok = record_step_into(sv, G);
+    close_open_captures(d);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(d->s, &graph);
+    ok = ok && ec == cudaSuccess && graph;
+    if (ok) ok = cudaGraphInstantiate(&G.exec, graph, 0) == cudaSuccess;
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();
+    return ok;
+}
+
+bool has_key(const StepGraph &g, const ibm3d_device *d) {
+    return g.key[0] == d->u[0] && g.key[1] == d->U[0] && g.key[2] == d->p && g.key[3] == d->N[0];
+}
+
+// After a recorded step ran and its stream is synchronised: the solve
+// reports, warnings, launch count and the pointer swaps.
+void finish_step(IBMSolver *sv, const StepGraph &G) {
+    ibm3d_device *d = sv->dev;
+    const bool mixed = d->precision == IBM3D_MIXED;
+    long long launches = G.fixed;
+    int rc;
+    if (mixed) {
+        rc = report(d->irmom, d->rep_mom);
+        launches += (long long)d->rep_mom.outer * G.mom_outer;
+    } else {
+        rc = report(d->kmom, d->rep_mom);
+    }
+    launches += (long long)std::max({d->rep_mom.iters[0], d->rep_mom.iters[1], d->rep_mom.iters[2]}) * G.mom_iter;
+    check_mom(sv, rc);
+    if (mixed) {
+        rc = report(d->irpres, d->rep_p);
+        launches += (long long)d->rep_p.outer * G.p_outer;
+    } else {
+        rc = report(d->kpres, d->rep_p);
+    }
+    launches += (long long)d->rep_p.iters[0] * G.p_iter;
+    check_pres(sv, rc);
+    note_launches((int)launches);
+    swap_fields(d);
+}
+
 // One step through its recorded graph.  Returns false when recording
 // failed (the caller then runs the step host-sequenced).
 bool graph_step(IBMSolver *sv) {
@@ -910,7 +964,7 @@ bool graph_step(IBMSolver *sv) {
     }
     StepGraph *G = nullptr;
     for (auto &g : d->graphs)
-        if (g.key[0] == d->u[0] && g.key[1] == d->U[0] && g.key[2] == d->p && g.key[3] == d->N[0]) G = &g;
+        if (has_key(g, d)) G = &g;
     if (!G) {
         StepGraph ng;
         if (!record_step(sv, ng)) {
@@ -923,28 +977,7 @@ bool graph_step(IBMSolver *sv) {
     }
     if (!cuda_check(sv, cudaGraphLaunch(G->exec, d->s), "graph launch")) return true;
     if (!cuda_check(sv, cudaStreamSynchronize(d->s), "time step")) return true;
-    const bool mixed = d->precision == IBM3D_MIXED;
-    long long launches = G->fixed;
-    int rc;
-    if (mixed) {
-        rc = report(d->irmom, d->rep_mom);
-        launches += (long long)d->rep_mom.outer * G->mom_outer;
-        launches += (long long)std::max({d->rep_mom.iters[0], d->rep_mom.iters[1], d->rep_mom.iters[2]}) * G->mom_iter;
-    } else {
-        rc = report(d->kmom, d->rep_mom);
-        launches += (long long)std::max({d->rep_mom.iters[0], d->rep_mom.iters[1], d->rep_mom.iters[2]}) * G->mom_iter;
-    }
-    check_mom(sv, rc);
-    if (mixed) {
-        rc = report(d->irpres, d->rep_p);
-        launches += (long long)d->rep_p.outer * G->p_outer + (long long)d->rep_p.iters[0] * G->p_iter;
-    } else {
-        rc = report(d->kpres, d->rep_p);
-        launches += (long long)d->rep_p.iters[0] * G->p_iter;
-    }
-    check_pres(sv, rc);
-    note_launches((int)launches);
-    swap_fields(d);
+    finish_step(sv, *G);
     return true;
 }
 
@@ -1430,19 +1463,27 @@ void IBMSolver_calc_tau_r(IBMSolver *s) {
 
 // ---------------------------------------------------------- iterate ---
 // src/ibm3d_fracstep.c:38-115
-void IBMSolver_iterate(IBMSolver *s, int num_time_steps, bool verbose) {
-    if (!check_ready(s, "IBMSolver_iterate")) return;
+namespace {
+// What every IBMSolver_iterate call does before its steps
+// (src/ibm3d_fracstep.c:40-56): outer fill, face velocities, ghost
+// update with solid NaNs, and N^{-1} = N^0 for the AB2 bootstrap.
+void iterate_prologue(IBMSolver *s) {
     ibm3d_device *d = s->dev;
-    const double start_time = s->time;
     d->status = IBM3D_OK;
     fill_outer(s);
     launch_interp_stag(d->s, d->g, d->ax[0], d->ax[1], d->ax[2], d->u, d->U);
     ghost_update(s, true);
-    {
-        const double f[3] = {s->ext_force.const_f1, s->ext_force.const_f2, s->ext_force.const_f3};
-        launch_conv_rhs(d->s, d->g, d->ax[0], d->ax[1], d->ax[2], d->bc, d->flag, conv_args(d), s->dt, f, 0);
-        swap3(d->N, d->Np);
-    }
+    const double f[3] = {s->ext_force.const_f1, s->ext_force.const_f2, s->ext_force.const_f3};
+    launch_conv_rhs(d->s, d->g, d->ax[0], d->ax[1], d->ax[2], d->bc, d->flag, conv_args(d), s->dt, f, 0);
+    swap3(d->N, d->Np);
+}
+}  // namespace
+
+void IBMSolver_iterate(IBMSolver *s, int num_time_steps, bool verbose) {
+    if (!check_ready(s, "IBMSolver_iterate")) return;
+    ibm3d_device *d = s->dev;
+    const double start_time = s->time;
+    iterate_prologue(s);
     struct timespec t0, t1;
     clock_gettime(CLOCK_REALTIME, &t0);
     for (int i = 1; i <= num_time_steps; i++) {
@@ -1793,3 +1834,177 @@ void Polyhedron_cpt(const Polyhedron *const poly, const int nx, const int ny, co
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------- batches ---
+// Many independent solvers advanced together: every batched step is ONE
+// CUDA graph launch whose parallel branches are the members' recorded steps
+// (each with its own device-side Krylov loops), so small cases share the
+// GPU instead of running one after another.  Each member computes exactly
+// what IBMSolver_iterate computes for it alone (same kernels, same order on
+// its own data).
+struct IBMBatch {
+    cudaStream_t s = nullptr;
+    cudaEvent_t fork = nullptr, t0 = nullptr, t1 = nullptr;
+    std::vector<IBMSolver *> members;
+    std::vector<cudaEvent_t> join;
+    struct Rec {
+        std::vector<const void *> key;
+        cudaGraphExec_t exec = nullptr;
+        std::vector<StepGraph> parts;
+    };
+    std::vector<Rec> cache;
+    int status = IBM3D_OK;
+};
+
+namespace {
+void batch_drop(IBMBatch *b) {
+    for (auto &r : b->cache)
+        if (r.exec) cudaGraphExecDestroy(r.exec);
+    b->cache.clear();
+}
+
+std::vector<const void *> batch_key(IBMBatch *b) {
+    std::vector<const void *> k;
+    for (IBMSolver *m : b->members) {
+        ibm3d_device *d = m->dev;
+        const GraphSig sig = graph_sig(m);
+        if (!(sig == d->gsig)) {
+            drop_graphs(d);
+            d->gsig = sig;
+        }
+        k.push_back(m);
+        k.push_back(d->u[0]);
+        k.push_back(d->U[0]);
+        k.push_back(d->p);
+        k.push_back(d->N[0]);
+    }
+    return k;
+}
+
+bool batch_record(IBMBatch *b, IBMBatch::Rec &R) {
+    bool ok = cudaStreamBeginCapture(b->s, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    if (ok) ok = cudaEventRecord(b->fork, b->s) == cudaSuccess;
+    R.parts.assign(b->members.size(), StepGraph{});
+    for (size_t q = 0; ok && q < b->members.size(); q++) {
+        ibm3d_device *d = b->members[q]->dev;
+        ok = cudaStreamWaitEvent(d->s, b->fork, 0) == cudaSuccess;
+        if (ok) ok = record_step_into(b->members[q], R.parts[q]);
+
+        if (ok) ok = cudaEventRecord(b->join[q], d->s) == cudaSuccess;
+        if (ok) ok = cudaStreamWaitEvent(b->s, b->join[q], 0) == cudaSuccess;
+    }
+    // A failed recording can leave a loop-body capture open on an aux
+    // stream; close those before the parent capture.
+    for (IBMSolver *m : b->members) close_open_captures(m->dev);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(b->s, &graph);
+    ok = ok && ec == cudaSuccess && graph;
+    if (ok) ok = cudaGraphInstantiate(&R.exec, graph, 0) == cudaSuccess;
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();
+    return ok;
+}
+}  // namespace
+
+IBMBatch *IBMBatch_new(void) {
+    IBMBatch *b = new IBMBatch();
+    if (cudaStreamCreateWithFlags(&b->s, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreate(&b->t0) != cudaSuccess || cudaEventCreate(&b->t1) != cudaSuccess) {
+        fprintf(stderr, "error: IBMBatch_new: no usable GPU\n");
+        b->status = IBM3D_ECUDA;
+    }
+    return b;
+}
+
+void IBMBatch_destroy(IBMBatch *b) {
+    if (!b) return;
+    batch_drop(b);
+    for (auto e : b->join) cudaEventDestroy(e);
+    if (b->fork) cudaEventDestroy(b->fork);
+    if (b->t0) cudaEventDestroy(b->t0);
+    if (b->t1) cudaEventDestroy(b->t1);
+    if (b->s) cudaStreamDestroy(b->s);
+    delete b;
+}
+
+int IBMBatch_add(IBMBatch *b, IBMSolver *s) {
+    if (!b || !s || !s->dev || !s->dev->assembled) {
+        fprintf(stderr, "error: IBMBatch_add: the solver must be assembled first\n");
+        return -1;
+    }
+    for (IBMSolver *m : b->members)
+        if (m == s) return 0;
+    cudaEvent_t e;
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return -1;
+    b->members.push_back(s);
+    b->join.push_back(e);
+    batch_drop(b);
+    return 0;
+}
+
+int IBMBatch_remove(IBMBatch *b, IBMSolver *s) {
+    for (size_t q = 0; q < b->members.size(); q++)
+        if (b->members[q] == s) {
+            b->members.erase(b->members.begin() + q);
+            cudaEventDestroy(b->join[q]);
+            b->join.erase(b->join.begin() + q);
+            batch_drop(b);
+            return 0;
+        }
+    return -1;
+}
+
+int IBMBatch_size(const IBMBatch *b) { return b ? (int)b->members.size() : 0; }
+
+double IBMBatch_iterate(IBMBatch *b, int nsteps) {
+    if (!b || b->members.empty() || nsteps < 1) return 0.0;
+    b->status = IBM3D_OK;
+    std::vector<double> start(b->members.size());
+    for (size_t q = 0; q < b->members.size(); q++) {
+        IBMSolver *m = b->members[q];
+        start[q] = m->time;
+        iterate_prologue(m);
+        cudaEventRecord(b->join[q], m->dev->s);
+        cudaStreamWaitEvent(b->s, b->join[q], 0);
+    }
+    cudaEventRecord(b->t0, b->s);
+    for (int i = 1; i <= nsteps; i++) {
+        const std::vector<const void *> key = batch_key(b);
+        IBMBatch::Rec *R = nullptr;
+        for (auto &r : b->cache)
+            if (r.key == key) R = &r;
+        if (!R) {
+            if (b->cache.size() >= 4) batch_drop(b);
+            IBMBatch::Rec nr;
+            nr.key = key;
+            if (!batch_record(b, nr)) {
+                fprintf(stderr, "error: IBMBatch_iterate: recording the batched step failed\n");
+                b->status = IBM3D_ECUDA;
+                return -1;
+            }
+            b->cache.push_back(nr);
+            R = &b->cache.back();
+        }
+        if (cudaGraphLaunch(R->exec, b->s) != cudaSuccess || cudaStreamSynchronize(b->s) != cudaSuccess) {
+            fprintf(stderr, "error: IBMBatch_iterate: %s\n", cudaGetErrorString(cudaGetLastError()));
+            b->status = IBM3D_ECUDA;
+            return -1;
+        }
+        for (size_t q = 0; q < b->members.size(); q++) {
+            IBMSolver *m = b->members[q];
+            finish_step(m, R->parts[q]);
+            m->iter++;
+            m->time = start[q] + m->dt * i;
+            m->dev->max_div = *m->dev->maxdiv_h;
+            if (m->dev->status != IBM3D_OK && m->dev->status != IBM3D_ENOCONV) b->status = m->dev->status;
+        }
+    }
+    cudaEventRecord(b->t1, b->s);
+    cudaEventSynchronize(b->t1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, b->t0, b->t1);
+    return ms;
+}
+
+int IBMBatch_last_status(const IBMBatch *b) { return b ? b->status : IBM3D_EARG; }

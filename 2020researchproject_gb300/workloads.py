@@ -15,6 +15,8 @@ no dataset to download.
   uses BC_PRESSURE, src/main.c:138-140), free-slip sides, Re 300.
 * ``channel`` - channel LES: 2pi x 2 x pi, tanh-stretched walls in y,
   periodic x and z, constant body force 2/Re, Smagorinsky Cs = 0.1.
+* ``ensemble`` - 64 independent immersed-body cases of uneven size (boxes
+  or spheres, Re 50-500) for batched stepping.
 """
 from __future__ import annotations
 
@@ -62,6 +64,68 @@ def channel(nx=128, ny=96, nz=128, Re=16200.0, dt=2e-3, cs=0.1):
                 zf=geometry.uniform_faces(0.0, np.pi, nz), re=Re, dt=dt, force=(2.0 / Re, 0.0, 0.0),
                 smag=cs, bc=["W per", "E per", "S wall", "N wall", "D per", "U per"],
                 init="poiseuille")
+
+
+def _body_stl(kind, params, key):
+    """STL file of a synthetic body (cached per key)."""
+    path = _STL_CACHE.get(key)
+    if path is None or not os.path.exists(path):
+        fd, path = tempfile.mkstemp(prefix=f"{kind}_", suffix=".stl")
+        os.close(fd)
+        if kind == "sphere":
+            v, f = geometry.icosphere(params["subdivisions"], params["radius"], params["center"])
+        else:
+            v, f = geometry.box_union(params["boxes"])
+        geometry.write_stl(path, v, f)
+        _STL_CACHE[key] = path
+    return path
+
+
+def _boxes(rng, nbox, lo=-1.8, hi=1.8, gap=0.15, tries=200):
+    """1-4 axis-aligned boxes with sides U[0.5, 2] inside [lo, hi]^3 that
+    neither overlap nor touch (a gap of at least `gap`)."""
+    out = []
+    for _ in range(tries):
+        if len(out) == nbox:
+            break
+        side = rng.uniform(0.5, 2.0, size=3)
+        c = rng.uniform(lo + side / 2, hi - side / 2)
+        b = (c - side / 2, c + side / 2)
+        if all(np.any(b[0] > o[1] + gap) or np.any(o[0] > b[1] + gap) for o in out):
+            out.append(b)
+    return [(tuple(map(float, b[0])), tuple(map(float, b[1]))) for b in out]
+
+
+def ensemble(ncases=64, seed=2024):
+    """Seeded ensemble of independent immersed-body cases: grids
+    Nx ~ U[32, 96], Ny, Nz ~ U[32, 64] on [-4, 8] x [-3, 3]^2, Re ~ U[50, 500],
+    body = 1-4 non-touching boxes of side U[0.5, 2] or a sphere of diameter
+    U[0.5, 1.5] (3-times subdivided icosphere), uniform inflow, pressure
+    outlet, free-slip sides, dt = CFL 0.25 on the finest spacing."""
+    rng = np.random.Generator(np.random.Philox(seed))
+    cases = []
+    for c in range(ncases):
+        nx = int(rng.integers(32, 97))
+        ny = int(rng.integers(32, 65))
+        nz = int(rng.integers(32, 65))
+        Re = float(rng.uniform(50.0, 500.0))
+        xf = geometry.uniform_faces(-4.0, 8.0, nx)
+        yf = geometry.uniform_faces(-3.0, 3.0, ny)
+        zf = geometry.uniform_faces(-3.0, 3.0, nz)
+        h = min(12.0 / nx, 6.0 / ny, 6.0 / nz)
+        if rng.uniform() < 0.5:
+            d = float(rng.uniform(0.5, 1.5))
+            stl = _body_stl("sphere", dict(subdivisions=3, radius=d / 2, center=(0.0, 0.0, 0.0)),
+                            ("sphere", round(d, 12)))
+            body = f"sphere D={d:.3f}"
+        else:
+            boxes = _boxes(rng, int(rng.integers(1, 5)))
+            stl = _body_stl("boxes", dict(boxes=boxes), ("boxes", tuple(boxes)))
+            body = f"{len(boxes)} boxes"
+        cases.append(dict(name=f"ens{c:02d}_{nx}x{ny}x{nz}", xf=xf, yf=yf, zf=zf, re=Re, dt=0.25 * h,
+                          bc=["W vel 1 0 0", "E press 0", "S slip", "N slip", "D slip", "U slip"],
+                          stl=stl, init=(1.0, 0.0, 0.0, 0.0), body=body))
+    return cases
 
 
 _BC = {"vel": "BC_VELOCITY_COMPONENT", "press": "BC_PRESSURE", "wall": "BC_STATIONARY_WALL",

@@ -145,6 +145,24 @@ int IBMSolver_host_unregister(void *ptr);
 /* Device name of the solver's GPU (for logs). */
 const char *IBMSolver_device_name(IBMSolver *);
 
+/* Batches: independent solvers (any grids, bodies, Re; same GPU) advanced
+   together.  Each batched step is one CUDA graph launch whose parallel
+   branches are the members' recorded steps, so small cases overlap on the
+   GPU.  A member's results are bitwise those of IBMSolver_iterate on the
+   same solver alone.  Members must be assembled; adding or removing a
+   member re-records the batched step at its next use.  IBMBatch_iterate
+   runs nsteps steps of every member (with the reference's per-call
+   prologue, as IBMSolver_iterate) and returns the device milliseconds
+   (CUDA events on the batch stream), or -1 on error. */
+typedef struct IBMBatch IBMBatch;
+IBMBatch *IBMBatch_new(void);
+void IBMBatch_destroy(IBMBatch *);
+int IBMBatch_add(IBMBatch *, IBMSolver *);
+int IBMBatch_remove(IBMBatch *, IBMSolver *);
+int IBMBatch_size(const IBMBatch *);
+double IBMBatch_iterate(IBMBatch *, int nsteps);
+int IBMBatch_last_status(const IBMBatch *);
+
 #ifdef __cplusplus
 }
 #endif
