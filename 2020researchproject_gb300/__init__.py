@@ -115,6 +115,7 @@ def load_library(path: str = LIB_PATH):
         "IBMSolver_kernel_launches": (ctypes.c_longlong, []),
         "IBMSolver_host_register": (i, [vp, ctypes.c_size_t]),
         "IBMSolver_host_unregister": (i, [vp]),
+        "IBMSolver_device_bytes": (ctypes.c_size_t, [vp]),
         "IBMBatch_new": (vp, []),
         "IBMBatch_destroy": (None, [vp]),
         "IBMBatch_add": (i, [vp, vp]),
@@ -197,10 +198,14 @@ class IBMSolver:
         if st not in (0, 1):
             raise IBM3DError(f"{what}: {STATUS.get(st, st)}")
 
-    def __del__(self):
+    def close(self):
+        """Destroys the solver now (frees its device memory)."""
         if getattr(self, "_s", None):
             self._lib.IBMSolver_destroy(self._s)
             self._s = None
+
+    def __del__(self):
+        self.close()
 
     # ------------------------------------------------------------ setup
     def set_grid(self, xf, yf, zf):
@@ -349,6 +354,10 @@ class IBMSolver:
                     res_u=list(st.res_u), res_p=st.res_p, max_div=st.max_div,
                     mg_levels=st.mg_levels, cpt_fallback=st.cpt_fallback,
                     outer_u=st.outer_u, outer_p=st.outer_p)
+
+    def device_bytes(self):
+        """Device memory taken by assembly (bytes)."""
+        return int(self._lib.IBMSolver_device_bytes(self._s))
 
     def set_profiling(self, on=True):
         self._lib.IBMSolver_set_profiling(self._s, 1 if on else 0)

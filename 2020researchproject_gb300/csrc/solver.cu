@@ -107,6 +107,7 @@ struct ibm3d_device {
     int les = 0;
     int cpt_fallback = 0;
     bool abort_on_error = true;
+    size_t dev_bytes = 0;   // device memory taken by assembly (free-memory difference)
     // Recorded steps.
     bool use_graphs = true;
     int mg_sweeps[5] = {5, 5, 1, 1, 8};  // multigrid sweeps: fine pre/post, coarse pre/post, coarsest
@@ -1242,6 +1243,8 @@ void IBMSolver_assemble(IBMSolver *s) {
         return;
     }
     host_metrics(s);
+    size_t free0 = 0, total0 = 0;
+    cudaMemGetInfo(&free0, &total0);
     Grid &g = d->g;
     g.nx = s->Nx;
     g.ny = s->Ny;
@@ -1294,6 +1297,9 @@ void IBMSolver_assemble(IBMSolver *s) {
         return;
     }
     if (!cuda_check(s, cudaStreamSynchronize(d->s), "assemble")) return;
+    size_t free1 = 0, total1 = 0;
+    cudaMemGetInfo(&free1, &total1);
+    d->dev_bytes = free0 > free1 ? free0 - free1 : 0;
     d->assembled = true;
     d->status = IBM3D_OK;
 }
@@ -1839,14 +1845,19 @@ void Polyhedron_cpt(const Polyhedron *const poly, const int nx, const int ny, co
 // Many independent solvers advanced together: every batched step is ONE
 // CUDA graph launch whose parallel branches are the members' recorded steps
 // (each with its own device-side Krylov loops), so small cases share the
-// GPU instead of running one after another.  Each member computes exactly
-// what IBMSolver_iterate computes for it alone (same kernels, same order on
-// its own data).
+// GPU instead of running one after another.  A member's batched steps
+// since it joined form one run: they compute exactly what one
+// IBMSolver_iterate call of that many steps computes for it alone (same
+// kernels, same order on its own data); the reference's per-call prologue
+// runs when it joins, or again if it was stepped outside the batch.
 struct IBMBatch {
     cudaStream_t s = nullptr;
     cudaEvent_t fork = nullptr, t0 = nullptr, t1 = nullptr;
     std::vector<IBMSolver *> members;
     std::vector<cudaEvent_t> join;
+    std::vector<int> next_iter;     // member's iter after its last batched step; -1: not started
+    std::vector<double> run_start;  // member's time when its run in the batch began
+    std::vector<int> run_steps;     // batched steps of that run so far
     struct Rec {
         std::vector<const void *> key;
         cudaGraphExec_t exec = nullptr;
@@ -1939,6 +1950,9 @@ int IBMBatch_add(IBMBatch *b, IBMSolver *s) {
     if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return -1;
     b->members.push_back(s);
     b->join.push_back(e);
+    b->next_iter.push_back(-1);
+    b->run_start.push_back(0.0);
+    b->run_steps.push_back(0);
     batch_drop(b);
     return 0;
 }
@@ -1949,6 +1963,9 @@ int IBMBatch_remove(IBMBatch *b, IBMSolver *s) {
             b->members.erase(b->members.begin() + q);
             cudaEventDestroy(b->join[q]);
             b->join.erase(b->join.begin() + q);
+            b->next_iter.erase(b->next_iter.begin() + q);
+            b->run_start.erase(b->run_start.begin() + q);
+            b->run_steps.erase(b->run_steps.begin() + q);
             batch_drop(b);
             return 0;
         }
@@ -1960,11 +1977,14 @@ int IBMBatch_size(const IBMBatch *b) { return b ? (int)b->members.size() : 0; }
 double IBMBatch_iterate(IBMBatch *b, int nsteps) {
     if (!b || b->members.empty() || nsteps < 1) return 0.0;
     b->status = IBM3D_OK;
-    std::vector<double> start(b->members.size());
     for (size_t q = 0; q < b->members.size(); q++) {
         IBMSolver *m = b->members[q];
-        start[q] = m->time;
-        iterate_prologue(m);
+        if (b->next_iter[q] != m->iter) {  // joined, or stepped outside the batch: a new run
+            b->run_start[q] = m->time;
+            b->run_steps[q] = 0;
+            iterate_prologue(m);
+        }
+        m->dev->status = IBM3D_OK;
         cudaEventRecord(b->join[q], m->dev->s);
         cudaStreamWaitEvent(b->s, b->join[q], 0);
     }
@@ -1995,7 +2015,9 @@ double IBMBatch_iterate(IBMBatch *b, int nsteps) {
             IBMSolver *m = b->members[q];
             finish_step(m, R->parts[q]);
             m->iter++;
-            m->time = start[q] + m->dt * i;
+            b->run_steps[q]++;
+            b->next_iter[q] = m->iter;
+            m->time = b->run_start[q] + m->dt * b->run_steps[q];
             m->dev->max_div = *m->dev->maxdiv_h;
             if (m->dev->status != IBM3D_OK && m->dev->status != IBM3D_ENOCONV) b->status = m->dev->status;
         }
@@ -2008,3 +2030,5 @@ double IBMBatch_iterate(IBMBatch *b, int nsteps) {
 }
 
 int IBMBatch_last_status(const IBMBatch *b) { return b ? b->status : IBM3D_EARG; }
+
+size_t IBMSolver_device_bytes(const IBMSolver *s) { return s && s->dev ? s->dev->dev_bytes : 0; }

@@ -367,8 +367,13 @@ def bench_gb300(args):
                    "max_div": st["max_div"], "mg_levels": st["mg_levels"]},
         "profile_ms": {k: [v[0], round(v[1], 3)] for k, v in sorted(prof.items())},
     }
+    lv = s.get_field("lvset")
+    s.close()
+    head["solver"] = None
+    if rank == 0 and world == 1 and not args.no_extras:
+        line["ensemble"] = ensemble_arm(ibm, wl, args)
+        line["serving"] = serving_arm(ibm, wl, args)
     if rank == 0 and world == 1 and not args.no_cpu:
-        lv = s.get_field("lvset")
         cv, done, secs, _ = run_cpu(case, lv, steps=2, warmup=0, threads=os.cpu_count() or 1, sample_budget_s=25)
         line["cpu_baseline"] = {"value": round(cv, 4), "unit": "Mcell-steps/s", "cores": os.cpu_count() or 1,
                                 "kind": "port",
@@ -379,6 +384,63 @@ def bench_gb300(args):
     return 0
 
 
+def ensemble_arm(ibm, wl, args, steps=5):
+    """Batched ensemble (64 seeded immersed-body cases of uneven size): the
+    mixed-precision batched step (one CUDA graph launch per step for all
+    cases) against the plain FP64 step run case by case, and the FP64
+    batched step."""
+    cases = wl.ensemble()
+    cells = sum((len(c["xf"]) - 1) * (len(c["yf"]) - 1) * (len(c["zf"]) - 1) for c in cases)
+    out = {"cases": len(cases), "cells": cells, "steps": steps, "unit": "Mcell-steps/s",
+           "workload": "64 cases, grids 32-96 x 32-64 x 32-64, boxes or spheres, Re 50-500, seed 2024"}
+    for mode in ("mixed", "fp64"):
+        solvers = []
+        for c in cases:
+            sv = wl.build_solver(ibm, c, tol=MOM_TOL, div_tol=DIV_TOL)
+            sv.set_precision(ibm.MIXED if mode == "mixed" else ibm.FP64)
+            sv.init_flow_array(*wl.initial_state(c))
+            solvers.append(sv)
+        b = ibm.Batch(solvers)
+        b.iterate(1)
+        ms = b.iterate(steps)
+        out[f"{mode}_batched"] = round(cells * steps / ms / 1e3, 3)
+        out[f"{mode}_batched_ms_per_step"] = round(ms / steps, 2)
+        out[f"{mode}_max_div"] = max(sv.stats()["max_div"] for sv in solvers)
+        if mode == "fp64":
+            seq = sum(sv.time_iterate(steps) for sv in solvers)
+            out["fp64_alone"] = round(cells * steps / seq / 1e3, 3)
+        del b
+        for sv in solvers:
+            sv.close()
+    out["mixed_batched_vs_fp64_alone"] = round(out["mixed_batched"] / out["fp64_alone"], 3)
+    return out
+
+
+def serving_arm(ibm, wl, args, njobs=40):
+    """Continuous-batching server on seeded Poisson arrivals (20 jobs/s):
+    cavity / sphere / box-cluster jobs, grids 32^3 to 96x64x64, 20-100
+    steps, mixed precision; p50/p99 job latency and aggregate throughput,
+    against the same jobs run one by one on the plain FP64 step."""
+    serve = importlib.import_module("2020researchproject_gb300.serve")
+    jobs = serve.poisson_jobs(njobs=njobs)
+    res = serve.Server(ibm, precision="mixed").run(jobs)
+    dev_ms = 0.0
+    for j in jobs:
+        sv = wl.build_solver(ibm, j.case, tol=MOM_TOL, div_tol=DIV_TOL)
+        sv.set_precision(ibm.FP64)
+        sv.init_flow_array(*wl.initial_state(j.case))
+        dev_ms += sv.time_iterate(j.steps)
+        sv.close()
+    alone = res["cell_steps"] / dev_ms / 1e3
+    return {"jobs": njobs, "arrival_rate_per_s": 20.0,
+            "workload": "cavity/sphere/box jobs, grids 32^3..96x64x64, 20-100 steps, Re 100-1000, seed 4242",
+            "latency_p50_s": round(res["latency_p50_s"], 3), "latency_p99_s": round(res["latency_p99_s"], 3),
+            "mcell_steps_per_s": round(res["mcell_steps_per_s"], 3), "max_active": res["max_active"],
+            "wall_s": round(res["wall_s"], 2), "max_div": res["max_div"],
+            "fp64_alone_device_mcell_steps_per_s": round(alone, 3),
+            "served_vs_fp64_alone": round(res["mcell_steps_per_s"] / alone, 3)}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -386,6 +448,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-extras", action="store_true", help="skip the ensemble and serving measurements")
     ap.add_argument("--host-loop", action="store_true",
                     help="host-sequenced steps instead of recorded graphs (same kernels; for ncu launch lists, "
                          "which do not list kernels inside graph loops)")

@@ -142,18 +142,24 @@ long long IBMSolver_kernel_launches(void);
 int IBMSolver_host_register(void *ptr, size_t bytes);
 int IBMSolver_host_unregister(void *ptr);
 
+/* Device memory the solver's assembly took (bytes; the drop in free device
+   memory across IBMSolver_assemble), for admission by HBM footprint. */
+size_t IBMSolver_device_bytes(const IBMSolver *);
+
 /* Device name of the solver's GPU (for logs). */
 const char *IBMSolver_device_name(IBMSolver *);
 
 /* Batches: independent solvers (any grids, bodies, Re; same GPU) advanced
    together.  Each batched step is one CUDA graph launch whose parallel
    branches are the members' recorded steps, so small cases overlap on the
-   GPU.  A member's results are bitwise those of IBMSolver_iterate on the
-   same solver alone.  Members must be assembled; adding or removing a
-   member re-records the batched step at its next use.  IBMBatch_iterate
-   runs nsteps steps of every member (with the reference's per-call
-   prologue, as IBMSolver_iterate) and returns the device milliseconds
-   (CUDA events on the batch stream), or -1 on error. */
+   GPU.  A member's batched steps since it joined form one run: bitwise the
+   results of one IBMSolver_iterate call of that many steps on the same
+   solver alone (the reference's per-call prologue runs when the member
+   joins, or again after it was stepped outside the batch).  Members must
+   be assembled; adding or removing a member re-records the batched step
+   at its next use.  IBMBatch_iterate runs nsteps steps of every member and
+   returns the device milliseconds (CUDA events on the batch stream), or
+   -1 on error. */
 typedef struct IBMBatch IBMBatch;
 IBMBatch *IBMBatch_new(void);
 void IBMBatch_destroy(IBMBatch *);

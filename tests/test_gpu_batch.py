@@ -35,8 +35,7 @@ def test_batch_members_equal_solo_runs(precision):
     for c in cases:
         s = build_case(ibm, c, tol=1e-8)
         s.set_precision(mode)
-        s.iterate(2)
-        s.iterate(1)
+        s.iterate(3)                      # one run of 3 steps
         solo.append((_fields(s), s.stats()))
 
     members = []
@@ -58,13 +57,13 @@ def test_batch_members_equal_solo_runs(precision):
 
 def test_batch_membership_changes_between_steps():
     """A solver stepped partly alone, partly in a batch whose other members
-    come and go, ends where stepping it alone ends."""
+    come and go, ends where the same runs alone end: its batched steps form
+    one run from the moment it joined."""
     ibm = package()
     ref_case, other = load_golden("sphere"), load_golden("cavity")
     alone = build_case(ibm, ref_case, tol=1e-8)
     alone.iterate(1)
-    alone.iterate(1)
-    alone.iterate(1)
+    alone.iterate(3)
 
     s = build_case(ibm, ref_case, tol=1e-8)
     t = build_case(ibm, other, tol=1e-8)
@@ -73,8 +72,14 @@ def test_batch_membership_changes_between_steps():
     batch.iterate(1)                      # with a partner
     batch.remove(t)
     batch.iterate(1)                      # partner gone
-    assert s.stats()["iter"] == 3
+    u = build_case(ibm, other, tol=1e-8)
+    batch.add(u)                          # a newcomer
+    batch.iterate(1)
+    assert s.stats()["iter"] == 4
     assert _same(_fields(s), _fields(alone))
+    u_alone = build_case(ibm, other, tol=1e-8)
+    u_alone.iterate(1)
+    assert _same(_fields(u), _fields(u_alone))
 
 
 def test_ensemble_cases_step_in_a_batch():
