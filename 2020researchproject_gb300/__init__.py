@@ -96,6 +96,7 @@ def load_library(path: str = LIB_PATH):
         "IBMSolver_export_lvset_flag": (None, [vp, ctypes.c_char_p]),
         "IBMSolver_export_intermediate": (None, [vp, ctypes.c_char_p]),
         "IBMSolver_last_status": (i, [vp]),
+        "IBMSolver_last_message": (ctypes.c_char_p, [vp]),
         "IBMSolver_set_div_tol": (None, [vp, d]),
         "IBMSolver_set_precision": (None, [vp, i]),
         "IBMSolver_set_graphs": (None, [vp, i]),
@@ -196,7 +197,8 @@ class IBMSolver:
     def _check(self, what):
         st = self._lib.IBMSolver_last_status(self._s)
         if st not in (0, 1):
-            raise IBM3DError(f"{what}: {STATUS.get(st, st)}")
+            msg = self._lib.IBMSolver_last_message(self._s) or b""
+            raise IBM3DError(f"{what}: {STATUS.get(st, st)}: {msg.decode(errors='replace')}")
 
     def close(self):
         """Destroys the solver now (frees its device memory)."""

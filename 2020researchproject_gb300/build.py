@@ -29,7 +29,7 @@ CUDA_SOURCES = {
     "setup_kernels.cu": ["-fmad=false"],
     "solver.cu": [],
 }
-CXX_SOURCES = ["geo3d.cpp"]
+CXX_SOURCES = ["geo3d.cpp", "ncfile.cpp"]
 
 
 def _nvcc():

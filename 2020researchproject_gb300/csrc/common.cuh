@@ -22,12 +22,6 @@ enum { BCT_VELOCITY = 0, BCT_PRESSURE = 1, BCT_WALL = 2, BCT_SLIP = 3,
 // Face order of the reference's bc[] array: north, east, south, west, down, up.
 enum { F_N = 0, F_E = 1, F_S = 2, F_W = 3, F_D = 4, F_U = 5 };
 
-struct Grid {
-    int nx, ny, nz;
-    long long sx, sy;   // strides of i and j (k stride is 1)
-    long long ncell;    // (nx+4)(ny+4)(nz+4)
-};
-
 // Exact unsigned 32-bit division by a run-time constant d >= 1 with one
 // multiply-high (Granlund & Montgomery, "Division by invariant integers
 // using multiplication", PLDI 1994, round-up variant):
@@ -53,6 +47,22 @@ __device__ __forceinline__ uint32_t fdiv(const FastDiv &f, uint32_t n) {
     return (t + ((n - t) >> 1)) >> (f.l - 1);
 }
 
+struct Grid {
+    int nx, ny, nz;
+    long long sx, sy;   // strides of i and j (k stride is 1)
+    long long ncell;    // (nx+4)(ny+4)(nz+4)
+    // Fast dividers (set with the sizes by set_grid_dividers): padded
+    // strides sx, sy and interior sizes nz, ny.
+    FastDiv dsx, dsy, dnz, dny;
+};
+
+inline void set_grid_dividers(Grid &g) {
+    g.dsx = make_fastdiv((uint32_t)g.sx);
+    g.dsy = make_fastdiv((uint32_t)g.sy);
+    g.dnz = make_fastdiv((uint32_t)g.nz);
+    g.dny = make_fastdiv((uint32_t)g.ny);
+}
+
 __host__ __device__ inline long long cidx(const Grid &g, int i, int j, int k) {
     return (long long)(i + 2) * g.sx + (long long)(j + 2) * g.sy + (k + 2);
 }
@@ -68,6 +78,21 @@ __device__ __forceinline__ void cijk_fast(const Grid &g, const FastDiv &dx, cons
     i = (int)I - 2;
     j = (int)J - 2;
     k = (int)(r - J * (uint32_t)g.sy) - 2;
+}
+
+// cijk_fast with the grid's own dividers.
+__device__ __forceinline__ void cijk_g(const Grid &g, long long idx, int &i, int &j, int &k) {
+    cijk_fast(g, g.dsx, g.dsy, idx, i, j, k);
+}
+
+// Interior index q (k fastest, then j, then i) -> (i, j, k).
+__device__ __forceinline__ void ijk_interior(const Grid &g, long long q, int &i, int &j, int &k) {
+    const uint32_t Q = (uint32_t)q;
+    const uint32_t r = fdiv(g.dnz, Q);
+    k = (int)(Q - r * (uint32_t)g.nz);
+    const uint32_t I = fdiv(g.dny, r);
+    j = (int)(r - I * (uint32_t)g.ny);
+    i = (int)I;
 }
 
 __host__ __device__ inline void cijk(const Grid &g, long long idx, int &i, int &j, int &k) {

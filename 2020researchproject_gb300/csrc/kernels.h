@@ -75,4 +75,9 @@ void launch_interp_stag(cudaStream_t s, const Grid &g, const Axis &ax, const Axi
 void launch_ghost_update(cudaStream_t s, const GhostArgs &a, double *const u[3], double *p);
 void launch_solid_nan(cudaStream_t s, const Grid &g, const uint8_t *flag, double *const u[3], double *p);
 
+// Result export: float u, v, w, p, vorticity, Q, each (nx+4)(ny+4)(nz+4)
+// values in [z][y][x] order, into out (6 such arrays).  ny + 4 <= 65535.
+void launch_export_fields(cudaStream_t s, const Grid &g, const Axis &ax, const Axis &ay, const Axis &az,
+                          const double *const u[3], const double *p, float *out);
+
 }  // namespace ibm

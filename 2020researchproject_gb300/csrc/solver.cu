@@ -22,6 +22,7 @@
 #include "kernels.h"
 #include "krylov.h"
 #include "multigrid.h"
+#include "ncfile.h"
 #include "prof.h"
 #include "setup.h"
 
@@ -119,6 +120,7 @@ struct ibm3d_device {
     SolveReport rep_mom, rep_p;
     double max_div = 0.0;
     int status = IBM3D_OK;
+    char message[512] = {0};  // text of the last error
     bool assembled = false;
     Prof prof;
 };
@@ -131,13 +133,16 @@ constexpr int kUpdateBlocks = 608;
 int ncell_of(const IBMSolver *s) { return (s->Nx + 4) * (s->Ny + 4) * (s->Nz + 4); }
 
 void set_status(IBMSolver *s, int code, const char *fmt, ...) {
-    if (s && s->dev) s->dev->status = code;
+    char text[512];
     va_list ap;
     va_start(ap, fmt);
-    fprintf(stderr, "error: ");
-    vfprintf(stderr, fmt, ap);
-    fprintf(stderr, "\n");
+    vsnprintf(text, sizeof text, fmt, ap);
     va_end(ap);
+    if (s && s->dev) {
+        s->dev->status = code;
+        memcpy(s->dev->message, text, sizeof text);
+    }
+    fprintf(stderr, "error: %s\n", text);
     if (s && s->dev && s->dev->abort_on_error && code != IBM3D_ENOCONV) std::exit(255);
 }
 
@@ -1252,6 +1257,7 @@ void IBMSolver_assemble(IBMSolver *s) {
     g.sy = s->Nz + 4;
     g.sx = (long long)(s->Ny + 4) * g.sy;
     g.ncell = (long long)(s->Nx + 4) * g.sx;
+    set_grid_dividers(g);
     release_device(d);
     d->s = nullptr;
     cuda_check(s, cudaStreamCreateWithFlags(&d->s, cudaStreamNonBlocking), "stream");
@@ -1376,56 +1382,159 @@ void IBMSolver_init_flow_array(IBMSolver *s, const double *u1, const double *u2,
 }
 
 // ----------------------------------------------------------- export ---
+// Exact-resume state: header, then the padded FP64 u1, u2, u3, p in the
+// solver's own layout.  These four fields and (iter, time) are all the
+// state a later IBMSolver_iterate call reads: its prologue recomputes the
+// face velocities and the previous convection term from u
+// (src/ibm3d_fracstep.c:40-56).
 struct StateHeader {
     char magic[8];
     int nx, ny, nz, iter;
     double time;
 };
 
-void IBMSolver_export_result(IBMSolver *s, const char *name) {
-    if (!check_ready(s, "IBMSolver_export_result")) return;
-    IBMSolver_sync_host(s);
-    std::string path = std::string(name) + ".ibm3d";
+namespace {
+
+bool write_state(IBMSolver *s, const std::string &path) {
     FILE *f = fopen(path.c_str(), "wb");
-    if (!f) {
-        set_status(s, IBM3D_EARG, "cannot open file \"%s\"", path.c_str());
-        return;
-    }
+    if (!f) return false;
     StateHeader h{};
     memcpy(h.magic, "IBM3DST1", 8);
     h.nx = s->Nx; h.ny = s->Ny; h.nz = s->Nz; h.iter = s->iter; h.time = s->time;
     const size_t n = (size_t)ncell_of(s);
-    fwrite(&h, sizeof h, 1, f);
-    fwrite(s->u1, sizeof(double), n, f);
-    fwrite(s->u2, sizeof(double), n, f);
-    fwrite(s->u3, sizeof(double), n, f);
-    fwrite(s->p, sizeof(double), n, f);
-    fclose(f);
+    bool ok = fwrite(&h, sizeof h, 1, f) == 1;
+    for (double *a : {s->u1, s->u2, s->u3, s->p}) ok = ok && fwrite(a, sizeof(double), n, f) == n;
+    return fclose(f) == 0 && ok;
 }
 
-// src/ibm3d_init.c:45-224 (reads the state export_result writes).
-void IBMSolver_init_flow_file(IBMSolver *s, const char *name) {
-    if (!check_ready(s, "IBMSolver_init_flow_file")) return;
-    std::string path = std::string(name) + ".ibm3d";
+// 1: read into the host fields; 0: no such file; -1: a file that is not a
+// state of this grid (host fields untouched).
+int read_state(IBMSolver *s, const std::string &path) {
     FILE *f = fopen(path.c_str(), "rb");
-    if (!f) {
-        set_status(s, IBM3D_EARG, "cannot open file \"%s\"", path.c_str());
-        return;
-    }
+    if (!f) return 0;
     StateHeader h{};
     const size_t n = (size_t)ncell_of(s);
     bool ok = fread(&h, sizeof h, 1, f) == 1 && memcmp(h.magic, "IBM3DST1", 8) == 0 && h.nx == s->Nx &&
               h.ny == s->Ny && h.nz == s->Nz;
-    ok = ok && fread(s->u1, sizeof(double), n, f) == n && fread(s->u2, sizeof(double), n, f) == n &&
-         fread(s->u3, sizeof(double), n, f) == n && fread(s->p, sizeof(double), n, f) == n;
+    std::vector<double> buf(ok ? 4 * n : 0);
+    ok = ok && fread(buf.data(), sizeof(double), 4 * n, f) == 4 * n;
     fclose(f);
-    if (!ok) {
-        set_status(s, IBM3D_EARG, "\"%s\" is not a state file of this grid", path.c_str());
-        return;
-    }
-    upload_state(s, s->u1, s->u2, s->u3, s->p);
+    if (!ok) return -1;
+    double *dst[4] = {s->u1, s->u2, s->u3, s->p};
+    for (int q = 0; q < 4; q++) std::copy(buf.begin() + q * n, buf.begin() + (q + 1) * n, dst[q]);
     s->iter = h.iter;
     s->time = h.time;
+    return 1;
+}
+
+// The reference's result file (src/ibm3d_export.c:143-196): dimensions
+// time(1), x, y, z (padded sizes); time, x, y, z as double with axis and
+// units attributes; iter as a scalar int; u, v, w, p, vorticity, Q as
+// float [time][z][y][x].  The fields and vorticity/Q come from the GPU.
+bool write_result_nc(IBMSolver *s, const std::string &path) {
+    ibm3d_device *d = s->dev;
+    const long long plane = (long long)(s->Nx + 4) * (s->Ny + 4) * (s->Nz + 4);
+    if (s->Ny + 4 > 65535) {
+        set_status(s, IBM3D_EARG, "export: Ny + 4 = %d exceeds 65535", s->Ny + 4);
+        return false;
+    }
+    float *dbuf = nullptr;
+    if (!cuda_check(s, cudaMalloc(&dbuf, sizeof(float) * 6 * plane), "export buffer")) return false;
+    std::vector<float> h((size_t)(6 * plane));
+    launch_export_fields(d->s, d->g, d->ax[0], d->ax[1], d->ax[2], d->u, d->p, dbuf);
+    cudaMemcpyAsync(h.data(), dbuf, sizeof(float) * 6 * plane, cudaMemcpyDeviceToHost, d->s);
+    const bool dev_ok = cuda_check(s, cudaStreamSynchronize(d->s), "export");
+    cudaFree(dbuf);
+    if (!dev_ok) return false;
+
+    NcFile f;
+    f.dims = {{"time", 1}, {"x", s->Nx + 4}, {"y", s->Ny + 4}, {"z", s->Nz + 4}};
+    const double tval = s->time;
+    const int ival = s->iter;
+    f.vars.push_back({"time", NCT_DOUBLE, {0}, {{"axis", "T"}, {"units", "seconds"}}, &tval});
+    f.vars.push_back({"x", NCT_DOUBLE, {1}, {{"axis", "X"}, {"units", "meters"}}, s->xc});
+    f.vars.push_back({"y", NCT_DOUBLE, {2}, {{"axis", "Y"}, {"units", "meters"}}, s->yc});
+    f.vars.push_back({"z", NCT_DOUBLE, {3}, {{"axis", "Z"}, {"units", "meters"}}, s->zc});
+    f.vars.push_back({"iter", NCT_INT, {}, {}, &ival});
+    const char *names[6] = {"u", "v", "w", "p", "vorticity", "Q"};
+    const char *units[6] = {"m/s", "m/s", "m/s", "m/s", "1/s", "1/s^2"};
+    for (int q = 0; q < 6; q++)
+        f.vars.push_back({names[q], NCT_FLOAT, {0, 3, 2, 1}, {{"units", units[q]}}, h.data() + q * plane});
+    return nc_write(path, f);
+}
+
+// src/ibm3d_init.c:84-140: time, iter and the float u, v, w, p of a
+// result file, over the padded grid.  Same return codes as read_state.
+int read_result_nc(IBMSolver *s, const std::string &path) {
+    NcFile f;
+    FILE *probe = fopen(path.c_str(), "rb");
+    if (!probe) return 0;
+    fclose(probe);
+    if (!nc_read_header(path, f)) return -1;
+    auto dim = [&](const char *nm) -> long long {
+        for (auto &x : f.dims)
+            if (x.first == nm) return x.second;
+        return -1;
+    };
+    if (dim("x") != s->Nx + 4 || dim("y") != s->Ny + 4 || dim("z") != s->Nz + 4) return -1;
+    std::vector<double> tv, iv, fv[4];
+    const char *names[4] = {"u", "v", "w", "p"};
+    bool ok = nc_read_var(path, f, "time", tv) && nc_read_var(path, f, "iter", iv) && !tv.empty() && !iv.empty();
+    for (int q = 0; q < 4 && ok; q++) ok = nc_read_var(path, f, names[q], fv[q]);
+    const long long plane = (long long)(s->Nx + 4) * (s->Ny + 4) * (s->Nz + 4);
+    for (int q = 0; q < 4 && ok; q++) ok = (long long)fv[q].size() == plane;
+    if (!ok) return -1;
+    double *dst[4] = {s->u1, s->u2, s->u3, s->p};
+    const Grid &g = s->dev->g;
+    for (int k = -2; k < s->Nz + 2; k++)
+        for (int j = -2; j < s->Ny + 2; j++)
+            for (int i = -2; i < s->Nx + 2; i++) {
+                const long long o = ((long long)(k + 2) * (s->Ny + 4) + (j + 2)) * (s->Nx + 4) + (i + 2);
+                const long long P = cidx(g, i, j, k);
+                for (int q = 0; q < 4; q++) dst[q][P] = fv[q][o];
+            }
+    s->time = tv[0];
+    s->iter = (int)iv[0];
+    return 1;
+}
+
+}  // namespace
+
+// src/ibm3d_export.c:16-253.  Writes "<name>.nc" (the reference's float
+// result file) and "<name>.ibm3d" (the FP64 state for exact resume).
+void IBMSolver_export_result(IBMSolver *s, const char *name) {
+    if (!check_ready(s, "IBMSolver_export_result")) return;
+    IBMSolver_sync_host(s);
+    const std::string nc = std::string(name) + ".nc", st = std::string(name) + ".ibm3d";
+    if (!write_result_nc(s, nc)) {
+        if (s->dev->status == IBM3D_OK) set_status(s, IBM3D_EARG, "cannot write file \"%s\"", nc.c_str());
+        return;
+    }
+    if (!write_state(s, st)) set_status(s, IBM3D_EARG, "cannot write file \"%s\"", st.c_str());
+}
+
+// src/ibm3d_init.c:45-224.  Reads "<name>.ibm3d" when it exists (the
+// exact FP64 state export_result writes beside the result file), else the
+// float fields, time and iter of "<name>.nc" as the reference does.
+void IBMSolver_init_flow_file(IBMSolver *s, const char *name) {
+    if (!check_ready(s, "IBMSolver_init_flow_file")) return;
+    const std::string st = std::string(name) + ".ibm3d", nc = std::string(name) + ".nc";
+    int r = read_state(s, st);
+    const std::string used = r != 0 ? st : nc;
+    if (r == 0) r = read_result_nc(s, nc);
+    if (r == 0) {
+        set_status(s, IBM3D_EARG, "cannot open file \"%s\"", nc.c_str());
+        return;
+    }
+    if (r < 0) {
+        set_status(s, IBM3D_EARG, "\"%s\" is not a flow file of this grid", used.c_str());
+        return;
+    }
+    const int iter = s->iter;
+    const double time = s->time;
+    upload_state(s, s->u1, s->u2, s->u3, s->p);
+    s->iter = iter;
+    s->time = time;
 }
 
 void IBMSolver_export_lvset_flag(IBMSolver *s, const char *name) {
@@ -1525,6 +1634,8 @@ void IBMSolver_iterate(IBMSolver *s, int num_time_steps, bool verbose) {
 
 // ------------------------------------------------------- extensions ---
 int IBMSolver_last_status(const IBMSolver *s) { return s && s->dev ? s->dev->status : IBM3D_EARG; }
+
+const char *IBMSolver_last_message(const IBMSolver *s) { return s && s->dev ? s->dev->message : ""; }
 
 const char *IBMSolver_status_string(int st) {
     switch (st) {

@@ -5,6 +5,8 @@
 // products with 1-D reciprocal tables built once at assembly: FP64
 // arithmetic, not HBM, is the scarce resource on GB300, and the tables cost
 // a few KB of L1-resident loads.
+#include <algorithm>
+
 #include "common.cuh"
 #include "kernels.h"
 
@@ -30,7 +32,7 @@ k_conv_rhs(const Grid g, const Axis ax, const Axis ay, const Axis az, const BCSe
     for (long long P = blockIdx.x * (long long)blockDim.x + threadIdx.x; P < n;
          P += (long long)gridDim.x * blockDim.x) {
         int i, j, k;
-        cijk(g, P, i, j, k);
+        cijk_g(g, P, i, j, k);
         int layer;
         const int f = owner_face(g, i, j, k, layer);
         if (f >= 0) {
@@ -108,9 +110,8 @@ k_smagorinsky(const Grid g, const Axis ax, const Axis ay, const Axis az, const u
     const long long n = (long long)g.nx * g.ny * g.nz;
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
          q += (long long)gridDim.x * blockDim.x) {
-        const int k = (int)(q % g.nz);
-        const int j = (int)((q / g.nz) % g.ny);
-        const int i = (int)(q / ((long long)g.nz * g.ny));
+        int i, j, k;
+        ijk_interior(g, q, i, j, k);
         const long long P = cidx(g, i, j, k);
         if (flag[P] != FLUID) continue;
         const long long sx = g.sx, sy = g.sy;
@@ -172,7 +173,7 @@ k_ustar_prhs(const Grid g, const Axis ax, const Axis ay, const Axis az, const BC
     for (long long P = blockIdx.x * (long long)blockDim.x + threadIdx.x; P < n;
          P += (long long)gridDim.x * blockDim.x) {
         int i, j, k;
-        cijk(g, P, i, j, k);
+        cijk_g(g, P, i, j, k);
         int layer;
         if (owner_face(g, i, j, k, layer) >= 0) {
             a.b[P] = 0.0;
@@ -225,9 +226,8 @@ k_update_next(const Grid g, const Axis ax, const Axis ay, const Axis az, const B
     const double NaN = __longlong_as_double(0x7ff8000000000000LL);
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
          q += (long long)gridDim.x * blockDim.x) {
-        const int k = (int)(q % g.nz);
-        const int j = (int)((q / g.nz) % g.ny);
-        const int i = (int)(q / ((long long)g.nz * g.ny));
+        int i, j, k;
+        ijk_interior(g, q, i, j, k);
         const long long P = cidx(g, i, j, k);
         const long long sx = g.sx, sy = g.sy;
         const int I = i + 2, J = j + 2, K = k + 2;
@@ -396,7 +396,7 @@ k_interp_stag(const Grid g, const Axis ax, const Axis ay, const Axis az, const d
     for (long long P = blockIdx.x * (long long)blockDim.x + threadIdx.x; P < n;
          P += (long long)gridDim.x * blockDim.x) {
         int i, j, k;
-        cijk(g, P, i, j, k);
+        cijk_g(g, P, i, j, k);
         if (i >= 0 && i <= g.nx) U1[P] = u1[P - g.sx] * ax.wm[i + 2] + u1[P] * ax.wp[i + 2];
         if (j >= 0 && j <= g.ny) U2[P] = u2[P - g.sy] * ay.wm[j + 2] + u2[P] * ay.wp[j + 2];
         if (k >= 0 && k <= g.nz) U3[P] = u3[P - 1] * az.wm[k + 2] + u3[P] * az.wp[k + 2];
@@ -474,9 +474,8 @@ __global__ void k_solid_nan(const Grid g, const uint8_t *__restrict__ flag, doub
     const double NaN = __longlong_as_double(0x7ff8000000000000LL);
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
          q += (long long)gridDim.x * blockDim.x) {
-        const int k = (int)(q % g.nz);
-        const int j = (int)((q / g.nz) % g.ny);
-        const int i = (int)(q / ((long long)g.nz * g.ny));
+        int i, j, k;
+        ijk_interior(g, q, i, j, k);
         const long long P = cidx(g, i, j, k);
         if (flag[P] == SOLID) u0[P] = u1[P] = u2[P] = p[P] = NaN;
     }
@@ -486,6 +485,102 @@ void launch_solid_nan(cudaStream_t s, const Grid &g, const uint8_t *flag, double
     const long long n = (long long)g.nx * g.ny * g.nz;
     k_solid_nan<<<grid_for(n, 256), 256, 0, s>>>(g, flag, u[0], u[1], u[2], p);
     note_launches(1);
+}
+
+// ------------------------------------------------------------- export ---
+// Result export (src/ibm3d_export.c:71-141): the four FP64 fields become
+// float arrays in the file's [z][y][x] order over the padded grid, and
+// vorticity magnitude and Q follow from those float values with the
+// reference's arithmetic: each gradient is a float difference divided by
+// a double coordinate difference, rounded to float; products and sums in
+// float, left to right; |omega| = float(sqrt(double(sum of squares))).
+// Neighbour indices are clamped to the padded range [0, N+3].
+
+// Tiled transpose: a 32x32 (i, k) tile of plane j, read k-contiguous and
+// written i-contiguous.
+__global__ void __launch_bounds__(256)
+k_export_transpose(const Grid g, const double *__restrict__ f0, const double *__restrict__ f1,
+                   const double *__restrict__ f2, const double *__restrict__ f3, float *__restrict__ out) {
+    __shared__ float tile[4][32][33];
+    const int NX = g.nx + 4, NY = g.ny + 4, NZ = g.nz + 4;
+    const int i0 = blockIdx.x * 32, k0 = blockIdx.y * 32, j = blockIdx.z;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const double *src[4] = {f0, f1, f2, f3};
+    for (int r = 0; r < 32; r += 8) {
+        const int i = i0 + ty + r, k = k0 + tx;
+        if (i < NX && k < NZ) {
+            const long long P = (long long)i * g.sx + (long long)j * g.sy + k;
+#pragma unroll
+            for (int f = 0; f < 4; f++) tile[f][ty + r][tx] = __double2float_rn(src[f][P]);
+        }
+    }
+    __syncthreads();
+    const long long plane = (long long)NX * NY * NZ;
+    for (int r = 0; r < 32; r += 8) {
+        const int k = k0 + ty + r, i = i0 + tx;
+        if (i < NX && k < NZ) {
+            const long long o = ((long long)k * NY + j) * NX + i;
+#pragma unroll
+            for (int f = 0; f < 4; f++) out[f * plane + o] = tile[f][tx][ty + r];
+        }
+    }
+}
+
+__device__ __forceinline__ float export_grad(float a, float b, double ca, double cb) {
+    return __double2float_rn(__ddiv_rn((double)__fsub_rn(a, b), __dsub_rn(ca, cb)));
+}
+
+// out holds u, v, w, p (NX*NY*NZ floats each, x fastest); vorticity and Q
+// are written after them.
+__global__ void __launch_bounds__(256)
+k_export_vort_q(const Grid g, const double *__restrict__ xc, const double *__restrict__ yc,
+                const double *__restrict__ zc, float *__restrict__ out) {
+    const int NX = g.nx + 4, NY = g.ny + 4, NZ = g.nz + 4;
+    const long long plane = (long long)NX * NY * NZ;
+    const float *u = out, *v = out + plane, *w = out + 2 * plane;
+    float *vort = out + 4 * plane, *q = out + 5 * plane;
+    for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < plane;
+         o += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(o % NX);
+        const int j = (int)(o / NX % NY);
+        const int k = (int)(o / ((long long)NX * NY));
+        const int ip = max(i - 1, 0), in = min(i + 1, NX - 1);
+        const int jp = max(j - 1, 0), jn = min(j + 1, NY - 1);
+        const int kp = max(k - 1, 0), kn = min(k + 1, NZ - 1);
+        const long long xn = o - i + in, xp = o - i + ip;
+        const long long yn = o + (long long)(jn - j) * NX, yp = o + (long long)(jp - j) * NX;
+        const long long zn = o + (long long)(kn - k) * NX * NY, zp = o + (long long)(kp - k) * NX * NY;
+        const double cxn = xc[in], cxp = xc[ip], cyn = yc[jn], cyp = yc[jp], czn = zc[kn], czp = zc[kp];
+        const float dudx = export_grad(u[xn], u[xp], cxn, cxp);
+        const float dudy = export_grad(u[yn], u[yp], cyn, cyp);
+        const float dudz = export_grad(u[zn], u[zp], czn, czp);
+        const float dvdx = export_grad(v[xn], v[xp], cxn, cxp);
+        const float dvdy = export_grad(v[yn], v[yp], cyn, cyp);
+        const float dvdz = export_grad(v[zn], v[zp], czn, czp);
+        const float dwdx = export_grad(w[xn], w[xp], cxn, cxp);
+        const float dwdy = export_grad(w[yn], w[yp], cyn, cyp);
+        const float dwdz = export_grad(w[zn], w[zp], czn, czp);
+        const float ox = __fsub_rn(dwdy, dvdz), oy = __fsub_rn(dudz, dwdx), oz = __fsub_rn(dvdx, dudy);
+        const float s2 = __fadd_rn(__fadd_rn(__fmul_rn(ox, ox), __fmul_rn(oy, oy)), __fmul_rn(oz, oz));
+        vort[o] = __double2float_rn(__dsqrt_rn((double)s2));
+        float t = __fadd_rn(__fmul_rn(dudx, dvdy), __fmul_rn(dvdy, dwdz));
+        t = __fadd_rn(t, __fmul_rn(dwdz, dudx));
+        t = __fsub_rn(t, __fmul_rn(dudy, dvdx));
+        t = __fsub_rn(t, __fmul_rn(dvdz, dwdy));
+        t = __fsub_rn(t, __fmul_rn(dudz, dwdx));
+        q[o] = t;
+    }
+}
+
+void launch_export_fields(cudaStream_t s, const Grid &g, const Axis &ax, const Axis &ay, const Axis &az,
+                          const double *const u[3], const double *p, float *out) {
+    const int NX = g.nx + 4, NY = g.ny + 4, NZ = g.nz + 4;
+    const dim3 tgrid((NX + 31) / 32, (NZ + 31) / 32, NY);
+    k_export_transpose<<<tgrid, dim3(32, 8), 0, s>>>(g, u[0], u[1], u[2], p, out);
+    const long long plane = (long long)NX * NY * NZ;
+    const long long blocks = std::min<long long>((plane + 255) / 256, 152LL * 64);
+    k_export_vort_q<<<(unsigned)blocks, 256, 0, s>>>(g, ax.c, ay.c, az.c, out);
+    note_launches(2);
 }
 
 }  // namespace ibm

@@ -28,6 +28,9 @@ enum {
     IBM3D_EUNSUPPORTED = 6  /* feature not available on the GPU path */
 };
 int IBMSolver_last_status(const IBMSolver *);
+/* Text of the last error set on this solver ("" if none); the reference
+   prints such errors and aborts (e.g. src/ibm3d_init.c:88-90). */
+const char *IBMSolver_last_message(const IBMSolver *);
 const char *IBMSolver_status_string(int status);
 
 /* Non-variadic forms of set_bc / set_ext_force / set_turb_model (same
