@@ -1382,46 +1382,81 @@ void IBMSolver_init_flow_array(IBMSolver *s, const double *u1, const double *u2,
 }
 
 // ----------------------------------------------------------- export ---
-// Exact-resume state: header, then the padded FP64 u1, u2, u3, p in the
-// solver's own layout.  These four fields and (iter, time) are all the
-// state a later IBMSolver_iterate call reads: its prologue recomputes the
-// face velocities and the previous convection term from u
-// (src/ibm3d_fracstep.c:40-56).
+// Exact-resume state: header, then every device field a later
+// IBMSolver_iterate call can read, in role order, as padded FP64 arrays.
+// u and p alone do not suffice: the reference double-buffers u, U, p and N
+// (src/ibm3d_fracstep.c:795-804) and update_next writes only fluid cells
+// of u_next, so after each swap the ghost cells and padding corners hold
+// the values of two steps back, which update_ghost reads for ghosts later
+// in its sweep (src/ibm3d_fracstep.c:1915-1976).  The reference's own
+// restart from its float file cannot reproduce those; this file does.
 struct StateHeader {
     char magic[8];
     int nx, ny, nz, iter;
     double time;
+    int nfields, pad;
 };
 
 namespace {
 
+constexpr int kStateFields = 26;
+
+// Device arrays of the state, in file order.
+void state_fields(ibm3d_device *d, double *f[kStateFields]) {
+    int q = 0;
+    for (int l = 0; l < 3; l++) f[q++] = d->u[l];
+    for (int l = 0; l < 3; l++) f[q++] = d->un[l];
+    for (int l = 0; l < 3; l++) f[q++] = d->U[l];
+    for (int l = 0; l < 3; l++) f[q++] = d->Un[l];
+    f[q++] = d->p;
+    f[q++] = d->pn;
+    for (int l = 0; l < 3; l++) f[q++] = d->N[l];
+    for (int l = 0; l < 3; l++) f[q++] = d->Np[l];
+    for (int l = 0; l < 6; l++) f[q++] = d->tau[l];
+}
+
 bool write_state(IBMSolver *s, const std::string &path) {
+    ibm3d_device *d = s->dev;
     FILE *f = fopen(path.c_str(), "wb");
     if (!f) return false;
     StateHeader h{};
-    memcpy(h.magic, "IBM3DST1", 8);
+    memcpy(h.magic, "IBM3DST2", 8);
     h.nx = s->Nx; h.ny = s->Ny; h.nz = s->Nz; h.iter = s->iter; h.time = s->time;
-    const size_t n = (size_t)ncell_of(s);
+    h.nfields = kStateFields;
+    const size_t n = (size_t)d->g.ncell;
     bool ok = fwrite(&h, sizeof h, 1, f) == 1;
-    for (double *a : {s->u1, s->u2, s->u3, s->p}) ok = ok && fwrite(a, sizeof(double), n, f) == n;
+    double *fld[kStateFields];
+    state_fields(d, fld);
+    std::vector<double> buf(n);
+    for (int q = 0; q < kStateFields && ok; q++) {
+        ok = cuda_check(s, cudaMemcpy(buf.data(), fld[q], n * sizeof(double), cudaMemcpyDeviceToHost), "state read");
+        ok = ok && fwrite(buf.data(), sizeof(double), n, f) == n;
+    }
     return fclose(f) == 0 && ok;
 }
 
-// 1: read into the host fields; 0: no such file; -1: a file that is not a
-// state of this grid (host fields untouched).
+// 1: read into the device fields (and u, p into the host mirrors); 0: no
+// such file; -1: a file that is not a state of this grid (nothing changed).
 int read_state(IBMSolver *s, const std::string &path) {
+    ibm3d_device *d = s->dev;
     FILE *f = fopen(path.c_str(), "rb");
     if (!f) return 0;
     StateHeader h{};
-    const size_t n = (size_t)ncell_of(s);
-    bool ok = fread(&h, sizeof h, 1, f) == 1 && memcmp(h.magic, "IBM3DST1", 8) == 0 && h.nx == s->Nx &&
-              h.ny == s->Ny && h.nz == s->Nz;
-    std::vector<double> buf(ok ? 4 * n : 0);
-    ok = ok && fread(buf.data(), sizeof(double), 4 * n, f) == 4 * n;
+    const size_t n = (size_t)d->g.ncell;
+    bool ok = fread(&h, sizeof h, 1, f) == 1 && memcmp(h.magic, "IBM3DST2", 8) == 0 && h.nx == s->Nx &&
+              h.ny == s->Ny && h.nz == s->Nz && h.nfields == kStateFields;
+    std::vector<double> buf(ok ? kStateFields * n : 0);
+    ok = ok && fread(buf.data(), sizeof(double), buf.size(), f) == buf.size();
     fclose(f);
     if (!ok) return -1;
-    double *dst[4] = {s->u1, s->u2, s->u3, s->p};
-    for (int q = 0; q < 4; q++) std::copy(buf.begin() + q * n, buf.begin() + (q + 1) * n, dst[q]);
+    double *fld[kStateFields];
+    state_fields(d, fld);
+    for (int q = 0; q < kStateFields; q++)
+        cudaMemcpyAsync(fld[q], buf.data() + q * n, n * sizeof(double), cudaMemcpyHostToDevice, d->s);
+    if (!cuda_check(s, cudaStreamSynchronize(d->s), "state upload")) return 1;
+    double *host[4] = {s->u1, s->u2, s->u3, s->p};
+    const int role[4] = {0, 1, 2, 12};
+    for (int q = 0; q < 4; q++) std::copy(buf.begin() + role[q] * n, buf.begin() + (role[q] + 1) * n, host[q]);
     s->iter = h.iter;
     s->time = h.time;
     return 1;
@@ -1530,6 +1565,7 @@ void IBMSolver_init_flow_file(IBMSolver *s, const char *name) {
         set_status(s, IBM3D_EARG, "\"%s\" is not a flow file of this grid", used.c_str());
         return;
     }
+    if (used == st) return;  // read_state uploaded every field
     const int iter = s->iter;
     const double time = s->time;
     upload_state(s, s->u1, s->u2, s->u3, s->p);
