@@ -47,6 +47,11 @@ class IBM3DError(RuntimeError):
     pass
 
 
+# double f(double t, double x, double y, double z): IBMSolverBCValFunc and
+# IBMSolverForceFunc (src/ibm3d.h).
+_VALFUNC = ctypes.CFUNCTYPE(ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double)
+
+
 class _Stats(ctypes.Structure):
     _fields_ = [("iter", ctypes.c_int), ("time", ctypes.c_double),
                 ("iters_u", ctypes.c_int * 3), ("iters_p", ctypes.c_int),
@@ -81,6 +86,8 @@ def load_library(path: str = LIB_PATH):
         "IBMSolver_set_params": (None, [vp, d, d]),
         "IBMSolver_set_bc_const": (None, [vp, i, i, d, d, d, d]),
         "IBMSolver_set_ext_force_const": (None, [vp, d, d, d]),
+        "IBMSolver_set_bc_func": (None, [vp, i, i, vp, vp, vp, vp]),
+        "IBMSolver_set_ext_force_func": (None, [vp, vp, vp, vp]),
         "IBMSolver_set_smagorinsky": (None, [vp, d]),
         "IBMSolver_set_obstacle": (None, [vp, vp]),
         "IBMSolver_set_linear_solver": (None, [vp, i, i, d]),
@@ -193,6 +200,7 @@ class IBMSolver:
         self._s = self._lib.IBMSolver_new(num_process, rank, Px, Py, Pz)
         self._check("IBMSolver_new")
         self.shape = None
+        self._callbacks = []
 
     def _check(self, what):
         st = self._lib.IBMSolver_last_status(self._s)
@@ -220,9 +228,24 @@ class IBMSolver:
     def set_params(self, Re, dt):
         self._lib.IBMSolver_set_params(self._s, Re, dt)
 
+    def _func(self, f):
+        """A C callback double(t, x, y, z) for f, kept alive with the solver."""
+        cb = _VALFUNC(f)
+        self._callbacks.append(cb)
+        return ctypes.cast(cb, ctypes.c_void_p)
+
     def set_bc(self, direction, bc_type, *values):
         """set_bc(DIR, BC_VELOCITY_COMPONENT, u1, u2, u3) | (DIR, BC_PRESSURE, p)
-        | (DIR, BC_VELOCITY_PERIODIC, p) | (DIR, other type)."""
+        | (DIR, BC_VELOCITY_PERIODIC, p) | (DIR, other type).  Values are
+        numbers (VAL_CONST) or callables f(t, x, y, z) (VAL_FUNC)."""
+        if values and all(callable(v) for v in values):
+            fs = [self._func(v) for v in values]
+            if bc_type == BC_VELOCITY_COMPONENT:
+                self._lib.IBMSolver_set_bc_func(self._s, direction, bc_type, fs[0], fs[1], fs[2], None)
+            else:
+                self._lib.IBMSolver_set_bc_func(self._s, direction, bc_type, None, None, None, fs[0])
+            self._check("set_bc")
+            return
         u = [0.0, 0.0, 0.0]
         p = 0.0
         if bc_type == BC_VELOCITY_COMPONENT:
@@ -232,7 +255,11 @@ class IBMSolver:
         self._lib.IBMSolver_set_bc_const(self._s, direction, bc_type, u[0], u[1], u[2], p)
 
     def set_ext_force(self, f1, f2, f3):
-        self._lib.IBMSolver_set_ext_force_const(self._s, f1, f2, f3)
+        """Constant force components, or callables f(t, x, y, z) (VAL_FUNC)."""
+        if all(callable(f) for f in (f1, f2, f3)):
+            self._lib.IBMSolver_set_ext_force_func(self._s, *(self._func(f) for f in (f1, f2, f3)))
+        else:
+            self._lib.IBMSolver_set_ext_force_const(self._s, f1, f2, f3)
 
     def set_turb_model(self, model, Cs=0.0):
         if model == TURBMODEL_SMAGORINSKY:

@@ -130,6 +130,13 @@ struct BCFace {
     double fv_a[2], fv_b[2];     // velocity Dirichlet / slip: u_o = fv_a*bc - fv_b*u_m
     double fe_a[2], fe_b[2];     // extrapolation: u_o = fe_a*u_(o+1in) - fe_b*u_(o+2in)
     double fp_a[2], fp_b[2];     // pressure Dirichlet: p_o = fp_a*bc - fp_b*p_m
+    // Sampled values of a VAL_FUNC face (null for constant values): one
+    // entry per outer line of the face over its padded tangential range
+    // (face_line), nt entries per quantity: u1, u2, u3 at [l*nt + t], p at
+    // [3*nt + t].  scur holds the values at the step's start time, snxt at
+    // its end time (src/ibm3d_fracstep.c:2001-2035).
+    const double *scur, *snxt;
+    int nt;
 };
 
 struct BCSet {
@@ -153,6 +160,21 @@ __host__ __device__ inline int owner_face(const Grid &g, int i, int j, int k, in
 }
 
 __host__ __device__ inline int face_axis(int f) { return (f == F_E || f == F_W) ? 0 : (f == F_N || f == F_S) ? 1 : 2; }
+
+// Outer line of face f through padded cell (i, j, k): its position in the
+// face's padded tangential range, (j, k) for x faces, (i, k) for y faces,
+// (i, j) for z faces.
+__host__ __device__ inline int face_line(const Grid &g, int f, int i, int j, int k) {
+    const int ax = face_axis(f);
+    if (ax == 0) return (j + 2) * (g.nz + 4) + (k + 2);
+    if (ax == 1) return (i + 2) * (g.nz + 4) + (k + 2);
+    return (i + 2) * (g.ny + 4) + (j + 2);
+}
+
+__host__ __device__ inline int face_lines(const Grid &g, int f) {
+    const int ax = face_axis(f);
+    return ax == 0 ? (g.ny + 4) * (g.nz + 4) : ax == 1 ? (g.nx + 4) * (g.nz + 4) : (g.nx + 4) * (g.ny + 4);
+}
 __host__ __device__ inline bool face_low(int f) { return f == F_W || f == F_S || f == F_D; }
 
 // Periodic image of a padded cell: every outer coordinate wrapped into the

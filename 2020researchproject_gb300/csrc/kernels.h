@@ -21,6 +21,7 @@ struct ConvArgs {
     const double *tau[6];
     double *N[3];
     double *b[3];
+    const double *force;   // sampled VAL_FUNC body force, 3 x ncell (null: the constant force)
 };
 
 struct TauArgs {
@@ -69,7 +70,9 @@ void launch_ustar_prhs(cudaStream_t s, const Grid &g, const Axis &ax, const Axis
 void launch_update_next(cudaStream_t s, const Grid &g, const Axis &ax, const Axis &ay, const Axis &az,
                         const BCSet &bc, const uint8_t *flag, const NextArgs &a, double dt, double *partials,
                         unsigned int *counter, double *maxdiv_out, int nblocks);
-void launch_fill_outer(cudaStream_t s, const Grid &g, const BCSet &bc, double *const u[3], double *p);
+// when: 0 fills with the values at the step's start time, 1 at its end
+// time (the two differ only for VAL_FUNC faces).
+void launch_fill_outer(cudaStream_t s, const Grid &g, const BCSet &bc, double *const u[3], double *p, int when);
 void launch_interp_stag(cudaStream_t s, const Grid &g, const Axis &ax, const Axis &ay, const Axis &az,
                         const double *const u[3], double *const U[3]);
 void launch_ghost_update(cudaStream_t s, const GhostArgs &a, double *const u[3], double *p);

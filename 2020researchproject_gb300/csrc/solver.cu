@@ -102,6 +102,18 @@ struct ibm3d_device {
     unsigned int *red_counter = nullptr;
     double *maxdiv_d = nullptr;
     double *maxdiv_h = nullptr;
+    // VAL_FUNC boundary values and body force, sampled on the host each
+    // step: per sampled face a block of 2 x 4 x nt values (start-time
+    // values, then end-time values; see BCFace), and 3 x ncell force values.
+    double *smp_d = nullptr, *smp_h = nullptr;
+    size_t smp_n = 0;
+    size_t smp_off[6] = {0, 0, 0, 0, 0, 0};
+    bool smp_face[6] = {false, false, false, false, false, false};
+    double smp_t[2] = {0, 0}, smp_dev_t[2] = {0, 0};
+    bool smp_valid = false, smp_dev_valid = false;
+    double *force_d = nullptr, *force_h = nullptr;
+    double force_t = 0, force_dev_t = 0;
+    bool force_valid = false, force_dev_valid = false;
     // Settings.
     double divtol = 0.0;
     int precision = IBM3D_FP64;
@@ -268,6 +280,13 @@ void release_device(ibm3d_device *d) {
     dfree(d->maxdiv_d);
     if (d->maxdiv_h) cudaFreeHost(d->maxdiv_h);
     d->maxdiv_h = nullptr;
+    dfree(d->smp_d);
+    dfree(d->force_d);
+    if (d->smp_h) cudaFreeHost(d->smp_h);
+    if (d->force_h) cudaFreeHost(d->force_h);
+    d->smp_h = d->force_h = nullptr;
+    d->smp_n = 0;
+    d->smp_valid = d->smp_dev_valid = d->force_valid = d->force_dev_valid = false;
     d->nghost = d->nlevels = 0;
     d->gargs = GhostArgs{};
     d->g_gidx = nullptr;
@@ -693,6 +712,7 @@ ConvArgs conv_args(ibm3d_device *d) {
     }
     for (int t = 0; t < 6; t++) a.tau[t] = d->tau[t];
     a.p = d->p;
+    a.force = d->force_d;
     return a;
 }
 
@@ -705,9 +725,129 @@ void calc_tau(IBMSolver *sv) {
     launch_smagorinsky(d->s, d->g, d->ax[0], d->ax[1], d->ax[2], d->flag, d->lvset, u, t, sv->turb_model.Cs);
 }
 
-void fill_outer(IBMSolver *sv) {
+// when: 0 at the step's start time (iterate prologue), 1 at its end.
+void fill_outer(IBMSolver *sv, int when) {
     ibm3d_device *d = sv->dev;
-    launch_fill_outer(d->s, d->g, d->bc, d->u, d->p);
+    launch_fill_outer(d->s, d->g, d->bc, d->u, d->p, when);
+}
+
+// ------------------------------------------------- VAL_FUNC sampling ---
+// The reference evaluates VAL_FUNC callbacks inside its loops
+// (src/ibm3d_fracstep.c:1978-2035): boundary values at the face centre of
+// each outer line at the current time (momentum right-hand side and outer
+// fills) and at time + dt (pressure-correction right-hand side), the body
+// force at every cell centre at the current time.  Here the host samples
+// them once per step into pinned buffers that are copied to the device
+// before the step's kernels; the kernels read the samples where they would
+// read the constant values.
+bool sampled_face(const IBMSolver *sv, int f) {
+    const IBMSolverBC &B = sv->bc[f];
+    return B.val_type == VAL_FUNC && (B.type == BC_VELOCITY_COMPONENT || B.type == BC_PRESSURE ||
+                                      B.type == BC_VELOCITY_PERIODIC);
+}
+
+bool alloc_samples(IBMSolver *sv) {
+    ibm3d_device *d = sv->dev;
+    size_t n = 0;
+    for (int f = 0; f < 6; f++) {
+        d->smp_face[f] = sampled_face(sv, f);
+        d->bc.f[f].scur = d->bc.f[f].snxt = nullptr;
+        d->bc.f[f].nt = face_lines(d->g, f);
+        d->smp_off[f] = n;
+        if (d->smp_face[f]) n += 8 * (size_t)d->bc.f[f].nt;
+    }
+    d->smp_n = n;
+    if (n) {
+        d->smp_d = dmalloc<double>(sv, n, "boundary samples");
+        if (!d->smp_d || !cuda_check(sv, cudaMallocHost(&d->smp_h, n * sizeof(double)), "boundary samples")) return false;
+        memset(d->smp_h, 0, n * sizeof(double));
+        for (int f = 0; f < 6; f++)
+            if (d->smp_face[f]) {
+                d->bc.f[f].scur = d->smp_d + d->smp_off[f];
+                d->bc.f[f].snxt = d->smp_d + d->smp_off[f] + 4 * (size_t)d->bc.f[f].nt;
+            }
+    }
+    if (sv->ext_force.val_type == VAL_FUNC) {
+        const size_t m = 3 * (size_t)d->g.ncell;
+        d->force_d = dmalloc<double>(sv, m, "force samples");
+        if (!d->force_d || !cuda_check(sv, cudaMallocHost(&d->force_h, m * sizeof(double)), "force samples"))
+            return false;
+        memset(d->force_h, 0, m * sizeof(double));
+    }
+    return true;
+}
+
+// Values of face f at time t into dst (4 x nt: u1, u2, u3, p).
+void sample_face(const IBMSolver *sv, int f, double t, double *dst) {
+    const IBMSolverBC &B = sv->bc[f];
+    const Grid &g = sv->dev->g;
+    const int nt = face_lines(g, f), ax = face_axis(f);
+    const bool low = face_low(f);
+    const bool vel = B.type == BC_VELOCITY_COMPONENT;
+    const int na = ax == 0 ? g.ny + 4 : g.nx + 4, nb = ax == 2 ? g.ny + 4 : g.nz + 4;
+    for (int a = 0; a < na; a++)
+        for (int b = 0; b < nb; b++) {
+            double x, y, z;
+            if (ax == 0) { x = low ? sv->xmin : sv->xmax; y = sv->yc[a]; z = sv->zc[b]; }
+            else if (ax == 1) { x = sv->xc[a]; y = low ? sv->ymin : sv->ymax; z = sv->zc[b]; }
+            else { x = sv->xc[a]; y = sv->yc[b]; z = low ? sv->zmin : sv->zmax; }
+            const int line = a * nb + b;
+            dst[line] = vel ? B.func_u1(t, x, y, z) : 0.0;
+            dst[nt + line] = vel ? B.func_u2(t, x, y, z) : 0.0;
+            dst[2 * nt + line] = vel ? B.func_u3(t, x, y, z) : 0.0;
+            dst[3 * nt + line] = vel ? 0.0 : B.func_p(t, x, y, z);
+        }
+}
+
+// Samples for a step from time t0 to t1 (the iterate prologue passes its
+// start time and the first step's end time), copied on stream st.
+void prepare_samples(IBMSolver *sv, cudaStream_t st, double t0, double t1) {
+    ibm3d_device *d = sv->dev;
+    if (d->smp_n) {
+        const bool have0 = d->smp_valid && d->smp_t[0] == t0, have1 = d->smp_valid && d->smp_t[1] == t1;
+        if (!(have0 && have1)) {
+            const bool rotate = d->smp_valid && d->smp_t[1] == t0;
+            for (int f = 0; f < 6; f++) {
+                if (!d->smp_face[f]) continue;
+                const size_t m = 4 * (size_t)d->bc.f[f].nt;
+                double *cur = d->smp_h + d->smp_off[f], *nxt = cur + m;
+                if (!have0) {
+                    if (rotate) memcpy(cur, nxt, m * sizeof(double));
+                    else sample_face(sv, f, t0, cur);
+                }
+                if (!have1) sample_face(sv, f, t1, nxt);
+            }
+            d->smp_t[0] = t0;
+            d->smp_t[1] = t1;
+            d->smp_valid = true;
+        }
+        if (!(d->smp_dev_valid && d->smp_dev_t[0] == t0 && d->smp_dev_t[1] == t1)) {
+            cudaMemcpyAsync(d->smp_d, d->smp_h, d->smp_n * sizeof(double), cudaMemcpyHostToDevice, st);
+            d->smp_dev_t[0] = t0;
+            d->smp_dev_t[1] = t1;
+            d->smp_dev_valid = true;
+        }
+    }
+    if (d->force_d) {
+        if (!(d->force_valid && d->force_t == t0)) {
+            const Grid &g = d->g;
+            const IBMSolverForceFunc fn[3] = {sv->ext_force.func_f1, sv->ext_force.func_f2, sv->ext_force.func_f3};
+            for (int i = 0; i < g.nx; i++)
+                for (int j = 0; j < g.ny; j++)
+                    for (int k = 0; k < g.nz; k++) {
+                        const long long P = cidx(g, i, j, k);
+                        const double x = sv->xc[i + 2], y = sv->yc[j + 2], z = sv->zc[k + 2];
+                        for (int l = 0; l < 3; l++) d->force_h[l * g.ncell + P] = fn[l](t0, x, y, z);
+                    }
+            d->force_t = t0;
+            d->force_valid = true;
+        }
+        if (!(d->force_dev_valid && d->force_dev_t == t0)) {
+            cudaMemcpyAsync(d->force_d, d->force_h, 3 * d->g.ncell * sizeof(double), cudaMemcpyHostToDevice, st);
+            d->force_dev_t = t0;
+            d->force_dev_valid = true;
+        }
+    }
 }
 
 void ghost_update(IBMSolver *sv, bool solids) {
@@ -881,7 +1021,7 @@ bool record_step_into(IBMSolver *sv, StepGraph &G) {
     if (ok) {
         stage_next(sv);
         swap_fields(d);
-        fill_outer(sv);
+        fill_outer(sv, 1);
         ghost_update(sv, false);
         cudaMemcpyAsync(d->maxdiv_h, d->maxdiv_d, sizeof(double), cudaMemcpyDeviceToHost, d->s);
         swap_fields(d);
@@ -1234,15 +1374,18 @@ void IBMSolver_assemble(IBMSolver *s) {
         set_status(s, IBM3D_EARG, "Inconsistent periodic boundary condition");
         return;
     }
-    if (s->ext_force.val_type != VAL_CONST) {
-        set_status(s, IBM3D_EUNSUPPORTED, "VAL_FUNC body forces are not supported on the GPU path");
-        return;
-    }
     for (int f = 0; f < 6; f++)
-        if (s->bc[f].val_type != VAL_CONST) {
-            set_status(s, IBM3D_EUNSUPPORTED, "VAL_FUNC boundary values are not supported on the GPU path");
+        if (sampled_face(s, f) &&
+            (s->bc[f].type == BC_VELOCITY_COMPONENT ? !(s->bc[f].func_u1 && s->bc[f].func_u2 && s->bc[f].func_u3)
+                                                    : !s->bc[f].func_p)) {
+            set_status(s, IBM3D_EARG, "VAL_FUNC boundary condition without a function");
             return;
         }
+    if (s->ext_force.val_type == VAL_FUNC &&
+        !(s->ext_force.func_f1 && s->ext_force.func_f2 && s->ext_force.func_f3)) {
+        set_status(s, IBM3D_EARG, "VAL_FUNC body force without a function");
+        return;
+    }
     if (s->turb_model.type != TURBMODEL_NONE && s->turb_model.type != TURBMODEL_SMAGORINSKY) {
         set_status(s, IBM3D_EUNSUPPORTED, "turbulence model %d is not implemented", (int)s->turb_model.type);
         return;
@@ -1268,7 +1411,7 @@ void IBMSolver_assemble(IBMSolver *s) {
     for (int f = 0; f < 6; f++)
         if (s->bc[f].type == BC_PRESSURE || s->bc[f].type == BC_VELOCITY_PERIODIC) d->bc.p_singular = 0;
     d->les = s->turb_model.type == TURBMODEL_SMAGORINSKY;
-    if (!upload_axes(s) || !alloc_fields(s)) return;
+    if (!upload_axes(s) || !alloc_fields(s) || !alloc_samples(s)) return;
     if (!build_levelset(s)) return;
     if (!build_ghosts(s)) return;
     build_coeffsum(s);
@@ -1621,7 +1764,8 @@ namespace {
 void iterate_prologue(IBMSolver *s) {
     ibm3d_device *d = s->dev;
     d->status = IBM3D_OK;
-    fill_outer(s);
+    prepare_samples(s, d->s, s->time, s->time + s->dt);
+    fill_outer(s, 0);
     launch_interp_stag(d->s, d->g, d->ax[0], d->ax[1], d->ax[2], d->u, d->U);
     ghost_update(s, true);
     const double f[3] = {s->ext_force.const_f1, s->ext_force.const_f2, s->ext_force.const_f3};
@@ -1638,10 +1782,11 @@ void IBMSolver_iterate(IBMSolver *s, int num_time_steps, bool verbose) {
     struct timespec t0, t1;
     clock_gettime(CLOCK_REALTIME, &t0);
     for (int i = 1; i <= num_time_steps; i++) {
+        prepare_samples(s, d->s, s->time, start_time + s->dt * i);
         if (!(d->use_graphs && !d->prof.on && graph_step(s))) {
             one_step(s);
             int t = d->prof.begin("fill_outer");
-            fill_outer(s);
+            fill_outer(s, 1);
             d->prof.end(t);
             t = d->prof.begin("ghost_update");
             ghost_update(s, false);
@@ -1712,6 +1857,23 @@ void IBMSolver_set_ext_force_const(IBMSolver *s, double f1, double f2, double f3
     s->ext_force.const_f1 = f1;
     s->ext_force.const_f2 = f2;
     s->ext_force.const_f3 = f3;
+}
+
+void IBMSolver_set_bc_func(IBMSolver *s, IBMSolverDirection dir, IBMSolverBCType type, IBMSolverBCValFunc f1,
+                           IBMSolverBCValFunc f2, IBMSolverBCValFunc f3, IBMSolverBCValFunc fp) {
+    if (type == BC_VELOCITY_COMPONENT)
+        set_bc_impl(s, dir, type, VAL_FUNC, kNaN, kNaN, kNaN, kNaN, f1, f2, f3, nullptr);
+    else if (type == BC_PRESSURE || type == BC_VELOCITY_PERIODIC)
+        set_bc_impl(s, dir, type, VAL_FUNC, kNaN, kNaN, kNaN, kNaN, nullptr, nullptr, nullptr, fp);
+    else
+        set_status(s, IBM3D_EARG, "IBMSolver_set_bc_func: type %d takes no boundary values", (int)type);
+}
+
+void IBMSolver_set_ext_force_func(IBMSolver *s, IBMSolverForceFunc f1, IBMSolverForceFunc f2, IBMSolverForceFunc f3) {
+    s->ext_force.val_type = VAL_FUNC;
+    s->ext_force.func_f1 = f1;
+    s->ext_force.func_f2 = f2;
+    s->ext_force.func_f3 = f3;
 }
 
 void IBMSolver_set_smagorinsky(IBMSolver *s, double Cs) {
@@ -2137,6 +2299,10 @@ double IBMBatch_iterate(IBMBatch *b, int nsteps) {
     }
     cudaEventRecord(b->t0, b->s);
     for (int i = 1; i <= nsteps; i++) {
+        for (size_t q = 0; q < b->members.size(); q++) {
+            IBMSolver *m = b->members[q];
+            prepare_samples(m, b->s, m->time, b->run_start[q] + m->dt * (b->run_steps[q] + 1));
+        }
         const std::vector<const void *> key = batch_key(b);
         IBMBatch::Rec *R = nullptr;
         for (auto &r : b->cache)

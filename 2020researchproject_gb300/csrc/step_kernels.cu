@@ -36,10 +36,11 @@ k_conv_rhs(const Grid g, const Axis ax, const Axis ay, const Axis az, const BCSe
         int layer;
         const int f = owner_face(g, i, j, k, layer);
         if (f >= 0) {
-            const bool vel = bc.f[f].type == BCT_VELOCITY;
-            a.b[0][P] = vel ? bc.f[f].val[0] : 0.0;
-            a.b[1][P] = vel ? bc.f[f].val[1] : 0.0;
-            a.b[2][P] = vel ? bc.f[f].val[2] : 0.0;
+            const BCFace &F = bc.f[f];
+            const bool vel = F.type == BCT_VELOCITY;
+            const double *sv = F.scur ? F.scur + face_line(g, f, i, j, k) : nullptr;
+#pragma unroll
+            for (int l = 0; l < 3; l++) a.b[l][P] = vel ? (sv ? sv[l * F.nt] : F.val[l]) : 0.0;
             continue;
         }
         if (flag[P] != FLUID) {
@@ -85,8 +86,9 @@ k_conv_rhs(const Grid g, const Axis ax, const Axis ay, const Axis az, const BCSe
                          (a.tau[t2][P + sy] - a.tau[t2][P - sy]) * gy +
                          (a.tau[t3][P + 1] - a.tau[t3][P - 1]) * gz;
             }
+            const double fl = a.force ? a.force[l * n + P] : ff[l];
             a.b[l][P] = -dt / 2 * (3 * Nl - a.Np[l][P]) - dt * dp + cdiag * uc + kW * uW + kE * uE + kS * uS +
-                        kN * uN + kD * uD + kU * uU + dt * ff[l] - dt * divtau;
+                        kN * uN + kD * uD + kU * uU + dt * fl - dt * divtau;
         }
     }
 }
@@ -175,8 +177,17 @@ k_ustar_prhs(const Grid g, const Axis ax, const Axis ay, const Axis az, const BC
         int i, j, k;
         cijk_g(g, P, i, j, k);
         int layer;
-        if (owner_face(g, i, j, k, layer) >= 0) {
-            a.b[P] = 0.0;
+        const int face = owner_face(g, i, j, k, layer);
+        if (face >= 0) {
+            // Pressure-Dirichlet rows: p_bc(t + dt) - p_bc(t), zero for
+            // constant values (src/ibm3d_fracstep.c:556-645).
+            const BCFace &F = bc.f[face];
+            double v = 0.0;
+            if (F.scur && (F.type == BCT_PRESSURE || F.type == BCT_VELPERIODIC)) {
+                const int t = 3 * F.nt + face_line(g, face, i, j, k);
+                v = F.snxt[t] - F.scur[t];
+            }
+            a.b[P] = v;
             continue;
         }
         const long long sx = g.sx, sy = g.sy;
@@ -282,16 +293,17 @@ void launch_update_next(cudaStream_t s, const Grid &g, const Axis &ax, const Axi
 // outer-layer fills.  Three launches keep the reference's face order
 // (x faces, then y faces reading the x-filled edges, then z faces).
 // ------------------------------------------------------------------------
-__device__ inline void fill_line(const BCFace &F, int f, double *u0, double *u1, double *u2, double *p,
-                                 long long c0, long long c1, long long o1, long long o2, long long img1,
+__device__ inline void fill_line(const BCFace &F, int f, const double *smp, double *u0, double *u1, double *u2,
+                                 double *p, long long c0, long long c1, long long o1, long long o2, long long img1,
                                  long long img2) {
     double *u[3] = {u0, u1, u2};
     const int axis = face_axis(f);
     switch (F.type) {
     case BCT_VELOCITY:
         for (int l = 0; l < 3; l++) {
-            u[l][o1] = F.fv_a[0] * F.val[l] - F.fv_b[0] * u[l][c0];
-            u[l][o2] = F.fv_a[1] * F.val[l] - F.fv_b[1] * u[l][c1];
+            const double v = smp ? smp[l * F.nt] : F.val[l];
+            u[l][o1] = F.fv_a[0] * v - F.fv_b[0] * u[l][c0];
+            u[l][o2] = F.fv_a[1] * v - F.fv_b[1] * u[l][c1];
         }
         break;
     case BCT_PRESSURE:
@@ -327,10 +339,12 @@ __device__ inline void fill_line(const BCFace &F, int f, double *u0, double *u1,
         p[o2] = p[c1];
         break;
     case BCT_PRESSURE:
-    case BCT_VELPERIODIC:
-        p[o1] = F.fp_a[0] * F.pval - F.fp_b[0] * p[c0];
-        p[o2] = F.fp_a[1] * F.pval - F.fp_b[1] * p[c1];
+    case BCT_VELPERIODIC: {
+        const double v = smp ? smp[3 * F.nt] : F.pval;
+        p[o1] = F.fp_a[0] * v - F.fp_b[0] * p[c0];
+        p[o2] = F.fp_a[1] * v - F.fp_b[1] * p[c1];
         break;
+    }
     case BCT_PERIODIC:
         p[o1] = p[img1];
         p[o2] = p[img2];
@@ -339,8 +353,8 @@ __device__ inline void fill_line(const BCFace &F, int f, double *u0, double *u1,
     }
 }
 
-__global__ void k_fill_outer(const Grid g, const BCSet bc, const int axis, double *u0, double *u1, double *u2,
-                             double *p) {
+__global__ void k_fill_outer(const Grid g, const BCSet bc, const int axis, const int when, double *u0, double *u1,
+                             double *u2, double *p) {
     // axis 0: lines over (j,k) interior; axis 1: (i in [-2,nx+2), k interior);
     // axis 2: (i in [-2,nx+2), j in [-2,ny+2)).
     long long n;
@@ -367,21 +381,27 @@ __global__ void k_fill_outer(const Grid g, const BCSet bc, const int axis, doubl
         base_hi = base_lo + (long long)(N - 1) * s;
         const int flo = axis == 0 ? F_W : axis == 1 ? F_S : F_D;
         const int fhi = axis == 0 ? F_E : axis == 1 ? F_N : F_U;
+        // Outer line of this (A, B): same position on both faces of the axis.
+        const int line = axis == 0 ? (A + 2) * (g.nz + 4) + (B + 2) : axis == 1 ? A * (g.nz + 4) + (B + 2)
+                                                                                : A * (g.ny + 4) + B;
+        const BCFace &Flo = bc.f[flo], &Fhi = bc.f[fhi];
+        const double *slo = Flo.scur ? (when ? Flo.snxt : Flo.scur) + line : nullptr;
+        const double *shi = Fhi.scur ? (when ? Fhi.snxt : Fhi.scur) + line : nullptr;
         // Low face: c0 = 0, c1 = 1, o1 = -1, o2 = -2; periodic images N-1, N-2.
-        fill_line(bc.f[flo], flo, u0, u1, u2, p, base_lo, base_lo + s, base_lo - s, base_lo - 2 * s,
+        fill_line(Flo, flo, slo, u0, u1, u2, p, base_lo, base_lo + s, base_lo - s, base_lo - 2 * s,
                   base_lo + (long long)(N - 1) * s, base_lo + (long long)(N - 2) * s);
         // High face: c0 = N-1, c1 = N-2, o1 = N, o2 = N+1; periodic images 0, 1.
-        fill_line(bc.f[fhi], fhi, u0, u1, u2, p, base_hi, base_hi - s, base_hi + s, base_hi + 2 * s, base_lo,
+        fill_line(Fhi, fhi, shi, u0, u1, u2, p, base_hi, base_hi - s, base_hi + s, base_hi + 2 * s, base_lo,
                   base_lo + s);
     }
 }
 
-void launch_fill_outer(cudaStream_t s, const Grid &g, const BCSet &bc, double *const u[3], double *p) {
+void launch_fill_outer(cudaStream_t s, const Grid &g, const BCSet &bc, double *const u[3], double *p, int when) {
     const long long nx = (long long)g.ny * g.nz, ny = (long long)(g.nx + 4) * g.nz,
                     nz = (long long)(g.nx + 4) * (g.ny + 4);
-    k_fill_outer<<<grid_for(nx, 128), 128, 0, s>>>(g, bc, 0, u[0], u[1], u[2], p);
-    k_fill_outer<<<grid_for(ny, 128), 128, 0, s>>>(g, bc, 1, u[0], u[1], u[2], p);
-    k_fill_outer<<<grid_for(nz, 128), 128, 0, s>>>(g, bc, 2, u[0], u[1], u[2], p);
+    k_fill_outer<<<grid_for(nx, 128), 128, 0, s>>>(g, bc, 0, when, u[0], u[1], u[2], p);
+    k_fill_outer<<<grid_for(ny, 128), 128, 0, s>>>(g, bc, 1, when, u[0], u[1], u[2], p);
+    k_fill_outer<<<grid_for(nz, 128), 128, 0, s>>>(g, bc, 2, when, u[0], u[1], u[2], p);
     note_launches(3);
 }
 

@@ -38,6 +38,18 @@ const char *IBMSolver_status_string(int status);
 void IBMSolver_set_bc_const(IBMSolver *, IBMSolverDirection, IBMSolverBCType,
                             double u1, double u2, double u3, double p);
 void IBMSolver_set_ext_force_const(IBMSolver *, double f1, double f2, double f3);
+/* Non-variadic forms of the VAL_FUNC calls (src/ibm3d_setup.c:306-327,
+   365-434): set_bc(dir, BC_VELOCITY_COMPONENT, VAL_FUNC, f1, f2, f3) and
+   set_bc(dir, BC_PRESSURE or BC_VELOCITY_PERIODIC, VAL_FUNC, fp) (the
+   unused functions may be NULL); set_ext_force(VAL_FUNC, f1, f2, f3).
+   The callbacks run on the host: once per step for every outer line of a
+   VAL_FUNC face (start and end time of the step) and, for a VAL_FUNC
+   force, for every interior cell centre at the step's start time. */
+void IBMSolver_set_bc_func(IBMSolver *, IBMSolverDirection, IBMSolverBCType,
+                           IBMSolverBCValFunc f1, IBMSolverBCValFunc f2, IBMSolverBCValFunc f3,
+                           IBMSolverBCValFunc fp);
+void IBMSolver_set_ext_force_func(IBMSolver *, IBMSolverForceFunc f1, IBMSolverForceFunc f2,
+                                  IBMSolverForceFunc f3);
 void IBMSolver_set_smagorinsky(IBMSolver *, double Cs);
 
 /* Pressure-solve stopping rule.  div_tol > 0: stop once the projected face

@@ -43,6 +43,9 @@ struct Oracle {
     double *kxW, *kxE, *kyS, *kyN, *kzD, *kzU;
     int bct[6];
     double bu[6][3], bp[6];
+    double (*bcfn[6][4])(double, double, double, double);
+    double (*ffn[3])(double, double, double, double);
+    double xmin, xmax, ymin, ymax, zmin, zmax;
     double f[3], cs, tol, divtol;
     int singular, threads;
     int *flag;
@@ -605,6 +608,19 @@ static int owner(const Oracle *o, int i, int j, int k, int *L) {
 
 static int wrap(int i, int n) { return i < 0 ? i + n : i >= n ? i - n : i; }
 
+/* Boundary value q (0-2: u1-u3, 3: p) of face f on the outer line through
+   padded cell (i, j, k) at time t: the constant, or the VAL_FUNC callback
+   at the face centre of that line, as bc_val_u / bc_val_p evaluate it
+   (src/ibm3d_fracstep.c:2001-2035). */
+static double bcval(const Oracle *o, int f, int q, double t, int i, int j, int k) {
+    if (!o->bcfn[f][q]) return q < 3 ? o->bu[f][q] : o->bp[f];
+    double x = C1(o->xc, i), y = C1(o->yc, j), z = C1(o->zc, k);
+    if (f == FW) x = o->xmin; else if (f == FE) x = o->xmax;
+    else if (f == FS) y = o->ymin; else if (f == FN) y = o->ymax;
+    else if (f == FD) z = o->zmin; else z = o->zmax;
+    return o->bcfn[f][q](t, x, y, z);
+}
+
 /* Row of A_u{type} (type 1..3) or A_p (type 4) applied to x at padded
    (i, j, k); restates create_matrix (src/ibm3d_setup.c:1566-2908). */
 static double row(const Oracle *o, int type, const double *x, int i, int j, int k) {
@@ -1117,9 +1133,12 @@ static void update_outer(Oracle *o) {
                         ea1 = C1(c, N - 1) - C1(c, N - 2); eb1 = C1(c, N) - C1(c, N - 1);
                         ea2 = C1(c, N) - C1(c, N - 1); eb2 = C1(c, N + 1) - C1(c, N);
                     }
+                    /* padded (i, j, k) of the line's first outer cell, for the face centre */
+                    const int li = axis == 0 ? 0 : A - 2, lj = axis == 0 ? A : axis == 1 ? 0 : B - 2;
+                    const int lk = axis == 2 ? 0 : B;
                     for (int l = 0; l < 3; l++) {
                         double *w = u[l];
-                        double bc = o->bu[f][l];
+                        double bc = t == BC_VEL ? bcval(o, f, l, o->time, li, lj, lk) : 0.0;
                         switch (t) {
                         case BC_VEL:
                             if (side == 0) {
@@ -1162,15 +1181,17 @@ static void update_outer(Oracle *o) {
                         p[o2] = p[c1];
                         break;
                     case BC_PRES:
-                    case BC_VELPER:
+                    case BC_VELPER: {
+                        const double pv = bcval(o, f, 3, o->time, li, lj, lk);
                         if (side == 0) {
-                            p[o1] = (pa1 + pb1) / pb1 * o->bp[f] - pa1 / pb1 * p[c0];
-                            p[o2] = (pa2 + pb2) / pb2 * o->bp[f] - pa2 / pb2 * p[c1];
+                            p[o1] = (pa1 + pb1) / pb1 * pv - pa1 / pb1 * p[c0];
+                            p[o2] = (pa2 + pb2) / pb2 * pv - pa2 / pb2 * p[c1];
                         } else {
-                            p[o1] = (pa1 + pb1) / pa1 * o->bp[f] - pb1 / pa1 * p[c0];
-                            p[o2] = (pa2 + pb2) / pa2 * o->bp[f] - pb2 / pa2 * p[c1];
+                            p[o1] = (pa1 + pb1) / pa1 * pv - pb1 / pa1 * p[c0];
+                            p[o2] = (pa2 + pb2) / pa2 * pv - pb2 / pa2 * p[c1];
                         }
                         break;
+                    }
                     case BC_PER:
                         p[o1] = p[i1];
                         p[o2] = p[i2];
@@ -1327,14 +1348,15 @@ static void calc_u_star(Oracle *o) {
                                      C1(o->kxW, i) * C3(u, i - 1, j, k) + C1(o->kxE, i) * C3(u, i + 1, j, k) +
                                      C1(o->kyS, j) * C3(u, i, j - 1, k) + C1(o->kyN, j) * C3(u, i, j + 1, k) +
                                      C1(o->kzD, k) * C3(u, i, j, k - 1) + C1(o->kzU, k) * C3(u, i, j, k + 1) +
-                                     dt * o->f[l] - dt * dtau;
+                                     dt * (o->ffn[l] ? o->ffn[l](o->time, C1(o->xc, i), C1(o->yc, j), C1(o->zc, k)) : o->f[l]) -
+                                     dt * dtau;
                 }
         /* Velocity-BC rows of the outer layers. */
         for (int i = -2; i < o->nx + 2; i++)
             for (int j = -2; j < o->ny + 2; j++)
                 for (int k = -2; k < o->nz + 2; k++) {
                     int L, f = owner(o, i, j, k, &L);
-                    if (f >= 0 && o->bct[f] == BC_VEL) C3(b, i, j, k) = o->bu[f][l];
+                    if (f >= 0 && o->bct[f] == BC_VEL) C3(b, i, j, k) = bcval(o, f, l, o->time, i, j, k);
                 }
         bicgstab(o, l + 1, b, o->us[l], 200, 0, &o->iters[l], &o->res[l]);
     }
@@ -1386,8 +1408,9 @@ static void calc_U_star(Oracle *o) {
             }
 }
 
-/* calc_p_prime (src/ibm3d_fracstep.c:489-707) with constant boundary
-   values, whose pressure increments p_bc(t+dt) - p_bc(t) are zero. */
+/* calc_p_prime (src/ibm3d_fracstep.c:489-707).  Outer rows of pressure
+   and velocity-periodic faces hold p_bc(t+dt) - p_bc(t) (:556-645), zero
+   for constant values. */
 static void calc_p_prime(Oracle *o) {
     double *b = o->b;
     memset(b, 0, sizeof(double) * o->nc);
@@ -1402,6 +1425,13 @@ static void calc_p_prime(Oracle *o) {
                             (YS(o->Us[1], i, j + 1, k) - YS(o->Us[1], i, j, k)) / C1(o->dy, j) +
                             (ZS(o->Us[2], i, j, k + 1) - ZS(o->Us[2], i, j, k)) / C1(o->dz, k));
                 C3(b, i, j, k) = v / C3(o->coeffsum, i, j, k);
+            }
+    for (int i = -2; i < o->nx + 2; i++)
+        for (int j = -2; j < o->ny + 2; j++)
+            for (int k = -2; k < o->nz + 2; k++) {
+                int L, f = owner(o, i, j, k, &L);
+                if (f >= 0 && o->bcfn[f][3] && (o->bct[f] == BC_PRES || o->bct[f] == BC_VELPER))
+                    C3(b, i, j, k) = bcval(o, f, 3, o->time + o->dt, i, j, k) - bcval(o, f, 3, o->time, i, j, k);
             }
     bicgstab(o, 4, b, o->pp, 1000, 1, &o->iters[3], &o->res[3]);
 }
@@ -1503,6 +1533,10 @@ Oracle *oracle_create(const OracleConfig *c) {
     o->tol = c->tol;
     o->divtol = c->div_tol;
     memcpy(o->f, c->force, sizeof o->f);
+    for (int l = 0; l < 3; l++) o->ffn[l] = c->force_fn[l];
+    o->xmin = c->xf[0]; o->xmax = c->xf[c->nx];
+    o->ymin = c->yf[0]; o->ymax = c->yf[c->ny];
+    o->zmin = c->zf[0]; o->zmax = c->zf[c->nz];
     o->singular = 1;
     for (int f = 0; f < 6; f++) {
         int t = c->bc_type[f];
@@ -1512,6 +1546,7 @@ Oracle *oracle_create(const OracleConfig *c) {
         o->bct[f] = t;
         for (int l = 0; l < 3; l++) o->bu[f][l] = c->bc_type[f] == BC_WALL ? 0 : c->bc_u[f][l];
         o->bp[f] = c->bc_p[f];
+        for (int q = 0; q < 4; q++) o->bcfn[f][q] = c->bc_fn[f][q];
         if (t == BC_PRES || t == BC_VELPER) o->singular = 0;
     }
     o->dx = dal(o->nx + 4); o->dy = dal(o->ny + 4); o->dz = dal(o->nz + 4);

@@ -31,6 +31,10 @@ typedef struct {
     const char *stl_path;           /* NULL: no obstacle */
     const double *lvset_in;         /* optional precomputed level set (padded); skips the CPT */
     int threads;                    /* OpenMP threads, 0 = runtime default */
+    /* VAL_FUNC values (src/ibm3d.h:52-80): per face u1, u2, u3, p; NULL
+       keeps the constant value.  Callbacks (t, x, y, z). */
+    double (*bc_fn[6][4])(double, double, double, double);
+    double (*force_fn[3])(double, double, double, double);
 } OracleConfig;
 
 typedef struct Oracle Oracle;

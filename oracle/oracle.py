@@ -25,7 +25,11 @@ class _Cfg(ctypes.Structure):
                 ("bc_type", ctypes.c_int * 6), ("bc_u", (ctypes.c_double * 3) * 6), ("bc_p", ctypes.c_double * 6),
                 ("force", ctypes.c_double * 3), ("smagorinsky_cs", ctypes.c_double),
                 ("tol", ctypes.c_double), ("div_tol", ctypes.c_double),
-                ("stl_path", ctypes.c_char_p), ("lvset_in", ctypes.c_void_p), ("threads", ctypes.c_int)]
+                ("stl_path", ctypes.c_char_p), ("lvset_in", ctypes.c_void_p), ("threads", ctypes.c_int),
+                ("bc_fn", (ctypes.c_void_p * 4) * 6), ("force_fn", ctypes.c_void_p * 3)]
+
+# double f(double t, double x, double y, double z)
+_FN = ctypes.CFUNCTYPE(ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double)
 
 
 _lib = None
@@ -60,7 +64,10 @@ def _p(a):
 
 class Oracle:
     """case: dict with grid faces xf/yf/zf, re, dt, bc (list like "W vel 1 0 0"),
-    optional force, smag, stl (path), tol, div_tol, lvset (padded array), threads."""
+    optional force, smag, stl (path), tol, div_tol, lvset (padded array), threads,
+    bc_funcs (list of (face, type, callables): VAL_FUNC faces, three callables
+    f(t, x, y, z) for "vel", one for "press" / "velper") and force_funcs
+    (three callables)."""
 
     def __init__(self, case):
         lib = load()
@@ -82,8 +89,20 @@ class Oracle:
                     c.bc_u[f][l] = vals[l]
             elif t[1] in ("press", "velper"):
                 c.bc_p[f] = vals[0]
+        for face, kind, fns in case.get("bc_funcs", []):
+            f = FACES[face]
+            c.bc_type[f] = BC_TYPES[kind]
+            slots = range(3) if kind == "vel" else (3,)
+            for q, fn in zip(slots, fns):
+                cb = _FN(fn)
+                self._keep.append(cb)
+                c.bc_fn[f][q] = ctypes.cast(cb, ctypes.c_void_p)
         for l, v in enumerate(case.get("force", (0, 0, 0))):
             c.force[l] = float(v)
+        for l, fn in enumerate(case.get("force_funcs", ())):
+            cb = _FN(fn)
+            self._keep.append(cb)
+            c.force_fn[l] = ctypes.cast(cb, ctypes.c_void_p)
         c.smagorinsky_cs = float(case.get("smag", -1.0))
         c.tol = float(case.get("tol", 1e-12))
         c.div_tol = float(case.get("div_tol", 0.0))

@@ -18,6 +18,10 @@
  *   smag CS
  *   stl PATH                           obstacle (omit for none)
  *   init const u v w p | init field    field: smooth analytic field below
+ *   bcfunc FACE TYPE KIND              VAL_FUNC boundary values: TYPE vel
+ *                                      (KIND pulse) or press / velper
+ *                                      (KIND ramp); functions below
+ *   forcefunc KIND                     VAL_FUNC body force (KIND swirl)
  *
  * Dumped (little-endian raw, padded (N+4)^3 cell layout, k fastest):
  *   flag.i32 lvset.f64 coeffsum.f64 ghost.txt  after IBMSolver_assemble
@@ -66,6 +70,17 @@ static double fx_v(double x, double y, double z) { return 0.2 * cos(1.7 * x) * s
 static double fx_w(double x, double y, double z) { return 0.25 * sin(1.1 * y + 0.3) * cos(0.9 * x) + 0.05 * x * z; }
 static double fx_p(double x, double y, double z) { return 0.1 * cos(x + 0.5 * y) + 0.05 * z * z; }
 
+/* Time-dependent boundary values and force for the VAL_FUNC cases.  Only
+   +, -, * so that the same expressions evaluated elsewhere (the GPU tests'
+   callbacks) give the same doubles. */
+static double pulse_u(double t, double x, double y, double z) { (void)x; return (1.0 + 3.0 * t) * (1.0 - 0.2 * y * y) * (1.0 - 0.25 * z * z); }
+static double pulse_v(double t, double x, double y, double z) { (void)x; (void)y; return 0.2 * t * z; }
+static double pulse_w(double t, double x, double y, double z) { (void)z; return -0.1 * t * y + 0.05 * x; }
+static double ramp_p(double t, double x, double y, double z) { (void)x; return 0.5 * t + 0.1 * y - 0.05 * z * t; }
+static double swirl_f1(double t, double x, double y, double z) { (void)x; (void)z; return 0.02 * (1.0 + t) * y; }
+static double swirl_f2(double t, double x, double y, double z) { (void)y; return -0.03 * x * t + 0.01 * z; }
+static double swirl_f3(double t, double x, double y, double z) { (void)z; return 0.01 * (x - y) * t; }
+
 int main(int argc, char **argv) {
     if (argc != 3) {
         fprintf(stderr, "usage: %s case-file out-dir\n", argv[0]);
@@ -84,8 +99,9 @@ int main(int argc, char **argv) {
     int init_field = 0;
     double iu = 0, iv = 0, iw = 0, ip = 0;
 
-    struct { int dir, type; double a, b, c; } bcs[16];
+    struct { int dir, type; double a, b, c; int func; } bcs[16];
     int nbc = 0;
+    int force_func = 0;
 
     char key[64];
     while (fscanf(cf, "%63s", key) == 1) {
@@ -112,11 +128,27 @@ int main(int argc, char **argv) {
             if (fscanf(cf, "%31s", kind) != 1) return 2;
             if (!strcmp(kind, "field")) init_field = 1;
             else if (fscanf(cf, "%lf %lf %lf %lf", &iu, &iv, &iw, &ip) != 4) return 2;
+        } else if (!strcmp(key, "bcfunc")) {
+            char face[8], type[16], kind[16];
+            if (fscanf(cf, "%7s %15s %15s", face, type, kind) != 3) return 2;
+            bcs[nbc].dir = face_dir(face);
+            bcs[nbc].a = bcs[nbc].b = bcs[nbc].c = 0;
+            bcs[nbc].func = 1;
+            if (!strcmp(type, "vel") && !strcmp(kind, "pulse")) bcs[nbc].type = BC_VELOCITY_COMPONENT;
+            else if (!strcmp(type, "press") && !strcmp(kind, "ramp")) bcs[nbc].type = BC_PRESSURE;
+            else if (!strcmp(type, "velper") && !strcmp(kind, "ramp")) bcs[nbc].type = BC_VELOCITY_PERIODIC;
+            else { fprintf(stderr, "bad bcfunc %s %s\n", type, kind); return 2; }
+            nbc++;
+        } else if (!strcmp(key, "forcefunc")) {
+            char kind[16];
+            if (fscanf(cf, "%15s", kind) != 1 || strcmp(kind, "swirl")) return 2;
+            force_func = 1;
         } else if (!strcmp(key, "bc")) {
             char face[8], type[16];
             if (fscanf(cf, "%7s %15s", face, type) != 2) return 2;
             bcs[nbc].dir = face_dir(face);
             bcs[nbc].a = bcs[nbc].b = bcs[nbc].c = 0;
+            bcs[nbc].func = 0;
             if (!strcmp(type, "vel")) {
                 bcs[nbc].type = BC_VELOCITY_COMPONENT;
                 if (fscanf(cf, "%lf %lf %lf", &bcs[nbc].a, &bcs[nbc].b, &bcs[nbc].c) != 3) return 2;
@@ -145,9 +177,17 @@ int main(int argc, char **argv) {
     IBMSolver *solver = IBMSolver_new(1, 0, 1, 1, 1);
     IBMSolver_set_grid(solver, NX, NY, NZ, xf, yf, zf);
     IBMSolver_set_params(solver, Re, dt);
-    IBMSolver_set_ext_force(solver, VAL_CONST, f1, f2, f3);
+    if (force_func) IBMSolver_set_ext_force(solver, VAL_FUNC, swirl_f1, swirl_f2, swirl_f3);
+    else IBMSolver_set_ext_force(solver, VAL_CONST, f1, f2, f3);
     if (cs >= 0) IBMSolver_set_turb_model(solver, TURBMODEL_SMAGORINSKY, cs);
     for (int b = 0; b < nbc; b++) {
+        if (bcs[b].func) {
+            if (bcs[b].type == BC_VELOCITY_COMPONENT)
+                IBMSolver_set_bc(solver, bcs[b].dir, BC_VELOCITY_COMPONENT, VAL_FUNC, pulse_u, pulse_v, pulse_w);
+            else
+                IBMSolver_set_bc(solver, bcs[b].dir, bcs[b].type, VAL_FUNC, ramp_p);
+            continue;
+        }
         switch (bcs[b].type) {
         case BC_VELOCITY_COMPONENT:
             IBMSolver_set_bc(solver, bcs[b].dir, BC_VELOCITY_COMPONENT, VAL_CONST, bcs[b].a, bcs[b].b, bcs[b].c);

@@ -36,7 +36,8 @@ def _stl(name, verts, faces):
 def cases():
     """Small cases that together put every boundary-condition type on every
     axis, a sphere and a box body, LES on periodic and wall boundaries,
-    stretched grids and a split iterate() call."""
+    stretched grids, split iterate() calls and time-dependent (VAL_FUNC)
+    boundary values and body force."""
     sphere2 = _stl("sphere_sub2.stl", *geometry.icosphere(2, 0.5))
     sphere1 = _stl("sphere_sub1_off.stl", *geometry.icosphere(1, 0.45, (0.3, -0.2, 0.1)))
     box = _stl("box.stl", *geometry.box_union([((-0.45, -0.35, -0.3), (0.35, 0.3, 0.25))]))
@@ -83,6 +84,28 @@ def cases():
             re=60, dt=0.01, calls=[1, 1],
             bc=["W slip", "E slip", "S vel 0.1 0.4 0", "N press 0", "D velper 0.05", "U velper 0.05"],
             stl=sphere1, init="field"),
+        # VAL_FUNC: time-dependent inflow on W, time-dependent outlet
+        # pressure on E, slip sides, time-dependent body force, sphere
+        # (src/ibm3d_fracstep.c:1978-2035); split call so time carries on.
+        "func_sphere": dict(
+            grid=(16, 12, 12),
+            xf=gf.body_clustered_faces(-1.6, 2.4, 16, 0.0, 1.2, 1.5),
+            yf=gf.body_clustered_faces(-1.4, 1.4, 12, 0.0, 1.2, 1.5),
+            zf=gf.body_clustered_faces(-1.4, 1.4, 12, 0.0, 1.2, 1.5),
+            re=50, dt=0.02, calls=[2, 2],
+            bc=["S slip", "N slip", "D slip", "U slip"],
+            bcfunc=["W vel pulse", "E press ramp"], forcefunc="swirl",
+            stl=sphere2, init="const 1 0 0 0"),
+        # VAL_FUNC on velocity-periodic x (pressure jump in time), velocity
+        # D and pressure U, walls S/N, box body, constant force.
+        "func_box": dict(
+            grid=(12, 10, 12),
+            xf=gf.uniform_faces(-1.2, 1.6, 12), yf=gf.body_clustered_faces(-1.0, 1.0, 10, 0, 0.7, 1.0),
+            zf=gf.uniform_faces(-0.9, 1.1, 12),
+            re=80, dt=0.01, calls=[3], force=(0.01, 0, 0),
+            bc=["S wall", "N wall"],
+            bcfunc=["W velper ramp", "E velper ramp", "D vel pulse", "U press ramp"],
+            stl=box, init="field"),
         # Velocity-periodic x, all-periodic y, velocity D, pressure U, LES.
         "mixed_les": dict(
             grid=(10, 8, 12),
@@ -104,6 +127,10 @@ def write_case_file(path, c):
         fh.write("calls " + " ".join(str(n) for n in c["calls"]) + "\n")
         for b in c["bc"]:
             fh.write("bc " + b + "\n")
+        for b in c.get("bcfunc", []):
+            fh.write("bcfunc " + b + "\n")
+        if "forcefunc" in c:
+            fh.write(f"forcefunc {c['forcefunc']}\n")
         if "force" in c:
             fh.write("force %r %r %r\n" % tuple(float(v) for v in c["force"]))
         if "smag" in c:

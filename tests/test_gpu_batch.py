@@ -27,7 +27,7 @@ def _same(a, b):
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_batch_members_equal_solo_runs(precision):
     ibm = package()
-    names = ["cavity", "sphere", "channel_les", "mixed_box"]
+    names = ["cavity", "sphere", "channel_les", "mixed_box", "func_sphere"]
     cases = [load_golden(n) for n in names]
     mode = ibm.MIXED if precision == "mixed" else ibm.FP64
 

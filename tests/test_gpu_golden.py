@@ -18,6 +18,7 @@ import os
 import numpy as np
 import pytest
 
+import valfuncs
 from conftest import GOLDEN, golden_cases, load_golden, rel_l2
 
 pytestmark = pytest.mark.gpu
@@ -42,6 +43,11 @@ def build_case(ibm, case, tol=1e-12):
     for b in m["bc"]:
         t = b.split()
         s.set_bc(getattr(ibm, _DIR[t[0]]), getattr(ibm, _BC[t[1]]), *[float(v) for v in t[2:]])
+    for b in m.get("bcfunc", []):                 # VAL_FUNC faces
+        face, kind, fn = b.split()
+        s.set_bc(getattr(ibm, _DIR[face]), getattr(ibm, _BC[kind]), *valfuncs.BC_FUNCS[fn])
+    if "forcefunc" in m:
+        s.set_ext_force(*valfuncs.FORCE_FUNCS[m["forcefunc"]])
     if "stl" in m:
         s.set_obstacle(ibm.Polyhedron(os.path.join(GOLDEN, m["stl"])))
     s.set_linear_solver(ibm.SOLVER_BiCGSTAB, ibm.PRECOND_AMG, tol)

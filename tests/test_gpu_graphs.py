@@ -18,7 +18,7 @@ FIELDS = ["u1", "u2", "u3", "p", "U1", "U2", "U3", "pprime", "u1star"]
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-@pytest.mark.parametrize("name", [n for n in golden_cases() if n in ("sphere", "channel_les", "cavity")])
+@pytest.mark.parametrize("name", [n for n in golden_cases() if n in ("sphere", "channel_les", "cavity", "func_sphere")])
 def test_graph_equals_host_loop(ibm, name, precision):
     case = load_golden(name)
     out = []

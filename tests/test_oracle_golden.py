@@ -10,6 +10,7 @@ import sys
 import numpy as np
 import pytest
 
+import valfuncs
 from conftest import GOLDEN, ROOT, golden_cases, load_golden, rel_l2
 
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -24,6 +25,10 @@ def oracle_case(case, **extra):
         c["smag"] = m["smag"]
     if "stl" in m:
         c["stl"] = os.path.join(GOLDEN, m["stl"])
+    if "bcfunc" in m:
+        c["bc_funcs"] = [(b.split()[0], b.split()[1], valfuncs.BC_FUNCS[b.split()[2]]) for b in m["bcfunc"]]
+    if "forcefunc" in m:
+        c["force_funcs"] = valfuncs.FORCE_FUNCS[m["forcefunc"]]
     c.update(extra)
     o = orc.Oracle(c)
     o.init(case["u1_0"], case["u2_0"], case["u3_0"], case["p_0"])
