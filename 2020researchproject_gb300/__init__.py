@@ -27,7 +27,7 @@ LIB_PATH = os.path.join(_PKG, "libibm3d_gb300.so")
 # Enums, values as in the reference's src/ibm3d.h:16-98.
 SOLVER_AMG, SOLVER_PCG, SOLVER_BiCGSTAB, SOLVER_GMRES = range(4)
 PRECOND_NONE, PRECOND_AMG = range(2)
-FP64, MIXED = 0, 1
+FP64, MIXED, MIXED_MG = 0, 1, 2
 DIR_NORTH, DIR_EAST, DIR_SOUTH, DIR_WEST, DIR_DOWN, DIR_UP = (1 << i for i in range(6))
 (BC_VELOCITY_COMPONENT, BC_PRESSURE, BC_STATIONARY_WALL, BC_FREE_SLIP_WALL,
  BC_SYMMETRIC, BC_ALL_PERIODIC, BC_VELOCITY_PERIODIC) = range(7)
@@ -77,6 +77,10 @@ def load_library(path: str = LIB_PATH):
         raise IBM3DError(f"{path} is missing: run __graft_entry__.build() "
                          "(the GB300 path has no CPU fallback)")
     os.environ.setdefault("IBM3D_NO_ABORT", "1")
+    # Batched steps run one graph branch per member: let the GPU work on up
+    # to 32 of them at once (CUDA's default is 8 hardware queues).  Takes
+    # effect if no CUDA context exists in this process yet.
+    os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
     lib = ctypes.CDLL(path)
     vp, d, i, dp, ip = ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p
     sig = {
@@ -87,6 +91,8 @@ def load_library(path: str = LIB_PATH):
         "IBMSolver_set_bc_const": (None, [vp, i, i, d, d, d, d]),
         "IBMSolver_set_ext_force_const": (None, [vp, d, d, d]),
         "IBMSolver_set_bc_func": (None, [vp, i, i, vp, vp, vp, vp]),
+        "IBMSolver_set_refinement": (None, [vp, d, d, i]),
+        "IBMSolver_set_gmres_restart": (None, [vp, i]),
         "IBMSolver_set_ext_force_func": (None, [vp, vp, vp, vp]),
         "IBMSolver_set_smagorinsky": (None, [vp, d]),
         "IBMSolver_set_obstacle": (None, [vp, vp]),
@@ -290,6 +296,14 @@ class IBMSolver:
         ms = self._lib.IBMSolver_time_kernel(self._s, code, int(reps), ctypes.byref(b))
         self._check("IBMSolver_time_kernel")
         return ms, b.value
+
+    def set_gmres_restart(self, restart=10):
+        self._lib.IBMSolver_set_gmres_restart(self._s, restart)
+        self._check("set_gmres_restart")
+
+    def set_refinement(self, inner_tol_mom=1e-5, inner_tol_p=1e-5, max_outer=12):
+        self._lib.IBMSolver_set_refinement(self._s, inner_tol_mom, inner_tol_p, max_outer)
+        self._check("set_refinement")
 
     def set_graphs(self, on=True):
         self._lib.IBMSolver_set_graphs(self._s, 1 if on else 0)

@@ -13,6 +13,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstring>
 #include <vector>
 
 #include "common.cuh"
@@ -737,6 +738,46 @@ static void launch_to32(cudaStream_t st, IRWork &w) {
     note_launches(1);
 }
 
+// ------------------------------------------- widened preconditioner --
+__global__ void __launch_bounds__(KTHREADS)
+k_narrow(const long long n, const double *__restrict__ r, float *r32, const int *gate) {
+    if (gate && *gate != KS_RUN) return;
+    GRID_STRIDE(P, n) r32[P] = (float)r[P];
+}
+
+__global__ void __launch_bounds__(KTHREADS)
+k_widen(const long long n, const float *__restrict__ z32, double *z, const int *gate) {
+    if (gate && *gate != KS_RUN) return;
+    GRID_STRIDE(P, n) z[P] = (double)z32[P];
+}
+
+int WidenedPreconditioner::allocate(long long ncell, Preconditioner<float> *m) {
+    release();
+    n = ncell;
+    m32 = m;
+    nblk = vector_blocks(n);
+    if (cudaMalloc(&r32, sizeof(float) * n) != cudaSuccess || cudaMalloc(&z32, sizeof(float) * n) != cudaSuccess) {
+        release();
+        return -1;
+    }
+    cudaMemset(r32, 0, sizeof(float) * n);
+    cudaMemset(z32, 0, sizeof(float) * n);
+    return 0;
+}
+
+void WidenedPreconditioner::release() {
+    if (r32) cudaFree(r32);
+    if (z32) cudaFree(z32);
+    r32 = z32 = nullptr;
+}
+
+void WidenedPreconditioner::apply(cudaStream_t s, const double *r, double *z, const int *gate) {
+    k_narrow<<<nblk, KTHREADS, 0, s>>>(n, r, r32, gate);
+    m32->apply(s, r32, z32, gate);
+    k_widen<<<nblk, KTHREADS, 0, s>>>(n, z32, z, gate);
+    note_launches(2);
+}
+
 static void launch_update(cudaStream_t st, IRWork &w, double *x) {
     if (w.nc == 3) k_ir_update<3><<<w.nblk, KTHREADS, 0, st>>>(w.n, x, w.e32, w.scal, w.inner.scal);
     else k_ir_update<1><<<w.nblk, KTHREADS, 0, st>>>(w.n, x, w.e32, w.scal, w.inner.scal);
@@ -953,5 +994,337 @@ void apply_operator(cudaStream_t st, const OpT<T> &A, int op, int comp, const T 
 
 template void apply_operator<double>(cudaStream_t, const OpT<double> &, int, int, const double *, double *);
 template void apply_operator<float>(cudaStream_t, const OpT<float> &, int, int, const float *, float *);
+
+// ================================================== flexible GMRES (FP64) ==
+// One restart cycle: V[0] = r / beta; for j = 0, 1, ...: z_j = M V[j]
+// (kept in Z[j]), w = A z_j, two classical Gram-Schmidt passes against
+// V[0..j], h[j+1][j] = ||w||, V[j+1] = w / h[j+1][j]; Givens rotations keep
+// the least-squares residual |g[j+1]| current.  The cycle ends when that
+// estimate passes the stopping test, at j = m, or on breakdown; then
+// x += Z y (H y = g) and the true residual r = b - A x decides whether
+// another cycle runs.  For the divergence rule the in-cycle estimate scales
+// the cycle's starting divergence maximum by |g[j+1]| / beta.
+enum { GM_RUN = 0, GM_DONE = 2, GM_MAXIT = 4 };
+
+int GmresWork::allocate(long long ncell, int restart, int maxblocks) {
+    release();
+    n = ncell;
+    m = std::max(1, std::min(restart, GM_MAX));
+    nblk = vector_blocks(ncell);
+    const size_t nvec = 2 * (size_t)m + 3;
+    if (cudaMalloc(&base, sizeof(double) * n * nvec) != cudaSuccess) return -1;
+    cudaMemset(base, 0, sizeof(double) * n * nvec);
+    V = base;
+    Z = V + (size_t)m * n;
+    w = Z + (size_t)m * n;
+    vin = w + n;
+    zj = vin + n;
+    if (cudaMalloc(&scal, sizeof(GScal)) != cudaSuccess) return -1;
+    cudaMemset(scal, 0, sizeof(GScal));
+    if (cudaMallocHost(&scal_h, sizeof(GScal)) != cudaSuccess) return -1;
+    memset(scal_h, 0, sizeof(GScal));
+    if (cudaMalloc(&partials, sizeof(double) * std::max(nblk, maxblocks) * (GM_MAX + 2)) != cudaSuccess) return -1;
+    if (cudaMalloc(&counter, sizeof(unsigned int)) != cudaSuccess) return -1;
+    cudaMemset(counter, 0, sizeof(unsigned int));
+    return 0;
+}
+
+void GmresWork::release() {
+    if (base) cudaFree(base);
+    if (scal) cudaFree(scal);
+    if (scal_h) cudaFreeHost(scal_h);
+    if (partials) cudaFree(partials);
+    if (counter) cudaFree(counter);
+    base = V = Z = w = vin = zj = nullptr;
+    scal = scal_h = nullptr;
+    partials = nullptr;
+    counter = nullptr;
+}
+
+// Residual w = b - A x (x_zero: w = b, x = 0 assumed), ||w||^2 (and ||b||^2
+// when x_zero), divergence max; the last block applies the stopping test
+// on this true residual and starts the next cycle (V[0] scale, g = beta e1).
+__global__ void __launch_bounds__(SW_THREADS)
+k_gm_residual(const OpT<double> A, const int op, const double *__restrict__ b, const double *__restrict__ x,
+              double *w, const int x_zero, GScal *gs, const double tol, const double divtol, const int m,
+              const int maxit, double *partials, unsigned int *counter, const LoopCtl lc) {
+    __shared__ double smem[32 * 2];
+    double sm = 0.0, mx = 0.0;
+    bool run[1] = {true};
+    auto acc = [&](long long P, double y) {
+        w[P] = y;
+        sm += y * y;
+        if (divtol > 0) mx = fmax(mx, (double)divw(A, P, y));
+    };
+    sweep_rows<double, 1>(
+        A, run, [&](int, long long P, int i, const Column<double> &q) {
+            acc(P, x_zero ? b[P] : b[P] - interior_row(A, op, x, P, i, q));
+        },
+        [&](int, long long P) { acc(P, x_zero ? b[P] : b[P] - op_row(A, op, 0, x, P)); });
+    double v[2] = {sm, mx};
+    reduce_and_finish<2, 1>(v, smem, partials, counter, [&](const double *tot) {
+        GScal &s = *gs;
+        if (x_zero) {
+            s.bnorm2 = tot[0];
+            s.iters = 0;
+            s.cycles = 0;
+            s.m = m;
+            s.tol = tol;
+            s.divtol = divtol;
+            s.maxit = maxit;
+        } else {
+            s.cycles += 1;
+        }
+        s.rnorm2 = tot[0];
+        s.divmax = tot[1];
+        const double beta = sqrt(tot[0]);
+        const bool done = s.bnorm2 == 0.0 || beta == 0.0 || converged(tot[0], s.bnorm2, tot[1], tol, divtol);
+        s.state = done ? GM_DONE : (s.iters >= maxit ? GM_MAXIT : GM_RUN);
+        s.beta0 = beta;
+        s.divmax0 = tot[1];
+        s.res = beta;
+        s.vscale = beta > 0 ? 1.0 / beta : 0.0;
+        s.j = 0;
+        for (int q = 0; q <= GM_MAX; q++) s.g[q] = 0.0;
+        s.g[0] = beta;
+        set_loop(lc, s.state == GM_RUN);
+    });
+}
+
+// Start of a cycle's Arnoldi loop: its condition.
+__global__ void k_gm_cycle(const GScal *gs, const LoopCtl lc) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) set_loop(lc, gs->state == GM_RUN);
+}
+
+// V[j] = vin = w * vscale.
+__global__ void __launch_bounds__(KTHREADS)
+k_gm_next(const long long n, const double *__restrict__ w, double *V, double *vin, const GScal *gs) {
+    const double sc = gs->vscale;
+    double *vj = V + (size_t)gs->j * n;
+    GRID_STRIDE(P, n) {
+        const double y = w[P] * sc;
+        vj[P] = y;
+        vin[P] = y;
+    }
+}
+
+// w = A z, Z[j] = z.
+__global__ void __launch_bounds__(SW_THREADS)
+k_gm_spmv(const OpT<double> A, const int op, const long long n, const double *__restrict__ z, double *w, double *Z,
+          const GScal *gs) {
+    double *zj = Z + (size_t)gs->j * n;
+    bool run[1] = {true};
+    sweep_rows<double, 1>(
+        A, run,
+        [&](int, long long P, int i, const Column<double> &q) {
+            w[P] = interior_row(A, op, z, P, i, q);
+            zj[P] = z[P];
+        },
+        [&](int, long long P) {
+            w[P] = op_row(A, op, 0, z, P);
+            zj[P] = z[P];
+        });
+}
+
+// c_i = (V[i], w) for i <= j into gs->c0 (pass 0) or gs->c1 (pass 1).
+template <int MM>
+__global__ void __launch_bounds__(KTHREADS)
+k_gm_dots(const long long n, const double *__restrict__ V, const double *__restrict__ w, GScal *gs, const int pass,
+          double *partials, unsigned int *counter) {
+    __shared__ double smem[32 * MM];
+    const int j = gs->j;
+    double a[MM];
+#pragma unroll
+    for (int i = 0; i < MM; i++) a[i] = 0.0;
+    GRID_STRIDE(P, n) {
+        const double wv = w[P];
+#pragma unroll
+        for (int i = 0; i < MM; i++)
+            if (i <= j) a[i] += V[(size_t)i * n + P] * wv;
+    }
+    reduce_and_finish<MM, MM>(a, smem, partials, counter, [&](const double *tot) {
+        double *c = pass == 0 ? gs->c0 : gs->c1;
+        for (int i = 0; i < MM; i++) c[i] = i <= j ? tot[i] : 0.0;
+    });
+}
+
+// w -= sum_{i<=j} c_i V[i] with c the projections of this pass; the final
+// pass also sums ||w||^2 and its last block closes the Arnoldi step: column
+// j of H (both passes' projections and ||w||), the rotations, the residual
+// estimate, the in-cycle stopping test, j + 1 and the loop condition.
+template <int MM>
+__global__ void __launch_bounds__(KTHREADS)
+k_gm_orth(const long long n, const double *__restrict__ V, double *w, GScal *gs, const int final_pass,
+          double *partials, unsigned int *counter, const LoopCtl lc) {
+    __shared__ double smem[32];
+    __shared__ double cs_[MM];
+    const int j = gs->j;
+    const double *c = final_pass ? gs->c1 : gs->c0;
+    if (threadIdx.x < MM) cs_[threadIdx.x] = threadIdx.x <= j ? c[threadIdx.x] : 0.0;
+    __syncthreads();
+    double ss = 0.0;
+    GRID_STRIDE(P, n) {
+        double y = w[P];
+        for (int i = 0; i <= j; i++) y -= cs_[i] * V[(size_t)i * n + P];
+        w[P] = y;
+        ss += y * y;
+    }
+    if (!final_pass) return;
+    double v[1] = {ss};
+    reduce_and_finish<1, 1>(v, smem, partials, counter, [&](const double *tot) {
+        GScal &s = *gs;
+        const int L = GM_MAX + 1;
+        double *hc = s.h + (size_t)j * L;
+        for (int i = 0; i <= j; i++) hc[i] = s.c0[i] + s.c1[i];
+        const double hn = sqrt(tot[0]);
+        hc[j + 1] = hn;
+        for (int i = 0; i < j; i++) {
+            const double t = s.cs[i] * hc[i] + s.sn[i] * hc[i + 1];
+            hc[i + 1] = -s.sn[i] * hc[i] + s.cs[i] * hc[i + 1];
+            hc[i] = t;
+        }
+        const double d = hypot(hc[j], hc[j + 1]);
+        bool breakdown = d == 0.0;
+        if (!breakdown) {
+            s.cs[j] = hc[j] / d;
+            s.sn[j] = hc[j + 1] / d;
+            hc[j] = d;
+            hc[j + 1] = 0.0;
+            s.g[j + 1] = -s.sn[j] * s.g[j];
+            s.g[j] = s.cs[j] * s.g[j];
+        }
+        s.res = fabs(s.g[j + 1]);
+        s.iters += 1;
+        s.j = j + 1;
+        s.vscale = hn > 0 ? 1.0 / hn : 0.0;
+        const bool est = (s.tol > 0 && s.res < s.tol * sqrt(s.bnorm2)) ||
+                         (s.divtol > 0 && s.beta0 > 0 && s.divmax0 * (s.res / s.beta0) <= 0.5 * s.divtol);
+        const bool more = !breakdown && !est && hn > 0 && s.j < s.m && s.iters < s.maxit;
+        s.more = more ? 1 : 0;
+        set_loop(lc, more);
+    });
+}
+
+// x += sum_{i<k} y_i Z[i] with H y = g solved (back substitution, k = j)
+// by every block for itself.
+__global__ void __launch_bounds__(KTHREADS)
+k_gm_update(const long long n, const double *__restrict__ Z, double *x, const GScal *gs) {
+    __shared__ double y[GM_MAX];
+    const int k = gs->j;
+    if (threadIdx.x == 0) {
+        const int L = GM_MAX + 1;
+        for (int i = k - 1; i >= 0; i--) {
+            double t = gs->g[i];
+            for (int l = i + 1; l < k; l++) t -= gs->h[(size_t)l * L + i] * y[l];
+            const double d = gs->h[(size_t)i * L + i];
+            y[i] = d != 0.0 ? t / d : 0.0;
+        }
+    }
+    __syncthreads();
+    GRID_STRIDE(P, n) {
+        double xv = x[P];
+        for (int i = 0; i < k; i++) xv += y[i] * Z[(size_t)i * n + P];
+        x[P] = xv;
+    }
+}
+
+static void gm_residual(cudaStream_t st, const OpT<double> &A, int op, GmresWork &w, const double *b,
+                        const double *x, int x_zero, const SolveParams &prm, LoopCtl lc) {
+    k_gm_residual<<<A.sw.nblocks, SW_THREADS, 0, st>>>(A, op, b, x, w.w, x_zero, w.scal, prm.tol, prm.divtol, w.m,
+                                                       prm.maxit, w.partials, w.counter, lc);
+    note_launches(1);
+}
+
+// One Arnoldi step (6 launches + the preconditioner's).
+static void gm_step(cudaStream_t st, const OpT<double> &A, int op, GmresWork &w, Preconditioner<double> *M,
+                    Prof *pf, LoopCtl lc) {
+    const long long n = w.n;
+    k_gm_next<<<w.nblk, KTHREADS, 0, st>>>(n, w.w, w.V, w.vin, w.scal);
+    note_launches(1);
+    const double *z = w.vin;
+    if (M) {
+        const int tm = prof_begin(pf, "mg_vcycle");
+        M->apply(st, w.vin, w.zj, nullptr);
+        prof_end(pf, tm);
+        z = w.zj;
+    }
+    const int tm = prof_begin(pf, "spmv_p");
+    k_gm_spmv<<<A.sw.nblocks, SW_THREADS, 0, st>>>(A, op, n, z, w.w, w.Z, w.scal);
+    note_launches(1);
+    prof_end(pf, tm);
+    const int to = prof_begin(pf, "gmres_orth");
+    for (int pass = 0; pass < 2; pass++) {
+        k_gm_dots<GM_MAX><<<w.nblk, KTHREADS, 0, st>>>(n, w.V, w.w, w.scal, pass, w.partials, w.counter);
+        k_gm_orth<GM_MAX><<<w.nblk, KTHREADS, 0, st>>>(n, w.V, w.w, w.scal, pass, w.partials, w.counter, lc);
+        note_launches(2);
+    }
+    prof_end(pf, to);
+}
+
+static void gm_update(cudaStream_t st, GmresWork &w, double *x) {
+    k_gm_update<<<w.nblk, KTHREADS, 0, st>>>(w.n, w.Z, x, w.scal);
+    note_launches(1);
+}
+
+static void gm_fetch(cudaStream_t st, GmresWork &w) {
+    cudaMemcpyAsync(w.scal_h, w.scal, sizeof(GScal), cudaMemcpyDeviceToHost, st);
+    cudaStreamSynchronize(st);
+}
+
+int report(const GmresWork &w, SolveReport &rep) {
+    rep = SolveReport();
+    const GScal &s = *w.scal_h;
+    rep.iters[0] = s.iters;
+    rep.outer = s.cycles;
+    rep.relres[0] = s.bnorm2 > 0 ? std::sqrt(s.rnorm2 / s.bnorm2) : 0.0;
+    rep.divmax[0] = s.divmax;
+    return s.state == GM_DONE ? 0 : 1;
+}
+
+int gmres(cudaStream_t st, const OpT<double> &A, int op, GmresWork &w, const double *b, double *x,
+          const SolveParams &prm, Preconditioner<double> *M, SolveReport &rep) {
+    const LoopCtl none;
+    cudaMemsetAsync(x, 0, sizeof(double) * w.n, st);
+    gm_residual(st, A, op, w, b, x, 1, prm, none);
+    gm_fetch(st, w);
+    while (w.scal_h->state == GM_RUN) {
+        do {
+            gm_step(st, A, op, w, M, prm.prof, none);
+            gm_fetch(st, w);
+        } while (w.scal_h->more);
+        gm_update(st, w, x);
+        gm_residual(st, A, op, w, b, x, 0, prm, none);
+        gm_fetch(st, w);
+    }
+    return report(w, rep);
+}
+
+int record_gmres(cudaStream_t st, const cudaStream_t *aux, const OpT<double> &A, int op, GmresWork &w,
+                 const double *b, double *x, const SolveParams &prm, Preconditioner<double> *M, int *fixed,
+                 int *per_cycle, int *per_iter) {
+    LoopCtl outer;
+    if (new_loop(st, outer) != 0) return -1;
+    cudaMemsetAsync(x, 0, sizeof(double) * w.n, st);
+    gm_residual(st, A, op, w, b, x, 1, prm, outer);
+    if (begin_while(st, outer, aux[0]) != 0) return -1;
+    {
+        cudaStream_t bs = aux[0];
+        LoopCtl inner;
+        if (new_loop(bs, inner) != 0) return -1;
+        k_gm_cycle<<<1, 32, 0, bs>>>(w.scal, inner);
+        note_launches(1);
+        if (begin_while(bs, inner, aux[1]) != 0) return -1;
+        gm_step(aux[1], A, op, w, M, nullptr, inner);
+        if (end_while(aux[1]) != 0) return -1;
+        gm_update(bs, w, x);
+        gm_residual(bs, A, op, w, b, x, 0, prm, outer);
+    }
+    if (end_while(aux[0]) != 0) return -1;
+    cudaMemcpyAsync(w.scal_h, w.scal, sizeof(GScal), cudaMemcpyDeviceToHost, st);
+    *fixed = 1;
+    *per_cycle = 3;
+    *per_iter = 6 + (M ? M->launches() : 0);
+    return 0;
+}
 
 }  // namespace ibm

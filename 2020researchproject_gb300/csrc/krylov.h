@@ -89,6 +89,22 @@ struct Preconditioner {
     virtual int launches() const = 0;
 };
 
+// FP64 Krylov vectors with an FP32 preconditioner: r is rounded to FP32,
+// the FP32 preconditioner applied, and z widened back to FP64.  The outer
+// BiCGSTAB keeps FP64 accuracy and convergence; the preconditioner (the
+// multigrid V-cycle, most of the solve's traffic) runs on half the bytes.
+struct WidenedPreconditioner : Preconditioner<double> {
+    Preconditioner<float> *m32 = nullptr;
+    float *r32 = nullptr, *z32 = nullptr;
+    long long n = 0;
+    int nblk = KBLOCKS;
+    ~WidenedPreconditioner() override { release(); }
+    int allocate(long long ncell, Preconditioner<float> *m);
+    void release();
+    void apply(cudaStream_t s, const double *r, double *z, const int *gate) override;
+    int launches() const override { return m32->launches() + 2; }
+};
+
 template <typename T>
 struct KrylovWork {
     long long n = 0;
@@ -121,6 +137,48 @@ struct IRWork {
     int allocate(long long ncell, int ncomp, bool precond, int maxblocks);
     void release();
 };
+
+// Restarted flexible GMRES (FP64, one component): the pressure solve of
+// SOLVER_GMRES (src/ibm3d_setup.c:1471-1477, restart length 10 there) and
+// of the mixed path, where the preconditioner (the FP32 V-cycle behind a
+// WidenedPreconditioner) is not an exact linear operator: the flexible
+// form keeps every preconditioned vector, so the solve does not depend on
+// it being one.  Classical Gram-Schmidt with one re-orthogonalisation pass.
+constexpr int GM_MAX = 32;  // largest restart length
+
+struct GScal {
+    double h[(GM_MAX + 1) * GM_MAX];  // Hessenberg after rotations, column j at h[j * (GM_MAX + 1) + i]
+    double cs[GM_MAX], sn[GM_MAX];    // Givens rotations
+    double g[GM_MAX + 1];             // rotated right-hand side beta e1
+    double c0[GM_MAX + 1], c1[GM_MAX + 1];  // projections of the two Gram-Schmidt passes
+    double bnorm2, rnorm2, beta0, divmax0, divmax, res, vscale, tol, divtol;
+    int j, m, iters, cycles, state, maxit;
+    int more;  // the Arnoldi loop continues (set by each step)
+};
+
+struct GmresWork {
+    long long n = 0;
+    int m = 0;
+    int nblk = KBLOCKS;
+    double *base = nullptr;
+    double *V = nullptr, *Z = nullptr;  // m basis vectors, m preconditioned vectors
+    double *w = nullptr, *vin = nullptr, *zj = nullptr;
+    GScal *scal = nullptr, *scal_h = nullptr;
+    double *partials = nullptr;
+    unsigned int *counter = nullptr;
+    ~GmresWork() { release(); }
+    int allocate(long long ncell, int restart, int maxblocks);
+    void release();
+};
+
+// Host loop: solves A x = b (OP_PRES) from x0 = 0 with the stopping test of
+// bicgstab (checked on the true residual at the end of each cycle).
+int gmres(cudaStream_t st, const OpT<double> &A, int op, GmresWork &w, const double *b, double *x,
+          const SolveParams &prm, Preconditioner<double> *M, SolveReport &rep);
+int record_gmres(cudaStream_t st, const cudaStream_t *aux, const OpT<double> &A, int op, GmresWork &w,
+                 const double *b, double *x, const SolveParams &prm, Preconditioner<double> *M, int *fixed,
+                 int *per_cycle, int *per_iter);
+int report(const GmresWork &w, SolveReport &rep);
 
 // Host loop.  Solves A x = b (nc components for OP_MOM, 1 for OP_PRES)
 // from x0 = 0.  Returns 0 when every component converged, 1 on reaching

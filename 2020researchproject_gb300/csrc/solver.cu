@@ -55,8 +55,8 @@ struct StepGraph {
 
 // Host parameters baked into recorded graphs.
 struct GraphSig {
-    int precision, les, use_mg;
-    double tol, divtol, Re, dt, f[3], cs;
+    int precision, les, use_mg, max_outer, solver, gm_restart;
+    double tol, divtol, Re, dt, f[3], cs, inner_tol[2];
     bool operator==(const GraphSig &o) const { return memcmp(this, &o, sizeof *this) == 0; }
 };
 
@@ -98,6 +98,9 @@ struct ibm3d_device {
     IRWork irmom, irpres;
     GMG<double> *mg = nullptr;
     GMG<float> *mg32 = nullptr;
+    WidenedPreconditioner pc64;   // FP32 multigrid under an FP64 Krylov solve
+    GmresWork gm;                 // SOLVER_GMRES pressure solves
+    int gm_restart = 10;          // restart length (the reference's KDim, src/ibm3d_setup.c:1474)
     double *red_partials = nullptr;
     unsigned int *red_counter = nullptr;
     double *maxdiv_d = nullptr;
@@ -125,6 +128,10 @@ struct ibm3d_device {
     bool use_graphs = true;
     int mg_sweeps[5] = {5, 5, 1, 1, 8};  // multigrid sweeps: fine pre/post, coarse pre/post, coarsest
     double mg_omega = 1.0;               // over-relaxation of the fine-grid smoother
+    // Mixed path: relative tolerance of each FP32 inner solve (momentum,
+    // pressure) and the refinement-cycle cap.
+    double inner_tol[2] = {1e-5, 1e-5};
+    int max_outer = 12;
     cudaStream_t aux[2] = {nullptr, nullptr};
     std::vector<StepGraph> graphs;
     GraphSig gsig{};
@@ -138,6 +145,12 @@ struct ibm3d_device {
 };
 
 namespace {
+
+// A batched step runs one graph branch per member; with CUDA's default of 8
+// hardware work queues most branches wait for a queue.  Ask for the maximum
+// (32) when the library is loaded, unless the host already chose a value;
+// it applies to CUDA contexts created after this point.
+__attribute__((constructor)) void ibm3d_queues() { setenv("CUDA_DEVICE_MAX_CONNECTIONS", "32", 0); }
 
 constexpr double kNaN = __builtin_nan("");
 constexpr int kUpdateBlocks = 608;
@@ -259,6 +272,8 @@ void release_device(ibm3d_device *d) {
     d->mg = nullptr;
     delete d->mg32;
     d->mg32 = nullptr;
+    d->pc64.release();
+    d->gm.release();
     d->kmom.release();
     d->kpres.release();
     d->irmom.release();
@@ -862,12 +877,15 @@ SolveParams mom_params(IBMSolver *sv) {
     SolveParams pm;
     pm.tol = sv->tol;
     pm.maxit = 200;
+    pm.inner_tol = sv->dev->inner_tol[0];
+    pm.max_outer = sv->dev->max_outer;
     pm.prof = &sv->dev->prof;
     return pm;
 }
 
 SolveParams pres_params(IBMSolver *sv) {
     SolveParams pp = mom_params(sv);
+    pp.inner_tol = sv->dev->inner_tol[1];
     pp.maxit = 1000;
     pp.divtol = sv->dev->divtol;
     if (pp.divtol > 0) pp.tol = 0.0;  // the divergence rule replaces the relative-residual rule
@@ -875,6 +893,21 @@ SolveParams pres_params(IBMSolver *sv) {
 }
 
 bool use_mg(const IBMSolver *sv) { return sv->precond_type == PRECOND_AMG || sv->linear_solver_type == SOLVER_AMG; }
+
+// Pressure solves with SOLVER_GMRES: flexible GMRES in FP64 (any precision
+// mode; the mixed modes precondition it with the FP32 multigrid).
+bool pres_gmres(const IBMSolver *sv) { return sv->linear_solver_type == SOLVER_GMRES; }
+
+// Which solve runs as FP64 refinement around FP32 BiCGSTAB.
+bool mom_ir(const ibm3d_device *d) { return d->precision != IBM3D_FP64; }
+bool pres_ir(const IBMSolver *sv) { return sv->dev->precision == IBM3D_MIXED && !pres_gmres(sv); }
+
+// Preconditioner of an FP64 pressure Krylov solve.
+Preconditioner<double> *pres_pc64(IBMSolver *sv) {
+    ibm3d_device *d = sv->dev;
+    if (!use_mg(sv)) return nullptr;
+    return d->precision != IBM3D_FP64 ? (Preconditioner<double> *)&d->pc64 : (Preconditioner<double> *)d->mg;
+}
 
 void stage_rhs(IBMSolver *sv) {
     ibm3d_device *d = sv->dev;
@@ -945,23 +978,23 @@ void check_pres(IBMSolver *sv, int rc) {
 void one_step(IBMSolver *sv) {
     ibm3d_device *d = sv->dev;
     Prof &pf = d->prof;
-    const bool mixed = d->precision == IBM3D_MIXED;
     stage_rhs(sv);
     const SolveParams pm = mom_params(sv);
     int t = pf.begin("mom_solve");
-    int rc = mixed ? solve_ir(d->s, d->A64, d->A32, OP_MOM, d->irmom, d->b, d->ustar, pm, nullptr, d->rep_mom)
+    int rc = mom_ir(d) ? solve_ir(d->s, d->A64, d->A32, OP_MOM, d->irmom, d->b, d->ustar, pm, nullptr, d->rep_mom)
                    : bicgstab<double>(d->s, d->A64, OP_MOM, d->kmom, d->b, d->ustar, pm, nullptr, d->rep_mom);
     pf.end(t);
     check_mom(sv, rc);
     stage_ustar(sv);
     const SolveParams pp = pres_params(sv);
     t = pf.begin("p_solve");
-    if (mixed)
+    if (pres_gmres(sv))
+        rc = gmres(d->s, d->A64, OP_PRES, d->gm, d->b, d->pp, pp, pres_pc64(sv), d->rep_p);
+    else if (pres_ir(sv))
         rc = solve_ir(d->s, d->A64, d->A32, OP_PRES, d->irpres, d->b, d->pp, pp, use_mg(sv) ? d->mg32 : nullptr,
                       d->rep_p);
     else
-        rc = bicgstab<double>(d->s, d->A64, OP_PRES, d->kpres, d->b, d->pp, pp, use_mg(sv) ? d->mg : nullptr,
-                              d->rep_p);
+        rc = bicgstab<double>(d->s, d->A64, OP_PRES, d->kpres, d->b, d->pp, pp, pres_pc64(sv), d->rep_p);
     pf.end(t);
     check_pres(sv, rc);
     stage_next(sv);
@@ -982,6 +1015,11 @@ GraphSig graph_sig(const IBMSolver *sv) {
     g.f[1] = sv->ext_force.const_f2;
     g.f[2] = sv->ext_force.const_f3;
     g.cs = sv->turb_model.Cs;
+    g.inner_tol[0] = sv->dev->inner_tol[0];
+    g.inner_tol[1] = sv->dev->inner_tol[1];
+    g.max_outer = sv->dev->max_outer;
+    g.solver = sv->linear_solver_type;
+    g.gm_restart = sv->dev->gm_restart;
     return g;
 }
 
@@ -991,7 +1029,6 @@ GraphSig graph_sig(const IBMSolver *sv) {
 // batch graph it joined); fills G's keys and launch accounting.
 bool record_step_into(IBMSolver *sv, StepGraph &G) {
     ibm3d_device *d = sv->dev;
-    const bool mixed = d->precision == IBM3D_MIXED;
     long long count = 0;
     g_redirect = &count;
     bool ok = true;
@@ -1000,7 +1037,7 @@ bool record_step_into(IBMSolver *sv, StepGraph &G) {
         stage_rhs(sv);
         SolveParams pm = mom_params(sv);
         pm.prof = nullptr;
-        if (mixed)
+        if (mom_ir(d))
             ok = record_ir(d->s, d->aux, d->A64, d->A32, OP_MOM, d->irmom, d->b, d->ustar, pm, nullptr, &mf, &mo,
                            &mi) == 0;
         else
@@ -1011,12 +1048,15 @@ bool record_step_into(IBMSolver *sv, StepGraph &G) {
         stage_ustar(sv);
         SolveParams pp = pres_params(sv);
         pp.prof = nullptr;
-        if (mixed)
+        if (pres_gmres(sv))
+            ok = record_gmres(d->s, d->aux, d->A64, OP_PRES, d->gm, d->b, d->pp, pp, pres_pc64(sv), &pf, &po,
+                              &pi) == 0;
+        else if (pres_ir(sv))
             ok = record_ir(d->s, d->aux, d->A64, d->A32, OP_PRES, d->irpres, d->b, d->pp, pp,
                            use_mg(sv) ? d->mg32 : nullptr, &pf, &po, &pi) == 0;
         else
-            ok = record_bicgstab<double>(d->s, d->aux, d->A64, OP_PRES, d->kpres, d->b, d->pp, pp,
-                                         use_mg(sv) ? d->mg : nullptr, &pf, &pi) == 0;
+            ok = record_bicgstab<double>(d->s, d->aux, d->A64, OP_PRES, d->kpres, d->b, d->pp, pp, pres_pc64(sv),
+                                         &pf, &pi) == 0;
     }
     if (ok) {
         stage_next(sv);
@@ -1076,10 +1116,9 @@ bool has_key(const StepGraph &g, const ibm3d_device *d) {
 // reports, warnings, launch count and the pointer swaps.
 void finish_step(IBMSolver *sv, const StepGraph &G) {
     ibm3d_device *d = sv->dev;
-    const bool mixed = d->precision == IBM3D_MIXED;
     long long launches = G.fixed;
     int rc;
-    if (mixed) {
+    if (mom_ir(d)) {
         rc = report(d->irmom, d->rep_mom);
         launches += (long long)d->rep_mom.outer * G.mom_outer;
     } else {
@@ -1087,7 +1126,10 @@ void finish_step(IBMSolver *sv, const StepGraph &G) {
     }
     launches += (long long)std::max({d->rep_mom.iters[0], d->rep_mom.iters[1], d->rep_mom.iters[2]}) * G.mom_iter;
     check_mom(sv, rc);
-    if (mixed) {
+    if (pres_gmres(sv)) {
+        rc = report(d->gm, d->rep_p);
+        launches += (long long)d->rep_p.outer * G.p_outer;
+    } else if (pres_ir(sv)) {
         rc = report(d->irpres, d->rep_p);
         launches += (long long)d->rep_p.outer * G.p_outer;
     } else {
@@ -1351,6 +1393,10 @@ void IBMSolver_set_linear_solver(IBMSolver *s, IBMSolverLinearSolverType type, I
     s->linear_solver_type = type;
     s->precond_type = precond;
     s->tol = tol;
+    ibm3d_device *d = s->dev;
+    if (d && d->assembled && type == SOLVER_GMRES && !d->gm.base &&
+        d->gm.allocate(d->g.ncell, d->gm_restart, d->A64.sw.nblocks) != 0)
+        set_status(s, IBM3D_ECUDA, "GMRES workspace allocation failed");
 }
 
 void IBMSolver_set_autosave(IBMSolver *s, const char *filename, int period) {
@@ -1443,6 +1489,14 @@ void IBMSolver_assemble(IBMSolver *s) {
     if (d->mg->setup(d->s, d->A64, d->A64, gcell, d->nghost, geom, mc) != 0 ||
         d->mg32->setup(d->s, d->A64, d->A32, gcell, d->nghost, geom, mc) != 0) {
         set_status(s, IBM3D_ECUDA, "multigrid setup failed");
+        return;
+    }
+    if (d->pc64.allocate(g.ncell, d->mg32) != 0) {
+        set_status(s, IBM3D_ECUDA, "preconditioner workspace allocation failed");
+        return;
+    }
+    if (pres_gmres(s) && d->gm.allocate(g.ncell, d->gm_restart, mb) != 0) {
+        set_status(s, IBM3D_ECUDA, "GMRES workspace allocation failed");
         return;
     }
     if (!cuda_check(s, cudaStreamSynchronize(d->s), "assemble")) return;
@@ -1883,6 +1937,30 @@ void IBMSolver_set_smagorinsky(IBMSolver *s, double Cs) {
 
 void IBMSolver_set_div_tol(IBMSolver *s, double div_tol) { s->dev->divtol = div_tol; }
 
+void IBMSolver_set_gmres_restart(IBMSolver *s, int restart) {
+    ibm3d_device *d = s->dev;
+    if (restart < 1 || restart > GM_MAX) {
+        set_status(s, IBM3D_EARG, "IBMSolver_set_gmres_restart: restart length in [1, %d]", GM_MAX);
+        return;
+    }
+    d->gm_restart = restart;
+    if (d->assembled && pres_gmres(s)) {
+        drop_graphs(d);
+        if (d->gm.allocate(d->g.ncell, restart, d->A64.sw.nblocks) != 0)
+            set_status(s, IBM3D_ECUDA, "GMRES workspace allocation failed");
+    }
+}
+
+void IBMSolver_set_refinement(IBMSolver *s, double inner_tol_mom, double inner_tol_p, int max_outer) {
+    if (!(inner_tol_mom > 0 && inner_tol_mom < 1) || !(inner_tol_p > 0 && inner_tol_p < 1) || max_outer < 1) {
+        set_status(s, IBM3D_EARG, "IBMSolver_set_refinement: tolerances in (0, 1) and max_outer >= 1");
+        return;
+    }
+    s->dev->inner_tol[0] = inner_tol_mom;
+    s->dev->inner_tol[1] = inner_tol_p;
+    s->dev->max_outer = max_outer;
+}
+
 void IBMSolver_set_multigrid(IBMSolver *s, int nu_pre, int nu_post, int nuc_pre, int nuc_post, int coarse_sweeps,
                              double omega) {
     ibm3d_device *d = s->dev;
@@ -1911,7 +1989,7 @@ void IBMSolver_set_graphs(IBMSolver *s, int on) {
 }
 
 void IBMSolver_set_precision(IBMSolver *s, int mode) {
-    if (mode != IBM3D_FP64 && mode != IBM3D_MIXED) {
+    if (mode != IBM3D_FP64 && mode != IBM3D_MIXED && mode != IBM3D_MIXED_MG) {
         set_status(s, IBM3D_EUNSUPPORTED, "precision mode %d is not available", mode);
         return;
     }
@@ -2056,7 +2134,7 @@ double IBMSolver_time_iterate(IBMSolver *s, int nsteps) {
 double IBMSolver_time_kernel(IBMSolver *s, int which, int reps, double *bytes) {
     if (!check_ready(s, "IBMSolver_time_kernel")) return -1;
     ibm3d_device *d = s->dev;
-    const bool mixed = d->precision == IBM3D_MIXED;
+    const bool mixed = d->precision != IBM3D_FP64;   // FP32 multigrid
     double b = 0;
     double ms = -1;
     cudaStreamSynchronize(d->s);
@@ -2070,7 +2148,7 @@ double IBMSolver_time_kernel(IBMSolver *s, int which, int reps, double *bytes) {
         cudaEventCreate(&e1);
         cudaEventRecord(e0, d->s);
         for (int q = 0; q < reps; q++) {
-            if (mixed) apply_operator<float>(d->s, d->A32, OP_PRES, 0, d->irpres.inner.r, d->irpres.inner.s);
+            if (pres_ir(s)) apply_operator<float>(d->s, d->A32, OP_PRES, 0, d->irpres.inner.r, d->irpres.inner.s);
             else apply_operator<double>(d->s, d->A64, OP_PRES, 0, d->kpres.r, d->kpres.s);
         }
         cudaEventRecord(e1, d->s);
@@ -2080,7 +2158,7 @@ double IBMSolver_time_kernel(IBMSolver *s, int which, int reps, double *bytes) {
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         ms = reps > 0 ? t / reps : 0;
-        const double w = mixed ? 4.0 : 8.0;
+        const double w = pres_ir(s) ? 4.0 : 8.0;
         b = (double)d->g.ncell * (3 * w + 1);
     } else {
         set_status(s, IBM3D_EARG, "IBMSolver_time_kernel: unknown kernel %d", which);

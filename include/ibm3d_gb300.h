@@ -61,9 +61,12 @@ void IBMSolver_set_div_tol(IBMSolver *, double div_tol);
    with an FP64 multigrid preconditioner, as the reference.  IBM3D_MIXED:
    FP64 iterative refinement (residuals, updates and the stopping test in
    FP64, on the exact FP64 rows) around FP32 BiCGSTAB solves with an FP32
-   multigrid preconditioner; it stops on the same FP64 criterion.  Every
-   other part of the step stays FP64 in both modes. */
-enum { IBM3D_FP64 = 0, IBM3D_MIXED = 1 };
+   multigrid preconditioner; it stops on the same FP64 criterion.
+   IBM3D_MIXED_MG: momentum as IBM3D_MIXED; the pressure solve is FP64
+   BiCGSTAB whose preconditioner is the FP32 multigrid V-cycle (input
+   rounded to FP32, output widened to FP64).  Every other part of the step
+   stays FP64 in all modes. */
+enum { IBM3D_FP64 = 0, IBM3D_MIXED = 1, IBM3D_MIXED_MG = 2 };
 void IBMSolver_set_precision(IBMSolver *, int mode);
 
 /* Step sequencing.  on (default): each time step runs as one recorded CUDA
@@ -82,6 +85,16 @@ void IBMSolver_set_graphs(IBMSolver *, int on);
    same residual or divergence test. */
 void IBMSolver_set_multigrid(IBMSolver *, int nu_pre, int nu_post, int nuc_pre, int nuc_post, int coarse_sweeps,
                              double omega);
+
+/* Restart length of SOLVER_GMRES pressure solves (1..32; default 10, the
+   reference's KDim).  The GMRES is flexible (it keeps every preconditioned
+   vector), so the FP32 multigrid of the mixed modes may precondition it. */
+void IBMSolver_set_gmres_restart(IBMSolver *, int restart);
+
+/* Mixed path (IBM3D_MIXED): relative tolerance of each FP32 inner solve of
+   the momentum and pressure refinement cycles, and the cycle cap.  The
+   outer FP64 stopping rule is unchanged.  Defaults 1e-5, 1e-5, 12. */
+void IBMSolver_set_refinement(IBMSolver *, double inner_tol_mom, double inner_tol_p, int max_outer);
 
 /* Initial state from host arrays in the padded (N+4)^3 layout, k fastest
    (u1, u2, u3, p).  Sets iter = 0 and time = 0 like init_flow_const. */

@@ -78,12 +78,15 @@ def test_setup_bit_exact(ibm, name):
         assert np.array_equal(coeff, case["ghost_coeff"])
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+_MODES = {"fp64": "FP64", "mixed": "MIXED", "mixed_mg": "MIXED_MG"}
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed_mg"])
 @pytest.mark.parametrize("name", golden_cases())
 def test_steps_match_reference(ibm, name, precision):
     case = load_golden(name)
     s = build_case(ibm, case)
-    s.set_precision(ibm.MIXED if precision == "mixed" else ibm.FP64)
+    s.set_precision(getattr(ibm, _MODES[precision]))
     calls = case["meta"]["calls"]
     report = []
     for c, n in enumerate(calls, start=1):
@@ -103,3 +106,24 @@ def test_steps_match_reference(ibm, name, precision):
     assert st["iter"] == sum(calls)
     if precision == "mixed":
         assert st["outer_p"] >= 1
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed_mg"])
+@pytest.mark.parametrize("name", ["sphere", "mixed_box", "func_sphere"])
+def test_gmres_steps_match_reference(ibm, name, precision):
+    """SOLVER_GMRES pressure solves (flexible GMRES, restart 10 as the
+    reference's KDim) reach the same fields as the reference's fixtures,
+    which hypre's BiCGSTAB produced: both solve to 1e-12."""
+    case = load_golden(name)
+    s = build_case(ibm, case)
+    s.set_linear_solver(ibm.SOLVER_GMRES, ibm.PRECOND_AMG, 1e-12)
+    s.set_precision(getattr(ibm, _MODES[precision]))
+    calls = case["meta"]["calls"]
+    for c, n in enumerate(calls, start=1):
+        s.iterate(n)
+        for f in ("u1", "u2", "u3", "p", "U1"):
+            got, ref = s.get_field(f), case[f"{f}_{c}"]
+            assert _same_nan(got, ref), f"{f} after call {c}: NaN mask differs"
+            err = rel_l2(got, ref)
+            assert err <= FIELD_TOL, f"{f} after call {c}: rel L2 {err:.3e}"
+    assert s.stats()["outer_p"] >= 1          # GMRES cycles
