@@ -21,6 +21,11 @@ import os
 
 import numpy as np
 
+# Batched steps run one graph branch (or stream) per member: let the GPU
+# work on up to 32 of them at once (CUDA's default is 8 hardware queues).
+# Set on import, before anything in this process creates a CUDA context.
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 _PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_PKG, "libibm3d_gb300.so")
 
@@ -77,10 +82,6 @@ def load_library(path: str = LIB_PATH):
         raise IBM3DError(f"{path} is missing: run __graft_entry__.build() "
                          "(the GB300 path has no CPU fallback)")
     os.environ.setdefault("IBM3D_NO_ABORT", "1")
-    # Batched steps run one graph branch per member: let the GPU work on up
-    # to 32 of them at once (CUDA's default is 8 hardware queues).  Takes
-    # effect if no CUDA context exists in this process yet.
-    os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
     lib = ctypes.CDLL(path)
     vp, d, i, dp, ip = ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p
     sig = {
@@ -137,6 +138,7 @@ def load_library(path: str = LIB_PATH):
         "IBMBatch_size": (i, [vp]),
         "IBMBatch_iterate": (d, [vp, i]),
         "IBMBatch_last_status": (i, [vp]),
+        "IBMBatch_set_combined": (None, [vp, i]),
         "Polyhedron_new": (vp, []),
         "Polyhedron_destroy": (None, [vp]),
         "Polyhedron_read_stl": (None, [vp, vp]),
@@ -421,12 +423,19 @@ class Batch:
     batched step (IBMBatch_* of include/ibm3d_gb300.h).  Each member gets
     exactly the results IBMSolver.iterate gives it alone."""
 
-    def __init__(self, solvers=()):
+    def __init__(self, solvers=(), combined=True):
         self._lib = load_library()
         self._b = self._lib.IBMBatch_new()
         self._members = []
+        if not combined:
+            self.set_combined(False)
         for s in solvers:
             self.add(s)
+
+    def set_combined(self, on=True):
+        """True: one graph launch per batched step (re-recorded on membership
+        changes); False: each member's own step graph on its own stream."""
+        self._lib.IBMBatch_set_combined(self._b, 1 if on else 0)
 
     def add(self, solver):
         if self._lib.IBMBatch_add(self._b, solver._s) != 0:

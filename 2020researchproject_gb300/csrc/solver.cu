@@ -1143,25 +1143,30 @@ void finish_step(IBMSolver *sv, const StepGraph &G) {
 
 // One step through its recorded graph.  Returns false when recording
 // failed (the caller then runs the step host-sequenced).
-bool graph_step(IBMSolver *sv) {
+// The recorded step for the solver's current field buffers (recorded on
+// first use); null when recording failed.
+StepGraph *step_graph(IBMSolver *sv) {
     ibm3d_device *d = sv->dev;
     const GraphSig sig = graph_sig(sv);
     if (!(sig == d->gsig)) {
         drop_graphs(d);
         d->gsig = sig;
     }
-    StepGraph *G = nullptr;
     for (auto &g : d->graphs)
-        if (has_key(g, d)) G = &g;
+        if (has_key(g, d)) return &g;
+    StepGraph ng;
+    if (!record_step(sv, ng)) return nullptr;
+    d->graphs.push_back(ng);
+    return &d->graphs.back();
+}
+
+bool graph_step(IBMSolver *sv) {
+    ibm3d_device *d = sv->dev;
+    StepGraph *G = step_graph(sv);
     if (!G) {
-        StepGraph ng;
-        if (!record_step(sv, ng)) {
-            fprintf(stderr, "warning: CUDA graph recording failed; stepping without graphs\n");
-            d->use_graphs = false;
-            return false;
-        }
-        d->graphs.push_back(ng);
-        G = &d->graphs.back();
+        fprintf(stderr, "warning: CUDA graph recording failed; stepping without graphs\n");
+        d->use_graphs = false;
+        return false;
     }
     if (!cuda_check(sv, cudaGraphLaunch(G->exec, d->s), "graph launch")) return true;
     if (!cuda_check(sv, cudaStreamSynchronize(d->s), "time step")) return true;
@@ -2251,6 +2256,7 @@ struct IBMBatch {
         std::vector<StepGraph> parts;
     };
     std::vector<Rec> cache;
+    int combined = 1;  // 1: one graph for all members; 0: each member's own step graph
     int status = IBM3D_OK;
 };
 
@@ -2376,7 +2382,45 @@ double IBMBatch_iterate(IBMBatch *b, int nsteps) {
         cudaStreamWaitEvent(b->s, b->join[q], 0);
     }
     cudaEventRecord(b->t0, b->s);
+    std::vector<StepGraph *> own(b->members.size(), nullptr);
     for (int i = 1; i <= nsteps; i++) {
+        if (!b->combined) {
+            // Each member's own recorded step on its own stream, all forked
+            // from and joined into the batch stream.
+            for (size_t q = 0; q < b->members.size(); q++) {
+                own[q] = step_graph(b->members[q]);
+                if (!own[q]) {
+                    fprintf(stderr, "error: IBMBatch_iterate: recording a member's step failed\n");
+                    b->status = IBM3D_ECUDA;
+                    return -1;
+                }
+            }
+            cudaEventRecord(b->fork, b->s);
+            for (size_t q = 0; q < b->members.size(); q++) {
+                IBMSolver *m = b->members[q];
+                cudaStreamWaitEvent(m->dev->s, b->fork, 0);
+                prepare_samples(m, m->dev->s, m->time, b->run_start[q] + m->dt * (b->run_steps[q] + 1));
+                cudaGraphLaunch(own[q]->exec, m->dev->s);
+                cudaEventRecord(b->join[q], m->dev->s);
+                cudaStreamWaitEvent(b->s, b->join[q], 0);
+            }
+            if (cudaStreamSynchronize(b->s) != cudaSuccess) {
+                fprintf(stderr, "error: IBMBatch_iterate: %s\n", cudaGetErrorString(cudaGetLastError()));
+                b->status = IBM3D_ECUDA;
+                return -1;
+            }
+            for (size_t q = 0; q < b->members.size(); q++) {
+                IBMSolver *m = b->members[q];
+                finish_step(m, *own[q]);
+                m->iter++;
+                b->run_steps[q]++;
+                b->next_iter[q] = m->iter;
+                m->time = b->run_start[q] + m->dt * b->run_steps[q];
+                m->dev->max_div = *m->dev->maxdiv_h;
+                if (m->dev->status != IBM3D_OK && m->dev->status != IBM3D_ENOCONV) b->status = m->dev->status;
+            }
+            continue;
+        }
         for (size_t q = 0; q < b->members.size(); q++) {
             IBMSolver *m = b->members[q];
             prepare_samples(m, b->s, m->time, b->run_start[q] + m->dt * (b->run_steps[q] + 1));
@@ -2421,5 +2465,11 @@ double IBMBatch_iterate(IBMBatch *b, int nsteps) {
 }
 
 int IBMBatch_last_status(const IBMBatch *b) { return b ? b->status : IBM3D_EARG; }
+
+void IBMBatch_set_combined(IBMBatch *b, int on) {
+    if (!b) return;
+    b->combined = on != 0;
+    batch_drop(b);
+}
 
 size_t IBMSolver_device_bytes(const IBMSolver *s) { return s && s->dev ? s->dev->dev_bytes : 0; }

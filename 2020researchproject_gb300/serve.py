@@ -100,8 +100,12 @@ class Server:
     a job is assembled (raised to what admitted jobs actually take)."""
 
     def __init__(self, ibm, precision="mixed", tol=1e-6, div_tol=1e-8, hbm_budget=None, bytes_per_cell=1500.0,
-                 keep_results=False):
+                 keep_results=False, combined=False):
         self.ibm = ibm
+        # False: each member steps through its own recorded graph (nothing is
+        # re-recorded when jobs arrive or finish); True: one graph per
+        # batched step, re-recorded on every membership change.
+        self.combined = combined
         self.mode = ibm.MIXED if precision == "mixed" else ibm.FP64
         self.tol, self.div_tol = tol, div_tol
         self.hbm_budget = hbm_budget
@@ -132,7 +136,9 @@ class Server:
         queue = collections.deque()
         active = []
         used = 0
-        batch = self.ibm.Batch()
+        # Membership changes every few steps here, so each member steps
+        # through its own recorded graph (nothing re-recorded on churn).
+        batch = self.ibm.Batch(combined=self.combined)
         batched_steps = 0
         max_active = 0
         t0 = time.perf_counter()

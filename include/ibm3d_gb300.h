@@ -196,6 +196,13 @@ int IBMBatch_remove(IBMBatch *, IBMSolver *);
 int IBMBatch_size(const IBMBatch *);
 double IBMBatch_iterate(IBMBatch *, int nsteps);
 int IBMBatch_last_status(const IBMBatch *);
+/* on (default): each batched step is one graph launch over all members,
+   re-recorded when the membership changes.  off: each member's own step
+   graph is launched on its own stream, forked from and joined into the
+   batch stream (one launch per member, nothing re-recorded when members
+   come and go: what a server with churning membership wants).  Results
+   are the same bit for bit either way. */
+void IBMBatch_set_combined(IBMBatch *, int on);
 
 #ifdef __cplusplus
 }

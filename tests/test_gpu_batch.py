@@ -24,8 +24,9 @@ def _same(a, b):
     return all(np.array_equal(a[f], b[f], equal_nan=True) for f in FIELDS)
 
 
+@pytest.mark.parametrize("combined", [True, False])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_batch_members_equal_solo_runs(precision):
+def test_batch_members_equal_solo_runs(precision, combined):
     ibm = package()
     names = ["cavity", "sphere", "channel_les", "mixed_box", "func_sphere"]
     cases = [load_golden(n) for n in names]
@@ -43,7 +44,7 @@ def test_batch_members_equal_solo_runs(precision):
         s = build_case(ibm, c, tol=1e-8)
         s.set_precision(mode)
         members.append(s)
-    batch = ibm.Batch(members)
+    batch = ibm.Batch(members, combined=combined)
     ms = batch.iterate(2)
     assert ms > 0
     batch.iterate(1)
@@ -55,7 +56,8 @@ def test_batch_members_equal_solo_runs(precision):
             assert st[k] == st0[k], f"{name} {k}: {st[k]} != {st0[k]}"
 
 
-def test_batch_membership_changes_between_steps():
+@pytest.mark.parametrize("combined", [True, False])
+def test_batch_membership_changes_between_steps(combined):
     """A solver stepped partly alone, partly in a batch whose other members
     come and go, ends where the same runs alone end: its batched steps form
     one run from the moment it joined."""
@@ -68,7 +70,7 @@ def test_batch_membership_changes_between_steps():
     s = build_case(ibm, ref_case, tol=1e-8)
     t = build_case(ibm, other, tol=1e-8)
     s.iterate(1)                          # alone
-    batch = ibm.Batch([s, t])
+    batch = ibm.Batch([s, t], combined=combined)
     batch.iterate(1)                      # with a partner
     batch.remove(t)
     batch.iterate(1)                      # partner gone

@@ -44,7 +44,7 @@ class FakeSolver:
 class FakeBatch:
     log = []
 
-    def __init__(self, members=()):
+    def __init__(self, members=(), combined=True):
         self.members = list(members)
 
     def add(self, s):
