@@ -130,7 +130,7 @@ class Server:
         """Serves `jobs` (arrival times relative to now); returns a summary."""
         budget = self.hbm_budget
         if budget is None:
-            free = _free_device_bytes()
+            free = _free_device_bytes(self.ibm)
             budget = int(0.8 * free) if free else 64 << 30
         pending = collections.deque(sorted(jobs, key=lambda j: j.arrival))
         queue = collections.deque()
@@ -186,7 +186,9 @@ class Server:
                 "max_div": max(j.result_stats["max_div"] for j in jobs)}
 
 
-def _free_device_bytes():
+def _free_device_bytes(ibm=None):
+    if ibm is not None and hasattr(ibm, "load_library"):
+        ibm.load_library()               # library first: its settings apply to the context
     try:
         import ctypes
         rt = ctypes.CDLL("libcudart.so.13")

@@ -16,7 +16,8 @@ def test_served_jobs_equal_jobs_run_alone():
     ibm = package()
     serve = importlib.import_module("2020researchproject_gb300.serve")
     wl = importlib.import_module("2020researchproject_gb300.workloads")
-    jobs = serve.poisson_jobs(njobs=6, rate=40.0, seed=77, grid_max=(48, 40, 40), steps=(3, 8))
+    # Enough steps per job that later jobs arrive while earlier ones step.
+    jobs = serve.poisson_jobs(njobs=6, rate=40.0, seed=77, grid_max=(48, 40, 40), steps=(20, 30))
     for j in jobs:                        # arrivals 10 ms apart: later jobs find earlier ones running
         j.arrival = 0.01 * j.id
     # A budget that holds any two jobs but not every three, so that later

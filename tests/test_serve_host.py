@@ -1,7 +1,8 @@
 """Host logic of the continuous-batching server (no GPU): admission in
-arrival order by device footprint, batched stepping, departures, and the
-latency summary, driven through a fake of the library's solver/batch API."""
+arrival order by device footprint, batched stepping, departures, and the latency summary,
+driven through a fake of the library's solver/batch API."""
 import importlib
+import time
 
 import numpy as np
 
@@ -56,6 +57,7 @@ class FakeBatch:
         FakeBatch.log.append(("remove", id(s)))
 
     def iterate(self, n=1):
+        time.sleep(0.02)                   # a step takes a while
         FakeBatch.log.append(("step", len(self.members)))
         for m in self.members:
             m.iter += n
@@ -116,3 +118,18 @@ def test_poisson_jobs_are_seeded_and_bounded():
     for j in a:
         nx, ny, nz = (len(j.case[k]) - 1 for k in ("xf", "yf", "zf"))
         assert 32 <= nx <= 48 and 32 <= ny <= 40 and 32 <= nz <= 40 and 5 <= j.steps <= 9
+
+
+def test_setup_failure_reaches_the_caller():
+    class Broken(FakeIBM):
+        class IBMSolver(FakeSolver):
+            def assemble(self):
+                raise RuntimeError("assembly failed")
+
+    srv = serve.Server(Broken(), hbm_budget=1 << 40, bytes_per_cell=100.0)
+    try:
+        srv.run(_jobs(), time_limit=30)
+    except RuntimeError as e:
+        assert "assembly failed" in str(e)
+    else:
+        raise AssertionError("the set-up error was swallowed")
