@@ -151,6 +151,24 @@ k_mg0_init(const OpT<T> c, const T *__restrict__ r, T *__restrict__ z, const Per
     }
 }
 
+// The same pass as a 3-D launch over the padded box (threads along k, no
+// index division): grid (ceil((nz+4)/32), ceil((ny+4)/8), nx+4).
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_mg0_init3(const OpT<T> c, const T *__restrict__ r, T *__restrict__ z, const Per3 per, const int *gate) {
+    MG_GATE(gate);
+    const Grid &g = c.g;
+    const int K = blockIdx.x * 32 + threadIdx.x, J = blockIdx.y * 8 + threadIdx.y, I = blockIdx.z;
+    if (K >= g.nz + 4 || J >= g.ny + 4) return;
+    const int i = I - 2, j = J - 2, k = K - 2;
+    const long long P = (long long)I * g.sx + (long long)J * g.sy + K;
+    T v = 0;
+    if (i >= 0 && i < g.nx && j >= 0 && j < g.ny && k >= 0 && k < g.nz &&
+        cell_color(i, j, k, g.nx, g.ny, g.nz, per.p) == 0 && c.flag[P] != GHOST)
+        v = r[P];
+    z[P] = v;
+}
+
 // Ghost rows of the smoother, Jacobi-style among ghosts (each reads the
 // values before the pass): a pass into tmp, then a scatter.
 
@@ -292,6 +310,109 @@ k_mg0_prolong(const OpT<T> c, T *z, const MGLevel<T> L1, const int *gate) {
     if (fl != FLUID && fl != GHOST) return;
     if (c.p_singular && P == c.pinned) return;
     z[P] += prolong_value(L1, i, j, k);
+}
+
+// Restriction when level 1 halves every axis: one thread per fine (j, k)
+// and coarse plane I (both fine planes 2I, 2I+1), the k pair summed by a
+// lane shuffle and the j pair through shared memory, so every load is a
+// coalesced row and the whole fine grid is in flight at once.  Grid
+// (ceil(nz/32), ceil(ny/8), L1.nx) of 32 x 8 threads.
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_mg0_restrict2(const OpT<T> c, const T *__restrict__ r, const T *__restrict__ z, MGLevel<T> L1, const int *gate) {
+    MG_GATE(gate);
+    __shared__ T part[8][33];
+    const Grid &g = c.g;
+    const int k = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 8 + threadIdx.y, I = blockIdx.z;
+    T acc = 0;
+    if (j < g.ny && k < g.nz) {
+        const int Jj = j + 2, Kk = k + 2;
+        const T vyz = c.d[1][Jj] * c.d[2][Kk];
+        const T kyz = c.ks[1][Jj] + c.ks[2][Kk];
+        const T kmy = c.km[1][Jj], kpy = c.kp[1][Jj], kmz = c.km[2][Kk], kpz = c.kp[2][Kk];
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int i = 2 * I + h;
+            if (i >= g.nx) break;
+            const long long P = cidx(g, i, j, k);
+            if (c.flag[P] != FLUID || (c.p_singular && P == c.pinned)) continue;
+            const int Ii = i + 2;
+            const T nb = c.km[0][Ii] * z[P - g.sx] + c.kp[0][Ii] * z[P + g.sx] + kmy * z[P - g.sy] +
+                         kpy * z[P + g.sy] + kmz * z[P - 1] + kpz * z[P + 1];
+            const T res = r[P] - (z[P] - c.dinv[P] * nb);
+            acc += c.d[0][Ii] * vyz * (c.ks[0][Ii] + kyz) * res;
+        }
+    }
+    acc += __shfl_down_sync(0xffffffffu, acc, 1);
+    part[threadIdx.y][threadIdx.x] = acc;
+    __syncthreads();
+    if ((threadIdx.y & 1) || (threadIdx.x & 1)) return;
+    const int J = blockIdx.y * 4 + (threadIdx.y >> 1), K = blockIdx.x * 16 + (threadIdx.x >> 1);
+    if (J < L1.ny && K < L1.nz) L1.R[lidx(L1, I, J, K)] = part[threadIdx.y][threadIdx.x] + part[threadIdx.y + 1][threadIdx.x];
+}
+
+// Prolongation when level 1 halves every axis: the block's fine tile (one
+// plane, 8 j x 32 k) reads its coarse neighbourhood (the two coarse planes
+// it touches, 6 x 18 cells of each) into shared memory once; the few
+// neighbours outside it (periodic wraps) are read from global memory.
+// Same arithmetic and order as prolong_value.
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_mg0_prolong2(const OpT<T> c, T *z, const MGLevel<T> C, const int *gate) {
+    MG_GATE(gate);
+    constexpr int TJ = 6, TK = 18;
+    __shared__ T tz[2][TJ][TK], ta[2][TJ][TK];
+    const int i = blockIdx.z;
+    const int k0 = blockIdx.x * 32, j0 = blockIdx.y * 8;
+    const int Jmin = (j0 >> 1) - 1, Kmin = (k0 >> 1) - 1;
+    const int Ipl[2] = {i >> 1, C.po[0][i]};
+    const int t = threadIdx.y * 32 + threadIdx.x;
+    if (t < 2 * TJ * TK) {
+        const int pl = t / (TJ * TK), jj = (t / TK) % TJ, kk = t % TK;
+        const int Ic = Ipl[pl], Jc = Jmin + jj, Kc = Kmin + kk;
+        T zv = 0, av = 0;
+        if (Ic >= 0 && Jc >= 0 && Jc < C.ny && Kc >= 0 && Kc < C.nz) {
+            const long long q = lidx(C, Ic, Jc, Kc);
+            zv = C.Z[q];
+            av = C.diag[q] == (T)0 ? (T)0 : (T)1;
+        }
+        tz[pl][jj][kk] = zv;
+        ta[pl][jj][kk] = av;
+    }
+    __syncthreads();
+    const int k = k0 + threadIdx.x, j = j0 + threadIdx.y;
+    if (k >= c.g.nz || j >= c.g.ny) return;
+    const long long P = cidx(c.g, i, j, k);
+    const uint8_t fl = c.flag[P];
+    if (fl != FLUID && fl != GHOST) return;
+    if (c.p_singular && P == c.pinned) return;
+    const int ys[2] = {j >> 1, C.po[1][j]}, zs[2] = {k >> 1, C.po[2][k]};
+    const T wx = C.pw[0][i], wy = C.pw[1][j], wz = C.pw[2][k];
+    const T wxs[2] = {wx, (T)1 - wx}, wys[2] = {wy, (T)1 - wy}, wzs[2] = {wz, (T)1 - wz};
+    T acc = 0, ws = 0;
+#pragma unroll
+    for (int a = 0; a < 2; a++)
+#pragma unroll
+        for (int b = 0; b < 2; b++)
+#pragma unroll
+            for (int cc = 0; cc < 2; cc++) {
+                if (Ipl[a] < 0 || ys[b] < 0 || zs[cc] < 0) continue;
+                const int jj = ys[b] - Jmin, kk = zs[cc] - Kmin;
+                T zv, act;
+                if (jj >= 0 && jj < TJ && kk >= 0 && kk < TK) {
+                    zv = tz[a][jj][kk];
+                    act = ta[a][jj][kk];
+                } else {
+                    const long long q = lidx(C, Ipl[a], ys[b], zs[cc]);
+                    zv = C.Z[q];
+                    act = C.diag[q] == (T)0 ? (T)0 : (T)1;
+                }
+                if (act == (T)0) continue;
+                const T w = wxs[a] * wys[b] * wzs[cc];
+                acc += w * zv;
+                ws += w;
+            }
+    z[P] += ws > (T)0 ? acc / ws : (T)0;
 }
 
 // ------------------------------------------------------ level building --
@@ -695,6 +816,20 @@ int GMG<T>::setup(cudaStream_t s, const OpT<double> &A64, const OpT<T> &A, const
     if (nghost > 0) ghost_tmp_ = (T *)dalloc(sizeof(T) * nghost, true);
     // Does any ghost interpolation stencil reach an outer cell?  Then the
     // ghost and outer rows of a sweep cannot share a launch.
+    {
+        std::vector<int> o1;
+        for (int i = -1; i <= g.nx; i++)
+            for (int j = -1; j <= g.ny; j++)
+                for (int k = -1; k <= g.nz; k++) {
+                    const int out = (i < 0 || i >= g.nx) + (j < 0 || j >= g.ny) + (k < 0 || k >= g.nz);
+                    if (out == 1) o1.push_back((int)cidx(g, i, j, k));
+                }
+        nout1_ = (int)o1.size();
+        outer1_ = (int *)dalloc(sizeof(int) * std::max<size_t>(1, o1.size()), true);
+        if (!outer1_) return -1;
+        if (!o1.empty())  // after dalloc's clearing, on the same stream (pageable source: staged at the call)
+            cudaMemcpyAsync(outer1_, o1.data(), sizeof(int) * o1.size(), cudaMemcpyHostToDevice, s);
+    }
     ghost_reads_outer_ = false;
     if (nghost > 0) {
         std::vector<int> gidx(8 * (size_t)nghost);
@@ -807,17 +942,30 @@ int GMG<T>::smooth0(cudaStream_t s, const T *r, T *z, int sweeps, bool from_zero
     const dim3 blk(32, 8, 1);
     const dim3 grd(seam ? (g.nz + 31) / 32 : (g.nz + 63) / 64, (g.ny + 7) / 8, (g.nx + MG0_PLANES - 1) / MG0_PLANES);
     int k = 0;
+    auto tb = [&](const char *nm) { return prof_ ? prof_->begin(nm) : -1; };
+    auto te = [&](int t) {
+        if (prof_) prof_->end(t);
+    };
     for (int it = 0; it < sweeps; it++) {
+        const int tc = tb("mg0_color");
         for (int col = 0; col < (seam ? 4 : 2); col++, k++) {
             if (it == 0 && col == 0 && from_zero)
-                k_mg0_init<T><<<nblk(g.ncell, 256), 256, 0, s>>>(A_, r, z, per, gate);
+                k_mg0_init3<T><<<dim3((g.nz + 35) / 32, (g.ny + 11) / 8, g.nx + 4), dim3(32, 8), 0, s>>>(A_, r, z,
+                                                                                                   per, gate);
             else
                 k_mg0_color<T><<<grd, blk, 0, s>>>(A_, r, z, col, seam ? 0 : 1, per, (T)cfg_.omega, gate);
         }
+        te(tc);
+        const int to = tb("mg0_outer_ghost");
         const int gb = (nghost_ + 255) / 256, ob = (A_.sw.nout + 255) / 256;
         if (!ghost_reads_outer_) {
-            k_mg0_outer<T><<<gb + ob, 256, 0, s>>>(A_, r, z, A_.sw.outer, A_.sw.nout, ghost_cell_, nghost_, gb,
-                                                  ghost_tmp_, gate);
+            // Before the last sweep only the layer-1 face cells (read by the
+            // next colour pass); after it every outer cell.
+            const bool last = it == sweeps - 1;
+            const int *ol = last ? A_.sw.outer : outer1_;
+            const int no = last ? A_.sw.nout : nout1_;
+            k_mg0_outer<T><<<gb + (no + 255) / 256, 256, 0, s>>>(A_, r, z, ol, no, ghost_cell_, nghost_, gb, ghost_tmp_,
+                                                                gate);
             k++;
         } else {  // a ghost stencil reaches an outer cell: ghosts first, outer rows after the scatter
             k_mg0_outer<T><<<gb, 256, 0, s>>>(A_, r, z, A_.sw.outer, 0, ghost_cell_, nghost_, gb, ghost_tmp_, gate);
@@ -831,6 +979,7 @@ int GMG<T>::smooth0(cudaStream_t s, const T *r, T *z, int sweeps, bool from_zero
             k_mg0_outer<T><<<ob, 256, 0, s>>>(A_, r, z, A_.sw.outer, A_.sw.nout, ghost_cell_, 0, 0, ghost_tmp_, gate);
             k++;
         }
+        te(to);
     }
     return k;
 }
@@ -849,10 +998,20 @@ void GMG<T>::apply(cudaStream_t s, const T *r, T *z, const int *gate) {
         return;
     }
     Per3 per{{per_[0], per_[1], per_[2]}};
+    auto tb = [&](const char *nm) { return prof_ ? prof_->begin(nm) : -1; };
+    auto te = [&](int t) {
+        if (prof_) prof_->end(t);
+    };
     k += smooth0(s, r, z, cfg_.nu_pre, true, gate);
     const MGLevel<T> &L1 = levels_[0];
-    k_mg0_restrict<T><<<l3_grid(L1.nx, L1.ny, L1.nz), l3_block(), 0, s>>>(A_, r, z, L1, gate);
+    int tp = tb("mg0_restrict");
+    if (L1.cx && L1.cy && L1.cz)
+        k_mg0_restrict2<T><<<dim3((g.nz + 31) / 32, (g.ny + 7) / 8, L1.nx), dim3(32, 8), 0, s>>>(A_, r, z, L1, gate);
+    else
+        k_mg0_restrict<T><<<l3_grid(L1.nx, L1.ny, L1.nz), l3_block(), 0, s>>>(A_, r, z, L1, gate);
     k++;
+    te(tp);
+    tp = tb("mgc_down");
     const int nl = (int)levels_.size();
     for (int l = 0; l < tail_; l++) {
         MGLevel<T> &L = levels_[l];
@@ -872,9 +1031,13 @@ void GMG<T>::apply(cudaStream_t s, const T *r, T *z, const int *gate) {
         k_mgc_restrict<T><<<l3_grid(C.nx, C.ny, C.nz), l3_block(), 0, s>>>(L, C, per, gate);
         k++;
     }
+    te(tp);
+    tp = tb("mg_tail");
     k_mg_tail<T><<<1, TAIL_THREADS, tail_smem_, s>>>(dlevels_, tail_, nl, cfg_.nuc_pre, cfg_.nuc_post,
                                                      cfg_.coarse_sweeps, per, gate);
     k++;
+    te(tp);
+    tp = tb("mgc_up");
     for (int l = tail_ - 1; l >= 0; l--) {
         MGLevel<T> &L = levels_[l];
         const int ncol = level_colors(L, per_);
@@ -884,8 +1047,14 @@ void GMG<T>::apply(cudaStream_t s, const T *r, T *z, const int *gate) {
             for (int col = 0; col < ncol; col++, k++)
                 k_mgc_color<T><<<cgrid(L, ncol), l3_block(), 0, s>>>(L, col, ncol == 2, per, gate);
     }
-    k_mg0_prolong<T><<<l3_grid(g.nx, g.ny, g.nz), l3_block(), 0, s>>>(A_, z, L1, gate);
+    te(tp);
+    tp = tb("mg0_prolong");
+    if (L1.cx && L1.cy && L1.cz)
+        k_mg0_prolong2<T><<<l3_grid(g.nx, g.ny, g.nz), l3_block(), 0, s>>>(A_, z, L1, gate);
+    else
+        k_mg0_prolong<T><<<l3_grid(g.nx, g.ny, g.nz), l3_block(), 0, s>>>(A_, z, L1, gate);
     k++;
+    te(tp);
     k += smooth0(s, r, z, cfg_.nu_post, false, gate);
     note_launches(k);
     launches_ = k;

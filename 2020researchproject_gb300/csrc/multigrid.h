@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "krylov.h"
+#include "prof.h"
 
 namespace ibm {
 
@@ -73,6 +74,9 @@ class GMG : public Preconditioner<T> {
         cfg_.coarse_sweeps = coarse;
     }
     int nlevels() const { return (int)levels_.size() + 1; }
+    // Stage timers for the phases of a V-cycle (used only while p->on,
+    // i.e. host-sequenced steps with profiling on).
+    void set_prof(Prof *p) { prof_ = p; }
     // Average device time (ms) of one fine-grid colour pass over r, z
     // (reps launches between CUDA events on s); bytes: its algorithmic
     // bytes (z read once, r, 1/coeffsum, flag read and z written for the
@@ -84,12 +88,18 @@ class GMG : public Preconditioner<T> {
     GMGConfig cfg_{};
     std::vector<MGLevel<T>> levels_;
     int tail_ = 0;
+    Prof *prof_ = nullptr;
     size_t tail_smem_ = 0;
     MGLevel<T> *dlevels_ = nullptr;
     const int *ghost_cell_ = nullptr;
     int nghost_ = 0;
     T *ghost_tmp_ = nullptr;
     bool ghost_reads_outer_ = false;
+    // Layer-1 face cells of the outer layers: the only outer cells the
+    // colour passes read (edges, corners and layer 2 are set after the
+    // last sweep of each smoothing).
+    int *outer1_ = nullptr;
+    int nout1_ = 0;
     int per_[3] = {0, 0, 0};
     std::vector<void *> allocs_;
     int launches_ = 0;

@@ -1496,6 +1496,8 @@ void IBMSolver_assemble(IBMSolver *s) {
         set_status(s, IBM3D_ECUDA, "multigrid setup failed");
         return;
     }
+    d->mg->set_prof(&d->prof);
+    d->mg32->set_prof(&d->prof);
     if (d->pc64.allocate(g.ncell, d->mg32) != 0) {
         set_status(s, IBM3D_ECUDA, "preconditioner workspace allocation failed");
         return;
