@@ -68,6 +68,21 @@ def icosphere(subdivisions: int, radius: float = 0.5, center=(0.0, 0.0, 0.0)):
     return v32, f
 
 
+def bumpy_sphere(subdivisions: int, radius: float = 0.5, amp: float = 0.25, center=(0.0, 0.0, 0.0)):
+    """A star-shaped body with dents and bulges: the icosphere's unit
+    vertices moved radially by 1 + amp (x^2 y - 0.5 z^2 x + 0.3 y z), a
+    polynomial (only +, -, *), so the mesh is the same on every IEEE host.
+    ``subdivisions=6`` gives 81,920 triangles, 7 gives 327,680.  Faces keep
+    the sphere's outward orientation (a radial map with a positive factor
+    preserves it)."""
+    v, f = icosphere(subdivisions, 1.0)
+    u = v.astype(np.float64)
+    x, y, z = u[:, 0], u[:, 1], u[:, 2]
+    fac = 1.0 + amp * (x * x * y - 0.5 * z * z * x + 0.3 * y * z)
+    w = u * (radius * fac)[:, None] + np.asarray(center, dtype=np.float64)
+    return w.astype(np.float32), f
+
+
 def box_union(boxes):
     """Triangulate axis-aligned boxes ``[(lo(3), hi(3)), ...]`` (12 triangles
     each, outward CCW).  Boxes must not overlap or touch: the reference's

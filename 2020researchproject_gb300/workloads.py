@@ -41,6 +41,19 @@ def icosphere_stl(subdivisions=5, radius=0.5, center=(0.0, 0.0, 0.0)):
     return path
 
 
+def bumpy_stl(subdivisions=6, radius=0.5):
+    """A large dented body (geometry.bumpy_sphere): 81,920 triangles for 6
+    subdivisions, 327,680 for 7."""
+    key = ("bumpy", subdivisions, radius)
+    path = _STL_CACHE.get(key)
+    if path is None or not os.path.exists(path):
+        fd, path = tempfile.mkstemp(prefix="bumpy%d_" % subdivisions, suffix=".stl")
+        os.close(fd)
+        geometry.write_stl(path, *geometry.bumpy_sphere(subdivisions, radius))
+        _STL_CACHE[key] = path
+    return path
+
+
 def cavity(n=64, Re=1000.0, dt=1e-3):
     f = geometry.uniform_faces(0.0, 1.0, n)
     return dict(name=f"cavity{n}", xf=f, yf=f.copy(), zf=f.copy(), re=Re, dt=dt,

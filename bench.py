@@ -373,6 +373,7 @@ def bench_gb300(args):
     if rank == 0 and world == 1 and not args.no_extras:
         line["ensemble"] = ensemble_arm(ibm, wl, args)
         line["serving"] = serving_arm(ibm, wl, args)
+        line["large_body_setup"] = large_body_arm(ibm, wl)
     if rank == 0 and world == 1 and not args.no_cpu:
         cv, done, secs, _ = run_cpu(case, lv, steps=2, warmup=0, threads=os.cpu_count() or 1, sample_budget_s=25)
         line["cpu_baseline"] = {"value": round(cv, 4), "unit": "Mcell-steps/s", "cores": os.cpu_count() or 1,
@@ -413,6 +414,26 @@ def ensemble_arm(ibm, wl, args, steps=5):
         for sv in solvers:
             sv.close()
     out["mixed_batched_vs_fp64_alone"] = round(out["mixed_batched"] / out["fp64_alone"], 3)
+    return out
+
+
+def large_body_arm(ibm, wl):
+    """Set-up at scale: assembly (closest-point transform, flags, ghost
+    stencils, operators, multigrid) of the sphere192x128x128 grid around a
+    dented body of 81,920 and 327,680 triangles, host wall time, after a
+    first assembly of the same case (warm caches and context)."""
+    out = {"grid": "192x128x128", "unit": "s"}
+    for sub in (6, 7):
+        case = wl.sphere()
+        case["stl"] = wl.bumpy_stl(sub)
+        times = []
+        for _ in range(2):
+            t0 = time.perf_counter()
+            s = wl.build_solver(ibm, case, tol=MOM_TOL, div_tol=DIV_TOL)
+            times.append(time.perf_counter() - t0)
+            ghosts = len(s.ghost_stencils()[0])
+            s.close()
+        out[f"triangles_{20 * 4 ** sub}"] = {"assemble_s": round(times[-1], 3), "ghost_cells": ghosts}
     return out
 
 

@@ -32,6 +32,25 @@ def load_golden(name):
     return out
 
 
+def case_stl(meta):
+    """Path of a golden case's body: a committed STL next to the fixtures,
+    or, for "stl_gen" cases (meshes too large to commit), the same mesh
+    regenerated into the temporary directory (deterministic: only +, -, *,
+    / and sqrt, so it is the mesh the fixture was made with)."""
+    if "stl_gen" not in meta:
+        return os.path.join(GOLDEN, meta["stl"])
+    import tempfile
+    gen = meta["stl_gen"]
+    path = os.path.join(tempfile.gettempdir(), f"ibm3d_golden_{gen}.stl")
+    if not os.path.exists(path):
+        geometry = importlib.import_module("2020researchproject_gb300.geometry")
+        assert gen.startswith("bumpy"), gen
+        tmp = path + f".{os.getpid()}"
+        geometry.write_stl(tmp, *geometry.bumpy_sphere(int(gen[5:])))
+        os.replace(tmp, path)
+    return path
+
+
 def rel_l2(a, b, mask=None):
     a = np.asarray(a, dtype=np.float64)
     b = np.asarray(b, dtype=np.float64)

@@ -33,6 +33,13 @@ def _stl(name, verts, faces):
     return path
 
 
+def _generated(gen):
+    """A mesh too large to commit, written to the temporary directory."""
+    path = os.path.join(tempfile.gettempdir(), f"ibm3d_golden_{gen}.stl")
+    geometry.write_stl(path, *geometry.bumpy_sphere(int(gen[5:])))
+    return path
+
+
 def cases():
     """Small cases that together put every boundary-condition type on every
     axis, a sphere and a box body, LES on periodic and wall boundaries,
@@ -106,6 +113,21 @@ def cases():
             bc=["S wall", "N wall"],
             bcfunc=["W velper ramp", "E velper ramp", "D vel pulse", "U press ramp"],
             stl=box, init="field"),
+        # A large body: 81,920 triangles with dents and bulges (the mesh is
+        # regenerated by the tests, not committed), W inflow, E outlet.
+        "bumpy_stl": dict(
+            grid=(40, 36, 36),
+            xf=gf.body_clustered_faces(-1.2, 1.6, 40, 0.0, 0.8, 1.5),
+            yf=gf.body_clustered_faces(-1.0, 1.0, 36, 0.0, 0.8, 1.5),
+            zf=gf.body_clustered_faces(-1.0, 1.0, 36, 0.0, 0.8, 1.5),
+            re=100, dt=0.01, calls=[1],
+            bc=["W vel 1 0 0", "E press 0", "S slip", "N slip", "D slip", "U slip"],
+            stl=_generated("bumpy6"), stl_gen="bumpy6", init="const 1 0 0 0",
+            # The first step from uniform flow past a large body has a steep
+            # pressure: a relative residual of 1e-12 still leaves 1e-8 in the
+            # fields, so the parity tests solve to 1e-14 (the reference's
+            # solve landed within 1e-11 of that).
+            solve_tol=1e-14),
         # Velocity-periodic x, all-periodic y, velocity D, pressure U, LES.
         "mixed_les": dict(
             grid=(10, 8, 12),
@@ -176,7 +198,9 @@ def run_case(name, c):
                 out[f"{f}_{s}"] = load(f"{f}_{s}.f64", "<f8", shape)
         meta = dict(c)
         meta.pop("xf"), meta.pop("yf"), meta.pop("zf")
-        if "stl" in meta:
+        if "stl_gen" in meta:
+            meta.pop("stl")
+        elif "stl" in meta:
             meta["stl"] = os.path.basename(meta["stl"])
         meta["force"] = list(meta.get("force", (0, 0, 0)))
         out["meta"] = np.array(json.dumps(meta))

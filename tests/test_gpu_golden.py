@@ -19,7 +19,7 @@ import numpy as np
 import pytest
 
 import valfuncs
-from conftest import GOLDEN, golden_cases, load_golden, rel_l2
+from conftest import GOLDEN, case_stl, golden_cases, load_golden, rel_l2
 
 pytestmark = pytest.mark.gpu
 
@@ -48,8 +48,8 @@ def build_case(ibm, case, tol=1e-12):
         s.set_bc(getattr(ibm, _DIR[face]), getattr(ibm, _BC[kind]), *valfuncs.BC_FUNCS[fn])
     if "forcefunc" in m:
         s.set_ext_force(*valfuncs.FORCE_FUNCS[m["forcefunc"]])
-    if "stl" in m:
-        s.set_obstacle(ibm.Polyhedron(os.path.join(GOLDEN, m["stl"])))
+    if "stl" in m or "stl_gen" in m:
+        s.set_obstacle(ibm.Polyhedron(case_stl(m)))
     s.set_linear_solver(ibm.SOLVER_BiCGSTAB, ibm.PRECOND_AMG, tol)
     s.assemble()
     s.init_flow_array(case["u1_0"], case["u2_0"], case["u3_0"], case["p_0"])
@@ -85,7 +85,7 @@ _MODES = {"fp64": "FP64", "mixed": "MIXED", "mixed_mg": "MIXED_MG"}
 @pytest.mark.parametrize("name", golden_cases())
 def test_steps_match_reference(ibm, name, precision):
     case = load_golden(name)
-    s = build_case(ibm, case)
+    s = build_case(ibm, case, tol=case["meta"].get("solve_tol", 1e-12))
     s.set_precision(getattr(ibm, _MODES[precision]))
     calls = case["meta"]["calls"]
     report = []

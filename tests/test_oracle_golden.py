@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 
 import valfuncs
-from conftest import GOLDEN, ROOT, golden_cases, load_golden, rel_l2
+from conftest import GOLDEN, ROOT, case_stl, golden_cases, load_golden, rel_l2
 
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 import oracle as orc  # noqa: E402
@@ -20,11 +20,11 @@ import oracle as orc  # noqa: E402
 def oracle_case(case, **extra):
     m = case["meta"]
     c = dict(xf=case["xf"], yf=case["yf"], zf=case["zf"], re=m["re"], dt=m["dt"], bc=m["bc"],
-             force=m["force"], tol=1e-12)
+             force=m["force"], tol=m.get("solve_tol", 1e-12))
     if "smag" in m:
         c["smag"] = m["smag"]
-    if "stl" in m:
-        c["stl"] = os.path.join(GOLDEN, m["stl"])
+    if "stl" in m or "stl_gen" in m:
+        c["stl"] = case_stl(m)
     if "bcfunc" in m:
         c["bc_funcs"] = [(b.split()[0], b.split()[1], valfuncs.BC_FUNCS[b.split()[2]]) for b in m["bcfunc"]]
     if "forcefunc" in m:
