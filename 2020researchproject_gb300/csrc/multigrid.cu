@@ -81,7 +81,7 @@ __device__ inline T prolong_value(const MGLevel<T> &C, int i, int j, int k) {
 // its colour.  init = 1 (colour 0 only, z undefined on entry) applies the
 // pass to z = 0: colour-0 cells get r, every other padded cell 0 (the
 // sweep over all cells then covers the whole array).
-constexpr int MG0_PLANES = 4;
+constexpr int MG0_PLANES = 2;
 
 template <typename T>
 __global__ void __launch_bounds__(256)
@@ -664,11 +664,13 @@ __global__ void __launch_bounds__(256) k_mgc_prolong(const MGLevel<T> C, MGLevel
 }
 
 // Whole V-cycle over levels [first, nlev) inside one thread block, with
-// every level's arrays copied into shared memory and one thread per cell
-// (levels of at most TAIL_THREADS cells).  R of level `first` is read from
-// global memory and its Z written back; the prolongation tables stay in
-// global memory.
+// every level's arrays copied into shared memory; each thread takes cells
+// tid, tid + TAIL_THREADS, ... (levels of at most TAIL_CELLS cells).  R of
+// level `first` is read from global memory and its Z written back; the
+// prolongation tables stay in global memory.
 constexpr int TAIL_THREADS = 1024;
+constexpr int TAIL_CELLS = TAIL_THREADS;
+constexpr size_t TAIL_SMEM_MAX = 200 * 1024;
 
 template <typename T>
 __global__ void __launch_bounds__(TAIL_THREADS)
@@ -696,33 +698,33 @@ k_mg_tail(const MGLevel<T> *__restrict__ lv, const int first, const int nlev, co
     __syncthreads();
     for (int l = first; l < nlev; l++) {
         const MGLevel<T> &G = lv[l], &L = loc[l - first];
-        if (tid < L.n) {
-            L.Tx[tid] = G.Tx[tid];
-            L.Ty[tid] = G.Ty[tid];
-            L.Tz[tid] = G.Tz[tid];
-            L.diag[tid] = G.diag[tid];
-            L.R[tid] = l == first ? G.R[tid] : (T)0;
-            L.Z[tid] = 0;
+        for (int c = tid; c < L.n; c += TAIL_THREADS) {
+            L.Tx[c] = G.Tx[c];
+            L.Ty[c] = G.Ty[c];
+            L.Tz[c] = G.Tz[c];
+            L.diag[c] = G.diag[c];
+            L.R[c] = l == first ? G.R[c] : (T)0;
+            L.Z[c] = 0;
         }
     }
     __syncthreads();
-    // This thread's cell on level l.
-    auto cell = [&](const MGLevel<T> &L, int &I, int &J, int &K) {
+    // Cell c of level L.
+    auto cell = [&](const MGLevel<T> &L, int c, int &I, int &J, int &K) {
         const int nyz = L.ny * L.nz;
-        I = tid / nyz;
-        const int rem = tid - I * nyz;
+        I = c / nyz;
+        const int rem = c - I * nyz;
         J = rem / L.nz;
         K = rem - J * L.nz;
-        return tid < L.n;
     };
     auto sweep = [&](const MGLevel<T> &L, int nsw) {
-        int I, J, K;
-        const bool own = cell(L, I, J, K);
-        const int col = own ? cell_color(I, J, K, L.nx, L.ny, L.nz, per.p) : -1;
         const int ncol = level_colors(L, per.p);
         for (int s = 0; s < nsw; s++)
-            for (int c = 0; c < ncol; c++) {
-                if (col == c) coarse_relax(L, I, J, K, per.p);
+            for (int col = 0; col < ncol; col++) {
+                for (int c = tid; c < L.n; c += TAIL_THREADS) {
+                    int I, J, K;
+                    cell(L, c, I, J, K);
+                    if (cell_color(I, J, K, L.nx, L.ny, L.nz, per.p) == col) coarse_relax(L, I, J, K, per.p);
+                }
                 __syncthreads();
             }
     };
@@ -731,20 +733,26 @@ k_mg_tail(const MGLevel<T> *__restrict__ lv, const int first, const int nlev, co
         sweep(L, l == nlev - 1 ? csweeps : nu1);
         if (l < nlev - 1) {
             const MGLevel<T> &C = loc[l + 1 - first];
-            int I, J, K;
-            if (cell(C, I, J, K)) C.R[tid] = coarse_restrict_value(L, C, I, J, K, per.p);
+            for (int c = tid; c < C.n; c += TAIL_THREADS) {
+                int I, J, K;
+                cell(C, c, I, J, K);
+                C.R[c] = coarse_restrict_value(L, C, I, J, K, per.p);
+            }
             __syncthreads();
         }
     }
     for (int l = nlev - 2; l >= first; l--) {
         const MGLevel<T> &L = loc[l - first], &C = loc[l + 1 - first];
-        int I, J, K;
-        if (cell(L, I, J, K) && L.diag[tid] != (T)0) L.Z[tid] += prolong_value(C, I, J, K);
+        for (int c = tid; c < L.n; c += TAIL_THREADS) {
+            int I, J, K;
+            cell(L, c, I, J, K);
+            if (L.diag[c] != (T)0) L.Z[c] += prolong_value(C, I, J, K);
+        }
         __syncthreads();
         sweep(L, nu2);
     }
     const MGLevel<T> &G = lv[first], &L = loc[0];
-    if (tid < L.n) G.Z[tid] = L.Z[tid];
+    for (int c = tid; c < L.n; c += TAIL_THREADS) G.Z[c] = L.Z[c];
 }
 
 // Shared memory the tail kernel needs for levels [first, nlev).
@@ -906,7 +914,9 @@ int GMG<T>::setup(cudaStream_t s, const OpT<double> &A64, const OpT<T> &A, const
     }
     // The coarsest levels with at most TAIL_THREADS cells each run in the tail.
     tail_ = (int)levels_.size() - 1;
-    while (tail_ > 0 && levels_[tail_ - 1].n <= TAIL_THREADS && (int)levels_.size() - (tail_ - 1) <= 16) tail_--;
+    while (tail_ > 0 && levels_[tail_ - 1].n <= TAIL_CELLS && (int)levels_.size() - (tail_ - 1) <= 16 &&
+           tail_bytes(levels_, tail_ - 1) <= TAIL_SMEM_MAX)
+        tail_--;
     if (!levels_.empty()) {
         tail_smem_ = tail_bytes(levels_, tail_);
         // The limit is a property of the kernel, shared by every solver in
