@@ -94,6 +94,7 @@ def load_library(path: str = LIB_PATH):
         "IBMSolver_set_bc_func": (None, [vp, i, i, vp, vp, vp, vp]),
         "IBMSolver_set_refinement": (None, [vp, d, d, i]),
         "IBMSolver_set_gmres_restart": (None, [vp, i]),
+        "IBMSolver_autotune": (d, [vp, i, ip]),
         "IBMSolver_set_ext_force_func": (None, [vp, vp, vp, vp]),
         "IBMSolver_set_smagorinsky": (None, [vp, d]),
         "IBMSolver_set_obstacle": (None, [vp, vp]),
@@ -298,6 +299,14 @@ class IBMSolver:
         ms = self._lib.IBMSolver_time_kernel(self._s, code, int(reps), ctypes.byref(b))
         self._check("IBMSolver_time_kernel")
         return ms, b.value
+
+    def autotune(self, steps=2):
+        """Picks the multigrid sweeps by timing `steps` steps per candidate
+        (state restored afterwards); returns (ms per step, sweeps)."""
+        best = np.zeros(5, dtype=np.int32)
+        ms = self._lib.IBMSolver_autotune(self._s, int(steps), _ptr(best))
+        self._check("autotune")
+        return ms, tuple(int(v) for v in best)
 
     def set_gmres_restart(self, restart=10):
         self._lib.IBMSolver_set_gmres_restart(self._s, restart)

@@ -2138,6 +2138,66 @@ double IBMSolver_time_iterate(IBMSolver *s, int nsteps) {
     return ms;
 }
 
+// Picks the pressure multigrid's smoother sweeps for this case and
+// arithmetic mode by measurement: from the current state, each candidate
+// runs `steps` recorded steps (after one untimed step that records its
+// graphs) and the fastest wins.  The state (every field a step reads, time
+// and iteration count) is restored after each trial and at the end, so the
+// run continues exactly as if the tuner had not run.
+double IBMSolver_autotune(IBMSolver *s, int steps, int *best_out) {
+    if (!check_ready(s, "IBMSolver_autotune")) return -1;
+    ibm3d_device *d = s->dev;
+    if (steps < 1) steps = 1;
+    static const int cand[][5] = {{5, 5, 1, 1, 8}, {4, 4, 1, 1, 8}, {6, 6, 1, 1, 8}, {3, 3, 1, 1, 8},
+                                  {4, 4, 2, 2, 8}, {3, 3, 2, 2, 8}, {5, 5, 2, 2, 16}, {2, 2, 2, 2, 8}};
+    const int ncand = (int)(sizeof cand / sizeof cand[0]);
+    const size_t n = (size_t)d->g.ncell;
+    double *save = nullptr;
+    if (!cuda_check(s, cudaMalloc(&save, sizeof(double) * n * kStateFields), "autotune state")) return -1;
+    // By role (the steps swap the buffers behind the roles).
+    auto copy_state = [&](bool out) {
+        double *fld[kStateFields];
+        state_fields(d, fld);
+        for (int q = 0; q < kStateFields; q++)
+            cudaMemcpyAsync(out ? save + q * n : fld[q], out ? fld[q] : save + q * n, sizeof(double) * n,
+                            cudaMemcpyDeviceToDevice, d->s);
+    };
+    copy_state(true);
+    const int iter0 = s->iter;
+    const double time0 = s->time;
+    const double omega = d->mg_omega;
+    int keep[5];
+    for (int q = 0; q < 5; q++) keep[q] = d->mg_sweeps[q];
+    double best = -1;
+    int bi = -1;
+    for (int c = 0; c < ncand && d->status != IBM3D_ECUDA; c++) {
+        IBMSolver_set_multigrid(s, cand[c][0], cand[c][1], cand[c][2], cand[c][3], cand[c][4], omega);
+        copy_state(false);
+        s->iter = iter0;
+        s->time = time0;
+        IBMSolver_iterate(s, 1, false);  // records this configuration's graphs
+        copy_state(false);
+        s->iter = iter0;
+        s->time = time0;
+        const double ms = IBMSolver_time_iterate(s, steps) / steps;
+        if (d->status != IBM3D_OK && d->status != IBM3D_ENOCONV) break;
+        if (best < 0 || ms < best) {
+            best = ms;
+            bi = c;
+        }
+    }
+    const int *w = bi >= 0 ? cand[bi] : keep;
+    IBMSolver_set_multigrid(s, w[0], w[1], w[2], w[3], w[4], omega);
+    copy_state(false);
+    s->iter = iter0;
+    s->time = time0;
+    cuda_check(s, cudaStreamSynchronize(d->s), "autotune");
+    cudaFree(save);
+    if (best_out)
+        for (int q = 0; q < 5; q++) best_out[q] = w[q];
+    return best;
+}
+
 double IBMSolver_time_kernel(IBMSolver *s, int which, int reps, double *bytes) {
     if (!check_ready(s, "IBMSolver_time_kernel")) return -1;
     ibm3d_device *d = s->dev;

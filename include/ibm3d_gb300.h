@@ -91,6 +91,13 @@ void IBMSolver_set_multigrid(IBMSolver *, int nu_pre, int nu_post, int nuc_pre, 
    vector), so the FP32 multigrid of the mixed modes may precondition it. */
 void IBMSolver_set_gmres_restart(IBMSolver *, int restart);
 
+/* Autotuner: times `steps` recorded steps of this case, from its current
+   state, under each of a fixed set of multigrid sweep configurations
+   (fine pre/post, coarse pre/post, coarsest), keeps the fastest (written
+   to best[5] when best is not NULL) and returns its milliseconds per step.
+   The solver's state is restored, so the run continues unchanged. */
+double IBMSolver_autotune(IBMSolver *, int steps, int *best);
+
 /* Mixed path (IBM3D_MIXED): relative tolerance of each FP32 inner solve of
    the momentum and pressure refinement cycles, and the cycle cap.  The
    outer FP64 stopping rule is unchanged.  Defaults 1e-5, 1e-5, 12. */
