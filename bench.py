@@ -241,6 +241,10 @@ def _timed_arm(ibm, wl, case, precision, args, world, u0, headline=False):
     setup_s = time.perf_counter() - t0
     s.init_flow_array(*u0)
     tuned = None
+    if args.no_tune and precision == "mixed" and args.mixed_form == "MIXED_MG":
+        s.set_precision(ibm.MIXED_MG)
+    if args.no_tune and args.mg_sweeps:
+        s.set_multigrid(*[int(v) for v in args.mg_sweeps.split(",")], 1.0)
     if not args.no_tune:
         # The autotuner picks the multigrid sweeps (and, for the mixed step,
         # which of the two mixed solver forms) from the state after one
@@ -488,7 +492,10 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-extras", action="store_true", help="skip the ensemble and serving measurements")
-    ap.add_argument("--no-tune", action="store_true", help="default multigrid sweeps, no autotuning")
+    ap.add_argument("--no-tune", action="store_true", help="no autotuning: default (or the given) settings")
+    ap.add_argument("--mixed-form", default="MIXED", choices=["MIXED", "MIXED_MG"],
+                    help="with --no-tune: the mixed step's solver form")
+    ap.add_argument("--mg-sweeps", default="", help="with --no-tune: multigrid sweeps 'pre,post,cpre,cpost,coarsest'")
     ap.add_argument("--host-loop", action="store_true",
                     help="host-sequenced steps instead of recorded graphs (same kernels; for ncu launch lists, "
                          "which do not list kernels inside graph loops)")
