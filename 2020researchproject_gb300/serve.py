@@ -106,7 +106,7 @@ class Server:
         # re-recorded when jobs arrive or finish); True: one graph per
         # batched step, re-recorded on every membership change.
         self.combined = combined
-        self.mode = ibm.MIXED if precision == "mixed" else ibm.FP64
+        self.mode = {"mixed": ibm.MIXED, "mixed_mg": ibm.MIXED_MG}.get(precision, ibm.FP64)
         self.tol, self.div_tol = tol, div_tol
         self.hbm_budget = hbm_budget
         self.bytes_per_cell = bytes_per_cell
