@@ -37,7 +37,19 @@ struct Per3 {
 
 // Every V-cycle kernel returns at once while *gate (when given) is not
 // KS_RUN: the solve it serves has converged.
+// V-cycle kernels are launched with programmatic dependent launch: each
+// waits for its predecessor's results (griddepcontrol.wait) before any
+// read, then at once lets its successor's blocks be scheduled
+// (griddepcontrol.launch_dependents); a successor's blocks start only once
+// every block of this grid has started, and then wait at their own top.
+// This hides the launch gap between the many short kernels of a V-cycle.
+__device__ __forceinline__ void pdl_enter() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;");
+}
+
 #define MG_GATE(gate)                       \
+    pdl_enter();                            \
     if ((gate) && *(gate) != KS_RUN) return;
 
 template <typename T>
@@ -272,6 +284,23 @@ static inline dim3 l3_block() { return dim3(L3_TK, L3_TJ, 1); }
     const int J = blockIdx.y * L3_TJ + threadIdx.y;                     \
     const int I = blockIdx.z;                                           \
     if (K >= (NZ) || J >= (NY)) return;
+
+// Launch with the programmatic-stream-serialization attribute (see
+// pdl_enter); the kernels still wait for their predecessor before reading.
+template <typename... KArgs, typename... Args>
+static void launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
+}
 
 // Residual of the fine normalised rows, scaled to conductance form
 // (Vol * coeffsum * r) and summed into the level-1 cells.
@@ -960,10 +989,10 @@ int GMG<T>::smooth0(cudaStream_t s, const T *r, T *z, int sweeps, bool from_zero
         const int tc = tb("mg0_color");
         for (int col = 0; col < (seam ? 4 : 2); col++, k++) {
             if (it == 0 && col == 0 && from_zero)
-                k_mg0_init3<T><<<dim3((g.nz + 35) / 32, (g.ny + 11) / 8, g.nx + 4), dim3(32, 8), 0, s>>>(A_, r, z,
+                launch_pdl(k_mg0_init3<T>, dim3((g.nz + 35) / 32, (g.ny + 11) / 8, g.nx + 4), dim3(32, 8), 0, s, A_, r, z,
                                                                                                    per, gate);
             else
-                k_mg0_color<T><<<grd, blk, 0, s>>>(A_, r, z, col, seam ? 0 : 1, per, (T)cfg_.omega, gate);
+                launch_pdl(k_mg0_color<T>, grd, blk, 0, s, A_, r, z, col, seam ? 0 : 1, per, (T)cfg_.omega, gate);
         }
         te(tc);
         const int to = tb("mg0_outer_ghost");
@@ -974,19 +1003,19 @@ int GMG<T>::smooth0(cudaStream_t s, const T *r, T *z, int sweeps, bool from_zero
             const bool last = it == sweeps - 1;
             const int *ol = last ? A_.sw.outer : outer1_;
             const int no = last ? A_.sw.nout : nout1_;
-            k_mg0_outer<T><<<gb + (no + 255) / 256, 256, 0, s>>>(A_, r, z, ol, no, ghost_cell_, nghost_, gb, ghost_tmp_,
+            launch_pdl(k_mg0_outer<T>, gb + (no + 255) / 256, 256, 0, s, A_, r, z, ol, no, ghost_cell_, nghost_, gb, ghost_tmp_,
                                                                 gate);
             k++;
         } else {  // a ghost stencil reaches an outer cell: ghosts first, outer rows after the scatter
-            k_mg0_outer<T><<<gb, 256, 0, s>>>(A_, r, z, A_.sw.outer, 0, ghost_cell_, nghost_, gb, ghost_tmp_, gate);
+            launch_pdl(k_mg0_outer<T>, gb, 256, 0, s, A_, r, z, A_.sw.outer, 0, ghost_cell_, nghost_, gb, ghost_tmp_, gate);
             k++;
         }
         if (nghost_ > 0) {
-            k_mg0_ghost_scatter<T><<<nblk(nghost_, 128), 128, 0, s>>>(ghost_cell_, nghost_, ghost_tmp_, z, gate);
+            launch_pdl(k_mg0_ghost_scatter<T>, nblk(nghost_, 128), 128, 0, s, ghost_cell_, nghost_, ghost_tmp_, z, gate);
             k++;
         }
         if (ghost_reads_outer_) {
-            k_mg0_outer<T><<<ob, 256, 0, s>>>(A_, r, z, A_.sw.outer, A_.sw.nout, ghost_cell_, 0, 0, ghost_tmp_, gate);
+            launch_pdl(k_mg0_outer<T>, ob, 256, 0, s, A_, r, z, A_.sw.outer, A_.sw.nout, ghost_cell_, 0, 0, ghost_tmp_, gate);
             k++;
         }
         te(to);
@@ -1016,9 +1045,9 @@ void GMG<T>::apply(cudaStream_t s, const T *r, T *z, const int *gate) {
     const MGLevel<T> &L1 = levels_[0];
     int tp = tb("mg0_restrict");
     if (L1.cx && L1.cy && L1.cz)
-        k_mg0_restrict2<T><<<dim3((g.nz + 31) / 32, (g.ny + 7) / 8, L1.nx), dim3(32, 8), 0, s>>>(A_, r, z, L1, gate);
+        launch_pdl(k_mg0_restrict2<T>, dim3((g.nz + 31) / 32, (g.ny + 7) / 8, L1.nx), dim3(32, 8), 0, s, A_, r, z, L1, gate);
     else
-        k_mg0_restrict<T><<<l3_grid(L1.nx, L1.ny, L1.nz), l3_block(), 0, s>>>(A_, r, z, L1, gate);
+        launch_pdl(k_mg0_restrict<T>, l3_grid(L1.nx, L1.ny, L1.nz), l3_block(), 0, s, A_, r, z, L1, gate);
     k++;
     te(tp);
     tp = tb("mgc_down");
@@ -1030,20 +1059,20 @@ void GMG<T>::apply(cudaStream_t s, const T *r, T *z, const int *gate) {
         for (int it = 0; it < cfg_.nuc_pre; it++)
             for (int col = 0; col < ncol; col++, k++) {
                 if (it == 0 && col == 0)
-                    k_mgc_init<T><<<l3_grid(L.nx, L.ny, L.nz), l3_block(), 0, s>>>(L, per, gate);
+                    launch_pdl(k_mgc_init<T>, l3_grid(L.nx, L.ny, L.nz), l3_block(), 0, s, L, per, gate);
                 else
-                    k_mgc_color<T><<<cgrid(L, ncol), l3_block(), 0, s>>>(L, col, ncol == 2, per, gate);
+                    launch_pdl(k_mgc_color<T>, cgrid(L, ncol), l3_block(), 0, s, L, col, ncol == 2, per, gate);
             }
         if (cfg_.nuc_pre == 0) {
-            k_fill0<T><<<nblk(L.n, 256), 256, 0, s>>>(L.Z, L.n, gate);
+            launch_pdl(k_fill0<T>, nblk(L.n, 256), 256, 0, s, L.Z, L.n, gate);
             k++;
         }
-        k_mgc_restrict<T><<<l3_grid(C.nx, C.ny, C.nz), l3_block(), 0, s>>>(L, C, per, gate);
+        launch_pdl(k_mgc_restrict<T>, l3_grid(C.nx, C.ny, C.nz), l3_block(), 0, s, L, C, per, gate);
         k++;
     }
     te(tp);
     tp = tb("mg_tail");
-    k_mg_tail<T><<<1, TAIL_THREADS, tail_smem_, s>>>(dlevels_, tail_, nl, cfg_.nuc_pre, cfg_.nuc_post,
+    launch_pdl(k_mg_tail<T>, 1, TAIL_THREADS, tail_smem_, s, dlevels_, tail_, nl, cfg_.nuc_pre, cfg_.nuc_post,
                                                      cfg_.coarse_sweeps, per, gate);
     k++;
     te(tp);
@@ -1051,18 +1080,18 @@ void GMG<T>::apply(cudaStream_t s, const T *r, T *z, const int *gate) {
     for (int l = tail_ - 1; l >= 0; l--) {
         MGLevel<T> &L = levels_[l];
         const int ncol = level_colors(L, per_);
-        k_mgc_prolong<T><<<l3_grid(L.nx, L.ny, L.nz), l3_block(), 0, s>>>(levels_[l + 1], L, gate);
+        launch_pdl(k_mgc_prolong<T>, l3_grid(L.nx, L.ny, L.nz), l3_block(), 0, s, levels_[l + 1], L, gate);
         k++;
         for (int it = 0; it < cfg_.nuc_post; it++)
             for (int col = 0; col < ncol; col++, k++)
-                k_mgc_color<T><<<cgrid(L, ncol), l3_block(), 0, s>>>(L, col, ncol == 2, per, gate);
+                launch_pdl(k_mgc_color<T>, cgrid(L, ncol), l3_block(), 0, s, L, col, ncol == 2, per, gate);
     }
     te(tp);
     tp = tb("mg0_prolong");
     if (L1.cx && L1.cy && L1.cz)
-        k_mg0_prolong2<T><<<l3_grid(g.nx, g.ny, g.nz), l3_block(), 0, s>>>(A_, z, L1, gate);
+        launch_pdl(k_mg0_prolong2<T>, l3_grid(g.nx, g.ny, g.nz), l3_block(), 0, s, A_, z, L1, gate);
     else
-        k_mg0_prolong<T><<<l3_grid(g.nx, g.ny, g.nz), l3_block(), 0, s>>>(A_, z, L1, gate);
+        launch_pdl(k_mg0_prolong<T>, l3_grid(g.nx, g.ny, g.nz), l3_block(), 0, s, A_, z, L1, gate);
     k++;
     te(tp);
     k += smooth0(s, r, z, cfg_.nu_post, false, gate);
