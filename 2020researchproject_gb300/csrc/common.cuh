@@ -186,6 +186,35 @@ __host__ __device__ inline long long periodic_image(const Grid &g, int i, int j,
     return cidx(g, i, j, k);
 }
 
+// ------------------------------------------------ dependent launches --
+// The step's kernels are launched with programmatic dependent launch: each
+// waits for its predecessor's results (griddepcontrol.wait) before any
+// read, then at once lets its successor's blocks be scheduled
+// (griddepcontrol.launch_dependents); a successor's blocks start only once
+// every block of this grid has started, and then wait at their own top.
+// This hides the launch gap between the many short kernels of a solve.
+// Launched without the attribute, both instructions do nothing.
+__device__ __forceinline__ void pdl_enter() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;");
+}
+
+// Launch with the programmatic-stream-serialization attribute.
+template <typename... KArgs, typename... Args>
+inline void launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
+}
+
 // ------------------------------------------------------------ reductions --
 // Deterministic two-level reductions: every block writes its partials to
 // partials[block][v]; the last block to finish reduces them in a fixed

@@ -111,6 +111,7 @@ __global__ void __launch_bounds__(KTHREADS)
 k_bicg_init(const long long n, const T *__restrict__ b, T *x, T *r, T *r0, T *p, T *v, KScal *sc, double *partials,
             unsigned int *counter, const double tol, const double divtol, const IRScal *__restrict__ outer,
             const double outer_tol, const double outer_divtol, const LoopCtl lc) {
+    pdl_enter();
     __shared__ double smem[32 * NC];
     typename AccT<T>::type a[NC];
 #pragma unroll
@@ -161,6 +162,7 @@ k_bicg_init(const long long n, const T *__restrict__ b, T *x, T *r, T *r0, T *p,
 template <typename T, int NC, bool VEC>
 __global__ void __launch_bounds__(KTHREADS)
 k_bicg_p(const long long n, const T *__restrict__ r, T *__restrict__ p, const T *__restrict__ v, const KScal *sc) {
+    pdl_enter();
 #pragma unroll
     for (int c = 0; c < NC; c++) {
         if (sc[c].state != KS_RUN) continue;
@@ -211,6 +213,7 @@ template <typename T, int NC>
 __global__ void __launch_bounds__(SW_THREADS)
 k_bicg_spmv_v(const OpT<T> A, const int op, const long long n, const T *__restrict__ ph, T *__restrict__ v,
               const T *__restrict__ r0, KScal *sc, double *partials, unsigned int *counter) {
+    pdl_enter();
     __shared__ double smem[32 * NC];
     typename AccT<T>::type a[NC];
     bool run[NC];
@@ -254,6 +257,7 @@ template <typename T, int NC, bool VEC>
 __global__ void __launch_bounds__(KTHREADS)
 k_bicg_s(const OpT<T> A, const long long n, const T *__restrict__ r, const T *__restrict__ v, T *__restrict__ s,
          KScal *sc, double *partials, unsigned int *counter) {
+    pdl_enter();
     __shared__ double smem[32 * (NC + 1)];
     typename AccT<T>::type a[NC];
 #pragma unroll
@@ -310,6 +314,7 @@ template <typename T, int NC>
 __global__ void __launch_bounds__(SW_THREADS)
 k_bicg_spmv_t(const OpT<T> A, const int op, const long long n, const T *__restrict__ sh, T *__restrict__ t,
               const T *__restrict__ s, KScal *sc, double *partials, unsigned int *counter) {
+    pdl_enter();
     __shared__ double smem[32 * 2 * NC];
     typename AccT<T>::type a[2 * NC];
     bool run[NC];
@@ -359,6 +364,7 @@ __global__ void __launch_bounds__(KTHREADS)
 k_bicg_xr(const OpT<T> A, const long long n, T *__restrict__ x, T *__restrict__ r, const T *__restrict__ r0,
           const T *__restrict__ ph, const T *__restrict__ sh, const T *__restrict__ s, const T *__restrict__ t,
           KScal *sc, double *partials, unsigned int *counter, const int maxit, const LoopCtl lc) {
+    pdl_enter();
     __shared__ double smem[32 * (2 * NC + 1)];
     typename AccT<T>::type a[2 * NC];
 #pragma unroll
@@ -445,6 +451,7 @@ k_bicg_xr(const OpT<T> A, const long long n, T *__restrict__ x, T *__restrict__ 
 template <typename T>
 __global__ void __launch_bounds__(SW_THREADS)
 k_apply(const OpT<T> A, const int op, const int comp, const T *__restrict__ x, T *y) {
+    pdl_enter();
     const bool run[1] = {true};
     sweep_rows<T, 1>(
         A, run, [&](int, long long P, int i, const Column<T> &q) { y[P] = interior_row(A, op, x, P, i, q); },
@@ -461,6 +468,7 @@ __global__ void __launch_bounds__(SW_THREADS)
 k_ir_residual(const OpT<double> A, const int op, const long long n, const double *__restrict__ b,
               const double *__restrict__ x, double *r, const int x_zero, IRScal *sc, const double tol,
               const double divtol, const int max_outer, double *partials, unsigned int *counter, const LoopCtl lc) {
+    pdl_enter();
     constexpr int NV = 3 * NC + 1;
     __shared__ double smem[32 * NV];
     double sm[2 * NC], mx[NC + 1];  // ||r||^2, ||b||^2 (x_zero only); max|r|, divergence max
@@ -521,6 +529,7 @@ k_ir_residual(const OpT<double> A, const int op, const long long n, const double
 template <int NC>
 __global__ void __launch_bounds__(KTHREADS)
 k_ir_to32(const long long n, const double *__restrict__ r, const IRScal *sc, float *b32) {
+    pdl_enter();
 #pragma unroll
     for (int c = 0; c < NC; c++) {
         const double s = sc[c].scale;
@@ -533,6 +542,7 @@ k_ir_to32(const long long n, const double *__restrict__ r, const IRScal *sc, flo
 template <int NC>
 __global__ void __launch_bounds__(KTHREADS)
 k_ir_update(const long long n, double *x, const float *__restrict__ e, IRScal *sc, const KScal *__restrict__ inner) {
+    pdl_enter();
 #pragma unroll
     for (int c = 0; c < NC; c++) {
         const double s = sc[c].scale;
@@ -648,10 +658,10 @@ template <typename T>
 static void launch_init(cudaStream_t st, KrylovWork<T> &w, const T *b, T *x, double tol, double divtol,
                         const IRScal *outer, double outer_tol, double outer_divtol, LoopCtl lc) {
     if (w.nc == 3)
-        k_bicg_init<T, 3><<<w.nblk, KTHREADS, 0, st>>>(w.n, b, x, w.r, w.r0, w.p, w.v, w.scal, w.partials,
+        launch_pdl(k_bicg_init<T, 3>, w.nblk, KTHREADS, 0, st, w.n, b, x, w.r, w.r0, w.p, w.v, w.scal, w.partials,
                                                        w.counter, tol, divtol, outer, outer_tol, outer_divtol, lc);
     else
-        k_bicg_init<T, 1><<<w.nblk, KTHREADS, 0, st>>>(w.n, b, x, w.r, w.r0, w.p, w.v, w.scal, w.partials,
+        launch_pdl(k_bicg_init<T, 1>, w.nblk, KTHREADS, 0, st, w.n, b, x, w.r, w.r0, w.p, w.v, w.scal, w.partials,
                                                        w.counter, tol, divtol, outer, outer_tol, outer_divtol, lc);
     note_launches(1);
 }
@@ -663,10 +673,10 @@ static void first_half(cudaStream_t st, const OpT<T> &A, int op, KrylovWork<T> &
     const int nc = w.nc;
     const int *gate = nc == 1 ? &w.scal[0].state : nullptr;
     const bool vec = n % 4 == 0;
-    if (nc == 3 && vec) k_bicg_p<T, 3, true><<<w.nblk, KTHREADS, 0, st>>>(n, w.r, w.p, w.v, w.scal);
-    else if (nc == 3) k_bicg_p<T, 3, false><<<w.nblk, KTHREADS, 0, st>>>(n, w.r, w.p, w.v, w.scal);
-    else if (vec) k_bicg_p<T, 1, true><<<w.nblk, KTHREADS, 0, st>>>(n, w.r, w.p, w.v, w.scal);
-    else k_bicg_p<T, 1, false><<<w.nblk, KTHREADS, 0, st>>>(n, w.r, w.p, w.v, w.scal);
+    if (nc == 3 && vec) launch_pdl(k_bicg_p<T, 3, true>, w.nblk, KTHREADS, 0, st, n, w.r, w.p, w.v, w.scal);
+    else if (nc == 3) launch_pdl(k_bicg_p<T, 3, false>, w.nblk, KTHREADS, 0, st, n, w.r, w.p, w.v, w.scal);
+    else if (vec) launch_pdl(k_bicg_p<T, 1, true>, w.nblk, KTHREADS, 0, st, n, w.r, w.p, w.v, w.scal);
+    else launch_pdl(k_bicg_p<T, 1, false>, w.nblk, KTHREADS, 0, st, n, w.r, w.p, w.v, w.scal);
     note_launches(1);
     if (M) {
         const int tm = prof_begin(pf, "mg_vcycle");
@@ -675,17 +685,17 @@ static void first_half(cudaStream_t st, const OpT<T> &A, int op, KrylovWork<T> &
     }
     const int tm = prof_begin(pf, op == OP_MOM ? "spmv_mom" : "spmv_p");
     if (nc == 3)
-        k_bicg_spmv_v<T, 3><<<A.sw.nblocks, SW_THREADS, 0, st>>>(A, op, n, w.ph, w.v, w.r0, w.scal, w.partials,
+        launch_pdl(k_bicg_spmv_v<T, 3>, A.sw.nblocks, SW_THREADS, 0, st, A, op, n, w.ph, w.v, w.r0, w.scal, w.partials,
                                                                 w.counter);
     else
-        k_bicg_spmv_v<T, 1><<<A.sw.nblocks, SW_THREADS, 0, st>>>(A, op, n, w.ph, w.v, w.r0, w.scal, w.partials,
+        launch_pdl(k_bicg_spmv_v<T, 1>, A.sw.nblocks, SW_THREADS, 0, st, A, op, n, w.ph, w.v, w.r0, w.scal, w.partials,
                                                                 w.counter);
     note_launches(1);
     prof_end(pf, tm);
-    if (nc == 3 && vec) k_bicg_s<T, 3, true><<<w.nblk, KTHREADS, 0, st>>>(A, n, w.r, w.v, w.s, w.scal, w.partials, w.counter);
-    else if (nc == 3) k_bicg_s<T, 3, false><<<w.nblk, KTHREADS, 0, st>>>(A, n, w.r, w.v, w.s, w.scal, w.partials, w.counter);
-    else if (vec) k_bicg_s<T, 1, true><<<w.nblk, KTHREADS, 0, st>>>(A, n, w.r, w.v, w.s, w.scal, w.partials, w.counter);
-    else k_bicg_s<T, 1, false><<<w.nblk, KTHREADS, 0, st>>>(A, n, w.r, w.v, w.s, w.scal, w.partials, w.counter);
+    if (nc == 3 && vec) launch_pdl(k_bicg_s<T, 3, true>, w.nblk, KTHREADS, 0, st, A, n, w.r, w.v, w.s, w.scal, w.partials, w.counter);
+    else if (nc == 3) launch_pdl(k_bicg_s<T, 3, false>, w.nblk, KTHREADS, 0, st, A, n, w.r, w.v, w.s, w.scal, w.partials, w.counter);
+    else if (vec) launch_pdl(k_bicg_s<T, 1, true>, w.nblk, KTHREADS, 0, st, A, n, w.r, w.v, w.s, w.scal, w.partials, w.counter);
+    else launch_pdl(k_bicg_s<T, 1, false>, w.nblk, KTHREADS, 0, st, A, n, w.r, w.v, w.s, w.scal, w.partials, w.counter);
     note_launches(1);
 }
 
@@ -700,10 +710,10 @@ static void second_half(cudaStream_t st, const OpT<T> &A, int op, KrylovWork<T> 
     }
     const int tm = prof_begin(pf, op == OP_MOM ? "spmv_mom" : "spmv_p");
     if (w.nc == 3)
-        k_bicg_spmv_t<T, 3><<<A.sw.nblocks, SW_THREADS, 0, st>>>(A, op, w.n, w.sh, w.t, w.s, w.scal, w.partials,
+        launch_pdl(k_bicg_spmv_t<T, 3>, A.sw.nblocks, SW_THREADS, 0, st, A, op, w.n, w.sh, w.t, w.s, w.scal, w.partials,
                                                                 w.counter);
     else
-        k_bicg_spmv_t<T, 1><<<A.sw.nblocks, SW_THREADS, 0, st>>>(A, op, w.n, w.sh, w.t, w.s, w.scal, w.partials,
+        launch_pdl(k_bicg_spmv_t<T, 1>, A.sw.nblocks, SW_THREADS, 0, st, A, op, w.n, w.sh, w.t, w.s, w.scal, w.partials,
                                                                 w.counter);
     note_launches(1);
     prof_end(pf, tm);
@@ -713,10 +723,10 @@ template <typename T>
 static void launch_xr(cudaStream_t st, const OpT<T> &A, KrylovWork<T> &w, T *x, int maxit, LoopCtl lc) {
 #define XR_ARGS A, w.n, x, w.r, w.r0, w.ph, w.sh, w.s, w.t, w.scal, w.partials, w.counter, maxit, lc
     const bool vec = w.n % 4 == 0;
-    if (w.nc == 3 && vec) k_bicg_xr<T, 3, true><<<w.nblk, KTHREADS, 0, st>>>(XR_ARGS);
-    else if (w.nc == 3) k_bicg_xr<T, 3, false><<<w.nblk, KTHREADS, 0, st>>>(XR_ARGS);
-    else if (vec) k_bicg_xr<T, 1, true><<<w.nblk, KTHREADS, 0, st>>>(XR_ARGS);
-    else k_bicg_xr<T, 1, false><<<w.nblk, KTHREADS, 0, st>>>(XR_ARGS);
+    if (w.nc == 3 && vec) launch_pdl(k_bicg_xr<T, 3, true>, w.nblk, KTHREADS, 0, st, XR_ARGS);
+    else if (w.nc == 3) launch_pdl(k_bicg_xr<T, 3, false>, w.nblk, KTHREADS, 0, st, XR_ARGS);
+    else if (vec) launch_pdl(k_bicg_xr<T, 1, true>, w.nblk, KTHREADS, 0, st, XR_ARGS);
+    else launch_pdl(k_bicg_xr<T, 1, false>, w.nblk, KTHREADS, 0, st, XR_ARGS);
 #undef XR_ARGS
     note_launches(1);
 }
@@ -724,29 +734,31 @@ static void launch_xr(cudaStream_t st, const OpT<T> &A, KrylovWork<T> &w, T *x, 
 static void launch_residual(cudaStream_t st, const OpT<double> &A64, int op, IRWork &w, const double *b,
                             const double *x, int x_zero, const SolveParams &prm, LoopCtl lc) {
     if (w.nc == 3)
-        k_ir_residual<3><<<A64.sw.nblocks, SW_THREADS, 0, st>>>(A64, op, w.n, b, x, w.r, x_zero, w.scal, prm.tol,
+        launch_pdl(k_ir_residual<3>, A64.sw.nblocks, SW_THREADS, 0, st, A64, op, w.n, b, x, w.r, x_zero, w.scal, prm.tol,
                                                                prm.divtol, prm.max_outer, w.partials, w.counter, lc);
     else
-        k_ir_residual<1><<<A64.sw.nblocks, SW_THREADS, 0, st>>>(A64, op, w.n, b, x, w.r, x_zero, w.scal, prm.tol,
+        launch_pdl(k_ir_residual<1>, A64.sw.nblocks, SW_THREADS, 0, st, A64, op, w.n, b, x, w.r, x_zero, w.scal, prm.tol,
                                                                prm.divtol, prm.max_outer, w.partials, w.counter, lc);
     note_launches(1);
 }
 
 static void launch_to32(cudaStream_t st, IRWork &w) {
-    if (w.nc == 3) k_ir_to32<3><<<w.nblk, KTHREADS, 0, st>>>(w.n, w.r, w.scal, w.b32);
-    else k_ir_to32<1><<<w.nblk, KTHREADS, 0, st>>>(w.n, w.r, w.scal, w.b32);
+    if (w.nc == 3) launch_pdl(k_ir_to32<3>, w.nblk, KTHREADS, 0, st, w.n, w.r, w.scal, w.b32);
+    else launch_pdl(k_ir_to32<1>, w.nblk, KTHREADS, 0, st, w.n, w.r, w.scal, w.b32);
     note_launches(1);
 }
 
 // ------------------------------------------- widened preconditioner --
 __global__ void __launch_bounds__(KTHREADS)
 k_narrow(const long long n, const double *__restrict__ r, float *r32, const int *gate) {
+    pdl_enter();
     if (gate && *gate != KS_RUN) return;
     GRID_STRIDE(P, n) r32[P] = (float)r[P];
 }
 
 __global__ void __launch_bounds__(KTHREADS)
 k_widen(const long long n, const float *__restrict__ z32, double *z, const int *gate) {
+    pdl_enter();
     if (gate && *gate != KS_RUN) return;
     GRID_STRIDE(P, n) z[P] = (double)z32[P];
 }
@@ -772,15 +784,15 @@ void WidenedPreconditioner::release() {
 }
 
 void WidenedPreconditioner::apply(cudaStream_t s, const double *r, double *z, const int *gate) {
-    k_narrow<<<nblk, KTHREADS, 0, s>>>(n, r, r32, gate);
+    launch_pdl(k_narrow, nblk, KTHREADS, 0, s, n, r, r32, gate);
     m32->apply(s, r32, z32, gate);
-    k_widen<<<nblk, KTHREADS, 0, s>>>(n, z32, z, gate);
+    launch_pdl(k_widen, nblk, KTHREADS, 0, s, n, z32, z, gate);
     note_launches(2);
 }
 
 static void launch_update(cudaStream_t st, IRWork &w, double *x) {
-    if (w.nc == 3) k_ir_update<3><<<w.nblk, KTHREADS, 0, st>>>(w.n, x, w.e32, w.scal, w.inner.scal);
-    else k_ir_update<1><<<w.nblk, KTHREADS, 0, st>>>(w.n, x, w.e32, w.scal, w.inner.scal);
+    if (w.nc == 3) launch_pdl(k_ir_update<3>, w.nblk, KTHREADS, 0, st, w.n, x, w.e32, w.scal, w.inner.scal);
+    else launch_pdl(k_ir_update<1>, w.nblk, KTHREADS, 0, st, w.n, x, w.e32, w.scal, w.inner.scal);
     note_launches(1);
 }
 
@@ -988,7 +1000,7 @@ int record_ir(cudaStream_t st, const cudaStream_t *aux, const OpT<double> &A64, 
 
 template <typename T>
 void apply_operator(cudaStream_t st, const OpT<T> &A, int op, int comp, const T *x, T *y) {
-    k_apply<T><<<A.sw.nblocks, SW_THREADS, 0, st>>>(A, op, comp, x, y);
+    launch_pdl(k_apply<T>, A.sw.nblocks, SW_THREADS, 0, st, A, op, comp, x, y);
     note_launches(1);
 }
 
@@ -1048,6 +1060,7 @@ __global__ void __launch_bounds__(SW_THREADS)
 k_gm_residual(const OpT<double> A, const int op, const double *__restrict__ b, const double *__restrict__ x,
               double *w, const int x_zero, GScal *gs, const double tol, const double divtol, const int m,
               const int maxit, double *partials, unsigned int *counter, const LoopCtl lc) {
+    pdl_enter();
     __shared__ double smem[32 * 2];
     double sm = 0.0, mx = 0.0;
     bool run[1] = {true};
@@ -1093,12 +1106,14 @@ k_gm_residual(const OpT<double> A, const int op, const double *__restrict__ b, c
 
 // Start of a cycle's Arnoldi loop: its condition.
 __global__ void k_gm_cycle(const GScal *gs, const LoopCtl lc) {
+    pdl_enter();
     if (threadIdx.x == 0 && blockIdx.x == 0) set_loop(lc, gs->state == GM_RUN);
 }
 
 // V[j] = vin = w * vscale.
 __global__ void __launch_bounds__(KTHREADS)
 k_gm_next(const long long n, const double *__restrict__ w, double *V, double *vin, const GScal *gs) {
+    pdl_enter();
     const double sc = gs->vscale;
     double *vj = V + (size_t)gs->j * n;
     GRID_STRIDE(P, n) {
@@ -1112,6 +1127,7 @@ k_gm_next(const long long n, const double *__restrict__ w, double *V, double *vi
 __global__ void __launch_bounds__(SW_THREADS)
 k_gm_spmv(const OpT<double> A, const int op, const long long n, const double *__restrict__ z, double *w, double *Z,
           const GScal *gs) {
+    pdl_enter();
     double *zj = Z + (size_t)gs->j * n;
     bool run[1] = {true};
     sweep_rows<double, 1>(
@@ -1131,6 +1147,7 @@ template <int MM>
 __global__ void __launch_bounds__(KTHREADS)
 k_gm_dots(const long long n, const double *__restrict__ V, const double *__restrict__ w, GScal *gs, const int pass,
           double *partials, unsigned int *counter) {
+    pdl_enter();
     __shared__ double smem[32 * MM];
     const int j = gs->j;
     double a[MM];
@@ -1156,6 +1173,7 @@ template <int MM>
 __global__ void __launch_bounds__(KTHREADS)
 k_gm_orth(const long long n, const double *__restrict__ V, double *w, GScal *gs, const int final_pass,
           double *partials, unsigned int *counter, const LoopCtl lc) {
+    pdl_enter();
     __shared__ double smem[32];
     __shared__ double cs_[MM];
     const int j = gs->j;
@@ -1209,6 +1227,7 @@ k_gm_orth(const long long n, const double *__restrict__ V, double *w, GScal *gs,
 // by every block for itself.
 __global__ void __launch_bounds__(KTHREADS)
 k_gm_update(const long long n, const double *__restrict__ Z, double *x, const GScal *gs) {
+    pdl_enter();
     __shared__ double y[GM_MAX];
     const int k = gs->j;
     if (threadIdx.x == 0) {
@@ -1230,7 +1249,7 @@ k_gm_update(const long long n, const double *__restrict__ Z, double *x, const GS
 
 static void gm_residual(cudaStream_t st, const OpT<double> &A, int op, GmresWork &w, const double *b,
                         const double *x, int x_zero, const SolveParams &prm, LoopCtl lc) {
-    k_gm_residual<<<A.sw.nblocks, SW_THREADS, 0, st>>>(A, op, b, x, w.w, x_zero, w.scal, prm.tol, prm.divtol, w.m,
+    launch_pdl(k_gm_residual, A.sw.nblocks, SW_THREADS, 0, st, A, op, b, x, w.w, x_zero, w.scal, prm.tol, prm.divtol, w.m,
                                                        prm.maxit, w.partials, w.counter, lc);
     note_launches(1);
 }
@@ -1239,7 +1258,7 @@ static void gm_residual(cudaStream_t st, const OpT<double> &A, int op, GmresWork
 static void gm_step(cudaStream_t st, const OpT<double> &A, int op, GmresWork &w, Preconditioner<double> *M,
                     Prof *pf, LoopCtl lc) {
     const long long n = w.n;
-    k_gm_next<<<w.nblk, KTHREADS, 0, st>>>(n, w.w, w.V, w.vin, w.scal);
+    launch_pdl(k_gm_next, w.nblk, KTHREADS, 0, st, n, w.w, w.V, w.vin, w.scal);
     note_launches(1);
     const double *z = w.vin;
     if (M) {
@@ -1249,20 +1268,20 @@ static void gm_step(cudaStream_t st, const OpT<double> &A, int op, GmresWork &w,
         z = w.zj;
     }
     const int tm = prof_begin(pf, "spmv_p");
-    k_gm_spmv<<<A.sw.nblocks, SW_THREADS, 0, st>>>(A, op, n, z, w.w, w.Z, w.scal);
+    launch_pdl(k_gm_spmv, A.sw.nblocks, SW_THREADS, 0, st, A, op, n, z, w.w, w.Z, w.scal);
     note_launches(1);
     prof_end(pf, tm);
     const int to = prof_begin(pf, "gmres_orth");
     for (int pass = 0; pass < 2; pass++) {
-        k_gm_dots<GM_MAX><<<w.nblk, KTHREADS, 0, st>>>(n, w.V, w.w, w.scal, pass, w.partials, w.counter);
-        k_gm_orth<GM_MAX><<<w.nblk, KTHREADS, 0, st>>>(n, w.V, w.w, w.scal, pass, w.partials, w.counter, lc);
+        launch_pdl(k_gm_dots<GM_MAX>, w.nblk, KTHREADS, 0, st, n, w.V, w.w, w.scal, pass, w.partials, w.counter);
+        launch_pdl(k_gm_orth<GM_MAX>, w.nblk, KTHREADS, 0, st, n, w.V, w.w, w.scal, pass, w.partials, w.counter, lc);
         note_launches(2);
     }
     prof_end(pf, to);
 }
 
 static void gm_update(cudaStream_t st, GmresWork &w, double *x) {
-    k_gm_update<<<w.nblk, KTHREADS, 0, st>>>(w.n, w.Z, x, w.scal);
+    launch_pdl(k_gm_update, w.nblk, KTHREADS, 0, st, w.n, w.Z, x, w.scal);
     note_launches(1);
 }
 
@@ -1311,7 +1330,7 @@ int record_gmres(cudaStream_t st, const cudaStream_t *aux, const OpT<double> &A,
         cudaStream_t bs = aux[0];
         LoopCtl inner;
         if (new_loop(bs, inner) != 0) return -1;
-        k_gm_cycle<<<1, 32, 0, bs>>>(w.scal, inner);
+        launch_pdl(k_gm_cycle, 1, 32, 0, bs, w.scal, inner);
         note_launches(1);
         if (begin_while(bs, inner, aux[1]) != 0) return -1;
         gm_step(aux[1], A, op, w, M, nullptr, inner);

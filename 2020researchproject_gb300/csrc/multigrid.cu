@@ -37,17 +37,6 @@ struct Per3 {
 
 // Every V-cycle kernel returns at once while *gate (when given) is not
 // KS_RUN: the solve it serves has converged.
-// V-cycle kernels are launched with programmatic dependent launch: each
-// waits for its predecessor's results (griddepcontrol.wait) before any
-// read, then at once lets its successor's blocks be scheduled
-// (griddepcontrol.launch_dependents); a successor's blocks start only once
-// every block of this grid has started, and then wait at their own top.
-// This hides the launch gap between the many short kernels of a V-cycle.
-__device__ __forceinline__ void pdl_enter() {
-    asm volatile("griddepcontrol.wait;" ::: "memory");
-    asm volatile("griddepcontrol.launch_dependents;");
-}
-
 #define MG_GATE(gate)                       \
     pdl_enter();                            \
     if ((gate) && *(gate) != KS_RUN) return;
@@ -284,23 +273,6 @@ static inline dim3 l3_block() { return dim3(L3_TK, L3_TJ, 1); }
     const int J = blockIdx.y * L3_TJ + threadIdx.y;                     \
     const int I = blockIdx.z;                                           \
     if (K >= (NZ) || J >= (NY)) return;
-
-// Launch with the programmatic-stream-serialization attribute (see
-// pdl_enter); the kernels still wait for their predecessor before reading.
-template <typename... KArgs, typename... Args>
-static void launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args... args) {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = grid;
-    cfg.blockDim = block;
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = s;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    at[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
-}
 
 // Residual of the fine normalised rows, scaled to conductance form
 // (Vol * coeffsum * r) and summed into the level-1 cells.
