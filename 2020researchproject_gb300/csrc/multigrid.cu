@@ -46,6 +46,46 @@ __host__ __device__ inline long long lidx(const MGLevel<T> &L, int I, int J, int
     return ((long long)I * L.ny + J) * L.nz + K;
 }
 
+// Whether a coarse diagonal marks an active cell, as an integer test on
+// its bits (inactive cells hold exactly +0), off the FP64 pipe.
+__device__ __forceinline__ bool active_bits(double d) { return __double_as_longlong(d) != 0; }
+__device__ __forceinline__ bool active_bits(float d) { return __float_as_int(d) != 0; }
+
+// Trilinear blend of the 8 coarse values v[a][b][c] (act: 1 active, 0
+// inactive or absent) with weights wxs[a] wys[b] wzs[c].  With all eight
+// active the weights sum to one: nested blend, no division (the common
+// case; FP64 division is slow on this part).  Otherwise the weights of the
+// active cells are renormalised.
+template <typename T>
+__device__ __forceinline__ T trilinear(const T (&v)[2][2][2], const bool (&act)[2][2][2], const T (&wxs)[2],
+                                       const T (&wys)[2], const T (&wzs)[2]) {
+    bool all = true;
+#pragma unroll
+    for (int a = 0; a < 2; a++)
+#pragma unroll
+        for (int b = 0; b < 2; b++)
+#pragma unroll
+            for (int c = 0; c < 2; c++) all = all && act[a][b][c];
+    if (all) {
+        const T y0 = wys[0] * (wzs[0] * v[0][0][0] + wzs[1] * v[0][0][1]) + wys[1] * (wzs[0] * v[0][1][0] + wzs[1] * v[0][1][1]);
+        const T y1 = wys[0] * (wzs[0] * v[1][0][0] + wzs[1] * v[1][0][1]) + wys[1] * (wzs[0] * v[1][1][0] + wzs[1] * v[1][1][1]);
+        return wxs[0] * y0 + wxs[1] * y1;
+    }
+    T acc = 0, ws = 0;
+#pragma unroll
+    for (int a = 0; a < 2; a++)
+#pragma unroll
+        for (int b = 0; b < 2; b++)
+#pragma unroll
+            for (int c = 0; c < 2; c++) {
+                if (!act[a][b][c]) continue;
+                const T w = wxs[a] * wys[b] * wzs[c];
+                acc += w * v[a][b][c];
+                ws += w;
+            }
+    return ws > (T)0 ? acc / ws : (T)0;
+}
+
 // Trilinear correction of fine cell (i, j, k) from coarse level C, over
 // active coarse cells only.
 template <typename T>
@@ -54,21 +94,22 @@ __device__ inline T prolong_value(const MGLevel<T> &C, int i, int j, int k) {
     const int xs[2] = {I, C.po[0][i]}, ys[2] = {J, C.po[1][j]}, zs[2] = {K, C.po[2][k]};
     const T wx = C.pw[0][i], wy = C.pw[1][j], wz = C.pw[2][k];
     const T wxs[2] = {wx, (T)1 - wx}, wys[2] = {wy, (T)1 - wy}, wzs[2] = {wz, (T)1 - wz};
-    T acc = 0, ws = 0;
+    T v[2][2][2];
+    bool act[2][2][2];
 #pragma unroll
     for (int a = 0; a < 2; a++)
 #pragma unroll
         for (int b = 0; b < 2; b++)
 #pragma unroll
             for (int c = 0; c < 2; c++) {
+                v[a][b][c] = 0;
+                act[a][b][c] = false;
                 if (xs[a] < 0 || ys[b] < 0 || zs[c] < 0) continue;
                 const long long q = lidx(C, xs[a], ys[b], zs[c]);
-                if (C.diag[q] == (T)0) continue;
-                const T w = wxs[a] * wys[b] * wzs[c];
-                acc += w * C.Z[q];
-                ws += w;
+                v[a][b][c] = C.Z[q];
+                act[a][b][c] = active_bits(C.diag[q]);
             }
-    return ws > (T)0 ? acc / ws : (T)0;
+    return trilinear(v, act, wxs, wys, wzs);
 }
 
 // ------------------------------------------------------------ level 0 --
@@ -356,13 +397,14 @@ k_mg0_restrict2(const OpT<T> c, const T *__restrict__ r, const T *__restrict__ z
 // plane, 8 j x 32 k) reads its coarse neighbourhood (the two coarse planes
 // it touches, 6 x 18 cells of each) into shared memory once; the few
 // neighbours outside it (periodic wraps) are read from global memory.
-// Same arithmetic and order as prolong_value.
+// Same arithmetic as prolong_value.
 template <typename T>
 __global__ void __launch_bounds__(256)
 k_mg0_prolong2(const OpT<T> c, T *z, const MGLevel<T> C, const int *gate) {
     MG_GATE(gate);
     constexpr int TJ = 6, TK = 18;
-    __shared__ T tz[2][TJ][TK], ta[2][TJ][TK];
+    __shared__ T tz[2][TJ][TK];
+    __shared__ bool ta[2][TJ][TK];
     const int i = blockIdx.z;
     const int k0 = blockIdx.x * 32, j0 = blockIdx.y * 8;
     const int Jmin = (j0 >> 1) - 1, Kmin = (k0 >> 1) - 1;
@@ -371,11 +413,12 @@ k_mg0_prolong2(const OpT<T> c, T *z, const MGLevel<T> C, const int *gate) {
     if (t < 2 * TJ * TK) {
         const int pl = t / (TJ * TK), jj = (t / TK) % TJ, kk = t % TK;
         const int Ic = Ipl[pl], Jc = Jmin + jj, Kc = Kmin + kk;
-        T zv = 0, av = 0;
+        T zv = 0;
+        bool av = false;
         if (Ic >= 0 && Jc >= 0 && Jc < C.ny && Kc >= 0 && Kc < C.nz) {
             const long long q = lidx(C, Ic, Jc, Kc);
             zv = C.Z[q];
-            av = C.diag[q] == (T)0 ? (T)0 : (T)1;
+            av = active_bits(C.diag[q]);
         }
         tz[pl][jj][kk] = zv;
         ta[pl][jj][kk] = av;
@@ -390,30 +433,28 @@ k_mg0_prolong2(const OpT<T> c, T *z, const MGLevel<T> C, const int *gate) {
     const int ys[2] = {j >> 1, C.po[1][j]}, zs[2] = {k >> 1, C.po[2][k]};
     const T wx = C.pw[0][i], wy = C.pw[1][j], wz = C.pw[2][k];
     const T wxs[2] = {wx, (T)1 - wx}, wys[2] = {wy, (T)1 - wy}, wzs[2] = {wz, (T)1 - wz};
-    T acc = 0, ws = 0;
+    T v[2][2][2];
+    bool act[2][2][2];
 #pragma unroll
     for (int a = 0; a < 2; a++)
 #pragma unroll
         for (int b = 0; b < 2; b++)
 #pragma unroll
             for (int cc = 0; cc < 2; cc++) {
+                v[a][b][cc] = 0;
+                act[a][b][cc] = false;
                 if (Ipl[a] < 0 || ys[b] < 0 || zs[cc] < 0) continue;
                 const int jj = ys[b] - Jmin, kk = zs[cc] - Kmin;
-                T zv, act;
                 if (jj >= 0 && jj < TJ && kk >= 0 && kk < TK) {
-                    zv = tz[a][jj][kk];
-                    act = ta[a][jj][kk];
+                    v[a][b][cc] = tz[a][jj][kk];
+                    act[a][b][cc] = ta[a][jj][kk];
                 } else {
                     const long long q = lidx(C, Ipl[a], ys[b], zs[cc]);
-                    zv = C.Z[q];
-                    act = C.diag[q] == (T)0 ? (T)0 : (T)1;
+                    v[a][b][cc] = C.Z[q];
+                    act[a][b][cc] = active_bits(C.diag[q]);
                 }
-                if (act == (T)0) continue;
-                const T w = wxs[a] * wys[b] * wzs[cc];
-                acc += w * zv;
-                ws += w;
             }
-    z[P] += ws > (T)0 ? acc / ws : (T)0;
+    z[P] += trilinear(v, act, wxs, wys, wzs);
 }
 
 // ------------------------------------------------------ level building --
