@@ -575,6 +575,12 @@ __global__ void k_mg_diag(MGLevel<double> L, const double *__restrict__ Gx, cons
     }
 }
 
+// 1 / diag of a level (computed in FP64), 0 for inactive cells.
+template <typename T>
+__global__ void k_inverse(const double *__restrict__ d, T *b, long long n) {
+    GRID_STRIDE(q, n) b[q] = d[q] == 0.0 ? (T)0 : (T)(1.0 / d[q]);
+}
+
 template <typename T>
 __global__ void k_convert(const double *__restrict__ a, T *b, long long n) {
     GRID_STRIDE(q, n) b[q] = (T)a[q];
@@ -591,7 +597,7 @@ __device__ inline void coarse_relax(const MGLevel<T> &L, int I, int J, int K, co
     }
     T s = L.R[q];
     for_neighbours(L, I, J, K, per, [&](long long m, T t) { s += t * L.Z[m]; });
-    L.Z[q] = s / d;
+    L.Z[q] = L.idiag ? s * L.idiag[q] : s / d;
 }
 
 template <typename T>
@@ -639,7 +645,7 @@ __global__ void __launch_bounds__(256) k_mgc_init(MGLevel<T> L, const Per3 per, 
     L3_INDEX(I, J, K, L.ny, L.nz);
     const long long q = lidx(L, I, J, K);
     const T d = L.diag[q];
-    L.Z[q] = (cell_color(I, J, K, L.nx, L.ny, L.nz, per.p) == 0 && d != (T)0) ? L.R[q] / d : (T)0;
+    L.Z[q] = (cell_color(I, J, K, L.nx, L.ny, L.nz, per.p) == 0 && d != (T)0) ? L.R[q] * L.idiag[q] : (T)0;
 }
 
 // Branch-free relaxation of coarse cell (I, J, K) on a level without
@@ -664,7 +670,7 @@ __device__ __forceinline__ void coarse_relax_open(const MGLevel<T> &L, int I, in
     s += (hn ? tn : (T)0) * zn;
     s += td * zd;
     s += (hu ? tu : (T)0) * zu;
-    L.Z[q] = d == (T)0 ? (T)0 : s / d;
+    L.Z[q] = d == (T)0 ? (T)0 : s * L.idiag[q];
 }
 
 // One colour pass on a coarse level; k pairs as on the fine grid when the
@@ -734,6 +740,7 @@ k_mg_tail(const MGLevel<T> *__restrict__ lv, const int first, const int nlev, co
             L.diag = q; q += n;
             L.R = q; q += n;
             L.Z = q; q += n;
+            L.idiag = nullptr;  // the tail divides by its shared-memory diag
             loc[l - first] = L;
         }
     }
@@ -944,7 +951,9 @@ int GMG<T>::setup(cudaStream_t s, const OpT<double> &A64, const OpT<T> &A, const
         const size_t bt = sizeof(T) * L.n;
         LT.Tx = (T *)dalloc(bt, true); LT.Ty = (T *)dalloc(bt, true); LT.Tz = (T *)dalloc(bt, true);
         LT.diag = (T *)dalloc(bt, true); LT.R = (T *)dalloc(bt, true); LT.Z = (T *)dalloc(bt, true);
-        if (!LT.Tx || !LT.Ty || !LT.Tz || !LT.diag || !LT.R || !LT.Z) return -1;
+        LT.idiag = (T *)dalloc(bt, true);
+        if (!LT.Tx || !LT.Ty || !LT.Tz || !LT.diag || !LT.R || !LT.Z || !LT.idiag) return -1;
+        k_inverse<T><<<nblk(L.n, 256), 256, 0, s>>>(L.diag, LT.idiag, L.n);
         k_convert<T><<<nblk(L.n, 256), 256, 0, s>>>(L.Tx, LT.Tx, L.n);
         k_convert<T><<<nblk(L.n, 256), 256, 0, s>>>(L.Ty, LT.Ty, L.n);
         k_convert<T><<<nblk(L.n, 256), 256, 0, s>>>(L.Tz, LT.Tz, L.n);

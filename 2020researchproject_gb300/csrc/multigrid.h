@@ -33,6 +33,7 @@ struct MGLevel {
     int cx, cy, cz;          // axis coarsened from the finer level
     T *Tx, *Ty, *Tz;         // conductance of the low face of each cell (wrap at 0 if periodic)
     T *diag;                 // sum of all couplings incl. Dirichlet boundaries; 0 = inactive
+    T *idiag;                // 1 / diag (0 = inactive), for the relaxations
     T *R, *Z;
     // Trilinear prolongation to the finer level, per axis, indexed by the
     // finer level's cell index: the second coarse cell (-1: none) and the
