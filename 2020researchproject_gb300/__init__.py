@@ -358,6 +358,16 @@ class IBMSolver:
         self._lib.IBMSolver_export_result(self._s, name.encode())
         self._check("export_result")
 
+    def export_lvset_flag(self, name):
+        """"<name>.nc": level set and flags over the padded grid."""
+        self._lib.IBMSolver_export_lvset_flag(self._s, name.encode())
+        self._check("export_lvset_flag")
+
+    def export_intermediate(self, name):
+        """"<name>.nc": the last step's u*, u~ and p'."""
+        self._lib.IBMSolver_export_intermediate(self._s, name.encode())
+        self._check("export_intermediate")
+
     # ---------------------------------------------------------- readback
     def _field_shape(self, name):
         nx, ny, nz = self.shape

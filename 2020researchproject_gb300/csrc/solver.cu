@@ -1777,36 +1777,95 @@ void IBMSolver_init_flow_file(IBMSolver *s, const char *name) {
     s->time = time;
 }
 
-void IBMSolver_export_lvset_flag(IBMSolver *s, const char *name) {
-    if (!check_ready(s, "IBMSolver_export_lvset_flag")) return;
-    std::string path = std::string(name) + ".lvset_flag";
-    FILE *f = fopen(path.c_str(), "wb");
-    if (!f) {
-        set_status(s, IBM3D_EARG, "cannot open file \"%s\"", path.c_str());
-        return;
-    }
-    const size_t n = (size_t)ncell_of(s);
-    fwrite(s->lvset, sizeof(double), n, f);
-    fwrite(s->flag, sizeof(int), n, f);
-    fclose(f);
+// Padded [i][j][k] cell array (solver layout) -> [k][j][i] (file layout).
+extern "C++" {
+namespace {
+template <typename Src, typename Dst>
+void to_file_layout(const IBMSolver *s, const Src *a, Dst *out) {
+    const int NX = s->Nx + 4, NY = s->Ny + 4, NZ = s->Nz + 4;
+    for (int i = 0; i < NX; i++)
+        for (int j = 0; j < NY; j++)
+            for (int k = 0; k < NZ; k++)
+                out[((size_t)k * NY + j) * NX + i] = (Dst)a[((size_t)i * NY + j) * NZ + k];
 }
 
+void coord_vars(IBMSolver *s, NcFile &f, int dx, int dy, int dz) {
+    f.vars.push_back({"x", NCT_DOUBLE, {dx}, {{"axis", "X"}, {"units", "meters"}}, s->xc});
+    f.vars.push_back({"y", NCT_DOUBLE, {dy}, {{"axis", "Y"}, {"units", "meters"}}, s->yc});
+    f.vars.push_back({"z", NCT_DOUBLE, {dz}, {{"axis", "Z"}, {"units", "meters"}}, s->zc});
+}
+}  // namespace
+}
+
+// src/ibm3d_export.c:262-435: "<name>.nc" with x, y, z and the level set
+// (float) and flags (int) as [z][y][x] over the padded grid.
+void IBMSolver_export_lvset_flag(IBMSolver *s, const char *name) {
+    if (!check_ready(s, "IBMSolver_export_lvset_flag")) return;
+    const size_t n = (size_t)ncell_of(s);
+    std::vector<int> flag(n);
+    IBMSolver_get_flag(s, flag.data());
+    std::vector<float> lv(n);
+    std::vector<int32_t> fl(n);
+    to_file_layout(s, s->lvset, lv.data());
+    to_file_layout(s, flag.data(), fl.data());
+    NcFile f;
+    f.dims = {{"x", s->Nx + 4}, {"y", s->Ny + 4}, {"z", s->Nz + 4}};
+    coord_vars(s, f, 0, 1, 2);
+    f.vars.push_back({"lvset", NCT_FLOAT, {2, 1, 0}, {}, lv.data()});
+    f.vars.push_back({"flag", NCT_INT, {2, 1, 0}, {}, fl.data()});
+    const std::string path = std::string(name) + ".nc";
+    if (!nc_write(path, f)) set_status(s, IBM3D_EARG, "cannot write file \"%s\"", path.c_str());
+}
+
+// src/ibm3d_export.c:437-650: "<name>.nc" with time, x, y, z, iter and the
+// last step's u*, u~ (per component) and p' as float [time][z][y][x].  u~
+// is not kept by the GPU step (it is folded into the face-velocity kernel),
+// so it is formed here as the reference's calc_u_tilde does
+// (src/ibm3d_fracstep.c:388-412): u* + dt (p(+1) - p(-1)) / (c(+1) - c(-1))
+// with the step's starting pressure, on [-1, N] in every axis, 0 elsewhere.
 void IBMSolver_export_intermediate(IBMSolver *s, const char *name) {
     if (!check_ready(s, "IBMSolver_export_intermediate")) return;
-    std::string path = std::string(name) + ".intermediate";
-    FILE *f = fopen(path.c_str(), "wb");
-    if (!f) {
-        set_status(s, IBM3D_EARG, "cannot open file \"%s\"", path.c_str());
-        return;
-    }
+    ibm3d_device *d = s->dev;
     const size_t n = (size_t)ncell_of(s);
-    std::vector<double> h(n);
-    const int which[7] = {IBM3D_F_USTAR1, IBM3D_F_USTAR2, IBM3D_F_USTAR3, IBM3D_F_PPRIME, IBM3D_F_U1, IBM3D_F_U2, IBM3D_F_U3};
-    for (int w : which) {
-        IBMSolver_get_field(s, w, h.data());
-        fwrite(h.data(), sizeof(double), n, f);
+    std::vector<double> us[3], pp(n), p0(n);
+    const int which[3] = {IBM3D_F_USTAR1, IBM3D_F_USTAR2, IBM3D_F_USTAR3};
+    for (int l = 0; l < 3; l++) {
+        us[l].resize(n);
+        IBMSolver_get_field(s, which[l], us[l].data());
     }
-    fclose(f);
+    IBMSolver_get_field(s, IBM3D_F_PPRIME, pp.data());
+    // The step's starting pressure is the second pressure buffer after it.
+    cudaMemcpy(p0.data(), d->pn, sizeof(double) * n, cudaMemcpyDeviceToHost);
+    std::vector<double> ut[3];
+    for (int l = 0; l < 3; l++) ut[l].assign(n, 0.0);
+    const Grid &g = d->g;
+    const double dt = s->dt;
+    for (int i = -1; i < s->Nx + 1; i++)
+        for (int j = -1; j < s->Ny + 1; j++)
+            for (int k = -1; k < s->Nz + 1; k++) {
+                const long long P = cidx(g, i, j, k);
+                ut[0][P] = us[0][P] + dt * (p0[P + g.sx] - p0[P - g.sx]) / (s->xc[i + 3] - s->xc[i + 1]);
+                ut[1][P] = us[1][P] + dt * (p0[P + g.sy] - p0[P - g.sy]) / (s->yc[j + 3] - s->yc[j + 1]);
+                ut[2][P] = us[2][P] + dt * (p0[P + 1] - p0[P - 1]) / (s->zc[k + 3] - s->zc[k + 1]);
+            }
+    std::vector<float> out[7];
+    const std::vector<double> *src[7] = {&us[0], &us[1], &us[2], &ut[0], &ut[1], &ut[2], &pp};
+    for (int q = 0; q < 7; q++) {
+        out[q].resize(n);
+        to_file_layout(s, src[q]->data(), out[q].data());
+    }
+    NcFile f;
+    f.dims = {{"time", 1}, {"x", s->Nx + 4}, {"y", s->Ny + 4}, {"z", s->Nz + 4}};
+    const double tval = s->time;
+    const int ival = s->iter;
+    f.vars.push_back({"time", NCT_DOUBLE, {0}, {{"axis", "T"}, {"units", "seconds"}}, &tval});
+    coord_vars(s, f, 1, 2, 3);
+    f.vars.push_back({"iter", NCT_INT, {}, {}, &ival});
+    const char *names[7] = {"u_star", "v_star", "w_star", "u_tilde", "v_tilde", "w_tilde", "p_prime"};
+    for (int q = 0; q < 7; q++)
+        f.vars.push_back({names[q], NCT_FLOAT, {0, 3, 2, 1}, {{"units", "m/s"}}, out[q].data()});
+    const std::string path = std::string(name) + ".nc";
+    if (!nc_write(path, f)) set_status(s, IBM3D_EARG, "cannot write file \"%s\"", path.c_str());
 }
 
 // -------------------------------------------------------------- turb ---

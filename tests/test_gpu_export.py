@@ -111,3 +111,70 @@ def test_restart_errors(ibm, tmp_path):
     with pytest.raises(ibm.IBM3DError, match="not a flow file of this grid"):
         s.init_flow_file(base)
     s.iterate(1)                      # a failed restart leaves the solver usable
+
+
+def test_lvset_flag_file(ibm, tmp_path):
+    """src/ibm3d_export.c:262-435: level set (float) and flags (int) as
+    [z][y][x] over the padded grid, with the cell-centre coordinates."""
+    case = load_golden("sphere")
+    s = build_case(ibm, case, tol=1e-8)
+    base = str(tmp_path / "geom")
+    s.export_lvset_flag(base)
+    f = _read_plain(base + ".nc")
+    nx, ny, nz = s.shape
+    assert f["_dims"] == {"x": nx + 4, "y": ny + 4, "z": nz + 4}
+    assert np.array_equal(f["lvset"], oexp.to_file_layout(s.get_field("lvset")), equal_nan=True)
+    assert np.array_equal(f["flag"], np.ascontiguousarray(s.get_flag().transpose(2, 1, 0)))
+    assert np.array_equal(f["flag"], np.ascontiguousarray(case["flag"].transpose(2, 1, 0)))
+
+
+def test_intermediate_file(ibm, tmp_path):
+    """src/ibm3d_export.c:437-650: the last step's u*, u~ and p' as float
+    [time][z][y][x]; u~ = u* + dt (p(+1) - p(-1)) / (c(+1) - c(-1)) with the
+    step's starting pressure on [-1, N] (src/ibm3d_fracstep.c:388-412).  The
+    starting pressure is p after the previous call with its outer and ghost
+    values refreshed at the start of this call (src/ibm3d_fracstep.c:45-48);
+    the state file holds it as the second pressure buffer."""
+    case = load_golden("sphere")
+    s = build_case(ibm, case, tol=1e-8)
+    s.iterate(1)
+    p_prev = s.get_field("p")
+    s.iterate(1)
+    base = str(tmp_path / "mid")
+    s.export_intermediate(base)
+    s.export_result(str(tmp_path / "state"))
+    f = _read_plain(base + ".nc")
+    assert int(f["iter"]) == 2
+    for var, fld in (("u_star", "u1star"), ("v_star", "u2star"), ("w_star", "u3star"), ("p_prime", "pprime")):
+        assert np.array_equal(f[var][0], oexp.to_file_layout(s.get_field(fld)), equal_nan=True), var
+    nx, ny, nz = s.shape
+    shape = (nx + 4, ny + 4, nz + 4)
+    n = shape[0] * shape[1] * shape[2]
+    state = np.fromfile(str(tmp_path / "state.ibm3d"), dtype=np.float64, offset=40, count=26 * n).reshape((26,) + shape)
+    p0 = state[13]                                           # role order: u, u_next, U, U_next, p, p_next, ...
+    fluid = np.zeros(shape, dtype=bool)
+    fluid[2:-2, 2:-2, 2:-2] = s.get_flag()[2:-2, 2:-2, 2:-2] == 1
+    assert np.array_equal(p0[fluid], p_prev[fluid])
+    dt = case["meta"]["dt"]
+    coords = (f["x"], f["y"], f["z"])
+    for ax, (var, fld) in enumerate((("u_tilde", "u1star"), ("v_tilde", "u2star"), ("w_tilde", "u3star"))):
+        us = s.get_field(fld)
+        want = np.zeros_like(us)
+        sl = [slice(1, m + 3) for m in (nx, ny, nz)]         # padded indices of [-1, N]
+        up, dn = list(sl), list(sl)
+        up[ax] = slice(2, (nx, ny, nz)[ax] + 4)
+        dn[ax] = slice(0, (nx, ny, nz)[ax] + 2)
+        c = coords[ax]
+        dc = c[2:] - c[:-2]
+        bshape = [1, 1, 1]
+        bshape[ax] = len(dc)
+        want[tuple(sl)] = us[tuple(sl)] + dt * (p0[tuple(up)] - p0[tuple(dn)]) / dc.reshape(bshape)
+        assert np.array_equal(f[var][0], oexp.to_file_layout(want), equal_nan=True), var
+
+
+def _read_plain(path):
+    sio = pytest.importorskip("scipy.io")
+    with sio.netcdf_file(path, "r", mmap=False) as f:
+        out = {k: np.array(v.data) for k, v in f.variables.items()}
+        out["_dims"] = dict(f.dimensions)
+    return out
