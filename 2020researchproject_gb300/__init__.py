@@ -33,6 +33,7 @@ LIB_PATH = os.path.join(_PKG, "libibm3d_gb300.so")
 SOLVER_AMG, SOLVER_PCG, SOLVER_BiCGSTAB, SOLVER_GMRES = range(4)
 PRECOND_NONE, PRECOND_AMG = range(2)
 FP64, MIXED, MIXED_MG = 0, 1, 2
+COARSEN_HALVE, COARSEN_SPACING = 0, 1
 DIR_NORTH, DIR_EAST, DIR_SOUTH, DIR_WEST, DIR_DOWN, DIR_UP = (1 << i for i in range(6))
 (BC_VELOCITY_COMPONENT, BC_PRESSURE, BC_STATIONARY_WALL, BC_FREE_SLIP_WALL,
  BC_SYMMETRIC, BC_ALL_PERIODIC, BC_VELOCITY_PERIODIC) = range(7)
@@ -94,6 +95,7 @@ def load_library(path: str = LIB_PATH):
         "IBMSolver_set_bc_func": (None, [vp, i, i, vp, vp, vp, vp]),
         "IBMSolver_set_refinement": (None, [vp, d, d, i]),
         "IBMSolver_set_gmres_restart": (None, [vp, i]),
+        "IBMSolver_set_coarsening": (None, [vp, i]),
         "IBMSolver_autotune": (d, [vp, i, ip]),
         "IBMSolver_set_ext_force_func": (None, [vp, vp, vp, vp]),
         "IBMSolver_set_smagorinsky": (None, [vp, d]),
@@ -307,6 +309,12 @@ class IBMSolver:
         ms = self._lib.IBMSolver_autotune(self._s, int(steps), _ptr(best))
         self._check("autotune")
         return ms, tuple(int(v) for v in best)
+
+    def set_coarsening(self, mode=COARSEN_SPACING):
+        """Pressure multigrid coarsening (before assemble): COARSEN_SPACING
+        or COARSEN_HALVE."""
+        self._lib.IBMSolver_set_coarsening(self._s, int(mode))
+        self._check("set_coarsening")
 
     def set_gmres_restart(self, restart=10):
         self._lib.IBMSolver_set_gmres_restart(self._s, restart)

@@ -1,6 +1,7 @@
 // Geometric multigrid preconditioner for the pressure-Poisson rows (see
 // multigrid.h for the design), instantiated in FP64 and FP32.
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <vector>
 
@@ -90,7 +91,7 @@ __device__ __forceinline__ T trilinear(const T (&v)[2][2][2], const bool (&act)[
 // active coarse cells only.
 template <typename T>
 __device__ inline T prolong_value(const MGLevel<T> &C, int i, int j, int k) {
-    const int I = C.cx ? i >> 1 : i, J = C.cy ? j >> 1 : j, K = C.cz ? k >> 1 : k;
+    const int I = C.pa[0][i], J = C.pa[1][j], K = C.pa[2][k];
     const int xs[2] = {I, C.po[0][i]}, ys[2] = {J, C.po[1][j]}, zs[2] = {K, C.po[2][k]};
     const T wx = C.pw[0][i], wy = C.pw[1][j], wz = C.pw[2][k];
     const T wxs[2] = {wx, (T)1 - wx}, wys[2] = {wy, (T)1 - wy}, wzs[2] = {wz, (T)1 - wz};
@@ -324,9 +325,9 @@ k_mg0_restrict(const OpT<T> c, const T *__restrict__ r, const T *__restrict__ z,
     L3_INDEX(I, J, K, L1.ny, L1.nz);
     const Grid &g = c.g;
     T acc = 0;
-    const int i0 = L1.cx ? 2 * I : I, i1 = L1.cx ? min(2 * I + 1, g.nx - 1) : I;
-    const int j0 = L1.cy ? 2 * J : J, j1 = L1.cy ? min(2 * J + 1, g.ny - 1) : J;
-    const int k0 = L1.cz ? 2 * K : K, k1 = L1.cz ? min(2 * K + 1, g.nz - 1) : K;
+    const int i0 = L1.ch[0][I], i1 = L1.ch[0][I + 1] - 1;
+    const int j0 = L1.ch[1][J], j1 = L1.ch[1][J + 1] - 1;
+    const int k0 = L1.ch[2][K], k1 = L1.ch[2][K + 1] - 1;
     for (int i = i0; i <= i1; i++)
         for (int j = j0; j <= j1; j++)
             for (int k = k0; k <= k1; k++) {
@@ -458,24 +459,32 @@ k_mg0_prolong2(const OpT<T> c, T *z, const MGLevel<T> C, const int *gate) {
 }
 
 // ------------------------------------------------------ level building --
+// Centre-distance ratios of a new level, per axis (n + 1 entries): [I] for
+// the low face of cell I (I = 0: the low boundary, or the periodic wrap),
+// [n] for the high boundary; each is (finer centre distance) / (coarse
+// centre distance) across the face (to the mirrored centre at a boundary).
+struct FaceRatio {
+    const double *r[3];
+};
+
 // Level 1 from the fine grid (FP64): conductances Vol*k of fluid-fluid
 // faces, pressure-Dirichlet boundary conductances, periodic wraps.
 __global__ void k_mg_build1(const OpT<double> c, MGLevel<double> L, double *Gx, double *Gy, double *Gz,
-                            const Per3 per) {
+                            const Per3 per, const FaceRatio fr) {
     const Grid &g = c.g;
     GRID_STRIDE(q, L.n) {
         const int K = (int)(q % L.nz);
         const int J = (int)((q / L.nz) % L.ny);
         const int I = (int)(q / ((long long)L.nz * L.ny));
-        const int i0 = L.cx ? 2 * I : I, i1 = L.cx ? min(2 * I + 1, g.nx - 1) : I;
-        const int j0 = L.cy ? 2 * J : J, j1 = L.cy ? min(2 * J + 1, g.ny - 1) : J;
-        const int k0 = L.cz ? 2 * K : K, k1 = L.cz ? min(2 * K + 1, g.nz - 1) : K;
+        const int i0 = L.ch[0][I], i1 = L.ch[0][I + 1] - 1;
+        const int j0 = L.ch[1][J], j1 = L.ch[1][J + 1] - 1;
+        const int k0 = L.ch[2][K], k1 = L.ch[2][K + 1] - 1;
         auto active = [&](int i, int j, int k) {
             const long long P = cidx(g, i, j, k);
             return c.flag[P] == FLUID && !(c.p_singular && P == c.pinned);
         };
         auto dirf = [](int t) { return t == BCT_PRESSURE || t == BCT_VELPERIODIC; };
-        double tx = 0, ty = 0, tz = 0, gx = 0, gy = 0, gz = 0;
+        double tx = 0, ty = 0, tz = 0, gl[3] = {0, 0, 0}, gh[3] = {0, 0, 0};
         for (int i = i0; i <= i1; i++)
             for (int j = j0; j <= j1; j++)
                 for (int k = k0; k <= k1; k++) {
@@ -495,33 +504,38 @@ __global__ void k_mg_build1(const OpT<double> c, MGLevel<double> L, double *Gx, 
                     }
                     const BCRow<double> &W = c.bc[F_W], &E = c.bc[F_E], &S = c.bc[F_S], &N = c.bc[F_N];
                     const BCRow<double> &D = c.bc[F_D], &U = c.bc[F_U];
-                    if (i == 0 && dirf(W.type)) gx += v * c.km[0][2] * (1 + W.dir_m[0] / W.dir_o[0]);
-                    if (i == g.nx - 1 && dirf(E.type)) gx += v * c.kp[0][g.nx + 1] * (1 + E.dir_m[0] / E.dir_o[0]);
-                    if (j == 0 && dirf(S.type)) gy += v * c.km[1][2] * (1 + S.dir_m[0] / S.dir_o[0]);
-                    if (j == g.ny - 1 && dirf(N.type)) gy += v * c.kp[1][g.ny + 1] * (1 + N.dir_m[0] / N.dir_o[0]);
-                    if (k == 0 && dirf(D.type)) gz += v * c.km[2][2] * (1 + D.dir_m[0] / D.dir_o[0]);
-                    if (k == g.nz - 1 && dirf(U.type)) gz += v * c.kp[2][g.nz + 1] * (1 + U.dir_m[0] / U.dir_o[0]);
+                    if (i == 0 && dirf(W.type)) gl[0] += v * c.km[0][2] * (1 + W.dir_m[0] / W.dir_o[0]);
+                    if (i == g.nx - 1 && dirf(E.type)) gh[0] += v * c.kp[0][g.nx + 1] * (1 + E.dir_m[0] / E.dir_o[0]);
+                    if (j == 0 && dirf(S.type)) gl[1] += v * c.km[1][2] * (1 + S.dir_m[0] / S.dir_o[0]);
+                    if (j == g.ny - 1 && dirf(N.type)) gh[1] += v * c.kp[1][g.ny + 1] * (1 + N.dir_m[0] / N.dir_o[0]);
+                    if (k == 0 && dirf(D.type)) gl[2] += v * c.km[2][2] * (1 + D.dir_m[0] / D.dir_o[0]);
+                    if (k == g.nz - 1 && dirf(U.type)) gh[2] += v * c.kp[2][g.nz + 1] * (1 + U.dir_m[0] / U.dir_o[0]);
                 }
-        const double fx = L.cx ? 0.5 : 1.0, fy = L.cy ? 0.5 : 1.0, fz = L.cz ? 0.5 : 1.0;
-        L.Tx[q] = (I == 0 && L.nx == 1) ? 0.0 : fx * tx;
-        L.Ty[q] = (J == 0 && L.ny == 1) ? 0.0 : fy * ty;
-        L.Tz[q] = (K == 0 && L.nz == 1) ? 0.0 : fz * tz;
-        Gx[q] = fx * gx;
-        Gy[q] = fy * gy;
-        Gz[q] = fz * gz;
+        L.Tx[q] = (I == 0 && L.nx == 1) ? 0.0 : fr.r[0][I] * tx;
+        L.Ty[q] = (J == 0 && L.ny == 1) ? 0.0 : fr.r[1][J] * ty;
+        L.Tz[q] = (K == 0 && L.nz == 1) ? 0.0 : fr.r[2][K] * tz;
+        Gx[q] = fr.r[0][0] * gl[0] + fr.r[0][L.nx] * gh[0];
+        Gy[q] = fr.r[1][0] * gl[1] + fr.r[1][L.ny] * gh[1];
+        Gz[q] = fr.r[2][0] * gl[2] + fr.r[2][L.nz] * gh[2];
     }
 }
 
 // Coarse level c from level f (FP64).
 __global__ void k_mg_buildc(const MGLevel<double> F, const double *__restrict__ fGx, const double *__restrict__ fGy,
-                            const double *__restrict__ fGz, MGLevel<double> C, double *Gx, double *Gy, double *Gz) {
+                            const double *__restrict__ fGz, MGLevel<double> C, double *Gx, double *Gy, double *Gz,
+                            const FaceRatio fr) {
     GRID_STRIDE(q, C.n) {
         const int K = (int)(q % C.nz);
         const int J = (int)((q / C.nz) % C.ny);
         const int I = (int)(q / ((long long)C.nz * C.ny));
-        const int i0 = C.cx ? 2 * I : I, i1 = C.cx ? min(2 * I + 1, F.nx - 1) : I;
-        const int j0 = C.cy ? 2 * J : J, j1 = C.cy ? min(2 * J + 1, F.ny - 1) : J;
-        const int k0 = C.cz ? 2 * K : K, k1 = C.cz ? min(2 * K + 1, F.nz - 1) : K;
+        const int i0 = C.ch[0][I], i1 = C.ch[0][I + 1] - 1;
+        const int j0 = C.ch[1][J], j1 = C.ch[1][J + 1] - 1;
+        const int k0 = C.ch[2][K], k1 = C.ch[2][K + 1] - 1;
+        // A Dirichlet conductance sits on a cell at the low or high end of
+        // its axis (both ends at once only on a one-cell axis, ratio 1).
+        auto bscale = [&](int a, int i, int nf, int nc) {
+            return i == 0 ? fr.r[a][0] : i == nf - 1 ? fr.r[a][nc] : 1.0;
+        };
         double tx = 0, ty = 0, tz = 0, gx = 0, gy = 0, gz = 0;
         for (int i = i0; i <= i1; i++)
             for (int j = j0; j <= j1; j++)
@@ -530,17 +544,16 @@ __global__ void k_mg_buildc(const MGLevel<double> F, const double *__restrict__ 
                     if (i == i0) tx += F.Tx[f];
                     if (j == j0) ty += F.Ty[f];
                     if (k == k0) tz += F.Tz[f];
-                    gx += fGx[f];
-                    gy += fGy[f];
-                    gz += fGz[f];
+                    gx += bscale(0, i, F.nx, C.nx) * fGx[f];
+                    gy += bscale(1, j, F.ny, C.ny) * fGy[f];
+                    gz += bscale(2, k, F.nz, C.nz) * fGz[f];
                 }
-        const double fx = C.cx ? 0.5 : 1.0, fy = C.cy ? 0.5 : 1.0, fz = C.cz ? 0.5 : 1.0;
-        C.Tx[q] = (I == 0 && C.nx == 1) ? 0.0 : fx * tx;
-        C.Ty[q] = (J == 0 && C.ny == 1) ? 0.0 : fy * ty;
-        C.Tz[q] = (K == 0 && C.nz == 1) ? 0.0 : fz * tz;
-        Gx[q] = fx * gx;
-        Gy[q] = fy * gy;
-        Gz[q] = fz * gz;
+        C.Tx[q] = (I == 0 && C.nx == 1) ? 0.0 : fr.r[0][I] * tx;
+        C.Ty[q] = (J == 0 && C.ny == 1) ? 0.0 : fr.r[1][J] * ty;
+        C.Tz[q] = (K == 0 && C.nz == 1) ? 0.0 : fr.r[2][K] * tz;
+        Gx[q] = gx;
+        Gy[q] = gy;
+        Gz[q] = gz;
     }
 }
 
@@ -620,9 +633,9 @@ __host__ __device__ inline int level_colors(const MGLevel<T> &L, const int *per)
 template <typename T>
 __device__ inline T coarse_restrict_value(const MGLevel<T> &F, const MGLevel<T> &C, int I, int J, int K,
                                           const int *per) {
-    const int i0 = C.cx ? 2 * I : I, i1 = C.cx ? min(2 * I + 1, F.nx - 1) : I;
-    const int j0 = C.cy ? 2 * J : J, j1 = C.cy ? min(2 * J + 1, F.ny - 1) : J;
-    const int k0 = C.cz ? 2 * K : K, k1 = C.cz ? min(2 * K + 1, F.nz - 1) : K;
+    const int i0 = C.ch[0][I], i1 = C.ch[0][I + 1] - 1;
+    const int j0 = C.ch[1][J], j1 = C.ch[1][J + 1] - 1;
+    const int k0 = C.ch[2][K], k1 = C.ch[2][K + 1] - 1;
     T acc = 0;
     for (int i = i0; i <= i1; i++)
         for (int j = j0; j <= j1; j++)
@@ -813,20 +826,64 @@ static size_t tail_bytes(const std::vector<MGLevel<T>> &lv, int first) {
 }
 
 // ------------------------------------------------------------- host --
-// Prolongation tables of one axis: fine centres xf (fine faces ff, nf
-// cells) into coarse centres (coarse faces cf, nc cells).
-static void prolong_axis(const std::vector<double> &ff, const std::vector<double> &cf, bool coarsened, bool periodic,
-                         std::vector<int> &po, std::vector<double> &pw) {
+// Groups of one axis of a new level: the first finer cell of each coarse
+// cell, then nf.  Halving: pairs (0, 1), (2, 3), ... (an odd last cell
+// alone; a one-cell axis stays).
+static std::vector<int> halve_groups(int nf) {
+    std::vector<int> ch;
+    for (int i = 0; i < nf; i += nf >= 2 ? 2 : 1) ch.push_back(i);
+    ch.push_back(nf);
+    return ch;
+}
+
+// By spacing: from the low end, a cell and its neighbour merge when their
+// joint width is at most H (finer faces ff).
+static std::vector<int> spacing_groups(const std::vector<double> &ff, double H) {
+    const int nf = (int)ff.size() - 1;
+    std::vector<int> ch;
+    int i = 0;
+    while (i < nf) {
+        ch.push_back(i);
+        i += (i + 1 < nf && ff[i + 2] - ff[i] <= H) ? 2 : 1;
+    }
+    ch.push_back(nf);
+    return ch;
+}
+
+// Centre-distance ratios of one axis (FaceRatio) for groups ch of the
+// finer faces ff.
+static std::vector<double> face_ratios(const std::vector<double> &ff, const std::vector<int> &ch, bool periodic) {
+    const int nf = (int)ff.size() - 1, nc = (int)ch.size() - 1;
+    std::vector<double> xf(nf), xc(nc), r(nc + 1, 1.0);
+    for (int i = 0; i < nf; i++) xf[i] = 0.5 * (ff[i] + ff[i + 1]);
+    for (int I = 0; I < nc; I++) xc[I] = 0.5 * (ff[ch[I]] + ff[ch[I + 1]]);
+    for (int I = 1; I < nc; I++) r[I] = (xf[ch[I]] - xf[ch[I] - 1]) / (xc[I] - xc[I - 1]);
+    if (periodic) {
+        const double Lp = ff[nf] - ff[0];
+        if (nc > 1) r[0] = r[nc] = (xf[0] + Lp - xf[nf - 1]) / (xc[0] + Lp - xc[nc - 1]);
+    } else {
+        r[0] = (xf[0] - ff[0]) / (xc[0] - ff[0]);
+        r[nc] = (ff[nf] - xf[nf - 1]) / (ff[nf] - xc[nc - 1]);
+    }
+    return r;
+}
+
+// Prolongation tables of one axis: fine centres (fine faces ff, nf cells)
+// into coarse centres (coarse faces cf, nc cells); pa: the coarse cell
+// covering each fine cell.  A fine cell alone in its group shares its
+// parent's centre (weight 1).
+static void prolong_axis(const std::vector<double> &ff, const std::vector<double> &cf, const std::vector<int> &pa,
+                         bool periodic, std::vector<int> &po, std::vector<double> &pw) {
     const int nf = (int)ff.size() - 1, nc = (int)cf.size() - 1;
     po.assign(nf, -1);
     pw.assign(nf, 1.0);
-    if (!coarsened) return;
+    if (nc == nf) return;
     std::vector<double> cc(nc);
     for (int I = 0; I < nc; I++) cc[I] = 0.5 * (cf[I] + cf[I + 1]);
     const double Lp = cf[nc] - cf[0];
     for (int i = 0; i < nf; i++) {
         const double x = 0.5 * (ff[i] + ff[i + 1]);
-        const int I = i >> 1;
+        const int I = pa[i];
         int o = x < cc[I] ? I - 1 : I + 1;
         double co;
         if (o < 0 || o >= nc) {
@@ -904,50 +961,94 @@ int GMG<T>::setup(cudaStream_t s, const OpT<double> &A64, const OpT<T> &A, const
     std::vector<double> faces[3] = {geom.f[0], geom.f[1], geom.f[2]};
     std::vector<MGLevel<double>> lv64;
     std::vector<double *> G;
-    while (true) {
-        const bool cx = nx >= 2, cy = ny >= 2, cz = nz >= 2;
-        if (!cx && !cy && !cz) break;
+    // Host tables are copied by cudaMemcpyAsync from pageable memory, which
+    // stages them at the call: the vectors may go out of scope after it.
+    auto upload = [&](const void *src, size_t bytes, bool keep) -> void * {
+        void *p = dalloc(bytes, keep);
+        if (p && bytes) cudaMemcpyAsync(p, src, bytes, cudaMemcpyHostToDevice, s);
+        return p;
+    };
+    // Finest width of the grid over the axes that can coarsen.
+    double hmin0 = 0.0;
+    for (int a = 0; a < 3; a++) {
+        if (geom.f[a].size() < 3) continue;
+        for (size_t i = 0; i + 1 < geom.f[a].size(); i++) {
+            const double w = geom.f[a][i + 1] - geom.f[a][i];
+            if (hmin0 == 0.0 || w < hmin0) hmin0 = w;
+        }
+    }
+    for (int level = 0;; level++) {
+        const int fn[3] = {nx, ny, nz};
+        if (nx < 2 && ny < 2 && nz < 2) break;
         if ((long long)nx * ny * nz <= 64 && !lv64.empty()) break;
+        std::vector<int> ch[3];
+        for (int a = 0; a < 3; a++) ch[a] = halve_groups(fn[a]);
+        if (cfg.coarsening == MG_COARSEN_SPACING) {
+            // Widest pair on any axis: at that threshold every pair merges.
+            double hmax = 0.0;
+            for (int a = 0; a < 3; a++)
+                for (int i = 0; i + 2 < (int)faces[a].size(); i++) hmax = std::max(hmax, faces[a][i + 2] - faces[a][i]);
+            const long long nfine = (long long)nx * ny * nz;
+            for (double H = 1.5 * std::ldexp(hmin0, level + 1);; H *= 1.25) {
+                long long m = 1;
+                for (int a = 0; a < 3; a++) {
+                    ch[a] = spacing_groups(faces[a], H);
+                    m *= (long long)ch[a].size() - 1;
+                }
+                if (2 * m <= nfine || H >= hmax) break;
+            }
+        }
         MGLevel<double> L{};
-        L.cx = cx; L.cy = cy; L.cz = cz;
-        L.nx = cx ? (nx + 1) / 2 : nx;
-        L.ny = cy ? (ny + 1) / 2 : ny;
-        L.nz = cz ? (nz + 1) / 2 : nz;
+        L.cx = nx >= 2 && ch[0] == halve_groups(nx);
+        L.cy = ny >= 2 && ch[1] == halve_groups(ny);
+        L.cz = nz >= 2 && ch[2] == halve_groups(nz);
+        L.nx = (int)ch[0].size() - 1;
+        L.ny = (int)ch[1].size() - 1;
+        L.nz = (int)ch[2].size() - 1;
         L.n = (long long)L.nx * L.ny * L.nz;
+        if (L.n == nx * (long long)ny * nz) break;  // nothing merges
+        const int cn[3] = {L.nx, L.ny, L.nz};
+        MGLevel<T> LT{};
+        LT.nx = L.nx; LT.ny = L.ny; LT.nz = L.nz; LT.n = L.n; LT.cx = L.cx; LT.cy = L.cy; LT.cz = L.cz;
+        std::vector<double> cfs[3];
+        FaceRatio fr{};
+        for (int a = 0; a < 3; a++) {
+            std::vector<int> pa(fn[a]);
+            for (int I = 0; I < cn[a]; I++)
+                for (int i = ch[a][I]; i < ch[a][I + 1]; i++) pa[i] = I;
+            std::vector<double> &cf = cfs[a];
+            cf.resize(cn[a] + 1);
+            for (int I = 0; I <= cn[a]; I++) cf[I] = faces[a][ch[a][I]];
+            const std::vector<double> rat = face_ratios(faces[a], ch[a], per_[a]);
+            std::vector<int> po;
+            std::vector<double> pw;
+            prolong_axis(faces[a], cf, pa, per_[a], po, pw);
+            std::vector<T> pwt(pw.begin(), pw.end());
+            const int *dch = (const int *)upload(ch[a].data(), sizeof(int) * ch[a].size(), true);
+            const int *dpa = (const int *)upload(pa.data(), sizeof(int) * pa.size(), true);
+            const int *dpo = (const int *)upload(po.data(), sizeof(int) * po.size(), true);
+            const T *dpw = (const T *)upload(pwt.data(), sizeof(T) * pwt.size(), true);
+            fr.r[a] = (const double *)upload(rat.data(), sizeof(double) * rat.size(), false);
+            if (!dch || !dpa || !dpo || !dpw || !fr.r[a]) return -1;
+            L.ch[a] = LT.ch[a] = dch;
+            L.pa[a] = LT.pa[a] = dpa;
+            LT.po[a] = dpo;
+            LT.pw[a] = dpw;
+        }
         const size_t b = sizeof(double) * L.n;
         L.Tx = (double *)dalloc(b, false); L.Ty = (double *)dalloc(b, false); L.Tz = (double *)dalloc(b, false);
         L.diag = (double *)dalloc(b, false);
         double *gx = (double *)dalloc(b, false), *gy = (double *)dalloc(b, false), *gz = (double *)dalloc(b, false);
         if (!L.Tx || !L.Ty || !L.Tz || !L.diag || !gx || !gy || !gz) return -1;
         if (lv64.empty()) {
-            k_mg_build1<<<nblk(L.n, 128), 128, 0, s>>>(A64, L, gx, gy, gz, per);
+            k_mg_build1<<<nblk(L.n, 128), 128, 0, s>>>(A64, L, gx, gy, gz, per, fr);
         } else {
             double **fg = &G[G.size() - 3];
-            k_mg_buildc<<<nblk(L.n, 128), 128, 0, s>>>(lv64.back(), fg[0], fg[1], fg[2], L, gx, gy, gz);
+            k_mg_buildc<<<nblk(L.n, 128), 128, 0, s>>>(lv64.back(), fg[0], fg[1], fg[2], L, gx, gy, gz, fr);
         }
         k_mg_diag<<<nblk(L.n, 128), 128, 0, s>>>(L, gx, gy, gz, per);
         G.push_back(gx); G.push_back(gy); G.push_back(gz);
-        // Coarse faces and the prolongation tables toward the finer level.
-        const int cn[3] = {L.nx, L.ny, L.nz}, fn[3] = {nx, ny, nz}, co[3] = {L.cx, L.cy, L.cz};
-        MGLevel<T> LT{};
-        LT.nx = L.nx; LT.ny = L.ny; LT.nz = L.nz; LT.n = L.n; LT.cx = L.cx; LT.cy = L.cy; LT.cz = L.cz;
-        for (int a = 0; a < 3; a++) {
-            std::vector<double> cf(cn[a] + 1);
-            for (int I = 0; I < cn[a]; I++) cf[I] = faces[a][co[a] ? 2 * I : I];
-            cf[cn[a]] = faces[a][fn[a]];
-            std::vector<int> po;
-            std::vector<double> pw;
-            prolong_axis(faces[a], cf, co[a], per_[a], po, pw);
-            std::vector<T> pwt(pw.begin(), pw.end());
-            int *dpo = (int *)dalloc(sizeof(int) * po.size(), true);
-            T *dpw = (T *)dalloc(sizeof(T) * pwt.size(), true);
-            if (!dpo || !dpw) return -1;
-            cudaMemcpyAsync(dpo, po.data(), sizeof(int) * po.size(), cudaMemcpyHostToDevice, s);
-            cudaMemcpyAsync(dpw, pwt.data(), sizeof(T) * pwt.size(), cudaMemcpyHostToDevice, s);
-            LT.po[a] = dpo;
-            LT.pw[a] = dpw;
-            faces[a] = cf;
-        }
+        for (int a = 0; a < 3; a++) faces[a] = cfs[a];
         const size_t bt = sizeof(T) * L.n;
         LT.Tx = (T *)dalloc(bt, true); LT.Ty = (T *)dalloc(bt, true); LT.Tz = (T *)dalloc(bt, true);
         LT.diag = (T *)dalloc(bt, true); LT.R = (T *)dalloc(bt, true); LT.Z = (T *)dalloc(bt, true);

@@ -7,11 +7,28 @@
 // Coarser levels carry a masked, symmetric cell-centred Laplacian in
 // conductance form: a fine fluid-fluid face has conductance
 // T = A_face dt / (2 Re dc) = Vol k_nb; a coarse face sums the fine faces it
-// covers, halved when the face-normal axis was coarsened; faces touching a
-// ghost, solid or pinned cell carry none (Neumann); pressure-Dirichlet
-// boundaries fold into the diagonal and periodic ones wrap.  Residuals are
-// restricted as Vol coeffsum r (the conductance form of a normalised row)
-// by summation; corrections are prolongated trilinearly in cell-centre
+// covers, scaled by (finer centre distance) / (coarse centre distance)
+// across it, so a coarse level is the rediscretised operator of its own
+// cells; faces touching a ghost, solid or pinned cell carry none
+// (Neumann); pressure-Dirichlet boundaries fold into the diagonal and
+// periodic ones wrap.
+//
+// Coarsening.  A coarse cell covers one or two consecutive cells of the
+// finer level along each axis (tensor-product groups).  Halving every
+// axis (MG_COARSEN_HALVE) leaves the 5:1 cells of body-clustered grids
+// 5:1 on every level, where point Gauss-Seidel barely smooths the weakly
+// coupled direction.  By spacing (MG_COARSEN_SPACING, the default), level
+// L merges a pair of neighbouring cells only while their joint width stays
+// within 1.5 x 2^(L+1) x the finest width of the grid: the small cells of
+// the clustered region merge first and the large far-field cells wait
+// until the others have grown to their size (semi-coarsening toward
+// isotropic cells).  A level is kept at no more than half the cells of the
+// one before (the threshold grows until it is), so a V-cycle costs at most
+// about twice its finest level.  On a uniform grid both rules give the
+// same halving.
+//
+// Residuals are restricted as Vol coeffsum r (the conductance form of a
+// normalised row) by summation; corrections are prolongated trilinearly in cell-centre
 // coordinates (renormalised over active coarse cells), which on the
 // stretched benchmark grids cuts the Krylov iterations by a third against
 // piecewise-constant transfer.  Smoothers are colour-ordered Gauss-Seidel
@@ -30,7 +47,7 @@ template <typename T>
 struct MGLevel {
     int nx, ny, nz;
     long long n;
-    int cx, cy, cz;          // axis coarsened from the finer level
+    int cx, cy, cz;          // axis halved uniformly from the finer level (cells 2I, 2I+1)
     T *Tx, *Ty, *Tz;         // conductance of the low face of each cell (wrap at 0 if periodic)
     T *diag;                 // sum of all couplings incl. Dirichlet boundaries; 0 = inactive
     T *idiag;                // 1 / diag (0 = inactive), for the relaxations
@@ -40,13 +57,20 @@ struct MGLevel {
     // weight of the cell's own parent.
     const int *po[3];
     const T *pw[3];
+    // Groups, per axis: cell I covers finer cells ch[a][I] .. ch[a][I+1]-1
+    // (one or two); pa[a][i] is the cell covering finer cell i.
+    const int *ch[3];
+    const int *pa[3];
 };
+
+enum { MG_COARSEN_HALVE = 0, MG_COARSEN_SPACING = 1 };
 
 struct GMGConfig {
     int nu_pre = 5, nu_post = 5;    // fine grid
     int nuc_pre = 1, nuc_post = 1;  // coarse levels above the coarsest
     int coarse_sweeps = 8;          // coarsest level
     double omega = 1.0;             // over-relaxation of the fine-grid fluid rows
+    int coarsening = MG_COARSEN_SPACING;
 };
 
 // Host geometry of the fine grid: interior face coordinates per axis.

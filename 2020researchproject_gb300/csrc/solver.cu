@@ -128,6 +128,7 @@ struct ibm3d_device {
     bool use_graphs = true;
     int mg_sweeps[5] = {5, 5, 1, 1, 8};  // multigrid sweeps: fine pre/post, coarse pre/post, coarsest
     double mg_omega = 1.0;               // over-relaxation of the fine-grid smoother
+    int mg_coarsening = IBM3D_COARSEN_SPACING;
     // Mixed path: relative tolerance of each FP32 inner solve (momentum,
     // pressure) and the refinement-cycle cap.
     double inner_tol[2] = {1e-5, 1e-5};
@@ -1488,6 +1489,7 @@ void IBMSolver_assemble(IBMSolver *s) {
     mc.nuc_post = d->mg_sweeps[3];
     mc.coarse_sweeps = d->mg_sweeps[4];
     mc.omega = d->mg_omega;
+    mc.coarsening = d->mg_coarsening == IBM3D_COARSEN_HALVE ? MG_COARSEN_HALVE : MG_COARSEN_SPACING;
     const int *gcell = d->nghost ? d->gargs.cell : nullptr;
     d->mg = new GMG<double>();
     d->mg32 = new GMG<float>();
@@ -2047,6 +2049,18 @@ void IBMSolver_set_multigrid(IBMSolver *s, int nu_pre, int nu_post, int nuc_pre,
         d->mg32->set_omega(omega);
     }
     drop_graphs(d);
+}
+
+void IBMSolver_set_coarsening(IBMSolver *s, int mode) {
+    if (mode != IBM3D_COARSEN_HALVE && mode != IBM3D_COARSEN_SPACING) {
+        set_status(s, IBM3D_EARG, "IBMSolver_set_coarsening: unknown mode %d", mode);
+        return;
+    }
+    if (s->dev->mg) {
+        set_status(s, IBM3D_EARG, "IBMSolver_set_coarsening: call it before IBMSolver_assemble");
+        return;
+    }
+    s->dev->mg_coarsening = mode;
 }
 
 void IBMSolver_set_graphs(IBMSolver *s, int on) {

@@ -147,8 +147,9 @@ _BC = {"vel": "BC_VELOCITY_COMPONENT", "press": "BC_PRESSURE", "wall": "BC_STATI
 _DIR = {"N": "DIR_NORTH", "E": "DIR_EAST", "S": "DIR_SOUTH", "W": "DIR_WEST", "D": "DIR_DOWN", "U": "DIR_UP"}
 
 
-def build_solver(ibm, case, tol=1e-6, div_tol=0.0):
-    """Create and assemble an IBMSolver for ``case`` (ibm = the package)."""
+def build_solver(ibm, case, tol=1e-6, div_tol=0.0, coarsening=None):
+    """Create and assemble an IBMSolver for ``case`` (ibm = the package);
+    coarsening: the pressure multigrid's (library default when None)."""
     s = ibm.IBMSolver()
     s.set_grid(case["xf"], case["yf"], case["zf"])
     s.set_params(case["re"], case["dt"])
@@ -163,6 +164,8 @@ def build_solver(ibm, case, tol=1e-6, div_tol=0.0):
     s.set_linear_solver(ibm.SOLVER_BiCGSTAB, ibm.PRECOND_AMG, tol)
     if div_tol > 0:
         s.set_div_tol(div_tol)
+    if coarsening is not None:
+        s.set_coarsening(coarsening)
     s.assemble()
     return s
 
