@@ -95,7 +95,7 @@ def load_library(path: str = LIB_PATH):
         "IBMSolver_set_bc_func": (None, [vp, i, i, vp, vp, vp, vp]),
         "IBMSolver_set_refinement": (None, [vp, d, d, i]),
         "IBMSolver_set_gmres_restart": (None, [vp, i]),
-        "IBMSolver_set_coarsening": (None, [vp, i]),
+        "IBMSolver_set_coarsening": (None, [vp, i, d]),
         "IBMSolver_autotune": (d, [vp, i, ip]),
         "IBMSolver_set_ext_force_func": (None, [vp, vp, vp, vp]),
         "IBMSolver_set_smagorinsky": (None, [vp, d]),
@@ -310,10 +310,10 @@ class IBMSolver:
         self._check("autotune")
         return ms, tuple(int(v) for v in best)
 
-    def set_coarsening(self, mode=COARSEN_SPACING):
+    def set_coarsening(self, mode=COARSEN_SPACING, width_ratio=0.0):
         """Pressure multigrid coarsening (before assemble): COARSEN_SPACING
-        or COARSEN_HALVE."""
-        self._lib.IBMSolver_set_coarsening(self._s, int(mode))
+        (width_ratio: its merge threshold, 0 = default) or COARSEN_HALVE."""
+        self._lib.IBMSolver_set_coarsening(self._s, int(mode), float(width_ratio))
         self._check("set_coarsening")
 
     def set_gmres_restart(self, restart=10):

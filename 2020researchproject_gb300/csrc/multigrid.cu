@@ -316,31 +316,54 @@ static inline dim3 l3_block() { return dim3(L3_TK, L3_TJ, 1); }
     const int I = blockIdx.z;                                           \
     if (K >= (NZ) || J >= (NY)) return;
 
-// Residual of the fine normalised rows, scaled to conductance form
-// (Vol * coeffsum * r) and summed into the level-1 cells.
+// Restriction of the fine normalised rows' residual, scaled to
+// conductance form (Vol * coeffsum * r), into a level 1 whose groups are
+// uneven: a block takes 4 x 16 coarse cells (J, K) of coarse plane I.  Its
+// 32 x 8 threads each take one fine (j, k) under the tile (coalesced rows
+// along k), summed over the plane group in x, into shared memory; 64 of
+// them then add up each coarse cell's one to four entries.  Grid
+// (ceil(nz1/16), ceil(ny1/4), nx1).
 template <typename T>
 __global__ void __launch_bounds__(256)
-k_mg0_restrict(const OpT<T> c, const T *__restrict__ r, const T *__restrict__ z, MGLevel<T> L1, const int *gate) {
+k_mg0_restrict_g(const OpT<T> c, const T *__restrict__ r, const T *__restrict__ z, MGLevel<T> L1, const int *gate) {
     MG_GATE(gate);
-    L3_INDEX(I, J, K, L1.ny, L1.nz);
+    __shared__ T part[8][33];
     const Grid &g = c.g;
+    const int I = blockIdx.z;
+    const int J0 = blockIdx.y * 4, K0 = blockIdx.x * 16;
+    const int J1 = min(J0 + 4, L1.ny), K1 = min(K0 + 16, L1.nz);
+    const int jb = L1.ch[1][J0], je = L1.ch[1][J1];
+    const int kb = L1.ch[2][K0], ke = L1.ch[2][K1];
+    const int j = jb + threadIdx.y, k = kb + threadIdx.x;
     T acc = 0;
-    const int i0 = L1.ch[0][I], i1 = L1.ch[0][I + 1] - 1;
-    const int j0 = L1.ch[1][J], j1 = L1.ch[1][J + 1] - 1;
-    const int k0 = L1.ch[2][K], k1 = L1.ch[2][K + 1] - 1;
-    for (int i = i0; i <= i1; i++)
-        for (int j = j0; j <= j1; j++)
-            for (int k = k0; k <= k1; k++) {
-                const long long P = cidx(g, i, j, k);
-                if (c.flag[P] != FLUID || (c.p_singular && P == c.pinned)) continue;
-                const int Ii = i + 2, Jj = j + 2, Kk = k + 2;
-                const T nb = c.km[0][Ii] * z[P - g.sx] + c.kp[0][Ii] * z[P + g.sx] + c.km[1][Jj] * z[P - g.sy] +
-                             c.kp[1][Jj] * z[P + g.sy] + c.km[2][Kk] * z[P - 1] + c.kp[2][Kk] * z[P + 1];
-                const T res = r[P] - (z[P] - c.dinv[P] * nb);
-                const T vol = c.d[0][Ii] * c.d[1][Jj] * c.d[2][Kk];
-                acc += vol * (c.ks[0][Ii] + c.ks[1][Jj] + c.ks[2][Kk]) * res;
-            }
-    L1.R[lidx(L1, I, J, K)] = acc;
+    if (j < je && k < ke) {
+        const int Jj = j + 2, Kk = k + 2;
+        const T vyz = c.d[1][Jj] * c.d[2][Kk];
+        const T kyz = c.ks[1][Jj] + c.ks[2][Kk];
+        const T kmy = c.km[1][Jj], kpy = c.kp[1][Jj], kmz = c.km[2][Kk], kpz = c.kp[2][Kk];
+        const int i0 = L1.ch[0][I], i1 = L1.ch[0][I + 1];
+        for (int i = i0; i < i1; i++) {
+            const long long P = cidx(g, i, j, k);
+            if (c.flag[P] != FLUID || (c.p_singular && P == c.pinned)) continue;
+            const int Ii = i + 2;
+            const T nb = c.km[0][Ii] * z[P - g.sx] + c.kp[0][Ii] * z[P + g.sx] + kmy * z[P - g.sy] +
+                         kpy * z[P + g.sy] + kmz * z[P - 1] + kpz * z[P + 1];
+            const T res = r[P] - (z[P] - c.dinv[P] * nb);
+            acc += c.d[0][Ii] * vyz * (c.ks[0][Ii] + kyz) * res;
+        }
+    }
+    part[threadIdx.y][threadIdx.x] = acc;
+    __syncthreads();
+    const int t = threadIdx.y * 32 + threadIdx.x;
+    if (t >= 64) return;
+    const int J = J0 + (t >> 4), K = K0 + (t & 15);
+    if (J >= J1 || K >= K1) return;
+    const int ja = L1.ch[1][J] - jb, jz = L1.ch[1][J + 1] - jb;
+    const int ka = L1.ch[2][K] - kb, kz = L1.ch[2][K + 1] - kb;
+    T sum = 0;
+    for (int y = ja; y < jz; y++)
+        for (int x = ka; x < kz; x++) sum += part[y][x];
+    L1.R[lidx(L1, I, J, K)] = sum;
 }
 
 template <typename T>
@@ -630,16 +653,47 @@ __host__ __device__ inline int level_colors(const MGLevel<T> &L, const int *per)
     return seam ? 4 : 2;
 }
 
+// The residual of cell (I, J, K) on a level without periodic axes, every
+// load issued up front (as coarse_relax_open).
+template <typename T>
+__device__ __forceinline__ T coarse_residual_open(const MGLevel<T> &L, int I, int J, int K) {
+    const long long sx = (long long)L.ny * L.nz, sy = L.nz;
+    const long long q = lidx(L, I, J, K);
+    const bool he = I < L.nx - 1, hn = J < L.ny - 1, hu = K < L.nz - 1;
+    const long long qw = I > 0 ? q - sx : q, qe = he ? q + sx : q;
+    const long long qs = J > 0 ? q - sy : q, qn = hn ? q + sy : q;
+    const long long qd = K > 0 ? q - 1 : q, qu = hu ? q + 1 : q;
+    const T d = L.diag[q], R = L.R[q], zc = L.Z[q];
+    const T tw = L.Tx[q], te = L.Tx[qe], ts = L.Ty[q], tn = L.Ty[qn], td = L.Tz[q], tu = L.Tz[qu];
+    const T zw = L.Z[qw], ze = L.Z[qe], zs = L.Z[qs], zn = L.Z[qn], zd = L.Z[qd], zu = L.Z[qu];
+    T s = R - d * zc;
+    s += tw * zw;
+    s += (he ? te : (T)0) * ze;
+    s += ts * zs;
+    s += (hn ? tn : (T)0) * zn;
+    s += td * zd;
+    s += (hu ? tu : (T)0) * zu;
+    return d == (T)0 ? (T)0 : s;
+}
+
+// Restricted residual of coarse cell (I, J, K): the sum over the finer
+// cells it covers.  skip >= 0: the finer level's last pass was a red/black
+// Gauss-Seidel pass over colour `skip`, whose cells then have zero
+// residual up to rounding; they are left out.
 template <typename T>
 __device__ inline T coarse_restrict_value(const MGLevel<T> &F, const MGLevel<T> &C, int I, int J, int K,
-                                          const int *per) {
+                                          const int *per, int skip) {
     const int i0 = C.ch[0][I], i1 = C.ch[0][I + 1] - 1;
     const int j0 = C.ch[1][J], j1 = C.ch[1][J + 1] - 1;
     const int k0 = C.ch[2][K], k1 = C.ch[2][K + 1] - 1;
+    const bool open = !per[0] && !per[1] && !per[2];
     T acc = 0;
     for (int i = i0; i <= i1; i++)
         for (int j = j0; j <= j1; j++)
-            for (int k = k0; k <= k1; k++) acc += coarse_residual(F, i, j, k, per);
+            for (int k = k0; k <= k1; k++) {
+                if (((i + j + k) & 1) == skip) continue;
+                acc += open ? coarse_residual_open(F, i, j, k) : coarse_residual(F, i, j, k, per);
+            }
     return acc;
 }
 
@@ -709,10 +763,10 @@ k_mgc_color(MGLevel<T> L, const int color, const int pairs, const Per3 per, cons
 
 template <typename T>
 __global__ void __launch_bounds__(256)
-k_mgc_restrict(const MGLevel<T> F, MGLevel<T> C, const Per3 per, const int *gate) {
+k_mgc_restrict(const MGLevel<T> F, MGLevel<T> C, const Per3 per, const int skip, const int *gate) {
     MG_GATE(gate);
     L3_INDEX(I, J, K, C.ny, C.nz);
-    C.R[lidx(C, I, J, K)] = coarse_restrict_value(F, C, I, J, K, per.p);
+    C.R[lidx(C, I, J, K)] = coarse_restrict_value(F, C, I, J, K, per.p, skip);
 }
 
 template <typename T>
@@ -725,10 +779,10 @@ __global__ void __launch_bounds__(256) k_mgc_prolong(const MGLevel<T> C, MGLevel
 }
 
 // Whole V-cycle over levels [first, nlev) inside one thread block, with
-// every level's arrays copied into shared memory; each thread takes cells
+// every level's arrays and its transfer tables (groups, parents,
+// prolongation weights) copied into shared memory; each thread takes cells
 // tid, tid + TAIL_THREADS, ... (levels of at most TAIL_CELLS cells).  R of
-// level `first` is read from global memory and its Z written back; the
-// prolongation tables stay in global memory.
+// level `first` is read from global memory and its Z written back.
 constexpr int TAIL_THREADS = 1024;
 constexpr int TAIL_CELLS = TAIL_THREADS;
 constexpr size_t TAIL_SMEM_MAX = 200 * 1024;
@@ -756,8 +810,39 @@ k_mg_tail(const MGLevel<T> *__restrict__ lv, const int first, const int nlev, co
             L.idiag = nullptr;  // the tail divides by its shared-memory diag
             loc[l - first] = L;
         }
+        // Transfer tables of the levels below `first` (toward their finer
+        // level): weights first (alignment of T), then the int tables.
+        for (int l = first + 1; l < nlev; l++) {
+            const int nf[3] = {lv[l - 1].nx, lv[l - 1].ny, lv[l - 1].nz};
+            for (int a = 0; a < 3; a++) {
+                loc[l - first].pw[a] = q;
+                q += nf[a];
+            }
+        }
+        int *qi = reinterpret_cast<int *>(q);
+        for (int l = first + 1; l < nlev; l++) {
+            MGLevel<T> &L = loc[l - first];
+            const int nf[3] = {lv[l - 1].nx, lv[l - 1].ny, lv[l - 1].nz}, nc[3] = {L.nx, L.ny, L.nz};
+            for (int a = 0; a < 3; a++) {
+                L.po[a] = qi; qi += nf[a];
+                L.pa[a] = qi; qi += nf[a];
+                L.ch[a] = qi; qi += nc[a] + 1;
+            }
+        }
     }
     __syncthreads();
+    for (int l = first + 1; l < nlev; l++) {
+        const MGLevel<T> &G = lv[l], &L = loc[l - first];
+        const int nf[3] = {lv[l - 1].nx, lv[l - 1].ny, lv[l - 1].nz}, nc[3] = {L.nx, L.ny, L.nz};
+        for (int a = 0; a < 3; a++) {
+            for (int c = tid; c < nf[a]; c += TAIL_THREADS) {
+                const_cast<T *>(L.pw[a])[c] = G.pw[a][c];
+                const_cast<int *>(L.po[a])[c] = G.po[a][c];
+                const_cast<int *>(L.pa[a])[c] = G.pa[a][c];
+            }
+            for (int c = tid; c <= nc[a]; c += TAIL_THREADS) const_cast<int *>(L.ch[a])[c] = G.ch[a][c];
+        }
+    }
     for (int l = first; l < nlev; l++) {
         const MGLevel<T> &G = lv[l], &L = loc[l - first];
         for (int c = tid; c < L.n; c += TAIL_THREADS) {
@@ -798,7 +883,7 @@ k_mg_tail(const MGLevel<T> *__restrict__ lv, const int first, const int nlev, co
             for (int c = tid; c < C.n; c += TAIL_THREADS) {
                 int I, J, K;
                 cell(C, c, I, J, K);
-                C.R[c] = coarse_restrict_value(L, C, I, J, K, per.p);
+                C.R[c] = coarse_restrict_value(L, C, I, J, K, per.p, nu1 > 0 && level_colors(L, per.p) == 2 ? 1 : -1);
             }
             __syncthreads();
         }
@@ -817,11 +902,16 @@ k_mg_tail(const MGLevel<T> *__restrict__ lv, const int first, const int nlev, co
     for (int c = tid; c < L.n; c += TAIL_THREADS) G.Z[c] = L.Z[c];
 }
 
-// Shared memory the tail kernel needs for levels [first, nlev).
+// Shared memory the tail kernel needs for levels [first, nlev): six
+// arrays per level and the transfer tables of the levels below `first`.
 template <typename T>
 static size_t tail_bytes(const std::vector<MGLevel<T>> &lv, int first) {
     size_t b = 0;
     for (int l = first; l < (int)lv.size(); l++) b += 6 * sizeof(T) * (size_t)lv[l].n;
+    for (int l = first + 1; l < (int)lv.size(); l++) {
+        const int nf[3] = {lv[l - 1].nx, lv[l - 1].ny, lv[l - 1].nz}, nc[3] = {lv[l].nx, lv[l].ny, lv[l].nz};
+        for (int a = 0; a < 3; a++) b += (sizeof(T) + 2 * sizeof(int)) * (size_t)nf[a] + sizeof(int) * (nc[a] + 1);
+    }
     return b;
 }
 
@@ -989,7 +1079,7 @@ int GMG<T>::setup(cudaStream_t s, const OpT<double> &A64, const OpT<T> &A, const
             for (int a = 0; a < 3; a++)
                 for (int i = 0; i + 2 < (int)faces[a].size(); i++) hmax = std::max(hmax, faces[a][i + 2] - faces[a][i]);
             const long long nfine = (long long)nx * ny * nz;
-            for (double H = 1.5 * std::ldexp(hmin0, level + 1);; H *= 1.25) {
+            for (double H = cfg.width_ratio * std::ldexp(hmin0, level + 1);; H *= 1.25) {
                 long long m = 1;
                 for (int a = 0; a < 3; a++) {
                     ch[a] = spacing_groups(faces[a], H);
@@ -1170,7 +1260,8 @@ void GMG<T>::apply(cudaStream_t s, const T *r, T *z, const int *gate) {
     if (L1.cx && L1.cy && L1.cz)
         launch_pdl(k_mg0_restrict2<T>, dim3((g.nz + 31) / 32, (g.ny + 7) / 8, L1.nx), dim3(32, 8), 0, s, A_, r, z, L1, gate);
     else
-        launch_pdl(k_mg0_restrict<T>, l3_grid(L1.nx, L1.ny, L1.nz), l3_block(), 0, s, A_, r, z, L1, gate);
+        launch_pdl(k_mg0_restrict_g<T>, dim3((L1.nz + 15) / 16, (L1.ny + 3) / 4, L1.nx), dim3(32, 8), 0, s, A_, r, z,
+                   L1, gate);
     k++;
     te(tp);
     tp = tb("mgc_down");
@@ -1190,7 +1281,9 @@ void GMG<T>::apply(cudaStream_t s, const T *r, T *z, const int *gate) {
             launch_pdl(k_fill0<T>, nblk(L.n, 256), 256, 0, s, L.Z, L.n, gate);
             k++;
         }
-        launch_pdl(k_mgc_restrict<T>, l3_grid(C.nx, C.ny, C.nz), l3_block(), 0, s, L, C, per, gate);
+        // After a red/black pre-smoothing the last colour's residuals are 0.
+        const int skip = cfg_.nuc_pre > 0 && ncol == 2 ? 1 : -1;
+        launch_pdl(k_mgc_restrict<T>, l3_grid(C.nx, C.ny, C.nz), l3_block(), 0, s, L, C, per, skip, gate);
         k++;
     }
     te(tp);

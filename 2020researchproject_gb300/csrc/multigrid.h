@@ -19,7 +19,8 @@
 // 5:1 on every level, where point Gauss-Seidel barely smooths the weakly
 // coupled direction.  By spacing (MG_COARSEN_SPACING, the default), level
 // L merges a pair of neighbouring cells only while their joint width stays
-// within 1.5 x 2^(L+1) x the finest width of the grid: the small cells of
+// within width_ratio x 2^(L+1) x the finest width of the grid (1.5 by
+// default): the small cells of
 // the clustered region merge first and the large far-field cells wait
 // until the others have grown to their size (semi-coarsening toward
 // isotropic cells).  A level is kept at no more than half the cells of the
@@ -71,6 +72,7 @@ struct GMGConfig {
     int coarse_sweeps = 8;          // coarsest level
     double omega = 1.0;             // over-relaxation of the fine-grid fluid rows
     int coarsening = MG_COARSEN_SPACING;
+    double width_ratio = 1.5;       // spacing rule: merge while the pair is within width_ratio x the target
 };
 
 // Host geometry of the fine grid: interior face coordinates per axis.

@@ -129,6 +129,7 @@ struct ibm3d_device {
     int mg_sweeps[5] = {5, 5, 1, 1, 8};  // multigrid sweeps: fine pre/post, coarse pre/post, coarsest
     double mg_omega = 1.0;               // over-relaxation of the fine-grid smoother
     int mg_coarsening = IBM3D_COARSEN_SPACING;
+    double mg_width_ratio = 1.5;
     // Mixed path: relative tolerance of each FP32 inner solve (momentum,
     // pressure) and the refinement-cycle cap.
     double inner_tol[2] = {1e-5, 1e-5};
@@ -1490,6 +1491,7 @@ void IBMSolver_assemble(IBMSolver *s) {
     mc.coarse_sweeps = d->mg_sweeps[4];
     mc.omega = d->mg_omega;
     mc.coarsening = d->mg_coarsening == IBM3D_COARSEN_HALVE ? MG_COARSEN_HALVE : MG_COARSEN_SPACING;
+    mc.width_ratio = d->mg_width_ratio;
     const int *gcell = d->nghost ? d->gargs.cell : nullptr;
     d->mg = new GMG<double>();
     d->mg32 = new GMG<float>();
@@ -2051,9 +2053,13 @@ void IBMSolver_set_multigrid(IBMSolver *s, int nu_pre, int nu_post, int nuc_pre,
     drop_graphs(d);
 }
 
-void IBMSolver_set_coarsening(IBMSolver *s, int mode) {
+void IBMSolver_set_coarsening(IBMSolver *s, int mode, double width_ratio) {
     if (mode != IBM3D_COARSEN_HALVE && mode != IBM3D_COARSEN_SPACING) {
         set_status(s, IBM3D_EARG, "IBMSolver_set_coarsening: unknown mode %d", mode);
+        return;
+    }
+    if (!(width_ratio == 0.0 || (width_ratio >= 1.0 && width_ratio <= 64.0))) {
+        set_status(s, IBM3D_EARG, "IBMSolver_set_coarsening: width ratio %g outside [1, 64]", width_ratio);
         return;
     }
     if (s->dev->mg) {
@@ -2061,6 +2067,7 @@ void IBMSolver_set_coarsening(IBMSolver *s, int mode) {
         return;
     }
     s->dev->mg_coarsening = mode;
+    s->dev->mg_width_ratio = width_ratio == 0.0 ? 1.5 : width_ratio;
 }
 
 void IBMSolver_set_graphs(IBMSolver *s, int on) {

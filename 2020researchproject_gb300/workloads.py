@@ -165,7 +165,7 @@ def build_solver(ibm, case, tol=1e-6, div_tol=0.0, coarsening=None):
     if div_tol > 0:
         s.set_div_tol(div_tol)
     if coarsening is not None:
-        s.set_coarsening(coarsening)
+        s.set_coarsening(*coarsening) if isinstance(coarsening, tuple) else s.set_coarsening(coarsening)
     s.assemble()
     return s
 

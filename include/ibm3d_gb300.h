@@ -88,14 +88,15 @@ void IBMSolver_set_multigrid(IBMSolver *, int nu_pre, int nu_post, int nuc_pre, 
 
 /* Coarsening of the pressure multigrid (before IBMSolver_assemble).
    IBM3D_COARSEN_SPACING (default): a coarse level merges neighbouring
-   cells along an axis only while their joint width stays small against
-   the level's target width (1.5 x 2^(level+1) x the finest width), so the
-   small cells of a stretched grid coarsen first and the levels stay near
-   isotropic; each level keeps at most half the cells of the one before.
-   IBM3D_COARSEN_HALVE: every level halves every axis.  The two coincide on
-   uniform grids.  Tuning only: the solve stops on the same test. */
+   cells along an axis only while their joint width is at most
+   width_ratio x 2^(level+1) x the finest width (width_ratio in [1, 64];
+   0 = the default 1.5), so the small cells of a stretched grid coarsen
+   first and the levels stay near isotropic; each level keeps at most half
+   the cells of the one before.  IBM3D_COARSEN_HALVE: every level halves
+   every axis (width_ratio unused).  The two coincide on uniform grids.
+   Tuning only: the solve stops on the same test. */
 enum { IBM3D_COARSEN_HALVE = 0, IBM3D_COARSEN_SPACING = 1 };
-void IBMSolver_set_coarsening(IBMSolver *, int mode);
+void IBMSolver_set_coarsening(IBMSolver *, int mode, double width_ratio);
 
 /* Restart length of SOLVER_GMRES pressure solves (1..32; default 10, the
    reference's KDim).  The GMRES is flexible (it keeps every preconditioned
