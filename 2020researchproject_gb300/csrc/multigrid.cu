@@ -318,20 +318,23 @@ static inline dim3 l3_block() { return dim3(L3_TK, L3_TJ, 1); }
 
 // Restriction of the fine normalised rows' residual, scaled to
 // conductance form (Vol * coeffsum * r), into a level 1 whose groups are
-// uneven: a block takes 4 x 16 coarse cells (J, K) of coarse plane I.  Its
-// 32 x 8 threads each take one fine (j, k) under the tile (coalesced rows
-// along k), summed over the plane group in x, into shared memory; 64 of
-// them then add up each coarse cell's one to four entries.  Grid
-// (ceil(nz1/16), ceil(ny1/4), nx1).
+// uneven.  Tiles: coarse ranges [segj[b], segj[b+1]) x [segk[b], segk[b+1])
+// cut on the host so that each covers at most 8 fine rows and 32 fine
+// columns (as many as fit), ending on group boundaries.  A block takes one
+// tile of coarse plane I; its 32 x 8 threads each take one fine (j, k)
+// (coalesced rows along k), summed over the plane group in x, into shared
+// memory; then one thread per coarse cell adds up its one to four entries.
+// Grid (nsegk, nsegj, nx1).
 template <typename T>
 __global__ void __launch_bounds__(256)
-k_mg0_restrict_g(const OpT<T> c, const T *__restrict__ r, const T *__restrict__ z, MGLevel<T> L1, const int *gate) {
+k_mg0_restrict_g(const OpT<T> c, const T *__restrict__ r, const T *__restrict__ z, MGLevel<T> L1,
+                 const int *__restrict__ segj, const int *__restrict__ segk, const int *gate) {
     MG_GATE(gate);
     __shared__ T part[8][33];
     const Grid &g = c.g;
     const int I = blockIdx.z;
-    const int J0 = blockIdx.y * 4, K0 = blockIdx.x * 16;
-    const int J1 = min(J0 + 4, L1.ny), K1 = min(K0 + 16, L1.nz);
+    const int J0 = segj[blockIdx.y], J1 = segj[blockIdx.y + 1];
+    const int K0 = segk[blockIdx.x], K1 = segk[blockIdx.x + 1];
     const int jb = L1.ch[1][J0], je = L1.ch[1][J1];
     const int kb = L1.ch[2][K0], ke = L1.ch[2][K1];
     const int j = jb + threadIdx.y, k = kb + threadIdx.x;
@@ -354,10 +357,9 @@ k_mg0_restrict_g(const OpT<T> c, const T *__restrict__ r, const T *__restrict__ 
     }
     part[threadIdx.y][threadIdx.x] = acc;
     __syncthreads();
-    const int t = threadIdx.y * 32 + threadIdx.x;
-    if (t >= 64) return;
-    const int J = J0 + (t >> 4), K = K0 + (t & 15);
-    if (J >= J1 || K >= K1) return;
+    const int t = threadIdx.y * 32 + threadIdx.x, nk = K1 - K0;
+    if (t >= (J1 - J0) * nk) return;
+    const int J = J0 + t / nk, K = K0 + t % nk;
     const int ja = L1.ch[1][J] - jb, jz = L1.ch[1][J + 1] - jb;
     const int ka = L1.ch[2][K] - kb, kz = L1.ch[2][K + 1] - kb;
     T sum = 0;
@@ -807,7 +809,7 @@ k_mg_tail(const MGLevel<T> *__restrict__ lv, const int first, const int nlev, co
             L.diag = q; q += n;
             L.R = q; q += n;
             L.Z = q; q += n;
-            L.idiag = nullptr;  // the tail divides by its shared-memory diag
+            L.idiag = q; q += n;
             loc[l - first] = L;
         }
         // Transfer tables of the levels below `first` (toward their finer
@@ -850,28 +852,49 @@ k_mg_tail(const MGLevel<T> *__restrict__ lv, const int first, const int nlev, co
             L.Ty[c] = G.Ty[c];
             L.Tz[c] = G.Tz[c];
             L.diag[c] = G.diag[c];
+            L.idiag[c] = G.idiag[c];
             L.R[c] = l == first ? G.R[c] : (T)0;
             L.Z[c] = 0;
         }
     }
     __syncthreads();
-    // Cell c of level L.
-    auto cell = [&](const MGLevel<T> &L, int c, int &I, int &J, int &K) {
-        const int nyz = L.ny * L.nz;
-        I = c / nyz;
-        const int rem = c - I * nyz;
-        J = rem / L.nz;
-        K = rem - J * L.nz;
+    // Thread tid takes cell tid of a level (a level holds at most
+    // TAIL_THREADS cells): its coordinates and colour, computed once per
+    // phase of the level.
+    struct Pos {
+        int I, J, K, col;
     };
+    auto pos = [&](const MGLevel<T> &L) {
+        Pos p{0, 0, 0, -1};
+        if (tid < L.n) {
+            const int nyz = L.ny * L.nz;
+            p.I = tid / nyz;
+            const int rem = tid - p.I * nyz;
+            p.J = rem / L.nz;
+            p.K = rem - p.J * L.nz;
+            p.col = cell_color(p.I, p.J, p.K, L.nx, L.ny, L.nz, per.p);
+        }
+        return p;
+    };
+    // Colour passes of a level; a level of at most 32 cells runs in warp 0
+    // alone, its passes separated by warp barriers, and one block barrier
+    // after the last.
     auto sweep = [&](const MGLevel<T> &L, int nsw) {
+        const Pos p = pos(L);
         const int ncol = level_colors(L, per.p);
+        if (L.n <= 32) {
+            if (tid < 32)
+                for (int s = 0; s < nsw; s++)
+                    for (int col = 0; col < ncol; col++) {
+                        if (p.col == col) coarse_relax(L, p.I, p.J, p.K, per.p);
+                        __syncwarp();
+                    }
+            __syncthreads();
+            return;
+        }
         for (int s = 0; s < nsw; s++)
             for (int col = 0; col < ncol; col++) {
-                for (int c = tid; c < L.n; c += TAIL_THREADS) {
-                    int I, J, K;
-                    cell(L, c, I, J, K);
-                    if (cell_color(I, J, K, L.nx, L.ny, L.nz, per.p) == col) coarse_relax(L, I, J, K, per.p);
-                }
+                if (p.col == col) coarse_relax(L, p.I, p.J, p.K, per.p);
                 __syncthreads();
             }
     };
@@ -880,21 +903,16 @@ k_mg_tail(const MGLevel<T> *__restrict__ lv, const int first, const int nlev, co
         sweep(L, l == nlev - 1 ? csweeps : nu1);
         if (l < nlev - 1) {
             const MGLevel<T> &C = loc[l + 1 - first];
-            for (int c = tid; c < C.n; c += TAIL_THREADS) {
-                int I, J, K;
-                cell(C, c, I, J, K);
-                C.R[c] = coarse_restrict_value(L, C, I, J, K, per.p, nu1 > 0 && level_colors(L, per.p) == 2 ? 1 : -1);
-            }
+            const Pos p = pos(C);
+            const int skip = nu1 > 0 && level_colors(L, per.p) == 2 ? 1 : -1;
+            if (tid < C.n) C.R[tid] = coarse_restrict_value(L, C, p.I, p.J, p.K, per.p, skip);
             __syncthreads();
         }
     }
     for (int l = nlev - 2; l >= first; l--) {
         const MGLevel<T> &L = loc[l - first], &C = loc[l + 1 - first];
-        for (int c = tid; c < L.n; c += TAIL_THREADS) {
-            int I, J, K;
-            cell(L, c, I, J, K);
-            if (L.diag[c] != (T)0) L.Z[c] += prolong_value(C, I, J, K);
-        }
+        const Pos p = pos(L);
+        if (tid < L.n && L.diag[tid] != (T)0) L.Z[tid] += prolong_value(C, p.I, p.J, p.K);
         __syncthreads();
         sweep(L, nu2);
     }
@@ -902,12 +920,12 @@ k_mg_tail(const MGLevel<T> *__restrict__ lv, const int first, const int nlev, co
     for (int c = tid; c < L.n; c += TAIL_THREADS) G.Z[c] = L.Z[c];
 }
 
-// Shared memory the tail kernel needs for levels [first, nlev): six
+// Shared memory the tail kernel needs for levels [first, nlev): seven
 // arrays per level and the transfer tables of the levels below `first`.
 template <typename T>
 static size_t tail_bytes(const std::vector<MGLevel<T>> &lv, int first) {
     size_t b = 0;
-    for (int l = first; l < (int)lv.size(); l++) b += 6 * sizeof(T) * (size_t)lv[l].n;
+    for (int l = first; l < (int)lv.size(); l++) b += 7 * sizeof(T) * (size_t)lv[l].n;
     for (int l = first + 1; l < (int)lv.size(); l++) {
         const int nf[3] = {lv[l - 1].nx, lv[l - 1].ny, lv[l - 1].nz}, nc[3] = {lv[l].nx, lv[l].ny, lv[l].nz};
         for (int a = 0; a < 3; a++) b += (sizeof(T) + 2 * sizeof(int)) * (size_t)nf[a] + sizeof(int) * (nc[a] + 1);
@@ -1139,6 +1157,8 @@ int GMG<T>::setup(cudaStream_t s, const OpT<double> &A64, const OpT<T> &A, const
         k_mg_diag<<<nblk(L.n, 128), 128, 0, s>>>(L, gx, gy, gz, per);
         G.push_back(gx); G.push_back(gy); G.push_back(gz);
         for (int a = 0; a < 3; a++) faces[a] = cfs[a];
+        if (lv64.empty())
+            for (int a = 0; a < 3; a++) ch1_[a] = ch[a];
         const size_t bt = sizeof(T) * L.n;
         LT.Tx = (T *)dalloc(bt, true); LT.Ty = (T *)dalloc(bt, true); LT.Tz = (T *)dalloc(bt, true);
         LT.diag = (T *)dalloc(bt, true); LT.R = (T *)dalloc(bt, true); LT.Z = (T *)dalloc(bt, true);
@@ -1154,12 +1174,34 @@ int GMG<T>::setup(cudaStream_t s, const OpT<double> &A64, const OpT<T> &A, const
         nx = L.nx; ny = L.ny; nz = L.nz;
         if (L.n <= 64) break;
     }
+    // Tiles of the restriction into level 1 (k_mg0_restrict_g): coarse
+    // ranges covering at most 8 fine rows (j) and 32 fine columns (k).
+    if (!lv64.empty()) {
+        auto cut = [](const std::vector<int> &chv, int width) {
+            std::vector<int> seg{0};
+            const int nc = (int)chv.size() - 1;
+            for (int K = 0; K < nc;) {
+                int K1 = K + 1;
+                while (K1 < nc && chv[K1 + 1] - chv[K] <= width) K1++;
+                seg.push_back(K1);
+                K = K1;
+            }
+            return seg;
+        };
+        const std::vector<int> sj = cut(ch1_[1], 8), sk = cut(ch1_[2], 32);
+        nsegj_ = (int)sj.size() - 1;
+        nsegk_ = (int)sk.size() - 1;
+        segj_ = (int *)upload(sj.data(), sizeof(int) * sj.size(), true);
+        segk_ = (int *)upload(sk.data(), sizeof(int) * sk.size(), true);
+        if (!segj_ || !segk_) return -1;
+    }
     // The coarsest levels with at most TAIL_THREADS cells each run in the tail.
     tail_ = (int)levels_.size() - 1;
     while (tail_ > 0 && levels_[tail_ - 1].n <= TAIL_CELLS && (int)levels_.size() - (tail_ - 1) <= 16 &&
            tail_bytes(levels_, tail_ - 1) <= TAIL_SMEM_MAX)
         tail_--;
     if (!levels_.empty()) {
+        if (levels_[tail_].n > TAIL_CELLS) return -1;  // the tail takes one cell per thread
         tail_smem_ = tail_bytes(levels_, tail_);
         // The limit is a property of the kernel, shared by every solver in
         // the process: only ever raise it.
@@ -1260,8 +1302,8 @@ void GMG<T>::apply(cudaStream_t s, const T *r, T *z, const int *gate) {
     if (L1.cx && L1.cy && L1.cz)
         launch_pdl(k_mg0_restrict2<T>, dim3((g.nz + 31) / 32, (g.ny + 7) / 8, L1.nx), dim3(32, 8), 0, s, A_, r, z, L1, gate);
     else
-        launch_pdl(k_mg0_restrict_g<T>, dim3((L1.nz + 15) / 16, (L1.ny + 3) / 4, L1.nx), dim3(32, 8), 0, s, A_, r, z,
-                   L1, gate);
+        launch_pdl(k_mg0_restrict_g<T>, dim3(nsegk_, nsegj_, L1.nx), dim3(32, 8), 0, s, A_, r, z, L1,
+                   (const int *)segj_, (const int *)segk_, gate);
     k++;
     te(tp);
     tp = tb("mgc_down");

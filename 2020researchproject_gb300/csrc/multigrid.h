@@ -128,6 +128,10 @@ class GMG : public Preconditioner<T> {
     int *outer1_ = nullptr;
     int nout1_ = 0;
     int per_[3] = {0, 0, 0};
+    // Level 1's groups (host copy) and the restriction tiles cut from them.
+    std::vector<int> ch1_[3];
+    int *segj_ = nullptr, *segk_ = nullptr;
+    int nsegj_ = 0, nsegk_ = 0;
     std::vector<void *> allocs_;
     int launches_ = 0;
     // sweeps of the fine-grid smoother; from_zero: z is taken as 0 on entry
