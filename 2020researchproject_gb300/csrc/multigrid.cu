@@ -213,19 +213,26 @@ k_mg0_init3(const OpT<T> c, const T *__restrict__ r, T *__restrict__ z, const Pe
 }
 
 // Ghost rows of the smoother, Jacobi-style among ghosts (each reads the
-// values before the pass): a pass into tmp, then a scatter.
+// values before the pass): a pass into tmp, then a scatter.  The row
+// (1 - ws) z - sum(w z_stencil) = r is relaxed as
+// z += (r + sum - (1 - ws) z) * gidiv, with gidiv = 1 / max(1 - ws,
+// 2 sum|w on other ghosts|, 1e-3) set up per ghost: the exact row solve
+// wherever the ghost block is diagonally dominant by a factor two (then
+// the Jacobi pass over ghosts contracts), damped elsewhere.  Ghosts close
+// to the surface have 1 - ws down to ~0.01; relaxing them only partly
+// leaves a slowly converging error that doubled the Krylov iterations.
 
 template <typename T>
-__device__ __forceinline__ T ghost_value(const OpT<T> &c, const T *__restrict__ r, const T *__restrict__ z, int P) {
+__device__ __forceinline__ T ghost_value(const OpT<T> &c, const T *__restrict__ r, const T *__restrict__ z, int P,
+                                         const T *__restrict__ gidiv) {
     const int id = c.gid[P];
     T sum = 0;
     for (int e = 0; e < 8; e++) {
         const int q = c.gidx[8 * id + e];
         if (q >= 0) sum += c.gw[8 * id + e] * z[q];
     }
-    const T ws = c.gwself[id];
-    const T d = (T)1 - ws;
-    return d >= (T)0.25 ? (r[P] + sum) / d : ws * z[P] + r[P] + sum;
+    const T zp = z[P];
+    return zp + (r[P] + sum - ((T)1 - c.gwself[id]) * zp) * gidiv[id];
 }
 
 template <typename T>
@@ -291,11 +298,12 @@ __device__ __forceinline__ T outer_chain_value(const OpT<T> &c, const T *__restr
 template <typename T>
 __global__ void __launch_bounds__(256)
 k_mg0_outer(const OpT<T> c, const T *__restrict__ r, T *z, const int *__restrict__ outer, const int nout,
-            const int *__restrict__ gcell, const int ng, const int gblocks, T *tmp, const int *gate) {
+            const int *__restrict__ gcell, const int ng, const int gblocks, T *tmp, const T *__restrict__ gidiv,
+            const int *gate) {
     MG_GATE(gate);
     if ((int)blockIdx.x < gblocks) {
         const int g = blockIdx.x * blockDim.x + threadIdx.x;
-        if (g < ng) tmp[g] = ghost_value(c, r, z, gcell[g]);
+        if (g < ng) tmp[g] = ghost_value(c, r, z, gcell[g], gidiv);
         return;
     }
     const int t = (blockIdx.x - gblocks) * blockDim.x + threadIdx.x;
@@ -1054,14 +1062,35 @@ int GMG<T>::setup(cudaStream_t s, const OpT<double> &A64, const OpT<T> &A, const
     }
     ghost_reads_outer_ = false;
     if (nghost > 0) {
-        std::vector<int> gidx(8 * (size_t)nghost);
+        std::vector<int> gidx(8 * (size_t)nghost), gcell(nghost);
+        std::vector<double> gw(8 * (size_t)nghost), gws(nghost);
         cudaMemcpy(gidx.data(), A.gidx, sizeof(int) * gidx.size(), cudaMemcpyDeviceToHost);
+        cudaMemcpy(gcell.data(), ghost_cell, sizeof(int) * nghost, cudaMemcpyDeviceToHost);
+        cudaMemcpy(gw.data(), A64.gw, sizeof(double) * gw.size(), cudaMemcpyDeviceToHost);
+        cudaMemcpy(gws.data(), A64.gwself, sizeof(double) * nghost, cudaMemcpyDeviceToHost);
         for (int q : gidx) {
             if (q < 0) continue;
             int i, j, k;
             cijk(g, q, i, j, k);
             if (i < 0 || i >= g.nx || j < 0 || j >= g.ny || k < 0 || k >= g.nz) ghost_reads_outer_ = true;
         }
+        // Inverse divisors of the ghost relaxation (ghost_value), per
+        // ghost id (ghost id t is the ghost at padded cell gcell[t]).
+        std::vector<int> sorted(gcell);
+        std::sort(sorted.begin(), sorted.end());
+        std::vector<T> idiv(nghost);
+        for (int t = 0; t < nghost; t++) {
+            double wgg = 0.0;
+            for (int e = 0; e < 8; e++) {
+                const int q = gidx[8 * (size_t)t + e];
+                if (q >= 0 && q != gcell[t] && std::binary_search(sorted.begin(), sorted.end(), q))
+                    wgg += std::fabs(gw[8 * (size_t)t + e]);
+            }
+            idiv[t] = (T)(1.0 / std::max({1.0 - gws[t], 2.0 * wgg, 1e-3}));
+        }
+        ghost_idiv_ = (T *)dalloc(sizeof(T) * nghost, true);
+        if (!ghost_idiv_) return -1;
+        cudaMemcpyAsync(ghost_idiv_, idiv.data(), sizeof(T) * nghost, cudaMemcpyHostToDevice, s);
     }
 
     Per3 per{{per_[0], per_[1], per_[2]}};
@@ -1259,10 +1288,11 @@ int GMG<T>::smooth0(cudaStream_t s, const T *r, T *z, int sweeps, bool from_zero
             const int *ol = last ? A_.sw.outer : outer1_;
             const int no = last ? A_.sw.nout : nout1_;
             launch_pdl(k_mg0_outer<T>, gb + (no + 255) / 256, 256, 0, s, A_, r, z, ol, no, ghost_cell_, nghost_, gb, ghost_tmp_,
-                                                                gate);
+                       (const T *)ghost_idiv_, gate);
             k++;
         } else {  // a ghost stencil reaches an outer cell: ghosts first, outer rows after the scatter
-            launch_pdl(k_mg0_outer<T>, gb, 256, 0, s, A_, r, z, A_.sw.outer, 0, ghost_cell_, nghost_, gb, ghost_tmp_, gate);
+            launch_pdl(k_mg0_outer<T>, gb, 256, 0, s, A_, r, z, A_.sw.outer, 0, ghost_cell_, nghost_, gb, ghost_tmp_,
+                       (const T *)ghost_idiv_, gate);
             k++;
         }
         if (nghost_ > 0) {
@@ -1270,7 +1300,8 @@ int GMG<T>::smooth0(cudaStream_t s, const T *r, T *z, int sweeps, bool from_zero
             k++;
         }
         if (ghost_reads_outer_) {
-            launch_pdl(k_mg0_outer<T>, ob, 256, 0, s, A_, r, z, A_.sw.outer, A_.sw.nout, ghost_cell_, 0, 0, ghost_tmp_, gate);
+            launch_pdl(k_mg0_outer<T>, ob, 256, 0, s, A_, r, z, A_.sw.outer, A_.sw.nout, ghost_cell_, 0, 0, ghost_tmp_,
+                       (const T *)ghost_idiv_, gate);
             k++;
         }
         te(to);

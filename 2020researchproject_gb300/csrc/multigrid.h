@@ -121,6 +121,7 @@ class GMG : public Preconditioner<T> {
     const int *ghost_cell_ = nullptr;
     int nghost_ = 0;
     T *ghost_tmp_ = nullptr;
+    T *ghost_idiv_ = nullptr;  // per ghost id: inverse divisor of its relaxation
     bool ghost_reads_outer_ = false;
     // Layer-1 face cells of the outer layers: the only outer cells the
     // colour passes read (edges, corners and layer 2 are set after the
