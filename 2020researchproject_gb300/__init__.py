@@ -320,7 +320,7 @@ class IBMSolver:
         self._lib.IBMSolver_set_gmres_restart(self._s, restart)
         self._check("set_gmres_restart")
 
-    def set_refinement(self, inner_tol_mom=1e-5, inner_tol_p=1e-5, max_outer=12):
+    def set_refinement(self, inner_tol_mom=5e-7, inner_tol_p=1e-5, max_outer=12):
         self._lib.IBMSolver_set_refinement(self._s, inner_tol_mom, inner_tol_p, max_outer)
         self._check("set_refinement")
 

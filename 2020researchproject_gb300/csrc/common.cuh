@@ -273,6 +273,41 @@ __device__ inline void block_max(double (&v)[NV], double *smem) {
     }
 }
 
+// Block-level combine of NV per-thread values: entries [0, NS) summed,
+// [NS, NV) maxed (all >= 0).  The warp stage runs in the accumulator type
+// A (an FP32 kernel keeps its adds off the FP64 pipe); one value per warp
+// is widened to double for the stage across warps.  Fixed shape, so the
+// result is bitwise reproducible.  Valid in warp 0; smem holds 32 * NV
+// doubles.
+template <int NV, int NS, typename A>
+__device__ inline void block_reduce(const A (&v)[NV], double (&out)[NV], double *smem) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < NV; q++) {
+        A x = v[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const A y = __shfl_down_sync(0xffffffffu, x, o);
+            x = q < NS ? x + y : (x > y ? x : y);
+        }
+        if (lane == 0) smem[warp * NV + q] = (double)x;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = blockDim.x >> 5;
+#pragma unroll
+        for (int q = 0; q < NV; q++) {
+            double x = lane < nw ? smem[lane * NV + q] : 0.0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const double y = __shfl_down_sync(0xffffffffu, x, o);
+                x = q < NS ? x + y : fmax(x, y);
+            }
+            out[q] = x;
+        }
+    }
+}
+
 // Publishes this block's NV partials; returns true in EVERY thread of the
 // last block to finish (the same value across the block), which then
 // reduces all blocks' partials with reduce_partials.

@@ -70,26 +70,12 @@ __device__ __forceinline__ void set_loop(const LoopCtl &lc, bool cont) {
 // Reduction tail shared by the kernels below: block-level combine, then
 // the last block reduces all partials (NS sums first, then maxima) and
 // thread 0 runs `fin(tot)`.
-template <int NV, int NS, typename Fin>
-__device__ __forceinline__ void reduce_and_finish(double (&v)[NV], double *smem, double *partials,
+template <int NV, int NS, typename A, typename Fin>
+__device__ __forceinline__ void reduce_and_finish(const A (&v)[NV], double *smem, double *partials,
                                                   unsigned int *counter, Fin fin) {
     static_assert(NS >= 1 && NS <= NV, "at least one summed entry");
-    double sm[NS];
-#pragma unroll
-    for (int q = 0; q < NS; q++) sm[q] = v[q];
-    block_sum<NS>(sm, smem);
     double out[NV];
-#pragma unroll
-    for (int q = 0; q < NS; q++) out[q] = sm[q];
-    if constexpr (NV > NS) {
-        double mx[NV - NS];
-#pragma unroll
-        for (int q = NS; q < NV; q++) mx[q - NS] = v[q];
-        __syncthreads();
-        block_max<NV - NS>(mx, smem + 32 * NS);
-#pragma unroll
-        for (int q = NS; q < NV; q++) out[q] = mx[q - NS];
-    }
+    block_reduce<NV, NS>(v, out, smem);
     if (!publish_partials<NV>(out, partials, counter)) return;
     double tot[NV];
     reduce_partials<NV, NS>(partials, gridDim.x, tot, smem);
@@ -129,10 +115,7 @@ k_bicg_init(const long long n, const T *__restrict__ b, T *x, T *r, T *r0, T *p,
             a[c] += bv * bv;
         }
     }
-    double acc[NC];
-#pragma unroll
-    for (int c = 0; c < NC; c++) acc[c] = (double)a[c];
-    reduce_and_finish<NC, NC>(acc, smem, partials, counter, [&](const double *tot) {
+    reduce_and_finish<NC, NC>(a, smem, partials, counter, [&](const double *tot) {
         bool run = false;
         for (int c = 0; c < NC; c++) {
             KScal &s = sc[c];
@@ -184,19 +167,23 @@ k_bicg_p(const long long n, const T *__restrict__ r, T *__restrict__ p, const T 
 }
 
 // Calls f(c, P, i, q) for every interior row of this thread's column and
-// g(c, P) for its outer row, for each running component c.
+// g(c, P) for its outer row, for each running component c.  Components
+// one after the other (each component's rows in i order): only one
+// component's loads are live at a time, which keeps the 3-component
+// kernels' registers, and so their occupancy, in check.
 template <typename T, int NC, typename FI, typename FO>
 __device__ __forceinline__ void sweep_rows(const OpT<T> &A, const bool (&run)[NC], FI fi, FO fo) {
     int i0, i1, j, k;
     if (sweep_column(A.sw, A.g, i0, i1, j, k)) {
         if (j >= A.g.ny || k >= A.g.nz) return;
         const Column<T> q = column(A, j, k);
-        long long P = cidx(A.g, i0, j, k);
-#pragma unroll 2
-        for (int i = i0; i < i1; i++, P += A.g.sx) {
+        const long long P0 = cidx(A.g, i0, j, k);
 #pragma unroll
-            for (int c = 0; c < NC; c++)
-                if (run[c]) fi(c, P, i, q);
+        for (int c = 0; c < NC; c++) {
+            if (!run[c]) continue;
+            long long P = P0;
+#pragma unroll 2
+            for (int i = i0; i < i1; i++, P += A.g.sx) fi(c, P, i, q);
         }
     } else {
         const int t = sweep_outer(A.sw);
@@ -210,7 +197,7 @@ __device__ __forceinline__ void sweep_rows(const OpT<T> &A, const bool (&run)[NC
 
 // ------------------------------------------- v = A ph, alpha = rho/(r0,v) --
 template <typename T, int NC>
-__global__ void __launch_bounds__(SW_THREADS)
+__global__ void __launch_bounds__(SW_THREADS, (sizeof(T) == 4 || NC == 1) ? 4 : 2)
 k_bicg_spmv_v(const OpT<T> A, const int op, const long long n, const T *__restrict__ ph, T *__restrict__ v,
               const T *__restrict__ r0, KScal *sc, double *partials, unsigned int *counter) {
     pdl_enter();
@@ -236,10 +223,7 @@ k_bicg_spmv_v(const OpT<T> A, const int op, const long long n, const T *__restri
             v[o + P] = y;
             a[c] += r0[o + P] * y;
         });
-    double acc[NC];
-#pragma unroll
-    for (int c = 0; c < NC; c++) acc[c] = (double)a[c];
-    reduce_and_finish<NC, NC>(acc, smem, partials, counter, [&](const double *tot) {
+    reduce_and_finish<NC, NC>(a, smem, partials, counter, [&](const double *tot) {
         for (int c = 0; c < NC; c++) {
             KScal &s = sc[c];
             if (s.state != KS_RUN) continue;
@@ -292,10 +276,10 @@ k_bicg_s(const OpT<T> A, const long long n, const T *__restrict__ r, const T *__
             }
         }
     }
-    double acc[NC + 1];
+    typename AccT<T>::type acc[NC + 1];
 #pragma unroll
-    for (int c = 0; c < NC; c++) acc[c] = (double)a[c];
-    acc[NC] = (double)dmax;
+    for (int c = 0; c < NC; c++) acc[c] = a[c];
+    acc[NC] = dmax;
     reduce_and_finish<NC + 1, NC>(acc, smem, partials, counter, [&](const double *tot) {
         for (int c = 0; c < NC; c++) {
             KScal &st = sc[c];
@@ -311,7 +295,7 @@ k_bicg_s(const OpT<T> A, const long long n, const T *__restrict__ r, const T *__
 
 // --------------------------------------- t = A sh, omega = (t,s)/(t,t) --
 template <typename T, int NC>
-__global__ void __launch_bounds__(SW_THREADS)
+__global__ void __launch_bounds__(SW_THREADS, (sizeof(T) == 4 || NC == 1) ? 4 : 2)
 k_bicg_spmv_t(const OpT<T> A, const int op, const long long n, const T *__restrict__ sh, T *__restrict__ t,
               const T *__restrict__ s, KScal *sc, double *partials, unsigned int *counter) {
     pdl_enter();
@@ -339,10 +323,7 @@ k_bicg_spmv_t(const OpT<T> A, const int op, const long long n, const T *__restri
             a[2 * c] += y * s[o + P];
             a[2 * c + 1] += y * y;
         });
-    double acc[2 * NC];
-#pragma unroll
-    for (int q = 0; q < 2 * NC; q++) acc[q] = (double)a[q];
-    reduce_and_finish<2 * NC, 2 * NC>(acc, smem, partials, counter, [&](const double *tot) {
+    reduce_and_finish<2 * NC, 2 * NC>(a, smem, partials, counter, [&](const double *tot) {
         for (int c = 0; c < NC; c++) {
             KScal &st = sc[c];
             if (st.state != KS_RUN) continue;
@@ -416,10 +397,10 @@ k_bicg_xr(const OpT<T> A, const long long n, T *__restrict__ x, T *__restrict__ 
             }
         }
     }
-    double acc[2 * NC + 1];
+    typename AccT<T>::type acc[2 * NC + 1];
 #pragma unroll
-    for (int q = 0; q < 2 * NC; q++) acc[q] = (double)a[q];
-    acc[2 * NC] = (double)dmax;
+    for (int q = 0; q < 2 * NC; q++) acc[q] = a[q];
+    acc[2 * NC] = dmax;
     reduce_and_finish<2 * NC + 1, 2 * NC>(acc, smem, partials, counter, [&](const double *tot) {
         bool run = false;
         for (int c = 0; c < NC; c++) {

@@ -112,7 +112,7 @@ double IBMSolver_autotune(IBMSolver *, int steps, int *best);
 
 /* Mixed path (IBM3D_MIXED): relative tolerance of each FP32 inner solve of
    the momentum and pressure refinement cycles, and the cycle cap.  The
-   outer FP64 stopping rule is unchanged.  Defaults 1e-5, 1e-5, 12. */
+   outer FP64 stopping rule is unchanged.  Defaults 5e-7, 1e-5, 12. */
 void IBMSolver_set_refinement(IBMSolver *, double inner_tol_mom, double inner_tol_p, int max_outer);
 
 /* Initial state from host arrays in the padded (N+4)^3 layout, k fastest
