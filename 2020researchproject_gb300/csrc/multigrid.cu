@@ -721,8 +721,7 @@ __global__ void __launch_bounds__(256) k_mgc_init(MGLevel<T> L, const Per3 per, 
     MG_GATE(gate);
     L3_INDEX(I, J, K, L.ny, L.nz);
     const long long q = lidx(L, I, J, K);
-    const T d = L.diag[q];
-    L.Z[q] = (cell_color(I, J, K, L.nx, L.ny, L.nz, per.p) == 0 && d != (T)0) ? L.R[q] * L.idiag[q] : (T)0;
+    L.Z[q] = cell_color(I, J, K, L.nx, L.ny, L.nz, per.p) == 0 ? L.R[q] * L.idiag[q] : (T)0;
 }
 
 // Branch-free relaxation of coarse cell (I, J, K) on a level without
@@ -737,7 +736,7 @@ __device__ __forceinline__ void coarse_relax_open(const MGLevel<T> &L, int I, in
     const long long qw = I > 0 ? q - sx : q, qe = he ? q + sx : q;
     const long long qs = J > 0 ? q - sy : q, qn = hn ? q + sy : q;
     const long long qd = K > 0 ? q - 1 : q, qu = hu ? q + 1 : q;
-    const T d = L.diag[q], R = L.R[q];
+    const T R = L.R[q];
     const T tw = L.Tx[q], te = L.Tx[qe], ts = L.Ty[q], tn = L.Ty[qn], td = L.Tz[q], tu = L.Tz[qu];
     const T zw = L.Z[qw], ze = L.Z[qe], zs = L.Z[qs], zn = L.Z[qn], zd = L.Z[qd], zu = L.Z[qu];
     T s = R;
@@ -747,7 +746,8 @@ __device__ __forceinline__ void coarse_relax_open(const MGLevel<T> &L, int I, in
     s += (hn ? tn : (T)0) * zn;
     s += td * zd;
     s += (hu ? tu : (T)0) * zu;
-    L.Z[q] = d == (T)0 ? (T)0 : s * L.idiag[q];
+    // An inactive cell has 1/diag = 0 (and R = 0, no conductances): Z = 0.
+    L.Z[q] = s * L.idiag[q];
 }
 
 // One colour pass on a coarse level; k pairs as on the fine grid when the
