@@ -96,6 +96,7 @@ def load_library(path: str = LIB_PATH):
         "IBMSolver_set_refinement": (None, [vp, d, d, i]),
         "IBMSolver_set_gmres_restart": (None, [vp, i]),
         "IBMSolver_set_coarsening": (None, [vp, i, d]),
+        "IBMSolver_set_warm_start": (None, [vp, i]),
         "IBMSolver_autotune": (d, [vp, i, ip]),
         "IBMSolver_set_ext_force_func": (None, [vp, vp, vp, vp]),
         "IBMSolver_set_smagorinsky": (None, [vp, d]),
@@ -309,6 +310,11 @@ class IBMSolver:
         ms = self._lib.IBMSolver_autotune(self._s, int(steps), _ptr(best))
         self._check("autotune")
         return ms, tuple(int(v) for v in best)
+
+    def set_warm_start(self, on=True):
+        """Mixed modes: momentum solve from the current velocity (default on)."""
+        self._lib.IBMSolver_set_warm_start(self._s, 1 if on else 0)
+        self._check("set_warm_start")
 
     def set_coarsening(self, mode=COARSEN_SPACING, width_ratio=0.0):
         """Pressure multigrid coarsening (before assemble): COARSEN_SPACING

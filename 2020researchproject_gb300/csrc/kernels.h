@@ -73,6 +73,9 @@ void launch_update_next(cudaStream_t s, const Grid &g, const Axis &ax, const Axi
 // when: 0 fills with the values at the step's start time, 1 at its end
 // time (the two differ only for VAL_FUNC faces).
 void launch_fill_outer(cudaStream_t s, const Grid &g, const BCSet &bc, double *const u[3], double *p, int when);
+// x[l n + P] = u[l][P] (NaN, as on solid cells, becomes 0): the initial
+// guess of the momentum solve.
+void launch_velocity_guess(cudaStream_t s, const Grid &g, double *const u[3], double *x);
 void launch_interp_stag(cudaStream_t s, const Grid &g, const Axis &ax, const Axis &ay, const Axis &az,
                         const double *const u[3], double *const U[3]);
 void launch_ghost_update(cudaStream_t s, const GhostArgs &a, double *const u[3], double *p);

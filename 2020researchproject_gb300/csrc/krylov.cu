@@ -443,16 +443,21 @@ k_apply(const OpT<T> A, const int op, const int comp, const T *__restrict__ x, T
 // r = b - A x (or r = b while x is still zero), with per-component ||r||^2,
 // max|r| and the divergence max; the last block derives each component's
 // state, the FP32 scale 1/max|r| (0 for converged components), counts the
-// cycle and sets the outer loop condition.
+// cycle and sets the outer loop condition.  mode: IR_NEXT (a later cycle),
+// IR_ZERO (the first, x = 0), IR_GUESS (the first, x an initial guess);
+// the first also records ||b||^2 for the relative test.
+enum { IR_NEXT = 0, IR_ZERO = 1, IR_GUESS = 2 };
+
 template <int NC>
 __global__ void __launch_bounds__(SW_THREADS)
 k_ir_residual(const OpT<double> A, const int op, const long long n, const double *__restrict__ b,
-              const double *__restrict__ x, double *r, const int x_zero, IRScal *sc, const double tol,
+              const double *__restrict__ x, double *r, const int mode, IRScal *sc, const double tol,
               const double divtol, const int max_outer, double *partials, unsigned int *counter, const LoopCtl lc) {
     pdl_enter();
     constexpr int NV = 3 * NC + 1;
     __shared__ double smem[32 * NV];
-    double sm[2 * NC], mx[NC + 1];  // ||r||^2, ||b||^2 (x_zero only); max|r|, divergence max
+    const bool x_zero = mode == IR_ZERO, first = mode != IR_NEXT;
+    double sm[2 * NC], mx[NC + 1];  // ||r||^2, ||b||^2 (first cycle only); max|r|, divergence max
     bool run[NC];
 #pragma unroll
     for (int c = 0; c < NC; c++) {
@@ -465,7 +470,7 @@ k_ir_residual(const OpT<double> A, const int op, const long long n, const double
         const double bv = b[c * n + P];
         r[c * n + P] = y;
         sm[c] += y * y;
-        if (x_zero) sm[NC + c] += bv * bv;
+        if (first) sm[NC + c] += bv * bv;
         mx[c] = fmax(mx[c], fabs(y));
         if (divtol > 0) mx[NC] = fmax(mx[NC], (double)divw(A, P, y));
     };
@@ -488,7 +493,7 @@ k_ir_residual(const OpT<double> A, const int op, const long long n, const double
         bool go = false;
         for (int c = 0; c < NC; c++) {
             IRScal &s = sc[c];
-            if (x_zero) {
+            if (first) {
                 s.bnorm2 = tot[NC + c];
                 s.outer = 0;
                 s.inner = 0;
@@ -713,12 +718,12 @@ static void launch_xr(cudaStream_t st, const OpT<T> &A, KrylovWork<T> &w, T *x, 
 }
 
 static void launch_residual(cudaStream_t st, const OpT<double> &A64, int op, IRWork &w, const double *b,
-                            const double *x, int x_zero, const SolveParams &prm, LoopCtl lc) {
+                            const double *x, int mode, const SolveParams &prm, LoopCtl lc) {
     if (w.nc == 3)
-        launch_pdl(k_ir_residual<3>, A64.sw.nblocks, SW_THREADS, 0, st, A64, op, w.n, b, x, w.r, x_zero, w.scal, prm.tol,
+        launch_pdl(k_ir_residual<3>, A64.sw.nblocks, SW_THREADS, 0, st, A64, op, w.n, b, x, w.r, mode, w.scal, prm.tol,
                                                                prm.divtol, prm.max_outer, w.partials, w.counter, lc);
     else
-        launch_pdl(k_ir_residual<1>, A64.sw.nblocks, SW_THREADS, 0, st, A64, op, w.n, b, x, w.r, x_zero, w.scal, prm.tol,
+        launch_pdl(k_ir_residual<1>, A64.sw.nblocks, SW_THREADS, 0, st, A64, op, w.n, b, x, w.r, mode, w.scal, prm.tol,
                                                                prm.divtol, prm.max_outer, w.partials, w.counter, lc);
     note_launches(1);
 }
@@ -857,8 +862,8 @@ int solve_ir(cudaStream_t st, const OpT<double> &A64, const OpT<float> &A32, int
         cudaMemcpyAsync(w.scal_h, w.scal, sizeof(IRScal) * nc, cudaMemcpyDeviceToHost, st);
         cudaStreamSynchronize(st);
     };
-    cudaMemsetAsync(x, 0, sizeof(double) * n * nc, st);
-    launch_residual(st, A64, op, w, b, x, 1, prm, LoopCtl());
+    if (!prm.x_given) cudaMemsetAsync(x, 0, sizeof(double) * n * nc, st);
+    launch_residual(st, A64, op, w, b, x, prm.x_given ? IR_GUESS : IR_ZERO, prm, LoopCtl());
     fetch_outer();
     int outer = 0;
     while (!all_in(w.scal_h, nc, KS_DONE, KS_DONE, KS_DONE) && outer < prm.max_outer) {
@@ -867,7 +872,7 @@ int solve_ir(cudaStream_t st, const OpT<double> &A64, const OpT<float> &A32, int
         launch_init(st, w.inner, w.b32, w.e32, prm.inner_tol, 0.0, w.scal, prm.tol, prm.divtol, LoopCtl());
         host_loop(st, A32, op, w.inner, w.e32, prm.maxit, M32, prm.prof);
         launch_update(st, w, x);
-        launch_residual(st, A64, op, w, b, x, 0, prm, LoopCtl());
+        launch_residual(st, A64, op, w, b, x, IR_NEXT, prm, LoopCtl());
         fetch_outer();
     }
     return report(w, rep);
@@ -959,8 +964,8 @@ int record_ir(cudaStream_t st, const cudaStream_t *aux, const OpT<double> &A64, 
     const int nc = w.nc;
     LoopCtl outer;
     if (new_loop(st, outer) != 0) return -1;
-    cudaMemsetAsync(x, 0, sizeof(double) * n * nc, st);
-    launch_residual(st, A64, op, w, b, x, 1, prm, outer);
+    if (!prm.x_given) cudaMemsetAsync(x, 0, sizeof(double) * n * nc, st);
+    launch_residual(st, A64, op, w, b, x, prm.x_given ? IR_GUESS : IR_ZERO, prm, outer);
     if (begin_while(st, outer, aux[0]) != 0) return -1;
     {
         cudaStream_t bs = aux[0];
@@ -970,7 +975,7 @@ int record_ir(cudaStream_t st, const cudaStream_t *aux, const OpT<double> &A64, 
         launch_init(bs, w.inner, w.b32, w.e32, prm.inner_tol, 0.0, w.scal, prm.tol, prm.divtol, inner);
         if (record_loop(bs, aux[1], A32, op, w.inner, w.e32, prm.maxit, M32, inner, per_iter) != 0) return -1;
         launch_update(bs, w, x);
-        launch_residual(bs, A64, op, w, b, x, 0, prm, outer);
+        launch_residual(bs, A64, op, w, b, x, IR_NEXT, prm, outer);
     }
     if (end_while(aux[0]) != 0) return -1;
     cudaMemcpyAsync(w.scal_h, w.scal, sizeof(IRScal) * nc, cudaMemcpyDeviceToHost, st);

@@ -62,6 +62,7 @@ struct SolveParams {
     double inner_tol = 1e-5;  // iterative refinement: relative tolerance of each FP32 solve
     int max_outer = 12;
     Prof *prof = nullptr;     // optional stage timers around SpMV / preconditioner (host loop only)
+    bool x_given = false;     // iterative refinement: x holds the initial guess (else x = 0)
 };
 
 struct SolveReport {

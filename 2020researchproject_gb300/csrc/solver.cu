@@ -55,7 +55,7 @@ struct StepGraph {
 
 // Host parameters baked into recorded graphs.
 struct GraphSig {
-    int precision, les, use_mg, max_outer, solver, gm_restart;
+    int precision, les, use_mg, max_outer, solver, gm_restart, warm;
     double tol, divtol, Re, dt, f[3], cs, inner_tol[2];
     bool operator==(const GraphSig &o) const { return memcmp(this, &o, sizeof *this) == 0; }
 };
@@ -129,6 +129,7 @@ struct ibm3d_device {
     int mg_sweeps[5] = {5, 5, 1, 1, 8};  // multigrid sweeps: fine pre/post, coarse pre/post, coarsest
     double mg_omega = 1.0;               // over-relaxation of the fine-grid smoother
     int mg_coarsening = IBM3D_COARSEN_SPACING;
+    int warm_start = 1;                  // mixed modes: momentum solve from the current velocity
     double mg_width_ratio = 1.5;
     // Mixed path: relative tolerance of each FP32 inner solve (momentum,
     // pressure) and the refinement-cycle cap.
@@ -879,6 +880,8 @@ void ghost_update(IBMSolver *sv, bool solids) {
 
 // --------------------------------------------------------- time step ---
 // Stages of one fractional step (src/ibm3d_fracstep.c:60-74).
+bool mom_ir(const ibm3d_device *d);
+
 SolveParams mom_params(IBMSolver *sv) {
     SolveParams pm;
     pm.tol = sv->tol;
@@ -886,11 +889,20 @@ SolveParams mom_params(IBMSolver *sv) {
     pm.inner_tol = sv->dev->inner_tol[0];
     pm.max_outer = sv->dev->max_outer;
     pm.prof = &sv->dev->prof;
+    pm.x_given = mom_ir(sv->dev) && sv->dev->warm_start;
     return pm;
+}
+
+// The momentum unknown u* starts from the current velocity u^n (u* - u^n
+// is O(dt)) when the solve takes an initial guess.
+void momentum_guess(IBMSolver *sv, const SolveParams &pm) {
+    ibm3d_device *d = sv->dev;
+    if (pm.x_given) launch_velocity_guess(d->s, d->g, d->u, d->ustar);
 }
 
 SolveParams pres_params(IBMSolver *sv) {
     SolveParams pp = mom_params(sv);
+    pp.x_given = false;
     pp.inner_tol = sv->dev->inner_tol[1];
     pp.maxit = 1000;
     pp.divtol = sv->dev->divtol;
@@ -987,6 +999,7 @@ void one_step(IBMSolver *sv) {
     stage_rhs(sv);
     const SolveParams pm = mom_params(sv);
     int t = pf.begin("mom_solve");
+    momentum_guess(sv, pm);
     int rc = mom_ir(d) ? solve_ir(d->s, d->A64, d->A32, OP_MOM, d->irmom, d->b, d->ustar, pm, nullptr, d->rep_mom)
                    : bicgstab<double>(d->s, d->A64, OP_MOM, d->kmom, d->b, d->ustar, pm, nullptr, d->rep_mom);
     pf.end(t);
@@ -1011,6 +1024,7 @@ GraphSig graph_sig(const IBMSolver *sv) {
     GraphSig g;
     memset(&g, 0, sizeof g);
     g.precision = sv->dev->precision;
+    g.warm = sv->dev->warm_start;
     g.les = sv->dev->les;
     g.use_mg = use_mg(sv);
     g.tol = sv->tol;
@@ -1043,6 +1057,7 @@ bool record_step_into(IBMSolver *sv, StepGraph &G) {
         stage_rhs(sv);
         SolveParams pm = mom_params(sv);
         pm.prof = nullptr;
+        momentum_guess(sv, pm);
         if (mom_ir(d))
             ok = record_ir(d->s, d->aux, d->A64, d->A32, OP_MOM, d->irmom, d->b, d->ustar, pm, nullptr, &mf, &mo,
                            &mi) == 0;
@@ -2055,6 +2070,11 @@ void IBMSolver_set_multigrid(IBMSolver *s, int nu_pre, int nu_post, int nuc_pre,
         d->mg32->set_omega(omega);
     }
     drop_graphs(d);
+}
+
+void IBMSolver_set_warm_start(IBMSolver *s, int on) {
+    s->dev->warm_start = on != 0;
+    drop_graphs(s->dev);
 }
 
 void IBMSolver_set_coarsening(IBMSolver *s, int mode, double width_ratio) {

@@ -93,6 +93,28 @@ k_conv_rhs(const Grid g, const Axis ax, const Axis ay, const Axis az, const BCSe
     }
 }
 
+// ------------------------------------------------------------------------
+// Initial guess of the momentum solve: u* from u^n (NaN on solid cells,
+// where the solve's rows are the identity on a zero right-hand side, is
+// replaced by 0).
+// ------------------------------------------------------------------------
+__global__ void __launch_bounds__(256)
+k_velocity_guess(const long long n, const double *__restrict__ u0, const double *__restrict__ u1,
+                 const double *__restrict__ u2, double *__restrict__ x) {
+    for (long long P = blockIdx.x * (long long)blockDim.x + threadIdx.x; P < n;
+         P += (long long)gridDim.x * blockDim.x) {
+        const double a = u0[P], b = u1[P], c = u2[P];
+        x[P] = a == a ? a : 0.0;
+        x[n + P] = b == b ? b : 0.0;
+        x[2 * n + P] = c == c ? c : 0.0;
+    }
+}
+
+void launch_velocity_guess(cudaStream_t s, const Grid &g, double *const u[3], double *x) {
+    k_velocity_guess<<<grid_for(g.ncell, 256), 256, 0, s>>>(g.ncell, u[0], u[1], u[2], x);
+    note_launches(1);
+}
+
 void launch_conv_rhs(cudaStream_t s, const Grid &g, const Axis &ax, const Axis &ay, const Axis &az,
                      const BCSet &bc, const uint8_t *flag, const ConvArgs &a, double dt, const double f[3],
                      int les) {

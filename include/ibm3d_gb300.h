@@ -86,6 +86,13 @@ void IBMSolver_set_graphs(IBMSolver *, int on);
 void IBMSolver_set_multigrid(IBMSolver *, int nu_pre, int nu_post, int nuc_pre, int nuc_post, int coarse_sweeps,
                              double omega);
 
+/* Mixed modes: start the momentum solve from the current velocity (on,
+   the default) instead of zero.  u* differs from u^n by O(dt), so the
+   first FP64 refinement residual is small against ||b|| and the FP32
+   inner solve stops sooner; the stopping test (||r|| < tol ||b||) is the
+   same.  The plain FP64 step always starts from zero, as the reference. */
+void IBMSolver_set_warm_start(IBMSolver *, int on);
+
 /* Coarsening of the pressure multigrid (before IBMSolver_assemble).
    IBM3D_COARSEN_SPACING (default): a coarse level merges neighbouring
    cells along an axis only while their joint width is at most
