@@ -195,6 +195,65 @@ __device__ __forceinline__ void sweep_rows(const OpT<T> &A, const bool (&run)[NC
     }
 }
 
+// The same with x holding an initial guess: r = r0 = b - A x, p = v = 0,
+// ||b||^2 (the relative test stays relative to b), ||r||^2 and the
+// divergence max of r; a guess that already passes the stopping test ends
+// the solve before its first iteration.
+template <typename T, int NC>
+__global__ void __launch_bounds__(SW_THREADS)
+k_bicg_init_guess(const OpT<T> A, const int op, const long long n, const T *__restrict__ b, const T *__restrict__ x,
+                  T *r, T *r0, T *p, T *v, KScal *sc, double *partials, unsigned int *counter, const double tol,
+                  const double divtol, const LoopCtl lc) {
+    pdl_enter();
+    __shared__ double smem[32 * (2 * NC + 1)];
+    typename AccT<T>::type a[2 * NC + 1];
+    bool run[NC];
+#pragma unroll
+    for (int c = 0; c < NC; c++) {
+        a[c] = a[NC + c] = 0;
+        run[c] = true;
+    }
+    float dmax = 0.0f;
+    auto put = [&](int c, long long P, T y) {
+        const long long o = c * n;
+        const T bv = b[o + P];
+        r[o + P] = y;
+        r0[o + P] = y;
+        p[o + P] = 0;
+        v[o + P] = 0;
+        a[c] += bv * bv;
+        a[NC + c] += y * y;
+        if (divtol > 0) dmax = fmaxf(dmax, divw(A, P, y));
+    };
+    sweep_rows<T, NC>(
+        A, run,
+        [&](int c, long long P, int i, const Column<T> &q) {
+            put(c, P, b[c * n + P] - interior_row(A, op, x + c * n, P, i, q));
+        },
+        [&](int c, long long P) { put(c, P, b[c * n + P] - op_row(A, op, c, x + c * n, P)); });
+    a[2 * NC] = dmax;
+    reduce_and_finish<2 * NC + 1, 2 * NC>(a, smem, partials, counter, [&](const double *tot) {
+        bool go = false;
+        for (int c = 0; c < NC; c++) {
+            KScal &s = sc[c];
+            s.bnorm2 = tot[c];
+            s.rnorm2 = tot[NC + c];
+            s.rho = tot[NC + c];
+            s.alpha = 1.0;
+            s.omega = 1.0;
+            s.beta = 0.0;
+            s.iters = 0;
+            s.tol = tol;
+            s.divtol = divtol;
+            s.divmax = tot[2 * NC];
+            const bool done = tot[NC + c] == 0.0 || converged(tot[NC + c], tot[c], tot[2 * NC], tol, divtol);
+            s.state = done ? KS_DONE : KS_RUN;
+            go = go || !done;
+        }
+        set_loop(lc, go);
+    });
+}
+
 // ------------------------------------------- v = A ph, alpha = rho/(r0,v) --
 template <typename T, int NC>
 __global__ void __launch_bounds__(SW_THREADS, (sizeof(T) == 4 || NC == 1) ? 4 : 2)
@@ -652,6 +711,18 @@ static void launch_init(cudaStream_t st, KrylovWork<T> &w, const T *b, T *x, dou
     note_launches(1);
 }
 
+template <typename T>
+static void launch_init_guess(cudaStream_t st, const OpT<T> &A, int op, KrylovWork<T> &w, const T *b, const T *x,
+                              double tol, double divtol, LoopCtl lc) {
+    if (w.nc == 3)
+        launch_pdl(k_bicg_init_guess<T, 3>, A.sw.nblocks, SW_THREADS, 0, st, A, op, w.n, b, x, w.r, w.r0, w.p, w.v,
+                   w.scal, w.partials, w.counter, tol, divtol, lc);
+    else
+        launch_pdl(k_bicg_init_guess<T, 1>, A.sw.nblocks, SW_THREADS, 0, st, A, op, w.n, b, x, w.r, w.r0, w.p, w.v,
+                   w.scal, w.partials, w.counter, tol, divtol, lc);
+    note_launches(1);
+}
+
 // p update, preconditioner, v = A ph, s = r - alpha v.
 template <typename T>
 static void first_half(cudaStream_t st, const OpT<T> &A, int op, KrylovWork<T> &w, Preconditioner<T> *M, Prof *pf) {
@@ -844,7 +915,8 @@ static void host_loop(cudaStream_t st, const OpT<T> &A, int op, KrylovWork<T> &w
 template <typename T>
 int bicgstab(cudaStream_t st, const OpT<T> &A, int op, KrylovWork<T> &w, const T *b, T *x, const SolveParams &prm,
              Preconditioner<T> *M, SolveReport &rep) {
-    launch_init(st, w, b, x, prm.tol, prm.divtol, nullptr, 0.0, 0.0, LoopCtl());
+    if (prm.x_given) launch_init_guess(st, A, op, w, b, x, prm.tol, prm.divtol, LoopCtl());
+    else launch_init(st, w, b, x, prm.tol, prm.divtol, nullptr, 0.0, 0.0, LoopCtl());
     host_loop(st, A, op, w, x, prm.maxit, M, prm.prof);
     return report(w, rep);
 }
@@ -943,7 +1015,8 @@ int record_bicgstab(cudaStream_t st, const cudaStream_t *aux, const OpT<T> &A, i
                     T *x, const SolveParams &prm, Preconditioner<T> *M, int *fixed, int *per_iter) {
     LoopCtl lc;
     if (new_loop(st, lc) != 0) return -1;
-    launch_init(st, w, b, x, prm.tol, prm.divtol, nullptr, 0.0, 0.0, lc);
+    if (prm.x_given) launch_init_guess(st, A, op, w, b, x, prm.tol, prm.divtol, lc);
+    else launch_init(st, w, b, x, prm.tol, prm.divtol, nullptr, 0.0, 0.0, lc);
     if (record_loop(st, aux[0], A, op, w, x, prm.maxit, M, lc, per_iter) != 0) return -1;
     cudaMemcpyAsync(w.scal_h, w.scal, sizeof(KScal) * w.nc, cudaMemcpyDeviceToHost, st);
     *fixed = 1;

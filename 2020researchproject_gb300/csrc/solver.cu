@@ -900,9 +900,12 @@ void momentum_guess(IBMSolver *sv, const SolveParams &pm) {
     if (pm.x_given) launch_velocity_guess(d->s, d->g, d->u, d->ustar);
 }
 
+bool pres_gmres(const IBMSolver *sv);
+
 SolveParams pres_params(IBMSolver *sv) {
     SolveParams pp = mom_params(sv);
-    pp.x_given = false;
+    // The mixed modes start from the last step's pressure increment.
+    pp.x_given = sv->dev->precision != IBM3D_FP64 && sv->dev->warm_start && !pres_gmres(sv);
     pp.inner_tol = sv->dev->inner_tol[1];
     pp.maxit = 1000;
     pp.divtol = sv->dev->divtol;
@@ -1224,6 +1227,9 @@ void upload_state(IBMSolver *sv, const double *u1, const double *u2, const doubl
     cudaMemcpyAsync(d->u[1], u2, b, cudaMemcpyHostToDevice, d->s);
     cudaMemcpyAsync(d->u[2], u3, b, cudaMemcpyHostToDevice, d->s);
     cudaMemcpyAsync(d->p, p, b, cudaMemcpyHostToDevice, d->s);
+    // A new run: the pressure increment, a warm start's initial guess,
+    // starts from zero.
+    cudaMemsetAsync(d->pp, 0, b, d->s);
     cuda_check(sv, cudaStreamSynchronize(d->s), "state upload");
     sv->iter = 0;
     sv->time = 0;
@@ -1626,7 +1632,7 @@ struct StateHeader {
 
 namespace {
 
-constexpr int kStateFields = 26;
+constexpr int kStateFields = 27;
 
 // Device arrays of the state, in file order.
 void state_fields(ibm3d_device *d, double *f[kStateFields]) {
@@ -1640,6 +1646,7 @@ void state_fields(ibm3d_device *d, double *f[kStateFields]) {
     for (int l = 0; l < 3; l++) f[q++] = d->N[l];
     for (int l = 0; l < 3; l++) f[q++] = d->Np[l];
     for (int l = 0; l < 6; l++) f[q++] = d->tau[l];
+    f[q++] = d->pp;  // the last pressure increment: the next solve's initial guess
 }
 
 bool write_state(IBMSolver *s, const std::string &path) {
@@ -1647,7 +1654,7 @@ bool write_state(IBMSolver *s, const std::string &path) {
     FILE *f = fopen(path.c_str(), "wb");
     if (!f) return false;
     StateHeader h{};
-    memcpy(h.magic, "IBM3DST2", 8);
+    memcpy(h.magic, "IBM3DST3", 8);
     h.nx = s->Nx; h.ny = s->Ny; h.nz = s->Nz; h.iter = s->iter; h.time = s->time;
     h.nfields = kStateFields;
     const size_t n = (size_t)d->g.ncell;
@@ -1670,7 +1677,7 @@ int read_state(IBMSolver *s, const std::string &path) {
     if (!f) return 0;
     StateHeader h{};
     const size_t n = (size_t)d->g.ncell;
-    bool ok = fread(&h, sizeof h, 1, f) == 1 && memcmp(h.magic, "IBM3DST2", 8) == 0 && h.nx == s->Nx &&
+    bool ok = fread(&h, sizeof h, 1, f) == 1 && memcmp(h.magic, "IBM3DST3", 8) == 0 && h.nx == s->Nx &&
               h.ny == s->Ny && h.nz == s->Nz && h.nfields == kStateFields;
     std::vector<double> buf(ok ? kStateFields * n : 0);
     ok = ok && fread(buf.data(), sizeof(double), buf.size(), f) == buf.size();
@@ -2279,7 +2286,9 @@ double IBMSolver_autotune(IBMSolver *s, int steps, int *best_out) {
         copy_state(false);
         s->iter = iter0;
         s->time = time0;
-        IBMSolver_iterate(s, 1, false);  // records this configuration's graphs
+        // Records this configuration's graphs for both buffer parities (the
+        // steps alternate the field buffers), so the timed steps record none.
+        IBMSolver_iterate(s, 2, false);
         copy_state(false);
         s->iter = iter0;
         s->time = time0;

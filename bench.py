@@ -247,14 +247,15 @@ def _timed_arm(ibm, wl, case, precision, args, world, u0, headline=False):
         s.set_multigrid(*[int(v) for v in args.mg_sweeps.split(",")], 1.0)
     if not args.no_tune:
         # The autotuner picks the multigrid sweeps (and, for the mixed step,
-        # which of the two mixed solver forms) from the state after one
-        # step; the state is restored, and warm-up follows.
-        s.iterate(1)
+        # which of the two mixed solver forms) from the state after three
+        # steps (past the start-up transient, whose harder solves favour
+        # other settings); the state is restored, and warm-up follows.
+        s.iterate(3)
         modes = [("MIXED", ibm.MIXED), ("MIXED_MG", ibm.MIXED_MG)] if precision == "mixed" else [("FP64", ibm.FP64)]
         trials = []
         for name, mode in modes:
             s.set_precision(mode)
-            ms_t, sweeps = s.autotune(steps=2)
+            ms_t, sweeps = s.autotune(steps=4)
             trials.append((ms_t, name, mode, sweeps))
         ms_t, name, mode, sweeps = min(trials)
         s.set_precision(mode)
