@@ -63,13 +63,18 @@ def test_export_matches_oracle(ibm, tmp_path, name):
     assert np.isfinite(vort).sum() > 0
 
 
-def test_exact_resume_from_state_file(ibm, tmp_path):
+@pytest.mark.parametrize("precision", ["FP64", "MIXED_MG", "MIXED"])
+def test_exact_resume_from_state_file(ibm, tmp_path, precision):
+    """The mixed modes' warm starts read the last pressure increment: it is
+    part of the state, so a resumed run still continues bit for bit."""
     case = load_golden("sphere")
     a = build_case(ibm, case, tol=1e-8)
+    a.set_precision(getattr(ibm, precision))
     a.iterate(2)
     base = str(tmp_path / "ck")
     a.export_result(base)
     b = build_case(ibm, case, tol=1e-8)
+    b.set_precision(getattr(ibm, precision))
     b.init_flow_file(base)
     assert b.stats()["iter"] == 2 and b.stats()["time"] == a.stats()["time"]
     a.iterate(2)
