@@ -2259,8 +2259,9 @@ double IBMSolver_autotune(IBMSolver *s, int steps, int *best_out) {
     if (!check_ready(s, "IBMSolver_autotune")) return -1;
     ibm3d_device *d = s->dev;
     if (steps < 1) steps = 1;
-    static const int cand[][5] = {{5, 5, 1, 1, 8}, {4, 4, 1, 1, 8}, {6, 6, 1, 1, 8}, {3, 3, 1, 1, 8},
-                                  {4, 4, 2, 2, 8}, {3, 3, 2, 2, 8}, {5, 5, 2, 2, 16}, {2, 2, 2, 2, 8}};
+    static const int cand[][5] = {{5, 5, 1, 1, 8},  {4, 4, 1, 1, 8},  {6, 6, 1, 1, 8},  {3, 3, 1, 1, 8},
+                                  {4, 4, 2, 2, 8},  {3, 3, 2, 2, 8},  {5, 5, 2, 2, 16}, {2, 2, 2, 2, 8},
+                                  {4, 4, 2, 2, 16}, {6, 6, 2, 2, 16}, {3, 3, 2, 2, 16}, {5, 5, 1, 1, 16}};
     const int ncand = (int)(sizeof cand / sizeof cand[0]);
     const size_t n = (size_t)d->g.ncell;
     double *save = nullptr;
