@@ -174,28 +174,11 @@ k_mg0_color(const OpT<T> c, const T *__restrict__ r, T *__restrict__ z, const in
         if (upd[p]) z[Ps[p]] = val[p];
 }
 
-// The first colour pass of a V-cycle on z = 0, as one pass over the
-// whole padded array: colour-0 interior rows take r (r + dinv * 0, and
-// r for solid and pinned rows), every other cell 0.
-template <typename T>
-__global__ void __launch_bounds__(256)
-k_mg0_init(const OpT<T> c, const T *__restrict__ r, T *__restrict__ z, const Per3 per, const int *gate) {
-    MG_GATE(gate);
-    const Grid &g = c.g;
-    const long long n = g.ncell;
-    GRID_STRIDE(P, n) {
-        int i, j, k;
-        cijk_fast(g, c.fdx, c.fdy, P, i, j, k);
-        T v = 0;
-        if (i >= 0 && i < g.nx && j >= 0 && j < g.ny && k >= 0 && k < g.nz &&
-            cell_color(i, j, k, g.nx, g.ny, g.nz, per.p) == 0 && c.flag[P] != GHOST)
-            v = r[P];
-        z[P] = v;
-    }
-}
-
-// The same pass as a 3-D launch over the padded box (threads along k, no
-// index division): grid (ceil((nz+4)/32), ceil((ny+4)/8), nx+4).
+// The first colour pass of a V-cycle on z = 0, as one pass over the whole
+// padded array: colour-0 interior rows take r (r + dinv * 0, and r for
+// solid and pinned rows), every other cell 0.  A 3-D launch over the
+// padded box (threads along k, no index division): grid
+// (ceil((nz+4)/32), ceil((ny+4)/8), nx+4).
 template <typename T>
 __global__ void __launch_bounds__(256)
 k_mg0_init3(const OpT<T> c, const T *__restrict__ r, T *__restrict__ z, const Per3 per, const int *gate) {
