@@ -290,7 +290,7 @@ class IBMSolver:
     def set_div_tol(self, div_tol):
         self._lib.IBMSolver_set_div_tol(self._s, div_tol)
 
-    def set_multigrid(self, nu_pre=5, nu_post=5, nuc_pre=1, nuc_post=1, coarse_sweeps=8, omega=1.0):
+    def set_multigrid(self, nu_pre=3, nu_post=3, nuc_pre=2, nuc_post=2, coarse_sweeps=16, omega=1.0):
         self._lib.IBMSolver_set_multigrid(self._s, nu_pre, nu_post, nuc_pre, nuc_post, coarse_sweeps, float(omega))
         self._check("IBMSolver_set_multigrid")
 

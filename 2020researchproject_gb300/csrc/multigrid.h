@@ -67,9 +67,9 @@ struct MGLevel {
 enum { MG_COARSEN_HALVE = 0, MG_COARSEN_SPACING = 1 };
 
 struct GMGConfig {
-    int nu_pre = 5, nu_post = 5;    // fine grid
-    int nuc_pre = 1, nuc_post = 1;  // coarse levels above the coarsest
-    int coarse_sweeps = 8;          // coarsest level
+    int nu_pre = 3, nu_post = 3;    // fine grid
+    int nuc_pre = 2, nuc_post = 2;  // coarse levels above the coarsest
+    int coarse_sweeps = 16;         // coarsest level
     double omega = 1.0;             // over-relaxation of the fine-grid fluid rows
     int coarsening = MG_COARSEN_SPACING;
     double width_ratio = 1.5;       // spacing rule: merge while the pair is within width_ratio x the target

@@ -126,7 +126,7 @@ struct ibm3d_device {
     size_t dev_bytes = 0;   // device memory taken by assembly (free-memory difference)
     // Recorded steps.
     bool use_graphs = true;
-    int mg_sweeps[5] = {5, 5, 1, 1, 8};  // multigrid sweeps: fine pre/post, coarse pre/post, coarsest
+    int mg_sweeps[5] = {3, 3, 2, 2, 16};  // multigrid sweeps: fine pre/post, coarse pre/post, coarsest
     double mg_omega = 1.0;               // over-relaxation of the fine-grid smoother
     int mg_coarsening = IBM3D_COARSEN_SPACING;
     int warm_start = 1;                  // mixed modes: momentum solve from the current velocity

@@ -81,7 +81,7 @@ void IBMSolver_set_graphs(IBMSolver *, int on);
    coarse-grid correction on the fine grid (nu_pre, nu_post) and on the
    coarse levels (nuc_pre, nuc_post), sweeps on the coarsest level, and the
    over-relaxation weight of the fine-grid fluid rows (0 < omega < 2;
-   defaults 5, 5, 1, 1, 8, 1.0).  Tuning only: the solve still stops on the
+   defaults 3, 3, 2, 2, 16, 1.0).  Tuning only: the solve still stops on the
    same residual or divergence test. */
 void IBMSolver_set_multigrid(IBMSolver *, int nu_pre, int nu_post, int nuc_pre, int nuc_post, int coarse_sweeps,
                              double omega);
