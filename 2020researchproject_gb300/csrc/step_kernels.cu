@@ -24,7 +24,10 @@ static inline unsigned grid_for(long long n, int block) {
 // and subgrid-stress divergence.  Outer rows carry the velocity BC value
 // (VELOCITY faces) or 0; interior non-fluid rows are 0 and N is NaN there.
 // ------------------------------------------------------------------------
-__global__ void __launch_bounds__(256)
+// Two blocks per SM: 128 registers, no spills (218 unbounded, one block
+// per SM); the kernel is bound by the FP64 pipe, which more resident warps
+// keep busier.
+__global__ void __launch_bounds__(256, 2)
 k_conv_rhs(const Grid g, const Axis ax, const Axis ay, const Axis az, const BCSet bc,
            const uint8_t *__restrict__ flag, ConvArgs a, const double dt, const double f1,
            const double f2, const double f3, const int les) {
