@@ -64,7 +64,7 @@ struct ibm3d_device {
     cudaStream_t s = nullptr;
     Grid g{};
     int dev_id = 0;
-    char dev_name[256] = "";
+    char dev_name[288] = "";  // the device name (up to 256) and its " (sm_XY)"
     // Per-axis 1-D tables: 9 arrays of n+4 doubles each.
     double *tab[3] = {nullptr, nullptr, nullptr};
     Axis ax[3];
