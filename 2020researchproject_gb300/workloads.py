@@ -149,7 +149,8 @@ _DIR = {"N": "DIR_NORTH", "E": "DIR_EAST", "S": "DIR_SOUTH", "W": "DIR_WEST", "D
 
 def build_solver(ibm, case, tol=1e-6, div_tol=0.0, coarsening=None):
     """Create and assemble an IBMSolver for ``case`` (ibm = the package);
-    coarsening: the pressure multigrid's (library default when None)."""
+    coarsening: the pressure multigrid's mode, or (mode, width_ratio)
+    (library default when None)."""
     s = ibm.IBMSolver()
     s.set_grid(case["xf"], case["yf"], case["zf"])
     s.set_params(case["re"], case["dt"])
@@ -164,8 +165,10 @@ def build_solver(ibm, case, tol=1e-6, div_tol=0.0, coarsening=None):
     s.set_linear_solver(ibm.SOLVER_BiCGSTAB, ibm.PRECOND_AMG, tol)
     if div_tol > 0:
         s.set_div_tol(div_tol)
-    if coarsening is not None:
-        s.set_coarsening(*coarsening) if isinstance(coarsening, tuple) else s.set_coarsening(coarsening)
+    if isinstance(coarsening, tuple):            # (mode, width_ratio)
+        s.set_coarsening(*coarsening)
+    elif coarsening is not None:
+        s.set_coarsening(coarsening)
     s.assemble()
     return s
 
