@@ -495,9 +495,23 @@ extern "C" int Polyhedron_cpt_noalloc(const Polyhedron *const poly, const int nx
                                       const double *x, const double *y, const double *z, double *f,
                                       const double maxd) {
     using namespace ibm;
-    CptModel m;
-    build_cpt_model(poly, maxd, m);
+    if (!poly || !x || !y || !z || !f || nx <= 0 || ny <= 0 || nz <= 0) {
+        fprintf(stderr, "error: Polyhedron_cpt_noalloc: null pointer or non-positive grid size (%d x %d x %d)\n", nx,
+                ny, nz);
+        return -1;
+    }
+    // Sizes are checked against the array before any product can overflow:
+    // each axis is below 2^31 and the point count is compared in 64 bits.
     const long long n = (long long)nx * ny * nz;
+    if (n > (long long)(CPT_NOALLOC_BYTES / sizeof(double))) {
+        fprintf(stderr,
+                "error: Polyhedron_cpt_noalloc: a %d x %d x %d grid needs more than the %zu-byte static buffer; "
+                "use Polyhedron_cpt\n",
+                nx, ny, nz, CPT_NOALLOC_BYTES);
+        return -1;
+    }
+    CptModel m;
+    build_cpt_model(poly, maxd, m);  // host memory only
     // Layout of the scratch array, each piece 256-byte aligned.
     size_t off = 0;
     auto place = [&](size_t bytes) {
@@ -506,13 +520,13 @@ extern "C" int Polyhedron_cpt_noalloc(const Polyhedron *const poly, const int nx
         return at;
     };
     const size_t o_x = place(sizeof(double) * nx), o_y = place(sizeof(double) * ny), o_z = place(sizeof(double) * nz);
-    const size_t o_f = place(sizeof(double) * n);
+    const size_t o_f = place(sizeof(double) * (size_t)n);
     const size_t o_feat = place(sizeof(CptFeature) * m.features.size());
     const size_t o_tfs = place(sizeof(int) * m.tri_feat_start.size());
     const size_t o_tf = place(sizeof(int) * m.tri_feats.size());
     const size_t o_txyz = place(sizeof(float) * m.tri_xyz.size());
     const size_t o_node = place(sizeof(BVHNode) * m.nodes.size());
-    const size_t o_fb = place(sizeof(int) * n);
+    const size_t o_fb = place(sizeof(int) * (size_t)n);
     const size_t o_cnt = place(sizeof(int));
     if (off > CPT_NOALLOC_BYTES) {
         fprintf(stderr,
@@ -526,8 +540,19 @@ extern "C" int Polyhedron_cpt_noalloc(const Polyhedron *const poly, const int nx
     unsigned char *base = noalloc_scratch(dev);
     if (!base) return -1;
     const cudaStream_t s = 0;
+    // Every copy, the memset and every launch is checked: the array keeps
+    // the previous call's contents, so a step that failed silently would
+    // let the kernels run on the previous call's geometry.
+    cudaError_t err = cudaSuccess;
+    const char *what = "";
+    auto check = [&](cudaError_t e, const char *step) {
+        if (err == cudaSuccess && e != cudaSuccess) {
+            err = e;
+            what = step;
+        }
+    };
     auto up = [&](size_t o, const void *src, size_t bytes) {
-        if (bytes) cudaMemcpyAsync(base + o, src, bytes, cudaMemcpyHostToDevice, s);
+        if (bytes) check(cudaMemcpyAsync(base + o, src, bytes, cudaMemcpyHostToDevice, s), "upload");
     };
     up(o_x, x, sizeof(double) * nx);
     up(o_y, y, sizeof(double) * ny);
@@ -539,7 +564,7 @@ extern "C" int Polyhedron_cpt_noalloc(const Polyhedron *const poly, const int nx
     up(o_node, m.nodes.data(), sizeof(BVHNode) * m.nodes.size());
     // The array keeps the previous call's contents: the fallback counter
     // must start at zero every call.
-    cudaMemsetAsync(base + o_cnt, 0, sizeof(int), s);
+    check(cudaMemsetAsync(base + o_cnt, 0, sizeof(int), s), "counter reset");
     CptDev d{};
     d.feat = (const CptFeature *)(base + o_feat);
     d.nfeat = (int)m.features.size();
@@ -551,14 +576,34 @@ extern "C" int Polyhedron_cpt_noalloc(const Polyhedron *const poly, const int nx
     const double *dx = (const double *)(base + o_x), *dy = (const double *)(base + o_y), *dz = (const double *)(base + o_z);
     double *df = (double *)(base + o_f);
     int *fb_list = (int *)(base + o_fb), *fb_count = (int *)(base + o_cnt);
-    k_cpt<<<nblk(n, 128), 128, 0, s>>>(d, nx, ny, nz, dx, dy, dz, df, maxd, fb_list, fb_count);
     int nfb = 0;
-    cudaMemcpyAsync(&nfb, fb_count, sizeof(int), cudaMemcpyDeviceToHost, s);
-    if (cudaStreamSynchronize(s) != cudaSuccess) return -1;
-    if (nfb > 0) k_cpt_fallback<<<nfb < 4096 ? nfb : 4096, 256, 0, s>>>(d, nx, ny, nz, dx, dy, dz, df, fb_list, nfb);
-    k_cpt_fill<<<nblk((long long)nx * ny, 128), 128, 0, s>>>(df, nx, ny, nz, 2, maxd);
-    k_cpt_fill<<<nblk((long long)nx * nz, 128), 128, 0, s>>>(df, nx, ny, nz, 1, maxd);
-    k_cpt_fill<<<nblk((long long)ny * nz, 128), 128, 0, s>>>(df, nx, ny, nz, 0, maxd);
-    cudaMemcpyAsync(f, df, sizeof(double) * n, cudaMemcpyDeviceToHost, s);
-    return cudaStreamSynchronize(s) == cudaSuccess ? 0 : -1;
+    if (err == cudaSuccess) {
+        k_cpt<<<nblk(n, 128), 128, 0, s>>>(d, nx, ny, nz, dx, dy, dz, df, maxd, fb_list, fb_count);
+        check(cudaGetLastError(), "k_cpt launch");
+        check(cudaMemcpyAsync(&nfb, fb_count, sizeof(int), cudaMemcpyDeviceToHost, s), "fallback count read");
+        check(cudaStreamSynchronize(s), "k_cpt");
+    }
+    if (err == cudaSuccess && (nfb < 0 || nfb > n)) {
+        fprintf(stderr, "error: Polyhedron_cpt_noalloc: fallback count %d outside [0, %lld]\n", nfb, n);
+        return -1;
+    }
+    if (err == cudaSuccess) {
+        if (nfb > 0) {
+            k_cpt_fallback<<<nfb < 4096 ? nfb : 4096, 256, 0, s>>>(d, nx, ny, nz, dx, dy, dz, df, fb_list, nfb);
+            check(cudaGetLastError(), "k_cpt_fallback launch");
+        }
+        k_cpt_fill<<<nblk((long long)nx * ny, 128), 128, 0, s>>>(df, nx, ny, nz, 2, maxd);
+        check(cudaGetLastError(), "k_cpt_fill launch");
+        k_cpt_fill<<<nblk((long long)nx * nz, 128), 128, 0, s>>>(df, nx, ny, nz, 1, maxd);
+        check(cudaGetLastError(), "k_cpt_fill launch");
+        k_cpt_fill<<<nblk((long long)ny * nz, 128), 128, 0, s>>>(df, nx, ny, nz, 0, maxd);
+        check(cudaGetLastError(), "k_cpt_fill launch");
+        check(cudaMemcpyAsync(f, df, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, s), "result read-back");
+        check(cudaStreamSynchronize(s), "level-set kernels");
+    }
+    if (err != cudaSuccess) {
+        fprintf(stderr, "error: Polyhedron_cpt_noalloc: %s failed: %s\n", what, cudaGetErrorString(err));
+        return -1;
+    }
+    return 0;
 }

@@ -29,19 +29,40 @@ def _p(a):
 
 
 def test_noalloc_cpt_matches_allocating_entry_point():
+    """Consecutive calls that share the scratch array, on different bodies
+    and differently shaped grids: each must equal Polyhedron_cpt bit for
+    bit.  The second call's grid is smaller than the first and its body
+    (a box) differs, so contents left from the first call (geometry,
+    fallback list, output) would show."""
     ibm = package()
     fn = _noalloc(ibm.load_library())
-    poly = ibm.Polyhedron(os.path.join(GOLDEN, "sphere_sub2.stl"))
-    x = np.linspace(-1.7, 2.3, 23)
-    y = np.linspace(-1.4, 1.5, 19)
-    z = np.linspace(-1.3, 1.3, 17) ** 3 * 0.6 + np.linspace(-1.3, 1.3, 17) * 0.4
-    ref = poly.cpt(x, y, z)                       # Polyhedron_cpt, allocating
-    assert np.isfinite(ref).all() and (ref < 0).any() and (ref > 0).any()
-    for call in range(2):                         # two calls share the scratch array
+    sphere = ibm.Polyhedron(os.path.join(GOLDEN, "sphere_sub2.stl"))
+    box = ibm.Polyhedron(os.path.join(GOLDEN, "box.stl"))
+    zs = np.linspace(-1.3, 1.3, 17)
+    grids = [
+        (sphere, np.linspace(-1.7, 2.3, 23), np.linspace(-1.4, 1.5, 19), zs ** 3 * 0.6 + zs * 0.4),
+        (box, np.linspace(-0.9, 1.1, 11), np.linspace(-1.2, 0.8, 14), np.linspace(-0.7, 0.9, 9)),
+        (sphere, np.linspace(-1.7, 2.3, 23), np.linspace(-1.4, 1.5, 19), zs ** 3 * 0.6 + zs * 0.4),
+    ]
+    for call, (poly, x, y, z) in enumerate(grids):
+        ref = poly.cpt(x, y, z)                   # Polyhedron_cpt, allocating
+        assert np.isfinite(ref).all() and (ref < 0).any() and (ref > 0).any()
         out = np.full(ref.shape, -7.0)
         rc = fn(poly._p, len(x), len(y), len(z), _p(x), _p(y), _p(z), _p(out), 15.0)
         assert rc == 0, f"call {call} failed"
         assert np.array_equal(out, ref), f"call {call}: {int((out != ref).sum())} points differ"
+
+
+def test_noalloc_cpt_rejects_bad_sizes():
+    """Non-positive grid sizes are refused on the host, output untouched."""
+    ibm = package()
+    fn = _noalloc(ibm.load_library())
+    poly = ibm.Polyhedron(os.path.join(GOLDEN, "sphere_sub2.stl"))
+    x = np.linspace(-2, 2, 8)
+    out = np.full((8, 8, 8), 3.0)
+    for dims in ((0, 8, 8), (8, -3, 8), (8, 8, 0)):
+        assert fn(poly._p, *dims, _p(x), _p(x), _p(x), _p(out), 15.0) == -1
+    assert (out == 3.0).all()
 
 
 def test_noalloc_cpt_rejects_grids_beyond_its_buffer():
