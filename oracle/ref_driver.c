@@ -18,6 +18,10 @@
  *   smag CS
  *   stl PATH                           obstacle (omit for none)
  *   init const u v w p | init field    field: smooth analytic field below
+ *   init raw DIR                       u1.f64 u2.f64 u3.f64 p.f64 in DIR: padded
+ *                                      (N+4)^3 arrays written into the solver
+ *                                      after init_flow_const (what the GPU
+ *                                      library's IBMSolver_init_flow_array does)
  *   bcfunc FACE TYPE KIND              VAL_FUNC boundary values: TYPE vel
  *                                      (KIND pulse) or press / velper
  *                                      (KIND ramp); functions below
@@ -97,6 +101,7 @@ int main(int argc, char **argv) {
     double f1 = 0, f2 = 0, f3 = 0;
     char stl[1024] = "";
     int init_field = 0;
+    char init_dir[1024] = "";
     double iu = 0, iv = 0, iw = 0, ip = 0;
 
     struct { int dir, type; double a, b, c; int func; } bcs[16];
@@ -127,6 +132,7 @@ int main(int argc, char **argv) {
             char kind[32];
             if (fscanf(cf, "%31s", kind) != 1) return 2;
             if (!strcmp(kind, "field")) init_field = 1;
+            else if (!strcmp(kind, "raw")) { if (fscanf(cf, "%1023s", init_dir) != 1) return 2; }
             else if (fscanf(cf, "%lf %lf %lf %lf", &iu, &iv, &iw, &ip) != 4) return 2;
         } else if (!strcmp(key, "bcfunc")) {
             char face[8], type[16], kind[16];
@@ -246,6 +252,17 @@ int main(int argc, char **argv) {
 
     if (init_field) IBMSolver_init_flow_func(solver, fx_u, fx_v, fx_w, fx_p);
     else IBMSolver_init_flow_const(solver, iu, iv, iw, ip);
+    if (init_dir[0]) {
+        double *dst[4] = {solver->u1, solver->u2, solver->u3, solver->p};
+        const char *names[4] = {"u1.f64", "u2.f64", "u3.f64", "p.f64"};
+        for (int q = 0; q < 4; q++) {
+            char path[1100];
+            snprintf(path, sizeof path, "%s/%s", init_dir, names[q]);
+            FILE *fp = fopen(path, "rb");
+            if (!fp || fread(dst[q], sizeof(double), nc, fp) != nc) { perror(path); return 2; }
+            fclose(fp);
+        }
+    }
 
     dump(out, "u1_0.f64", solver->u1, nc * sizeof(double));
     dump(out, "u2_0.f64", solver->u2, nc * sizeof(double));
