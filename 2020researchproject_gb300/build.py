@@ -24,12 +24,13 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CUDA_SOURCES = {
     "step_kernels.cu": [],
+    "step32_kernels.cu": [],
     "krylov.cu": [],
     "multigrid.cu": [],
     "setup_kernels.cu": ["-fmad=false"],
     "solver.cu": [],
 }
-CXX_SOURCES = ["geo3d.cpp", "ncfile.cpp"]
+CXX_SOURCES = ["geo3d.cpp", "ncfile.cpp", "utils_abi.cpp"]
 
 
 def _nvcc():
@@ -74,7 +75,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
         objs.append(o)
         if _stale(o, [s] + headers):
             cmds.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math",
-                         "-I/usr/local/cuda/include", "-c", s, "-o", o])
+                         "-I/usr/local/cuda/include", "-I" + os.path.join(PKG, "..", "include"), "-c", s, "-o", o])
     with cf.ThreadPoolExecutor(max_workers=jobs or min(8, os.cpu_count() or 4)) as ex:
         for out in ex.map(_run, cmds):
             if verbose and out.strip():

@@ -17,6 +17,7 @@
 
 #include <stdbool.h>
 
+#include "ibm3d_mpi.h"
 #include "geo3d.h"
 
 #ifdef __cplusplus
