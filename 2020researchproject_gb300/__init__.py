@@ -32,7 +32,7 @@ LIB_PATH = os.path.join(_PKG, "libibm3d_gb300.so")
 # Enums, values as in the reference's src/ibm3d.h:16-98.
 SOLVER_AMG, SOLVER_PCG, SOLVER_BiCGSTAB, SOLVER_GMRES = range(4)
 PRECOND_NONE, PRECOND_AMG = range(2)
-FP64, MIXED, MIXED_MG = 0, 1, 2
+FP64, MIXED, MIXED_MG, MIXED32, MIXED32_IR = 0, 1, 2, 3, 4
 COARSEN_HALVE, COARSEN_SPACING = 0, 1
 DIR_NORTH, DIR_EAST, DIR_SOUTH, DIR_WEST, DIR_DOWN, DIR_UP = (1 << i for i in range(6))
 (BC_VELOCITY_COMPONENT, BC_PRESSURE, BC_STATIONARY_WALL, BC_FREE_SLIP_WALL,
@@ -46,7 +46,7 @@ FIELDS = ["u1", "u2", "u3", "p", "U1", "U2", "U3", "u1star", "u2star", "u3star",
           "U1star", "U2star", "U3star", "pprime", "N1", "N2", "N3", "lvset", "coeffsum",
           "tau11", "tau12", "tau13", "tau22", "tau23", "tau33"]
 STATUS = {0: "ok", 1: "no convergence", 2: "breakdown", 3: "CUDA error", 4: "invalid argument",
-          5: "mirror point outside grid", 6: "unsupported"}
+          5: "mirror point outside grid", 6: "unsupported", 7: "non-finite values"}
 
 
 class IBM3DError(RuntimeError):
@@ -64,7 +64,9 @@ class _Stats(ctypes.Structure):
                 ("res_u", ctypes.c_double * 3), ("res_p", ctypes.c_double),
                 ("max_div", ctypes.c_double), ("mg_levels", ctypes.c_int),
                 ("cpt_fallback", ctypes.c_int), ("outer_u", ctypes.c_int),
-                ("outer_p", ctypes.c_int)]
+                ("outer_p", ctypes.c_int), ("steps_total", ctypes.c_longlong),
+                ("iters_u_total", ctypes.c_longlong * 3), ("iters_p_total", ctypes.c_longlong),
+                ("outer_p_total", ctypes.c_longlong), ("max_div_max", ctypes.c_double)]
 
 
 _lib = None
@@ -97,6 +99,10 @@ def load_library(path: str = LIB_PATH):
         "IBMSolver_set_gmres_restart": (None, [vp, i]),
         "IBMSolver_set_coarsening": (None, [vp, i, d]),
         "IBMSolver_set_warm_start": (None, [vp, i]),
+        "IBMSolver_set_max_iters": (None, [vp, i, i]),
+        "IBMSolver_set_pressure_guess": (None, [vp, i]),
+        "IBMSolver_measure_fma_rate": (d, [i]),
+        "IBMSolver_check_fp32_conversions": (i, [ctypes.c_longlong, dp, ctypes.POINTER(ctypes.c_ulonglong)]),
         "IBMSolver_autotune": (d, [vp, i, ip]),
         "IBMSolver_set_ext_force_func": (None, [vp, vp, vp, vp]),
         "IBMSolver_set_smagorinsky": (None, [vp, d]),
@@ -163,6 +169,21 @@ def _ptr(a: np.ndarray):
 def kernel_launches() -> int:
     """Kernels the library has launched since it was loaded."""
     return int(load_library().IBMSolver_kernel_launches())
+
+
+def measure_fma_rate(fp64=True) -> float:
+    """Register-only FMA throughput of the GPU in TFLOP/s (FP64 or FP32)."""
+    return float(load_library().IBMSolver_measure_fma_rate(0 if fp64 else 1))
+
+
+def check_fp32_conversions(values) -> int:
+    """Mismatches between the integer-pipe FP64 <-> FP32 conversions of the
+    IBM3D_MIXED32 step and the GPU's conversion instructions on `values`."""
+    v = np.ascontiguousarray(values, dtype=np.float64)
+    bad = ctypes.c_ulonglong(0)
+    if load_library().IBMSolver_check_fp32_conversions(len(v), _ptr(v), ctypes.byref(bad)) != 0:
+        raise IBM3DError("IBMSolver_check_fp32_conversions failed")
+    return int(bad.value)
 
 
 def pin(a: np.ndarray) -> bool:
@@ -294,11 +315,14 @@ class IBMSolver:
         self._lib.IBMSolver_set_multigrid(self._s, nu_pre, nu_post, nuc_pre, nuc_post, coarse_sweeps, float(omega))
         self._check("IBMSolver_set_multigrid")
 
-    def time_kernel(self, which, reps=20):
+    def time_kernel(self, which, reps=20, cold=False):
         """(avg ms per launch, algorithmic bytes per launch) of a hot kernel:
-        which = "mg_color" or "spmv_p"."""
+        which = "mg_color", "spmv_p", "conv_rhs", "ustar_prhs" or
+        "update_next"; cold: the L2 is overwritten before each launch."""
         b = ctypes.c_double(0.0)
-        code = {"mg_color": 0, "spmv_p": 1}[which]
+        code = {"mg_color": 0, "spmv_p": 1, "conv_rhs": 2, "ustar_prhs": 3, "update_next": 4}[which]
+        if cold:
+            code |= 256
         ms = self._lib.IBMSolver_time_kernel(self._s, code, int(reps), ctypes.byref(b))
         self._check("IBMSolver_time_kernel")
         return ms, b.value
@@ -315,6 +339,17 @@ class IBMSolver:
         """Mixed modes: momentum solve from the current velocity (default on)."""
         self._lib.IBMSolver_set_warm_start(self._s, 1 if on else 0)
         self._check("set_warm_start")
+
+    def set_pressure_guess(self, mode=1):
+        """Warm-started pressure solves from the last increment (0) or its
+        linear extrapolation from the last two (1)."""
+        self._lib.IBMSolver_set_pressure_guess(self._s, int(mode))
+        self._check("set_pressure_guess")
+
+    def set_max_iters(self, max_mom=200, max_p=1000):
+        """Krylov iteration caps (the reference's 200 and 1000 by default)."""
+        self._lib.IBMSolver_set_max_iters(self._s, int(max_mom), int(max_p))
+        self._check("set_max_iters")
 
     def set_coarsening(self, mode=COARSEN_SPACING, width_ratio=0.0):
         """Pressure multigrid coarsening (before assemble): COARSEN_SPACING
@@ -431,7 +466,9 @@ class IBMSolver:
         return dict(iter=st.iter, time=st.time, iters_u=list(st.iters_u), iters_p=st.iters_p,
                     res_u=list(st.res_u), res_p=st.res_p, max_div=st.max_div,
                     mg_levels=st.mg_levels, cpt_fallback=st.cpt_fallback,
-                    outer_u=st.outer_u, outer_p=st.outer_p)
+                    outer_u=st.outer_u, outer_p=st.outer_p, steps_total=st.steps_total,
+                    iters_u_total=list(st.iters_u_total), iters_p_total=st.iters_p_total,
+                    outer_p_total=st.outer_p_total, max_div_max=st.max_div_max)
 
     def device_bytes(self):
         """Device memory taken by assembly (bytes)."""

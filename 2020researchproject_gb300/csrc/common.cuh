@@ -102,6 +102,45 @@ __host__ __device__ inline void cijk(const Grid &g, long long idx, int &i, int &
     k = (int)(r - (long long)(j + 2) * g.sy) - 2;
 }
 
+// ------------------------------------------------ FP64 <-> FP32 on INT --
+// On GB300 the conversion instructions between FP64 and FP32 run at the
+// FP64 rate (measured: one conversion costs about one FP64 FMA, ~1/70 of
+// an FP32 FMA), so the FP32 stages of the mixed step convert with 32-bit
+// integer operations on the IEEE-754 bit patterns instead.
+//
+// d2f_int: FP64 -> FP32, rounding to nearest with ties away from zero
+// (the first discarded mantissa bit is added to the kept ones; a carry
+// into the exponent is the correct next binade).  Magnitudes below the
+// smallest normal float give a signed zero, above the largest float Inf;
+// NaN stays NaN.
+__device__ __forceinline__ float d2f_int(double x) {
+    const int hi = __double2hiint(x);
+    const unsigned lo = (unsigned)__double2loint(x);
+    const unsigned sgn = (unsigned)hi & 0x80000000u;
+    const int em = hi & 0x7fffffff;     // exponent and the top 20 mantissa bits
+    const int t = em - (896 << 20);     // exponent bias 1023 -> 127
+    unsigned r = __funnelshift_l(lo, (unsigned)t, 3) + ((lo >> 28) & 1u);
+    if (t < (1 << 20)) r = 0u;
+    if (t >= (255 << 20)) r = (em > 0x7ff00000 || (em == 0x7ff00000 && lo != 0u)) ? 0x7fc00000u : 0x7f800000u;
+    return __uint_as_float(sgn | r);
+}
+
+// f2d_int: FP32 -> FP64, exact for normal floats, zero and Inf/NaN
+// (subnormal floats become signed zero).
+__device__ __forceinline__ double f2d_int(float f) {
+    const unsigned b = __float_as_uint(f);
+    const unsigned sgn = b & 0x80000000u, m = b & 0x7fffffffu;
+    unsigned hi = sgn | ((m >> 3) + (896u << 20)), lo = m << 29;
+    if (m < 0x00800000u) {
+        hi = sgn;
+        lo = 0u;
+    } else if (m >= 0x7f800000u) {
+        hi = sgn | 0x7ff00000u | ((m & 0x7fffffu) ? 0x80000u : 0u);
+        lo = 0u;
+    }
+    return __hiloint2double((int)hi, (int)lo);
+}
+
 // Per-axis 1-D tables (device pointers, N+4 entries, index i+2).
 struct Axis {
     const double *d;     // cell width
@@ -113,6 +152,11 @@ struct Axis {
     const double *rdcc;  // 1/(c(i+1)-c(i-1))      cell-centred gradient
     const double *km;    // Crank-Nicolson coefficient toward i-1 (kx_W)
     const double *kp;    // Crank-Nicolson coefficient toward i+1 (kx_E)
+};
+
+// FP32 copies of the tables the FP32 explicit stages read.
+struct AxisF {
+    const float *wm, *wp, *rd, *rdc, *rdcc, *km, *kp;
 };
 
 // Boundary face description with every coefficient the outer-layer rows
@@ -216,6 +260,11 @@ inline void launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t sme
 }
 
 // ------------------------------------------------------------ reductions --
+// Maximum that keeps NaN (fmax drops it): a non-finite value anywhere in a
+// maximum reduction reaches the host, which turns it into a status.
+__device__ __forceinline__ double nanmax(double a, double b) { return (a != a || b != b) ? a + b : fmax(a, b); }
+__device__ __forceinline__ float nanmax(float a, float b) { return (a != a || b != b) ? a + b : fmaxf(a, b); }
+
 // Deterministic two-level reductions: every block writes its partials to
 // partials[block][v]; the last block to finish reduces them in a fixed
 // order.
@@ -252,7 +301,7 @@ __device__ inline void block_max(double (&v)[NV], double *smem) {
     for (int q = 0; q < NV; q++) {
         double x = v[q];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) x = fmax(x, __shfl_down_sync(0xffffffffu, x, o));
+        for (int o = 16; o > 0; o >>= 1) x = nanmax(x, __shfl_down_sync(0xffffffffu, x, o));
         v[q] = x;
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -267,7 +316,7 @@ __device__ inline void block_max(double (&v)[NV], double *smem) {
         for (int q = 0; q < NV; q++) {
             double x = lane < nw ? smem[lane * NV + q] : 0.0;
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) x = fmax(x, __shfl_down_sync(0xffffffffu, x, o));
+            for (int o = 16; o > 0; o >>= 1) x = nanmax(x, __shfl_down_sync(0xffffffffu, x, o));
             v[q] = x;
         }
     }
@@ -288,7 +337,7 @@ __device__ inline void block_reduce(const A (&v)[NV], double (&out)[NV], double 
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             const A y = __shfl_down_sync(0xffffffffu, x, o);
-            x = q < NS ? x + y : (x > y ? x : y);
+            x = q < NS ? x + y : nanmax(x, y);
         }
         if (lane == 0) smem[warp * NV + q] = (double)x;
     }
@@ -301,7 +350,7 @@ __device__ inline void block_reduce(const A (&v)[NV], double (&out)[NV], double 
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
                 const double y = __shfl_down_sync(0xffffffffu, x, o);
-                x = q < NS ? x + y : fmax(x, y);
+                x = q < NS ? x + y : nanmax(x, y);
             }
             out[q] = x;
         }
@@ -341,7 +390,7 @@ __device__ inline void reduce_partials(const double *partials, int nblocks, doub
 #pragma unroll
         for (int q = 0; q < NV; q++) {
             const double x = __ldcg(partials + (size_t)b * NV + q);
-            v[q] = q < NS ? v[q] + x : fmax(v[q], x);
+            v[q] = q < NS ? v[q] + x : nanmax(v[q], x);
         }
     }
 #pragma unroll
@@ -350,7 +399,7 @@ __device__ inline void reduce_partials(const double *partials, int nblocks, doub
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             const double y = __shfl_down_sync(0xffffffffu, x, o);
-            x = q < NS ? x + y : fmax(x, y);
+            x = q < NS ? x + y : nanmax(x, y);
         }
         v[q] = x;
     }
@@ -368,7 +417,7 @@ __device__ inline void reduce_partials(const double *partials, int nblocks, doub
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
                 const double y = __shfl_down_sync(0xffffffffu, x, o);
-                x = q < NS ? x + y : fmax(x, y);
+                x = q < NS ? x + y : nanmax(x, y);
             }
             out[q] = x;
         }

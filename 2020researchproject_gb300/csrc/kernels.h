@@ -45,6 +45,38 @@ struct NextArgs {
     double *pn;
 };
 
+// FP32 explicit stages of the IBM3D_MIXED32 step (step32_kernels.cu).
+struct Conv32Args {
+    const double *u[3];
+    const double *U[3];
+    const double *p;
+    const float *Np[3];
+    const double *tau[6];
+    const double *force;   // sampled VAL_FUNC body force, 3 x ncell (null: the constant force)
+    float *N[3];
+    float *c;              // increment right-hand side, 3 x ncell
+};
+
+struct Ustar32Args {
+    const double *u[3];    // u^n
+    const float *e[3];     // momentum increment e = u* - u^n
+    const double *p;
+    const double *dinv;    // 1 / coeffsum on fluid rows
+    double *Us[3];
+    double *b;
+};
+
+struct Next32Args {
+    const double *u[3];    // u^n
+    const float *e[3];
+    const double *Us[3];
+    const double *p;
+    const double *pp;
+    double *un[3];
+    double *Un[3];
+    double *pn;
+};
+
 enum { GK_ARRAY = 0, GK_OLD = 1, GK_SKIP = 2 };
 
 struct GhostArgs {
@@ -80,6 +112,30 @@ void launch_interp_stag(cudaStream_t s, const Grid &g, const Axis &ax, const Axi
                         const double *const u[3], double *const U[3]);
 void launch_ghost_update(cudaStream_t s, const GhostArgs &a, double *const u[3], double *p);
 void launch_solid_nan(cudaStream_t s, const Grid &g, const uint8_t *flag, double *const u[3], double *p);
+
+struct IRScal;
+template <typename T>
+struct OpT;
+void launch_conv_rhs32(cudaStream_t s, const Grid &g, const AxisF axf[3], const OpT<float> &A, const BCSet &bc,
+                       const uint8_t *flag, const Conv32Args &a, double dt, const double f[3], int les,
+                       double *partials, unsigned int *counter, IRScal *out);
+void launch_ustar_prhs32(cudaStream_t s, const Grid &g, const AxisF axf[3], const Axis ax64[3], const BCSet &bc,
+                         const uint8_t *flag, const Ustar32Args &a, double dt, double Re);
+void launch_update_next32(cudaStream_t s, const Grid &g, const Axis ax64[3], const AxisF axf[3], const BCSet &bc,
+                          const uint8_t *flag, const Next32Args &a, double dt, double *partials,
+                          unsigned int *counter, double *maxdiv_out, int nblocks);
+void launch_widen_f32(cudaStream_t s, long long n, const float *x, double *y);
+void launch_ustar_from_increment(cudaStream_t s, long long n, const double *u, const float *e, double *y);
+// Compares d2f_int / f2d_int with the hardware conversions on n host
+// values; returns 0 and the mismatch count, or -1 on a CUDA error.
+int conversion_check(long long n, const double *x_host, unsigned long long *mismatches);
+
+// Warm-started pressure solve: pp <- 2 pp - prev once two increments are
+// known (hist >= 2), prev <- the old pp; then hist advances (up to 2).
+void launch_pressure_guess(cudaStream_t s, long long n, double *pp, double *prev, int *hist);
+
+// Register-only FMA throughput in TFLOP/s: which 0 FP64, 1 FP32.
+double fma_rate(int which);
 
 // Result export: float u, v, w, p, vorticity, Q, each (nx+4)(ny+4)(nz+4)
 // values in [z][y][x] order, into out (6 such arrays).  ny + 4 <= 65535.

@@ -59,7 +59,10 @@ __device__ __forceinline__ float divw(const OpT<T> &c, long long P, T y) {
 
 // Stopping test: ||r|| < tol ||b|| (tol > 0) or max weighted |r| <= divtol
 // (divtol > 0); either one that is enabled suffices.
+// A non-finite residual norm never passes (NaN in the vectors ends the
+// solve as a breakdown instead, see the dot-product checks below).
 __device__ __forceinline__ bool converged(double rn2, double bn2, double divmax, double tol, double divtol) {
+    if (!isfinite(rn2)) return false;
     return (tol > 0 && sqrt(rn2) < tol * sqrt(bn2)) || (divtol > 0 && divmax <= divtol);
 }
 
@@ -286,7 +289,9 @@ k_bicg_spmv_v(const OpT<T> A, const int op, const long long n, const T *__restri
         for (int c = 0; c < NC; c++) {
             KScal &s = sc[c];
             if (s.state != KS_RUN) continue;
-            if (tot[c] == 0.0) {
+            // A zero or non-finite (r0, v) ends the solve: NaN or Inf in
+            // the operands would otherwise run it to its iteration cap.
+            if (tot[c] == 0.0 || !isfinite(tot[c])) {
                 s.state = KS_BREAKDOWN;
                 continue;
             }
@@ -386,7 +391,7 @@ k_bicg_spmv_t(const OpT<T> A, const int op, const long long n, const T *__restri
         for (int c = 0; c < NC; c++) {
             KScal &st = sc[c];
             if (st.state != KS_RUN) continue;
-            if (tot[2 * c + 1] == 0.0) {
+            if (tot[2 * c + 1] == 0.0 || !isfinite(tot[2 * c + 1]) || !isfinite(tot[2 * c])) {
                 st.omega = 0.0;
                 st.state = KS_BREAKDOWN;
                 continue;
@@ -479,7 +484,7 @@ k_bicg_xr(const OpT<T> A, const long long n, T *__restrict__ x, T *__restrict__ 
             if (converged(tot[2 * c], st.bnorm2, tot[2 * NC], st.tol, st.divtol)) {
                 st.state = KS_DONE;
                 st.divmax = tot[2 * NC];
-            } else if (rho1 == 0.0) {
+            } else if (rho1 == 0.0 || !isfinite(rho1) || !isfinite(tot[2 * c])) {
                 st.state = KS_BREAKDOWN;
             }
             run = run || (st.state == KS_RUN && st.iters < maxit);
@@ -853,13 +858,20 @@ static void launch_update(cudaStream_t st, IRWork &w, double *x) {
     note_launches(1);
 }
 
+// Relative residual of a report: NaN when either norm is not finite (the
+// host turns that into a status), 0 for a zero right-hand side.
+static double relres(double rn2, double bn2) {
+    if (!std::isfinite(rn2) || !std::isfinite(bn2)) return NAN;
+    return bn2 > 0 ? std::sqrt(rn2 / bn2) : 0.0;
+}
+
 template <typename T>
 int report(const KrylovWork<T> &w, SolveReport &rep) {
     int status = 0;
     for (int c = 0; c < w.nc; c++) {
         const KScal &s = w.scal_h[c];
         rep.iters[c] = s.iters;
-        rep.relres[c] = s.bnorm2 > 0 ? std::sqrt(s.rnorm2 / s.bnorm2) : 0.0;
+        rep.relres[c] = relres(s.rnorm2, s.bnorm2);
         rep.divmax[c] = s.divmax;
         if (s.state == KS_BREAKDOWN) status = 2;
         else if (s.state != KS_DONE && status == 0) status = 1;
@@ -877,7 +889,7 @@ int report(const IRWork &w, SolveReport &rep) {
         const IRScal &s = w.scal_h[c];
         rep.iters[c] = s.inner;
         rep.outer = std::max(rep.outer, s.outer);
-        rep.relres[c] = s.bnorm2 > 0 ? std::sqrt(s.rnorm2 / s.bnorm2) : 0.0;
+        rep.relres[c] = relres(s.rnorm2, s.bnorm2);
         rep.divmax[c] = s.divmax;
         if (s.state != KS_DONE) status = 1;
     }
@@ -948,6 +960,28 @@ int solve_ir(cudaStream_t st, const OpT<double> &A64, const OpT<float> &A32, int
         fetch_outer();
     }
     return report(w, rep);
+}
+
+int solve_inc(cudaStream_t st, const OpT<float> &A32, int op, IRWork &w, const SolveParams &prm, SolveReport &rep) {
+    launch_init(st, w.inner, w.b32, w.e32, prm.inner_tol, 0.0, w.scal, prm.tol, 0.0, LoopCtl());
+    host_loop<float>(st, A32, op, w.inner, w.e32, prm.maxit, nullptr, prm.prof);
+    cudaMemcpyAsync(w.scal_h, w.scal, sizeof(IRScal) * w.nc, cudaMemcpyDeviceToHost, st);
+    cudaStreamSynchronize(st);
+    return report_inc(w, prm.tol, rep);
+}
+
+int report_inc(const IRWork &w, double tol, SolveReport &rep) {
+    rep = SolveReport();
+    int status = 0;
+    for (int c = 0; c < w.nc; c++) {
+        const KScal &s = w.inner.scal_h[c];
+        rep.iters[c] = s.iters;
+        rep.relres[c] = relres(s.rnorm2, w.scal_h[c].bnorm2);
+        rep.divmax[c] = 0.0;
+        if (s.state == KS_BREAKDOWN) status = 2;
+        else if (!(rep.relres[c] < tol) && rep.relres[c] != 0.0 && status == 0) status = 1;
+    }
+    return status;
 }
 
 // ------------------------------------------------------- recorded forms --
@@ -1054,6 +1088,18 @@ int record_ir(cudaStream_t st, const cudaStream_t *aux, const OpT<double> &A64, 
     cudaMemcpyAsync(w.scal_h, w.scal, sizeof(IRScal) * nc, cudaMemcpyDeviceToHost, st);
     *fixed = 1;
     *per_outer = 4;
+    return 0;
+}
+
+int record_inc(cudaStream_t st, const cudaStream_t *aux, const OpT<float> &A32, int op, IRWork &w,
+               const SolveParams &prm, int *fixed, int *per_iter) {
+    LoopCtl lc;
+    if (new_loop(st, lc) != 0) return -1;
+    launch_init(st, w.inner, w.b32, w.e32, prm.inner_tol, 0.0, w.scal, prm.tol, 0.0, lc);
+    if (record_loop<float>(st, aux[0], A32, op, w.inner, w.e32, prm.maxit, nullptr, lc, per_iter) != 0) return -1;
+    cudaMemcpyAsync(w.inner.scal_h, w.inner.scal, sizeof(KScal) * w.nc, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(w.scal_h, w.scal, sizeof(IRScal) * w.nc, cudaMemcpyDeviceToHost, st);
+    *fixed = 1;
     return 0;
 }
 
@@ -1261,7 +1307,7 @@ k_gm_orth(const long long n, const double *__restrict__ V, double *w, GScal *gs,
             hc[i] = t;
         }
         const double d = hypot(hc[j], hc[j + 1]);
-        bool breakdown = d == 0.0;
+        bool breakdown = d == 0.0 || !isfinite(d);
         if (!breakdown) {
             s.cs[j] = hc[j] / d;
             s.sn[j] = hc[j + 1] / d;
@@ -1354,7 +1400,7 @@ int report(const GmresWork &w, SolveReport &rep) {
     const GScal &s = *w.scal_h;
     rep.iters[0] = s.iters;
     rep.outer = s.cycles;
-    rep.relres[0] = s.bnorm2 > 0 ? std::sqrt(s.rnorm2 / s.bnorm2) : 0.0;
+    rep.relres[0] = relres(s.rnorm2, s.bnorm2);
     rep.divmax[0] = s.divmax;
     return s.state == GM_DONE ? 0 : 1;
 }

@@ -211,6 +211,18 @@ template <typename T>
 int report(const KrylovWork<T> &w, SolveReport &rep);
 int report(const IRWork &w, SolveReport &rep);
 
+// Increment solve (IBM3D_MIXED32 momentum): A32 e = c in FP32 from e = 0,
+// with c in w.b32 and ||b||^2, ||c||^2 per component already in w.scal
+// (written by the kernel that formed c).  Each component stops once
+// ||c - A e|| < max(inner_tol ||c||, tol ||b|| / 2), i.e. on the
+// reference's relative test ||b - A u*|| < tol ||b|| with a factor-2
+// margin for FP32 rounding.  The host loop and the recorded form; report
+// returns 0 when every component met tol, 1 otherwise, 2 on breakdown.
+int solve_inc(cudaStream_t st, const OpT<float> &A32, int op, IRWork &w, const SolveParams &prm, SolveReport &rep);
+int record_inc(cudaStream_t st, const cudaStream_t *aux, const OpT<float> &A32, int op, IRWork &w,
+               const SolveParams &prm, int *fixed, int *per_iter);
+int report_inc(const IRWork &w, double tol, SolveReport &rep);
+
 template <typename T>
 void apply_operator(cudaStream_t st, const OpT<T> &A, int op, int comp, const T *x, T *y);
 

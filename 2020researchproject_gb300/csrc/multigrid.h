@@ -108,7 +108,8 @@ class GMG : public Preconditioner<T> {
     // (reps launches between CUDA events on s); bytes: its algorithmic
     // bytes (z read once, r, 1/coeffsum, flag read and z written for the
     // updated half of the interior cells).
-    float time_color(cudaStream_t s, const T *r, T *z, int reps, double *bytes);
+    // timed = false: launches only (the caller times them).
+    float time_color(cudaStream_t s, const T *r, T *z, int reps, double *bytes, bool timed = true);
 
   private:
     OpT<T> A_{};

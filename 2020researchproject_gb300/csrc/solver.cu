@@ -12,6 +12,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <algorithm>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -55,7 +56,7 @@ struct StepGraph {
 
 // Host parameters baked into recorded graphs.
 struct GraphSig {
-    int precision, les, use_mg, max_outer, solver, gm_restart, warm;
+    int precision, les, use_mg, max_outer, solver, gm_restart, warm, p_guess;
     double tol, divtol, Re, dt, f[3], cs, inner_tol[2];
     bool operator==(const GraphSig &o) const { return memcmp(this, &o, sizeof *this) == 0; }
 };
@@ -68,6 +69,9 @@ struct ibm3d_device {
     // Per-axis 1-D tables: 9 arrays of n+4 doubles each.
     double *tab[3] = {nullptr, nullptr, nullptr};
     Axis ax[3];
+    // FP32 copies (wm, wp, rd, rdc, rdcc, km, kp) for the FP32 explicit stages.
+    float *tabf[3] = {nullptr, nullptr, nullptr};
+    AxisF axf[3];
     BCSet bc{};
     // Fields.
     double *fields = nullptr;
@@ -75,6 +79,14 @@ struct ibm3d_device {
     double *u[3], *un[3], *ustar, *U[3], *Un[3], *Us[3], *p, *pn, *pp, *N[3], *Np[3], *tau[6], *b, *lvset, *dinv;
     uint8_t *flag = nullptr;
     int *gid = nullptr;
+    // Pressure-guess extrapolation (IBMSolver_set_pressure_guess): the
+    // increment before the last one, and how many increments are known.
+    double *pp_prev = nullptr;
+    int *pp_hist = nullptr;
+    int p_guess = 0;
+    // IBM3D_MIXED32: N and N_prev in FP32 (6 arrays of ncell floats).
+    float *f32 = nullptr;
+    float *N32[3], *Np32[3];
     // Ghost cells.
     int nghost = 0, nlevels = 0;
     int *g_mem = nullptr;
@@ -130,6 +142,7 @@ struct ibm3d_device {
     double mg_omega = 1.0;               // over-relaxation of the fine-grid smoother
     int mg_coarsening = IBM3D_COARSEN_SPACING;
     int warm_start = 1;                  // mixed modes: momentum solve from the current velocity
+    int maxit_mom = 200, maxit_p = 1000; // Krylov iteration caps (src/ibm3d_setup.c:1411-1432, 1435-1563)
     double mg_width_ratio = 1.5;
     // Mixed path: relative tolerance of each FP32 inner solve (momentum,
     // pressure) and the refinement-cycle cap.
@@ -145,6 +158,9 @@ struct ibm3d_device {
     // Last-step statistics.
     SolveReport rep_mom, rep_p;
     double max_div = 0.0;
+    // Totals since assembly (IBMSolverStats).
+    long long steps_total = 0, iters_u_total[3] = {0, 0, 0}, iters_p_total = 0, outer_p_total = 0;
+    double max_div_max = 0.0;
     int status = IBM3D_OK;
     char message[512] = {0};  // text of the last error
     bool assembled = false;
@@ -290,8 +306,14 @@ void release_device(ibm3d_device *d) {
     dfree(d->sweep_outer);
     d->A64 = OpT<double>{};
     d->A32 = OpT<float>{};
-    for (int a = 0; a < 3; a++) dfree(d->tab[a]);
+    for (int a = 0; a < 3; a++) {
+        dfree(d->tab[a]);
+        dfree(d->tabf[a]);
+    }
     dfree(d->fields);
+    dfree(d->f32);
+    dfree(d->pp_prev);
+    dfree(d->pp_hist);
     dfree(d->flag);
     dfree(d->gid);
     dfree(d->g_mem);
@@ -386,6 +408,14 @@ bool upload_axes(IBMSolver *sv) {
         cudaMemcpyAsync(d->tab[a], h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, d->s);
         double *t = d->tab[a];
         d->ax[a] = Axis{t, t + n, t + 2 * n, t + 3 * n, t + 4 * n, t + 5 * n, t + 6 * n, t + 7 * n, t + 8 * n};
+        // FP32 copies of wm, wp, rd, rdc, rdcc, km, kp (rows 2..8).
+        std::vector<float> hf(7 * (size_t)n);
+        for (size_t q = 0; q < hf.size(); q++) hf[q] = (float)h[2 * (size_t)n + q];
+        d->tabf[a] = dmalloc<float>(sv, hf.size(), "FP32 axis tables");
+        if (!d->tabf[a]) return false;
+        cudaMemcpyAsync(d->tabf[a], hf.data(), sizeof(float) * hf.size(), cudaMemcpyHostToDevice, d->s);
+        float *f = d->tabf[a];
+        d->axf[a] = AxisF{f, f + n, f + 2 * n, f + 3 * n, f + 4 * n, f + 5 * n, f + 6 * n};
     }
     return true;
 }
@@ -418,6 +448,15 @@ bool alloc_fields(IBMSolver *sv) {
     d->b = take(3);
     d->lvset = take(1);
     d->dinv = take(1);
+    d->f32 = dmalloc<float>(sv, 6 * (size_t)n, "FP32 convection terms");
+    if (!d->f32) return false;
+    d->pp_prev = dmalloc<double>(sv, n, "pressure increment history");
+    d->pp_hist = dmalloc<int>(sv, 1, "pressure increment count");
+    if (!d->pp_prev || !d->pp_hist) return false;
+    for (int l = 0; l < 3; l++) {
+        d->N32[l] = d->f32 + (size_t)l * n;
+        d->Np32[l] = d->f32 + (size_t)(3 + l) * n;
+    }
     d->flag = dmalloc<uint8_t>(sv, n, "flags");
     d->gid = dmalloc<int>(sv, n, "ghost map");
     d->red_partials = dmalloc<double>(sv, 8 * 4096, "reduction partials");
@@ -738,6 +777,21 @@ ConvArgs conv_args(ibm3d_device *d) {
     return a;
 }
 
+Conv32Args conv32_args(ibm3d_device *d) {
+    Conv32Args a{};
+    for (int l = 0; l < 3; l++) {
+        a.u[l] = d->u[l];
+        a.U[l] = d->U[l];
+        a.Np[l] = d->Np32[l];
+        a.N[l] = d->N32[l];
+    }
+    for (int t = 0; t < 6; t++) a.tau[t] = d->tau[t];
+    a.p = d->p;
+    a.force = d->force_d;
+    a.c = d->irmom.b32;
+    return a;
+}
+
 void calc_tau(IBMSolver *sv) {
     ibm3d_device *d = sv->dev;
     if (!d->les) return;
@@ -885,7 +939,7 @@ bool mom_ir(const ibm3d_device *d);
 SolveParams mom_params(IBMSolver *sv) {
     SolveParams pm;
     pm.tol = sv->tol;
-    pm.maxit = 200;
+    pm.maxit = sv->dev->maxit_mom;
     pm.inner_tol = sv->dev->inner_tol[0];
     pm.max_outer = sv->dev->max_outer;
     pm.prof = &sv->dev->prof;
@@ -907,10 +961,17 @@ SolveParams pres_params(IBMSolver *sv) {
     // The mixed modes start from the last step's pressure increment.
     pp.x_given = sv->dev->precision != IBM3D_FP64 && sv->dev->warm_start && !pres_gmres(sv);
     pp.inner_tol = sv->dev->inner_tol[1];
-    pp.maxit = 1000;
+    pp.maxit = sv->dev->maxit_p;
     pp.divtol = sv->dev->divtol;
     if (pp.divtol > 0) pp.tol = 0.0;  // the divergence rule replaces the relative-residual rule
     return pp;
+}
+
+// With IBMSolver_set_pressure_guess(s, 1) a warm-started pressure solve
+// starts from the linear extrapolation of the last two increments.
+void pressure_guess(IBMSolver *sv, const SolveParams &pp) {
+    ibm3d_device *d = sv->dev;
+    if (pp.x_given && d->p_guess == 1) launch_pressure_guess(d->s, d->g.ncell, d->pp, d->pp_prev, d->pp_hist);
 }
 
 bool use_mg(const IBMSolver *sv) { return sv->precond_type == PRECOND_AMG || sv->linear_solver_type == SOLVER_AMG; }
@@ -919,9 +980,13 @@ bool use_mg(const IBMSolver *sv) { return sv->precond_type == PRECOND_AMG || sv-
 // mode; the mixed modes precondition it with the FP32 multigrid).
 bool pres_gmres(const IBMSolver *sv) { return sv->linear_solver_type == SOLVER_GMRES; }
 
-// Which solve runs as FP64 refinement around FP32 BiCGSTAB.
-bool mom_ir(const ibm3d_device *d) { return d->precision != IBM3D_FP64; }
-bool pres_ir(const IBMSolver *sv) { return sv->dev->precision == IBM3D_MIXED && !pres_gmres(sv); }
+// Which solve runs as FP64 refinement around FP32 BiCGSTAB, and which step
+// has the FP32 explicit stages and the FP32 increment momentum solve.
+bool mom_ir(const ibm3d_device *d) { return d->precision == IBM3D_MIXED || d->precision == IBM3D_MIXED_MG; }
+bool step32(const ibm3d_device *d) { return d->precision == IBM3D_MIXED32 || d->precision == IBM3D_MIXED32_IR; }
+bool pres_ir(const IBMSolver *sv) {
+    return (sv->dev->precision == IBM3D_MIXED || sv->dev->precision == IBM3D_MIXED32_IR) && !pres_gmres(sv);
+}
 
 // Preconditioner of an FP64 pressure Krylov solve.
 Preconditioner<double> *pres_pc64(IBMSolver *sv) {
@@ -938,12 +1003,31 @@ void stage_rhs(IBMSolver *sv) {
     calc_tau(sv);
     pf.end(t);
     t = pf.begin("conv_rhs");
-    launch_conv_rhs(d->s, d->g, d->ax[0], d->ax[1], d->ax[2], d->bc, d->flag, conv_args(d), sv->dt, f, d->les);
+    if (step32(d))
+        launch_conv_rhs32(d->s, d->g, d->axf, d->A32, d->bc, d->flag, conv32_args(d), sv->dt, f, d->les,
+                          d->red_partials, d->red_counter, d->irmom.scal);
+    else
+        launch_conv_rhs(d->s, d->g, d->ax[0], d->ax[1], d->ax[2], d->bc, d->flag, conv_args(d), sv->dt, f, d->les);
     pf.end(t);
 }
 
 void stage_ustar(IBMSolver *sv) {
     ibm3d_device *d = sv->dev;
+    if (step32(d)) {
+        Ustar32Args ua{};
+        for (int l = 0; l < 3; l++) {
+            ua.u[l] = d->u[l];
+            ua.e[l] = d->irmom.e32 + l * d->g.ncell;
+            ua.Us[l] = d->Us[l];
+        }
+        ua.p = d->p;
+        ua.dinv = d->dinv;
+        ua.b = d->b;
+        const int t = d->prof.begin("ustar_prhs");
+        launch_ustar_prhs32(d->s, d->g, d->axf, d->ax, d->bc, d->flag, ua, sv->dt, sv->Re);
+        d->prof.end(t);
+        return;
+    }
     UstarArgs ua{};
     for (int l = 0; l < 3; l++) {
         ua.us[l] = d->ustar + l * d->g.ncell;
@@ -958,6 +1042,24 @@ void stage_ustar(IBMSolver *sv) {
 
 void stage_next(IBMSolver *sv) {
     ibm3d_device *d = sv->dev;
+    if (step32(d)) {
+        Next32Args na{};
+        for (int l = 0; l < 3; l++) {
+            na.u[l] = d->u[l];
+            na.e[l] = d->irmom.e32 + l * d->g.ncell;
+            na.Us[l] = d->Us[l];
+            na.un[l] = d->un[l];
+            na.Un[l] = d->Un[l];
+        }
+        na.p = d->p;
+        na.pp = d->pp;
+        na.pn = d->pn;
+        const int t = d->prof.begin("update_next");
+        launch_update_next32(d->s, d->g, d->ax, d->axf, d->bc, d->flag, na, sv->dt, d->red_partials, d->red_counter,
+                             d->maxdiv_d, kUpdateBlocks);
+        d->prof.end(t);
+        return;
+    }
     NextArgs na{};
     for (int l = 0; l < 3; l++) {
         na.us[l] = d->ustar + l * d->g.ncell;
@@ -979,18 +1081,39 @@ void swap_fields(ibm3d_device *d) {
     swap3(d->U, d->Un);
     std::swap(d->p, d->pn);
     swap3(d->N, d->Np);
+    for (int l = 0; l < 3; l++) std::swap(d->N32[l], d->Np32[l]);
 }
 
+// Non-finite residuals mean NaN or Inf reached the solve (the initial
+// state, boundary values or force, or a run that diverged): the reference
+// would carry them on silently; here they end the iterate call with a
+// status.  Non-convergence warns and continues, as in the reference
+// (src/ibm3d_fracstep.c:363-369, 673-679, the same messages).
 void check_mom(IBMSolver *sv, int rc) {
+    for (int l = 0; l < 3; l++)
+        if (!std::isfinite(sv->dev->rep_mom.relres[l])) {
+            set_status(sv, IBM3D_ENONFINITE,
+                       "non-finite residual in the u%d_star solve at step %d: NaN or Inf in the state, boundary "
+                       "data or force",
+                       l, sv->iter + 1);
+            return;
+        }
     if (rc == 1) {
         for (int l = 0; l < 3; l++)
-            if (sv->dev->rep_mom.relres[l] >= sv->tol) fprintf(stderr, "warning: u%d_star did not converge\n", l + 1);
+            if (sv->dev->rep_mom.relres[l] >= sv->tol) fprintf(stderr, "warning: u%d_star did not converge\n", l);
     } else if (rc == 2) {
         set_status(sv, IBM3D_EBREAKDOWN, "breakdown in the momentum solve");
     }
 }
 
 void check_pres(IBMSolver *sv, int rc) {
+    if (!std::isfinite(sv->dev->rep_p.relres[0])) {
+        set_status(sv, IBM3D_ENONFINITE,
+                   "non-finite residual in the p_prime solve at step %d: NaN or Inf in the state, boundary data or "
+                   "force",
+                   sv->iter + 1);
+        return;
+    }
     if (rc == 1) fprintf(stderr, "warning: p_prime did not converge\n");
     else if (rc == 2) set_status(sv, IBM3D_EBREAKDOWN, "breakdown in the pressure solve");
 }
@@ -1003,12 +1126,14 @@ void one_step(IBMSolver *sv) {
     const SolveParams pm = mom_params(sv);
     int t = pf.begin("mom_solve");
     momentum_guess(sv, pm);
-    int rc = mom_ir(d) ? solve_ir(d->s, d->A64, d->A32, OP_MOM, d->irmom, d->b, d->ustar, pm, nullptr, d->rep_mom)
-                   : bicgstab<double>(d->s, d->A64, OP_MOM, d->kmom, d->b, d->ustar, pm, nullptr, d->rep_mom);
+    int rc = step32(d)  ? solve_inc(d->s, d->A32, OP_MOM, d->irmom, pm, d->rep_mom)
+             : mom_ir(d) ? solve_ir(d->s, d->A64, d->A32, OP_MOM, d->irmom, d->b, d->ustar, pm, nullptr, d->rep_mom)
+                         : bicgstab<double>(d->s, d->A64, OP_MOM, d->kmom, d->b, d->ustar, pm, nullptr, d->rep_mom);
     pf.end(t);
     check_mom(sv, rc);
     stage_ustar(sv);
     const SolveParams pp = pres_params(sv);
+    pressure_guess(sv, pp);
     t = pf.begin("p_solve");
     if (pres_gmres(sv))
         rc = gmres(d->s, d->A64, OP_PRES, d->gm, d->b, d->pp, pp, pres_pc64(sv), d->rep_p);
@@ -1043,6 +1168,7 @@ GraphSig graph_sig(const IBMSolver *sv) {
     g.max_outer = sv->dev->max_outer;
     g.solver = sv->linear_solver_type;
     g.gm_restart = sv->dev->gm_restart;
+    g.p_guess = sv->dev->p_guess;
     return g;
 }
 
@@ -1061,7 +1187,9 @@ bool record_step_into(IBMSolver *sv, StepGraph &G) {
         SolveParams pm = mom_params(sv);
         pm.prof = nullptr;
         momentum_guess(sv, pm);
-        if (mom_ir(d))
+        if (step32(d))
+            ok = record_inc(d->s, d->aux, d->A32, OP_MOM, d->irmom, pm, &mf, &mi) == 0;
+        else if (mom_ir(d))
             ok = record_ir(d->s, d->aux, d->A64, d->A32, OP_MOM, d->irmom, d->b, d->ustar, pm, nullptr, &mf, &mo,
                            &mi) == 0;
         else
@@ -1072,6 +1200,7 @@ bool record_step_into(IBMSolver *sv, StepGraph &G) {
         stage_ustar(sv);
         SolveParams pp = pres_params(sv);
         pp.prof = nullptr;
+        pressure_guess(sv, pp);
         if (pres_gmres(sv))
             ok = record_gmres(d->s, d->aux, d->A64, OP_PRES, d->gm, d->b, d->pp, pp, pres_pc64(sv), &pf, &po,
                               &pi) == 0;
@@ -1142,7 +1271,9 @@ void finish_step(IBMSolver *sv, const StepGraph &G) {
     ibm3d_device *d = sv->dev;
     long long launches = G.fixed;
     int rc;
-    if (mom_ir(d)) {
+    if (step32(d)) {
+        rc = report_inc(d->irmom, sv->tol, d->rep_mom);
+    } else if (mom_ir(d)) {
         rc = report(d->irmom, d->rep_mom);
         launches += (long long)d->rep_mom.outer * G.mom_outer;
     } else {
@@ -1200,16 +1331,18 @@ bool graph_step(IBMSolver *sv) {
 
 void print_row(IBMSolver *sv, int i, long elapsed_ms) {
     ibm3d_device *d = sv->dev;
+    // The reference's columns (src/ibm3d_fracstep.c:77-105), then this
+    // step's max|div U^{n+1}| over fluid cells, measured by k_update_next.
     if (sv->iter % 10 == 1 || i == 1) {
-        printf("\n  iter       u1 res       u2 res       u3 res        p res       time\n");
-        printf("---------------------------------------------------------------------\n");
+        printf("\n  iter       u1 res       u2 res       u3 res        p res       time   max|div U|\n");
+        printf("----------------------------------------------------------------------------------\n");
     }
     long hour = elapsed_ms / 3600000, min = elapsed_ms / 60000 % 60;
     long sec = elapsed_ms / 1000 % 60 + (elapsed_ms % 1000 > 500);
     if (sec >= 60) { sec -= 60; min += 1; }
     if (min >= 60) { min -= 60; hour += 1; }
-    printf("%6d   %10.4e   %10.4e   %10.4e   %10.4e   %02ld:%02ld:%02ld\n", sv->iter, d->rep_mom.relres[0],
-           d->rep_mom.relres[1], d->rep_mom.relres[2], d->rep_p.relres[0], hour, min, sec);
+    printf("%6d   %10.4e   %10.4e   %10.4e   %10.4e   %02ld:%02ld:%02ld   %10.4e\n", sv->iter, d->rep_mom.relres[0],
+           d->rep_mom.relres[1], d->rep_mom.relres[2], d->rep_p.relres[0], hour, min, sec, d->max_div);
 }
 
 bool check_ready(IBMSolver *sv, const char *fn) {
@@ -1228,8 +1361,10 @@ void upload_state(IBMSolver *sv, const double *u1, const double *u2, const doubl
     cudaMemcpyAsync(d->u[2], u3, b, cudaMemcpyHostToDevice, d->s);
     cudaMemcpyAsync(d->p, p, b, cudaMemcpyHostToDevice, d->s);
     // A new run: the pressure increment, a warm start's initial guess,
-    // starts from zero.
+    // starts from zero, with no history to extrapolate from.
     cudaMemsetAsync(d->pp, 0, b, d->s);
+    cudaMemsetAsync(d->pp_prev, 0, b, d->s);
+    cudaMemsetAsync(d->pp_hist, 0, sizeof(int), d->s);
     cuda_check(sv, cudaStreamSynchronize(d->s), "state upload");
     sv->iter = 0;
     sv->time = 0;
@@ -1627,12 +1762,13 @@ struct StateHeader {
     char magic[8];
     int nx, ny, nz, iter;
     double time;
-    int nfields, pad;
+    int nfields;
+    int pp_hist;   // pressure increments known to the guess extrapolation (0..2)
 };
 
 namespace {
 
-constexpr int kStateFields = 27;
+constexpr int kStateFields = 28;
 
 // Device arrays of the state, in file order.
 void state_fields(ibm3d_device *d, double *f[kStateFields]) {
@@ -1646,7 +1782,8 @@ void state_fields(ibm3d_device *d, double *f[kStateFields]) {
     for (int l = 0; l < 3; l++) f[q++] = d->N[l];
     for (int l = 0; l < 3; l++) f[q++] = d->Np[l];
     for (int l = 0; l < 6; l++) f[q++] = d->tau[l];
-    f[q++] = d->pp;  // the last pressure increment: the next solve's initial guess
+    f[q++] = d->pp;       // the last pressure increment: the next solve's initial guess
+    f[q++] = d->pp_prev;  // the one before (guess extrapolation)
 }
 
 bool write_state(IBMSolver *s, const std::string &path) {
@@ -1654,9 +1791,10 @@ bool write_state(IBMSolver *s, const std::string &path) {
     FILE *f = fopen(path.c_str(), "wb");
     if (!f) return false;
     StateHeader h{};
-    memcpy(h.magic, "IBM3DST3", 8);
+    memcpy(h.magic, "IBM3DST4", 8);
     h.nx = s->Nx; h.ny = s->Ny; h.nz = s->Nz; h.iter = s->iter; h.time = s->time;
     h.nfields = kStateFields;
+    cudaMemcpy(&h.pp_hist, d->pp_hist, sizeof(int), cudaMemcpyDeviceToHost);
     const size_t n = (size_t)d->g.ncell;
     bool ok = fwrite(&h, sizeof h, 1, f) == 1;
     double *fld[kStateFields];
@@ -1677,7 +1815,7 @@ int read_state(IBMSolver *s, const std::string &path) {
     if (!f) return 0;
     StateHeader h{};
     const size_t n = (size_t)d->g.ncell;
-    bool ok = fread(&h, sizeof h, 1, f) == 1 && memcmp(h.magic, "IBM3DST3", 8) == 0 && h.nx == s->Nx &&
+    bool ok = fread(&h, sizeof h, 1, f) == 1 && memcmp(h.magic, "IBM3DST4", 8) == 0 && h.nx == s->Nx &&
               h.ny == s->Ny && h.nz == s->Nz && h.nfields == kStateFields;
     std::vector<double> buf(ok ? kStateFields * n : 0);
     ok = ok && fread(buf.data(), sizeof(double), buf.size(), f) == buf.size();
@@ -1687,6 +1825,8 @@ int read_state(IBMSolver *s, const std::string &path) {
     state_fields(d, fld);
     for (int q = 0; q < kStateFields; q++)
         cudaMemcpyAsync(fld[q], buf.data() + q * n, n * sizeof(double), cudaMemcpyHostToDevice, d->s);
+    const int hist = h.pp_hist < 0 ? 0 : h.pp_hist > 2 ? 2 : h.pp_hist;
+    cudaMemcpyAsync(d->pp_hist, &hist, sizeof(int), cudaMemcpyHostToDevice, d->s);
     if (!cuda_check(s, cudaStreamSynchronize(d->s), "state upload")) return 1;
     double *host[4] = {s->u1, s->u2, s->u3, s->p};
     const int role[4] = {0, 1, 2, 12};
@@ -1911,6 +2051,17 @@ namespace {
 // What every IBMSolver_iterate call does before its steps
 // (src/ibm3d_fracstep.c:40-56): outer fill, face velocities, ghost
 // update with solid NaNs, and N^{-1} = N^0 for the AB2 bootstrap.
+void iterate_prologue(IBMSolver *s);
+
+// Adds a finished step's counts to the solver's totals.
+void account_step(ibm3d_device *d) {
+    d->steps_total++;
+    for (int l = 0; l < 3; l++) d->iters_u_total[l] += d->rep_mom.iters[l];
+    d->iters_p_total += d->rep_p.iters[0];
+    d->outer_p_total += d->rep_p.outer;
+    if (!(d->max_div <= d->max_div_max)) d->max_div_max = d->max_div;
+}
+
 void iterate_prologue(IBMSolver *s) {
     ibm3d_device *d = s->dev;
     d->status = IBM3D_OK;
@@ -1919,6 +2070,15 @@ void iterate_prologue(IBMSolver *s) {
     launch_interp_stag(d->s, d->g, d->ax[0], d->ax[1], d->ax[2], d->u, d->U);
     ghost_update(s, true);
     const double f[3] = {s->ext_force.const_f1, s->ext_force.const_f2, s->ext_force.const_f3};
+    if (step32(d)) {
+        launch_conv_rhs32(d->s, d->g, d->axf, d->A32, d->bc, d->flag, conv32_args(d), s->dt, f, 0, d->red_partials,
+                          d->red_counter, d->irmom.scal);
+        // The FP64 N buffers swap with them: recorded steps are keyed by
+        // the FP64 buffers' parity, which must follow the FP32 ones.
+        for (int l = 0; l < 3; l++) std::swap(d->N32[l], d->Np32[l]);
+        swap3(d->N, d->Np);
+        return;
+    }
     launch_conv_rhs(d->s, d->g, d->ax[0], d->ax[1], d->ax[2], d->bc, d->flag, conv_args(d), s->dt, f, 0);
     swap3(d->N, d->Np);
 }
@@ -1948,12 +2108,21 @@ void IBMSolver_iterate(IBMSolver *s, int num_time_steps, bool verbose) {
         s->iter++;
         s->time = start_time + s->dt * i;
         d->max_div = *d->maxdiv_h;
+        account_step(d);
+        // NaN anywhere near a fluid cell reaches max|div U| (its reduction
+        // keeps NaN) or a solve's residual.
+        if (d->status != IBM3D_ENONFINITE && !std::isfinite(d->max_div))
+            set_status(s, IBM3D_ENONFINITE,
+                       "non-finite max|div U| after step %d: NaN or Inf in the state, boundary data or force",
+                       s->iter);
+        const bool nonfinite = d->status == IBM3D_ENONFINITE;
         d->prof.flush();
         if (verbose && s->rank == 0) {
             clock_gettime(CLOCK_REALTIME, &t1);
             const long el = (t1.tv_sec * 1000 + t1.tv_nsec / 1000000) - (t0.tv_sec * 1000 + t0.tv_nsec / 1000000);
             print_row(s, i, el);
         }
+        if (nonfinite) return;
         if (s->autosave_period > 0 && s->iter % s->autosave_period == 0) {
             if (s->rank == 0) printf("\nAutosave...\n\n");
             char fn[1024];
@@ -1977,6 +2146,7 @@ const char *IBMSolver_status_string(int st) {
     case IBM3D_EARG: return "invalid argument";
     case IBM3D_EGEOM: return "ghost-cell mirror point outside the grid";
     case IBM3D_EUNSUPPORTED: return "unsupported on the GPU path";
+    case IBM3D_ENONFINITE: return "non-finite values in the time step";
     }
     return "unknown";
 }
@@ -2084,6 +2254,25 @@ void IBMSolver_set_warm_start(IBMSolver *s, int on) {
     drop_graphs(s->dev);
 }
 
+void IBMSolver_set_pressure_guess(IBMSolver *s, int mode) {
+    if (!s || !s->dev || mode < 0 || mode > 1) {
+        set_status(s, IBM3D_EARG, "IBMSolver_set_pressure_guess: mode %d", mode);
+        return;
+    }
+    s->dev->p_guess = mode;
+    drop_graphs(s->dev);
+}
+
+void IBMSolver_set_max_iters(IBMSolver *s, int max_mom, int max_p) {
+    if (!s || !s->dev || max_mom < 1 || max_p < 1) {
+        set_status(s, IBM3D_EARG, "IBMSolver_set_max_iters: caps must be >= 1 (%d, %d)", max_mom, max_p);
+        return;
+    }
+    s->dev->maxit_mom = max_mom;
+    s->dev->maxit_p = max_p;
+    drop_graphs(s->dev);
+}
+
 void IBMSolver_set_coarsening(IBMSolver *s, int mode, double width_ratio) {
     if (mode != IBM3D_COARSEN_HALVE && mode != IBM3D_COARSEN_SPACING) {
         set_status(s, IBM3D_EARG, "IBMSolver_set_coarsening: unknown mode %d", mode);
@@ -2107,7 +2296,8 @@ void IBMSolver_set_graphs(IBMSolver *s, int on) {
 }
 
 void IBMSolver_set_precision(IBMSolver *s, int mode) {
-    if (mode != IBM3D_FP64 && mode != IBM3D_MIXED && mode != IBM3D_MIXED_MG) {
+    if (mode != IBM3D_FP64 && mode != IBM3D_MIXED && mode != IBM3D_MIXED_MG && mode != IBM3D_MIXED32 &&
+        mode != IBM3D_MIXED32_IR) {
         set_status(s, IBM3D_EUNSUPPORTED, "precision mode %d is not available", mode);
         return;
     }
@@ -2121,6 +2311,17 @@ void IBMSolver_get_field(IBMSolver *s, int field, double *out) {
     const size_t n = g.ncell;
     const double *src = nullptr;
     int face = -1;
+    if (step32(d)) {
+        // The FP32 step keeps N in FP32 and u* as u^n + e (u^n is in the
+        // second buffer after the step): both are formed in their FP64
+        // arrays for read-back.
+        if (field >= IBM3D_F_N1 && field <= IBM3D_F_N3)
+            launch_widen_f32(d->s, (long long)n, d->Np32[field - IBM3D_F_N1], d->Np[field - IBM3D_F_N1]);
+        if (field >= IBM3D_F_USTAR1 && field <= IBM3D_F_USTAR3) {
+            const int l = field - IBM3D_F_USTAR1;
+            launch_ustar_from_increment(d->s, (long long)n, d->un[l], d->irmom.e32 + l * n, d->ustar + l * n);
+        }
+    }
     switch (field) {
     case IBM3D_F_U1: src = d->u[0]; break;
     case IBM3D_F_U2: src = d->u[1]; break;
@@ -2229,6 +2430,11 @@ void IBMSolver_get_stats(const IBMSolver *s, IBMSolverStats *out) {
     out->outer_u = d->rep_mom.outer;
     out->outer_p = d->rep_p.outer;
     out->cpt_fallback = d->cpt_fallback;
+    out->steps_total = d->steps_total;
+    for (int l = 0; l < 3; l++) out->iters_u_total[l] = d->iters_u_total[l];
+    out->iters_p_total = d->iters_p_total;
+    out->outer_p_total = d->outer_p_total;
+    out->max_div_max = d->max_div_max;
 }
 
 double IBMSolver_time_iterate(IBMSolver *s, int nsteps) {
@@ -2265,7 +2471,7 @@ double IBMSolver_autotune(IBMSolver *s, int steps, int *best_out) {
     const int ncand = (int)(sizeof cand / sizeof cand[0]);
     const size_t n = (size_t)d->g.ncell;
     double *save = nullptr;
-    if (!cuda_check(s, cudaMalloc(&save, sizeof(double) * n * kStateFields), "autotune state")) return -1;
+    if (!cuda_check(s, cudaMalloc(&save, sizeof(double) * (n * kStateFields + 1)), "autotune state")) return -1;
     // By role (the steps swap the buffers behind the roles).
     auto copy_state = [&](bool out) {
         double *fld[kStateFields];
@@ -2273,6 +2479,9 @@ double IBMSolver_autotune(IBMSolver *s, int steps, int *best_out) {
         for (int q = 0; q < kStateFields; q++)
             cudaMemcpyAsync(out ? save + q * n : fld[q], out ? fld[q] : save + q * n, sizeof(double) * n,
                             cudaMemcpyDeviceToDevice, d->s);
+        int *hist_save = (int *)(save + n * kStateFields);
+        cudaMemcpyAsync(out ? hist_save : d->pp_hist, out ? d->pp_hist : hist_save, sizeof(int),
+                        cudaMemcpyDeviceToDevice, d->s);
     };
     copy_state(true);
     const int iter0 = s->iter;
@@ -2315,40 +2524,89 @@ double IBMSolver_autotune(IBMSolver *s, int steps, int *best_out) {
 double IBMSolver_time_kernel(IBMSolver *s, int which, int reps, double *bytes) {
     if (!check_ready(s, "IBMSolver_time_kernel")) return -1;
     ibm3d_device *d = s->dev;
+    const bool cold = (which & IBM3D_K_COLD) != 0;
+    which &= ~IBM3D_K_COLD;
     const bool mixed = d->precision != IBM3D_FP64;   // FP32 multigrid
+    const bool f32 = step32(d);
+    const double ncell = (double)d->g.ncell, nint = (double)d->g.nx * d->g.ny * d->g.nz;
     double b = 0;
-    double ms = -1;
-    cudaStreamSynchronize(d->s);
-    if (which == IBM3D_K_MG_COLOR) {
+    std::function<void()> launch;
+    switch (which) {
+    case IBM3D_K_MG_COLOR:
         // Scratch vectors of the pressure solve of the current precision.
-        ms = mixed ? d->mg32->time_color(d->s, d->irpres.inner.r, d->irpres.inner.s, reps, &b)
-                   : d->mg->time_color(d->s, d->kpres.r, d->kpres.s, reps, &b);
-    } else if (which == IBM3D_K_SPMV_P) {
-        cudaEvent_t e0, e1;
-        cudaEventCreate(&e0);
-        cudaEventCreate(&e1);
-        cudaEventRecord(e0, d->s);
-        for (int q = 0; q < reps; q++) {
+        launch = [&]() {
+            double bb;
+            if (mixed) d->mg32->time_color(d->s, d->irpres.inner.r, d->irpres.inner.s, 1, &bb, false);
+            else d->mg->time_color(d->s, d->kpres.r, d->kpres.s, 1, &bb, false);
+            b = bb;
+        };
+        break;
+    case IBM3D_K_SPMV_P:
+        launch = [&]() {
             if (pres_ir(s)) apply_operator<float>(d->s, d->A32, OP_PRES, 0, d->irpres.inner.r, d->irpres.inner.s);
             else apply_operator<double>(d->s, d->A64, OP_PRES, 0, d->kpres.r, d->kpres.s);
+        };
+        b = ncell * (3 * (pres_ir(s) ? 4.0 : 8.0) + 1);
+        break;
+    case IBM3D_K_CONV_RHS:
+        // Reads u, U (3 each), p, N_prev (3), flag; writes N (3), b (3).
+        launch = [&]() { stage_rhs(s); };
+        b = ncell * (f32 ? 7 * 8.0 + 3 * 4.0 + 1 + 6 * 4.0 : 10 * 8.0 + 1 + 6 * 8.0);
+        break;
+    case IBM3D_K_USTAR_PRHS:
+        // Reads u* (or u^n and the FP32 increment), p, flag; writes U* (3), b.
+        launch = [&]() { stage_ustar(s); };
+        b = ncell * (f32 ? 3 * 8.0 + 3 * 4.0 + 8 + 1 + 8 + 4 * 8.0 : 4 * 8.0 + 1 + 4 * 8.0);
+        break;
+    case IBM3D_K_UPDATE_NEXT:
+        // Reads u* (or u^n and the increment), U* (3), p, p', flag; writes u, U (3 each), p.
+        launch = [&]() { stage_next(s); };
+        b = nint * (f32 ? 3 * 8.0 + 3 * 4.0 + 3 * 8.0 + 16 + 1 + 7 * 8.0 : 8 * 8.0 + 1 + 7 * 8.0);
+        break;
+    default:
+        set_status(s, IBM3D_EARG, "IBMSolver_time_kernel: unknown kernel %d", which);
+        return -1;
+    }
+    const bool prof_on = d->prof.on;
+    d->prof.on = false;
+    cudaStreamSynchronize(d->s);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    void *flush = nullptr;
+    const size_t flush_bytes = (size_t)256 << 20;   // twice the 129 MB L2
+    if (cold && cudaMalloc(&flush, flush_bytes) != cudaSuccess) flush = nullptr;
+    double total = 0;
+    if (cold && flush) {
+        for (int q = 0; q < reps; q++) {
+            cudaMemsetAsync(flush, q & 0xff, flush_bytes, d->s);
+            cudaEventRecord(e0, d->s);
+            launch();
+            cudaEventRecord(e1, d->s);
+            cudaEventSynchronize(e1);
+            float t = 0;
+            cudaEventElapsedTime(&t, e0, e1);
+            total += t;
         }
+    } else {
+        cudaEventRecord(e0, d->s);
+        for (int q = 0; q < reps; q++) launch();
         cudaEventRecord(e1, d->s);
         cudaEventSynchronize(e1);
         float t = 0;
         cudaEventElapsedTime(&t, e0, e1);
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
-        ms = reps > 0 ? t / reps : 0;
-        const double w = pres_ir(s) ? 4.0 : 8.0;
-        b = (double)d->g.ncell * (3 * w + 1);
-    } else {
-        set_status(s, IBM3D_EARG, "IBMSolver_time_kernel: unknown kernel %d", which);
-        return -1;
+        total = t;
     }
+    d->prof.on = prof_on;
+    if (flush) cudaFree(flush);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
     if (bytes) *bytes = b;
     if (!cuda_check(s, cudaGetLastError(), "IBMSolver_time_kernel")) return -1;
-    return ms;
+    return reps > 0 ? total / reps : 0;
 }
+
+double IBMSolver_measure_fma_rate(int which) { return ibm::fma_rate(which == 0 ? 0 : 1); }
 
 void IBMSolver_set_profiling(IBMSolver *s, int on) {
     s->dev->prof.reset();
@@ -2370,6 +2628,11 @@ int IBMSolver_get_profile(IBMSolver *s, int max, char names[][32], int *launches
 }
 
 long long IBMSolver_kernel_launches(void) { return ibm::g_launches.load(); }
+
+int IBMSolver_check_fp32_conversions(long long n, const double *values, unsigned long long *mismatches) {
+    if (n <= 0 || !values || !mismatches) return -1;
+    return ibm::conversion_check(n, values, mismatches);
+}
 
 int IBMSolver_host_register(void *ptr, size_t bytes) {
     return cudaHostRegister(ptr, bytes, cudaHostRegisterDefault) == cudaSuccess ? 0 : -1;
@@ -2593,6 +2856,7 @@ double IBMBatch_iterate(IBMBatch *b, int nsteps) {
                 b->next_iter[q] = m->iter;
                 m->time = b->run_start[q] + m->dt * b->run_steps[q];
                 m->dev->max_div = *m->dev->maxdiv_h;
+                account_step(m->dev);
                 if (m->dev->status != IBM3D_OK && m->dev->status != IBM3D_ENOCONV) b->status = m->dev->status;
             }
             continue;
@@ -2630,6 +2894,7 @@ double IBMBatch_iterate(IBMBatch *b, int nsteps) {
             b->next_iter[q] = m->iter;
             m->time = b->run_start[q] + m->dt * b->run_steps[q];
             m->dev->max_div = *m->dev->maxdiv_h;
+            account_step(m->dev);
             if (m->dev->status != IBM3D_OK && m->dev->status != IBM3D_ENOCONV) b->status = m->dev->status;
         }
     }

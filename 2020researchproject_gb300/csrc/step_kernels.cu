@@ -293,7 +293,7 @@ k_update_next(const Grid g, const Axis ax, const Axis ay, const Axis az, const B
         if (k == g.nz - 1) a.Un[2][P + 1] = Wu;
         if (fc == FLUID && !(bc.p_singular && i == 0 && j == 0 && k == 0)) {
             const double div = (Ue - Uw) * ax.rd[I] + (Vn - Vs) * ay.rd[J] + (Wu - Wd) * az.rd[K];
-            mdiv[0] = fmax(mdiv[0], fabs(div));
+            mdiv[0] = nanmax(mdiv[0], fabs(div));
         }
     }
     block_max<1>(mdiv, smem);
@@ -626,6 +626,82 @@ void launch_export_fields(cudaStream_t s, const Grid &g, const Axis &ax, const A
     const long long blocks = std::min<long long>((plane + 255) / 256, 152LL * 64);
     k_export_vort_q<<<(unsigned)blocks, 256, 0, s>>>(g, ax.c, ay.c, az.c, out);
     note_launches(2);
+}
+
+// ------------------------------------------------------------------------
+// Initial guess of a warm-started pressure solve: with two earlier
+// increments, the linear extrapolation 2 p'_{n-1} - p'_{n-2}; otherwise the
+// last increment as it stands.  prev receives p'_{n-1}.  The history count
+// is read here and advanced by k_pressure_history after this launch.
+// ------------------------------------------------------------------------
+__global__ void __launch_bounds__(256)
+k_pressure_guess(const long long n, double *__restrict__ pp, double *__restrict__ prev, const int *hist) {
+    const bool extrapolate = *hist >= 2;
+    for (long long P = blockIdx.x * (long long)blockDim.x + threadIdx.x; P < n;
+         P += (long long)gridDim.x * blockDim.x) {
+        const double a = pp[P];
+        if (extrapolate) pp[P] = 2 * a - prev[P];
+        prev[P] = a;
+    }
+}
+
+__global__ void k_pressure_history(int *hist) {
+    if (*hist < 2) *hist += 1;
+}
+
+void launch_pressure_guess(cudaStream_t s, long long n, double *pp, double *prev, int *hist) {
+    k_pressure_guess<<<grid_for(n, 256 * 8), 256, 0, s>>>(n, pp, prev, hist);
+    k_pressure_history<<<1, 1, 0, s>>>(hist);
+    note_launches(2);
+}
+
+// ------------------------------------------------------------------------
+// FMA throughput: 8 independent register chains per thread, no memory
+// traffic but one store per thread.
+// ------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) k_fma_rate(T *out, const T a, const T b, const int iters) {
+    T x[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) x[q] = (T)(threadIdx.x * 1e-3 + q);
+    for (int it = 0; it < iters; it++) {
+#pragma unroll
+        for (int q = 0; q < 8; q++) x[q] = x[q] * a + b;
+    }
+    T s = 0;
+#pragma unroll
+    for (int q = 0; q < 8; q++) s += x[q];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+double fma_rate(int which) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int blocks = 8 * (sms > 0 ? sms : 1), threads = 256;
+    const int iters = which == 0 ? 1024 : 65536;
+    void *out = nullptr;
+    if (cudaMalloc(&out, sizeof(double) * blocks * threads) != cudaSuccess) return -1;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    for (int rep = 0; rep < 3; rep++) {
+        cudaEventRecord(e0);
+        if (which == 0) k_fma_rate<double><<<blocks, threads>>>((double *)out, 0.999, 1e-3, iters);
+        else k_fma_rate<float><<<blocks, threads>>>((float *)out, 0.999f, 1e-3f, iters);
+        cudaEventRecord(e1);
+        cudaEventSynchronize(e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best) best = ms;
+    }
+    note_launches(3);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    if (cudaGetLastError() != cudaSuccess) return -1;
+    return 2.0 * 8.0 * iters * (double)blocks * threads / (best * 1e-3) / 1e12;
 }
 
 }  // namespace ibm

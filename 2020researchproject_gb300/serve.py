@@ -106,7 +106,8 @@ class Server:
         # re-recorded when jobs arrive or finish); True: one graph per
         # batched step, re-recorded on every membership change.
         self.combined = combined
-        self.mode = {"mixed": ibm.MIXED, "mixed_mg": ibm.MIXED_MG}.get(precision, ibm.FP64)
+        self.mode = {"mixed": ibm.MIXED, "mixed_mg": ibm.MIXED_MG, "mixed32": ibm.MIXED32,
+                     "mixed32_ir": ibm.MIXED32_IR}.get(precision, ibm.FP64)
         self.tol, self.div_tol = tol, div_tol
         self.hbm_budget = hbm_budget
         self.bytes_per_cell = bytes_per_cell

@@ -232,26 +232,29 @@ def _profiler_range(on):
 
 def _timed_arm(ibm, wl, case, precision, args, world, u0, headline=False):
     """Builds a solver for `case`, runs W warm-up steps and times K steps on
-    the device (CUDA events on the solver's stream), sampling clocks."""
+    the device (CUDA events on the solver's stream), sampling clocks.  The
+    solver's iteration totals before and after the timed region give the
+    mean Krylov iterations per timed step."""
     t0 = time.perf_counter()
     s = wl.build_solver(ibm, case, tol=MOM_TOL, div_tol=DIV_TOL)
-    s.set_precision(ibm.MIXED if precision == "mixed" else ibm.FP64)
+    s.set_precision(ibm.MIXED32 if precision == "mixed" else ibm.FP64)
     if args.host_loop:
         s.set_graphs(False)
     setup_s = time.perf_counter() - t0
     s.init_flow_array(*u0)
     tuned = None
-    if args.no_tune and precision == "mixed" and args.mixed_form == "MIXED_MG":
-        s.set_precision(ibm.MIXED_MG)
+    if args.no_tune and precision == "mixed":
+        s.set_precision(getattr(ibm, args.mixed_form))
     if args.no_tune and args.mg_sweeps:
         s.set_multigrid(*[int(v) for v in args.mg_sweeps.split(",")], 1.0)
     if not args.no_tune:
         # The autotuner picks the multigrid sweeps (and, for the mixed step,
-        # which of the two mixed solver forms) from the state after three
+        # which of the mixed solver forms) from the state after three
         # steps (past the start-up transient, whose harder solves favour
         # other settings); the state is restored, and warm-up follows.
         s.iterate(3)
-        modes = [("MIXED", ibm.MIXED), ("MIXED_MG", ibm.MIXED_MG)] if precision == "mixed" else [("FP64", ibm.FP64)]
+        modes = ([("MIXED", ibm.MIXED), ("MIXED_MG", ibm.MIXED_MG), ("MIXED32", ibm.MIXED32)]
+                 if precision == "mixed" else [("FP64", ibm.FP64)])
         trials = []
         for name, mode in modes:
             s.set_precision(mode)
@@ -265,6 +268,7 @@ def _timed_arm(ibm, wl, case, precision, args, world, u0, headline=False):
     s.iterate(args.warmup)
     _barrier(world)
     l0 = ibm.kernel_launches()
+    st0 = s.stats()
     gpu = 0 if world > 1 else int(os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0] or 0)
     with ClockSampler(gpu) as clk:
         if headline:
@@ -273,8 +277,13 @@ def _timed_arm(ibm, wl, case, precision, args, world, u0, headline=False):
         if headline:
             _profiler_range(False)
     launches = ibm.kernel_launches() - l0
+    st = s.stats()
+    n = max(1, st["steps_total"] - st0["steps_total"])
+    iters = {"k_u": sum(st["iters_u_total"][l] - st0["iters_u_total"][l] for l in range(3)) / (3.0 * n),
+             "k_p": (st["iters_p_total"] - st0["iters_p_total"]) / n,
+             "max_div_over_timed_steps": st["max_div_max"]}
     ms = _barrier_max(ms, world)
-    return {"solver": s, "ms": ms, "launches": launches, "launches_before": l0, "stats": s.stats(),
+    return {"solver": s, "ms": ms, "launches": launches, "launches_before": l0, "stats": st, "iters": iters,
             "clocks": clk.summary(), "setup_s": setup_s, "tuned": tuned}
 
 
@@ -289,6 +298,90 @@ def _vel_rel_l2(a, b):
     return (num / den) ** 0.5 if den > 0 else 0.0
 
 
+def step_roofline(ms_per_step, cells, k_u, k_p, mixed, les, peak):
+    """Step-level roofline from the algorithmic-bytes model of the step:
+    B_step = 336 + 3 k_u 144 + k_p B_pois (+ 104 with LES) bytes per cell,
+    B_pois = 492 with the FP64 multigrid, 318 with the FP32 one, with k_u
+    and k_p the measured Krylov iterations per step (momentum per
+    component, pressure)."""
+    b_pois = 318.0 if mixed else 492.0
+    b_step = 336.0 + 3 * k_u * 144.0 + k_p * b_pois + (104.0 if les else 0.0)
+    ach = b_step * cells / (ms_per_step / 1e3) / 1e9
+    return {"B_step": round(b_step, 1), "k_u": round(k_u, 2), "k_p": round(k_p, 2), "achieved": round(ach, 1),
+            "peak": peak, "unit": "GB/s", "frac": round(ach / peak, 4)}
+
+
+def e2e_loop(ibm, s, steps, world):
+    """The metric end to end through the C ABI with pinned host buffers:
+    per step, upload u1, u2, u3, p (IBMSolver_init_flow_array), one
+    IBMSolver_iterate(1), read the four fields back (IBMSolver_get_field)."""
+    fields = ["u1", "u2", "u3", "p"]
+    host = [s.get_field(f) for f in fields]
+    outs = [np.empty_like(h) for h in host]
+    pinned = all(ibm.pin(a) for a in host + outs)
+    _barrier(world)
+    t1 = time.perf_counter()
+    for _ in range(steps):
+        s.init_flow_array(*host)
+        s.iterate(1)
+        for q, f in enumerate(fields):
+            s.get_field_into(f, outs[q])
+        host, outs = outs, host
+    secs = _barrier_max(time.perf_counter() - t1, world)
+    for a in host + outs:
+        ibm.unpin(a)
+    return secs, 4 * host[0].nbytes, pinned
+
+
+def fp64_ops_per_launch(kernel):
+    """FP64 operations per launch (FMA = 2) of `kernel` from the committed
+    ncu summary (profiles/fp64_ops.txt: '<kernel> <workload> <ops>'), or
+    None."""
+    path = os.path.join(ROOT, "profiles", "fp64_ops.txt")
+    try:
+        for line in open(path):
+            t = line.split()
+            if len(t) >= 3 and not line.startswith("#") and t[0] == kernel:
+                return float(t[2])
+    except OSError:
+        pass
+    return None
+
+
+def error_vs_oracle(ibm, wl, case, u0, lvset, mixed_mode, steps=3):
+    """Velocity and pressure error of the GPU steps against the CPU oracle
+    (the restatement of the reference step, OpenMP on the host cores) from
+    the same initial state after `steps` steps: the oracle and the FP64 step
+    both solve to 1e-12; the mixed step and the FP64 step also at the
+    benchmark's tolerances (momentum 1e-6, max|div U| <= 1e-8)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+    t0 = time.perf_counter()
+    o = orc.Oracle(oracle_case(case, lvset, os.cpu_count() or 1, div_tol=0.0, tol=1e-12))
+    o.init(*u0)
+    o.iterate(steps)
+    ref_u = [o.get(f) for f in ("u1", "u2", "u3")]
+    ref_p = o.get("p")
+    oracle_s = time.perf_counter() - t0
+    out = {"steps": steps, "oracle_tol": 1e-12, "oracle_seconds": round(oracle_s, 1)}
+
+    def run(mode, tol, div_tol):
+        sv = wl.build_solver(ibm, case, tol=tol, div_tol=div_tol)
+        sv.set_precision(mode)
+        sv.init_flow_array(*u0)
+        sv.iterate(steps)
+        e = {"velocity_rel_l2": _vel_rel_l2([sv.get_field(f) for f in ("u1", "u2", "u3")], ref_u),
+             "pressure_rel_l2": _vel_rel_l2([sv.get_field("p")], [ref_p]),
+             "max_div": sv.stats()["max_div_max"]}
+        sv.close()
+        return e
+
+    out["fp64_tol_1e-12"] = run(ibm.FP64, 1e-12, 0.0)
+    out["fp64_benchmark_tol"] = run(ibm.FP64, MOM_TOL, DIV_TOL)
+    out["mixed_benchmark_tol"] = run(mixed_mode, MOM_TOL, DIV_TOL)
+    return out
+
+
 def bench_gb300(args):
     world, rank, local = _dist()
     if world > 1:
@@ -299,6 +392,7 @@ def bench_gb300(args):
     ncell = (len(case["xf"]) - 1) * (len(case["yf"]) - 1) * (len(case["zf"]) - 1)
     u0 = wl.initial_state(case)
     other = "fp64" if args.precision == "mixed" else "mixed"
+    peak, peak_src = measured_peak_gbs()
 
     # --- device-timed region of the headline arm, then of the other arm
     # (same workload, same initial state, same step count).
@@ -321,7 +415,12 @@ def bench_gb300(args):
     vel2 = [sec["solver"].get_field(f) for f in ("u1", "u2", "u3")]
     mixed_arm, fp64_arm = (head, sec) if args.precision == "mixed" else (sec, head)
     err = _vel_rel_l2(vel, vel2)
-    del sec["solver"]
+    mixed_mode = getattr(ibm, (mixed_arm["tuned"] or {}).get("mode", args.mixed_form))
+
+    # --- step-level roofline of both arms (measured iterations per step).
+    roof_step = {a: step_roofline(arm["ms"] / args.steps, ncell, arm["iters"]["k_u"], arm["iters"]["k_p"],
+                                  a == "mixed", False, peak)
+                 for a, arm in (("mixed", mixed_arm), ("fp64", fp64_arm))}
 
     # --- stage profile (host-sequenced step, CUDA events per stage).
     s.set_profiling(True)
@@ -330,35 +429,49 @@ def bench_gb300(args):
     s.set_profiling(False)
 
     # --- roofline of the dominant kernel: the fine-grid colour pass of the
-    # pressure multigrid (FP32 in the mixed step, FP64 in the plain one).
-    peak, peak_src = measured_peak_gbs()
+    # pressure multigrid (FP32 in the mixed step, FP64 in the plain one),
+    # back to back (as inside a V-cycle, L2-warm) and with the L2
+    # overwritten before each launch (cold).
     k_ms, k_bytes = s.time_kernel("mg_color", reps=50)
-    ach = k_bytes / (k_ms / 1e3) / 1e9
+    kc_ms, _ = s.time_kernel("mg_color", reps=20, cold=True)
     kname = "k_mg0_color_f32" if args.precision == "mixed" else "k_mg0_color_f64"
+    ach_cold = k_bytes / (kc_ms / 1e3) / 1e9
     roof = {"bound": "hbm", "kernel": f"{kname} (fine-grid Gauss-Seidel colour pass, pressure multigrid)",
-            "achieved": round(ach, 1), "peak": peak, "unit": "GB/s", "frac": round(ach / peak, 4),
-            "peak_source": peak_src, "traffic": traffic_per_launch(kname),
-            "bytes_per_launch": k_bytes, "avg_launch_us": round(k_ms * 1e3, 2)}
+            "achieved": round(ach_cold, 1), "peak": peak, "unit": "GB/s", "frac": round(ach_cold / peak, 4),
+            "peak_source": peak_src, "traffic": traffic_per_launch(kname), "bytes_per_launch": k_bytes,
+            "avg_launch_us": round(kc_ms * 1e3, 2), "timing": "cold L2 (256 MB written before each launch)",
+            "warm": {"avg_launch_us": round(k_ms * 1e3, 2), "achieved": round(k_bytes / (k_ms / 1e3) / 1e9, 1),
+                     "frac": round(k_bytes / (k_ms / 1e3) / 1e9 / peak, 4),
+                     "timing": "back-to-back launches, L2-resident as inside a V-cycle"},
+            "step": roof_step[args.precision]}
     sp_ms, sp_bytes = s.time_kernel("spmv_p", reps=50)
     spmv = {"achieved_gbs": round(sp_bytes / (sp_ms / 1e3) / 1e9, 1), "avg_launch_us": round(sp_ms * 1e3, 2),
             "bytes_per_launch": sp_bytes}
 
-    # --- end to end through the C ABI with pinned host buffers.
-    fields = ["u1", "u2", "u3", "p"]
-    host = [s.get_field(f) for f in fields]
-    outs = [np.empty_like(h) for h in host]
-    pinned = all(ibm.pin(a) for a in host + outs)
-    _barrier(world)
-    t1 = time.perf_counter()
-    for _ in range(args.steps):
-        s.init_flow_array(*host)
-        s.iterate(1)
-        for q, f in enumerate(fields):
-            s.get_field_into(f, outs[q])
-        host, outs = outs, host
-    e2e_s = _barrier_max(time.perf_counter() - t1, world)
+    # --- explicit stages of both arms: HBM fraction, and against the
+    # measured FP64 FMA rate where the FP64 pipe bounds them.
+    fp64_tf = ibm.measure_fma_rate(fp64=True)
+    fp32_tf = ibm.measure_fma_rate(fp64=False)
+    explicit = {}
+    for a, arm in (("mixed", mixed_arm), ("fp64", fp64_arm)):
+        sv = arm["solver"]
+        ks = {}
+        for kn in ("conv_rhs", "ustar_prhs", "update_next"):
+            t_ms, t_b = sv.time_kernel(kn, reps=10, cold=True)
+            e = {"avg_launch_us": round(t_ms * 1e3, 1), "bytes_per_launch": t_b,
+                 "hbm_frac": round(t_b / (t_ms / 1e3) / 1e9 / peak, 4)}
+            ops = fp64_ops_per_launch(("k_" + kn + ("32" if a == "mixed" else "")))
+            if ops is not None:
+                e["fp64_tflops"] = round(ops / (t_ms / 1e3) / 1e12, 3)
+                e["fp64_frac"] = round(ops / (t_ms / 1e3) / 1e12 / fp64_tf, 4)
+            ks[kn] = e
+        explicit[a] = ks
+
+    # --- end to end through the C ABI with pinned host buffers, both arms.
+    e2e_s, bytes_io, pinned = e2e_loop(ibm, s, args.steps, world)
     e2e = world * ncell * args.steps / e2e_s / 1e6
-    bytes_io = 4 * host[0].nbytes
+    e2e2_s, _, _ = e2e_loop(ibm, sec["solver"], args.steps, world)
+    e2e2 = world * ncell * args.steps / e2e2_s / 1e6
 
     st = head["stats"]
     line = {
@@ -380,20 +493,32 @@ def bench_gb300(args):
         "launches_before_timed": int(head["launches_before"]),
         "clocks": head["clocks"],
         other: {"value": round(value2, 3), "ms_per_step": round(sec["ms"] / args.steps, 3),
-                "iters_p": sec["stats"]["iters_p"], "max_div": sec["stats"]["max_div"], "autotuned": sec["tuned"],
-                "gpu_launches": int(sec["launches"]), "clocks": sec["clocks"]},
+                "iters_p": sec["stats"]["iters_p"], "iters_u": sec["stats"]["iters_u"],
+                "iters_per_step": sec["iters"], "max_div": sec["stats"]["max_div"], "autotuned": sec["tuned"],
+                "gpu_launches": int(sec["launches"]), "clocks": sec["clocks"],
+                "e2e": {"value": round(e2e2, 3), "unit": "Mcell-steps/s", "h2d_bytes_per_step": bytes_io,
+                        "d2h_bytes_per_step": bytes_io},
+                "roofline_step": roof_step[other]},
         "mixed_vs_fp64": round((mixed_arm["ms"] and fp64_arm["ms"] / mixed_arm["ms"]) or 0, 3),
         "error_vs_fp64": {"velocity_rel_l2": err, "max_div_mixed": mixed_arm["stats"]["max_div"],
                           "max_div_fp64": fp64_arm["stats"]["max_div"],
                           "note": f"after {args.warmup + args.steps} steps from the same state"},
         "solver": {"iters_p": st["iters_p"], "iters_u": st["iters_u"], "outer_p": st["outer_p"],
-                   "max_div": st["max_div"], "mg_levels": st["mg_levels"]},
+                   "iters_per_step": head["iters"], "max_div": st["max_div"], "mg_levels": st["mg_levels"]},
+        "fma_rate_tflops": {"fp64": round(fp64_tf, 3), "fp32": round(fp32_tf, 2),
+                            "how": "register-only FMA chains, 8 blocks of 256 per SM, best of 3"},
+        "explicit_kernels": explicit,
         "profile_ms": {k: [v[0], round(v[1], 3)] for k, v in sorted(prof.items())},
     }
     lv = s.get_field("lvset")
     s.close()
     head["solver"] = None
+    sec["solver"].close()
+    sec["solver"] = None
+    if rank == 0 and world == 1 and not args.no_oracle:
+        line["error_vs_oracle"] = error_vs_oracle(ibm, wl, case, u0, lv, mixed_mode)
     if rank == 0 and world == 1 and not args.no_extras:
+        line["configs"] = configs_arm(ibm, wl, args)
         line["ensemble"] = ensemble_arm(ibm, wl, args)
         line["serving"] = serving_arm(ibm, wl, args)
         line["large_body_setup"] = large_body_arm(ibm, wl)
@@ -408,11 +533,55 @@ def bench_gb300(args):
     return 0
 
 
-def ensemble_arm(ibm, wl, args, steps=5):
-    """Batched ensemble (64 seeded immersed-body cases of uneven size): the
-    mixed-precision batched step (one CUDA graph launch per step for all
-    cases) against the plain FP64 step run case by case, and the FP64
-    batched step."""
+def configs_arm(ibm, wl, args):
+    """The other single-case configurations at their sizes, mixed (the
+    FP32-stage step) and plain FP64: the 64^3 lid-driven cavity (200 steps
+    from rest, Re 1000, dt 1e-3; its velocity error against the reference's
+    own 200-step run solved to 1e-12, tests/golden/configs/c1_cavity64.npz)
+    and the 128x96x128 channel LES (a 50-step sample of its 2000-step run,
+    after 3 warm-up steps)."""
+    out = {}
+    ref = np.load(os.path.join(ROOT, "tests", "golden", "configs", "c1_cavity64.npz"))
+    c1 = wl.cavity(64, 1000.0, 1e-3)
+    cells = 64 ** 3
+    r = {"workload": "cavity64 (Re 1000, dt 1e-3, lid u = 1)", "cells": cells, "steps": 200}
+    for name, mode in (("mixed", ibm.MIXED32), ("fp64", ibm.FP64)):
+        sv = wl.build_solver(ibm, c1, tol=MOM_TOL, div_tol=DIV_TOL)
+        sv.set_precision(mode)
+        sv.init_flow_array(*wl.initial_state(c1))
+        sv.iterate(3)                                   # records the step graphs
+        sv.init_flow_array(*wl.initial_state(c1))       # from rest again
+        ms = sv.time_iterate(200)
+        r[name] = round(cells * 200 / ms / 1e3, 3)
+        r[name + "_error_vs_reference"] = _vel_rel_l2([sv.get_field(f) for f in ("u1", "u2", "u3")],
+                                                      [ref[f] for f in ("u1", "u2", "u3")])
+        r[name + "_max_div"] = sv.stats()["max_div_max"]
+        sv.close()
+    r["mixed_vs_fp64"] = round(r["mixed"] / r["fp64"], 3)
+    out["cavity64"] = r
+    c3 = wl.channel()
+    cells = 128 * 96 * 128
+    r = {"workload": "channel128x96x128 LES (Re_tau 180, Cs 0.1, dt 2e-3)", "cells": cells, "steps": 50,
+         "sample": "50 of the 2000 steps, after 3 warm-up steps"}
+    for name, mode in (("mixed", ibm.MIXED32), ("fp64", ibm.FP64)):
+        sv = wl.build_solver(ibm, c3, tol=MOM_TOL, div_tol=DIV_TOL)
+        sv.set_precision(mode)
+        sv.init_flow_array(*wl.initial_state(c3))
+        sv.iterate(3)
+        ms = sv.time_iterate(50)
+        r[name] = round(cells * 50 / ms / 1e3, 3)
+        r[name + "_max_div"] = sv.stats()["max_div_max"]
+        sv.close()
+    r["mixed_vs_fp64"] = round(r["mixed"] / r["fp64"], 3)
+    out["channel128x96x128"] = r
+    return out
+
+
+def ensemble_arm(ibm, wl, args, steps=300, alone_steps=30):
+    """Batched ensemble (64 seeded immersed-body cases of uneven size, 300
+    steps each): the mixed-precision batched step (one CUDA graph launch
+    per step for all cases) and the FP64 batched step, against the plain
+    FP64 step run case by case (rate from a 30-step sample of each case)."""
     cases = wl.ensemble()
     cells = sum((len(c["xf"]) - 1) * (len(c["yf"]) - 1) * (len(c["zf"]) - 1) for c in cases)
     out = {"cases": len(cases), "cells": cells, "steps": steps, "unit": "Mcell-steps/s",
@@ -421,24 +590,27 @@ def ensemble_arm(ibm, wl, args, steps=5):
         solvers = []
         for c in cases:
             sv = wl.build_solver(ibm, c, tol=MOM_TOL, div_tol=DIV_TOL)
-            # mixed: the FP64-Krylov / FP32-multigrid form (faster than the
-            # refinement form on these cases: 82 against 76 Mcell-steps/s)
-            sv.set_precision(ibm.MIXED_MG if mode == "mixed" else ibm.FP64)
+            sv.set_precision(ibm.MIXED32 if mode == "mixed" else ibm.FP64)
             sv.init_flow_array(*wl.initial_state(c))
             solvers.append(sv)
         b = ibm.Batch(solvers)
         b.iterate(1)
-        ms = b.iterate(steps)
-        out[f"{mode}_batched"] = round(cells * steps / ms / 1e3, 3)
-        out[f"{mode}_batched_ms_per_step"] = round(ms / steps, 2)
-        out[f"{mode}_max_div"] = max(sv.stats()["max_div"] for sv in solvers)
+        ms = b.iterate(steps - 1)
+        out[f"{mode}_batched"] = round(cells * (steps - 1) / ms / 1e3, 3)
+        out[f"{mode}_batched_ms_per_step"] = round(ms / (steps - 1), 2)
+        out[f"{mode}_max_div"] = max(sv.stats()["max_div_max"] for sv in solvers)
         if mode == "fp64":
-            seq = sum(sv.time_iterate(steps) for sv in solvers)
-            out["fp64_alone"] = round(cells * steps / seq / 1e3, 3)
+            seq = 0.0
+            for sv, c in zip(solvers, cases):
+                sv.init_flow_array(*wl.initial_state(c))
+                seq += sv.time_iterate(alone_steps)
+            out["fp64_alone"] = round(cells * alone_steps / seq / 1e3, 3)
+            out["fp64_alone_sample"] = f"{alone_steps} steps of each case from its initial state"
         del b
         for sv in solvers:
             sv.close()
     out["mixed_batched_vs_fp64_alone"] = round(out["mixed_batched"] / out["fp64_alone"], 3)
+    out["mixed_batched_vs_fp64_batched"] = round(out["mixed_batched"] / out["fp64_batched"], 3)
     return out
 
 
@@ -462,31 +634,34 @@ def large_body_arm(ibm, wl):
     return out
 
 
-def serving_arm(ibm, wl, args, njobs=32, steps=(100, 300)):
-    """Continuous-batching server on seeded Poisson arrivals (20 jobs/s):
-    cavity / sphere / box-cluster jobs, grids 32^3 to 96x64x64, 100-300
-    steps (the low end of the 100-1000 of the served stream, so that the
-    run ends in seconds while the GPU, not the arrival process, bounds the
-    throughput), mixed precision (FP64 Krylov, FP32 multigrid); p50/p99 job
-    latency and aggregate throughput, against the same jobs run one by one
-    on the plain FP64 step."""
+def serving_arm(ibm, wl, args, njobs=12, alone_steps=10):
+    """Continuous-batching server on the served stream's distribution:
+    seeded Poisson arrivals at 20 jobs/s of cavity / sphere / box-cluster
+    jobs, grids from 32^3 up to 256x128x128, Re 100-1000, 100-1000 steps (a
+    seeded sample of `njobs` jobs of that stream), mixed precision (the
+    FP32-stage step); p50/p99 job latency and aggregate throughput, against
+    the same jobs run one by one on the plain FP64 step (device time of a
+    10-step sample of each job, scaled to its step count)."""
     serve = importlib.import_module("2020researchproject_gb300.serve")
-    jobs = serve.poisson_jobs(njobs=njobs, steps=steps)
-    res = serve.Server(ibm, precision="mixed_mg").run(jobs)
+    jobs = serve.poisson_jobs(njobs=njobs, grid_max=(256, 128, 128), steps=(100, 1000))
+    res = serve.Server(ibm, precision="mixed32").run(jobs)
     dev_ms = 0.0
     for j in jobs:
         sv = wl.build_solver(ibm, j.case, tol=MOM_TOL, div_tol=DIV_TOL)
         sv.set_precision(ibm.FP64)
         sv.init_flow_array(*wl.initial_state(j.case))
-        dev_ms += sv.time_iterate(j.steps)
+        sv.iterate(2)
+        dev_ms += sv.time_iterate(alone_steps) * j.steps / alone_steps
         sv.close()
     alone = res["cell_steps"] / dev_ms / 1e3
     return {"jobs": njobs, "arrival_rate_per_s": 20.0,
-            "workload": f"cavity/sphere/box jobs, grids 32^3..96x64x64, {steps[0]}-{steps[1]} steps, Re 100-1000, "
-                        "seed 4242",
+            "workload": "cavity/sphere/box jobs, grids 32^3..256x128x128, 100-1000 steps, Re 100-1000, seed 4242 "
+                        f"(the first {njobs} jobs of the stream)",
+            "cell_steps": res["cell_steps"],
             "latency_p50_s": round(res["latency_p50_s"], 3), "latency_p99_s": round(res["latency_p99_s"], 3),
             "mcell_steps_per_s": round(res["mcell_steps_per_s"], 3), "max_active": res["max_active"],
             "wall_s": round(res["wall_s"], 2), "max_div": res["max_div"],
+            "admission": res.get("admission"),
             "fp64_alone_device_mcell_steps_per_s": round(alone, 3),
             "served_vs_fp64_alone": round(res["mcell_steps_per_s"] / alone, 3)}
 
@@ -498,9 +673,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
-    ap.add_argument("--no-extras", action="store_true", help="skip the ensemble and serving measurements")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the other configurations, the ensemble and serving measurements")
+    ap.add_argument("--no-oracle", action="store_true", help="skip the error against the CPU oracle")
     ap.add_argument("--no-tune", action="store_true", help="no autotuning: default (or the given) settings")
-    ap.add_argument("--mixed-form", default="MIXED", choices=["MIXED", "MIXED_MG"],
+    ap.add_argument("--mixed-form", default="MIXED32", choices=["MIXED", "MIXED_MG", "MIXED32"],
                     help="with --no-tune: the mixed step's solver form")
     ap.add_argument("--mg-sweeps", default="", help="with --no-tune: multigrid sweeps 'pre,post,cpre,cpost,coarsest'")
     ap.add_argument("--host-loop", action="store_true",

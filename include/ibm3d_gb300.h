@@ -25,7 +25,10 @@ enum {
     IBM3D_ECUDA = 3,        /* CUDA error or no usable GPU */
     IBM3D_EARG = 4,         /* invalid argument or call order */
     IBM3D_EGEOM = 5,        /* ghost-cell mirror point outside the grid */
-    IBM3D_EUNSUPPORTED = 6  /* feature not available on the GPU path */
+    IBM3D_EUNSUPPORTED = 6, /* feature not available on the GPU path */
+    IBM3D_ENONFINITE = 7    /* NaN or Inf in a step: in the initial state, the
+                               boundary data or force, or a diverging run; the
+                               iterate call stops after that step */
 };
 int IBMSolver_last_status(const IBMSolver *);
 /* Text of the last error set on this solver ("" if none); the reference
@@ -64,9 +67,21 @@ void IBMSolver_set_div_tol(IBMSolver *, double div_tol);
    multigrid preconditioner; it stops on the same FP64 criterion.
    IBM3D_MIXED_MG: momentum as IBM3D_MIXED; the pressure solve is FP64
    BiCGSTAB whose preconditioner is the FP32 multigrid V-cycle (input
-   rounded to FP32, output widened to FP64).  Every other part of the step
-   stays FP64 in all modes. */
-enum { IBM3D_FP64 = 0, IBM3D_MIXED = 1, IBM3D_MIXED_MG = 2 };
+   rounded to FP32, output widened to FP64).  In these three modes every
+   other part of the step stays FP64.
+   IBM3D_MIXED32: the explicit stages in FP32 as well - convection and the
+   momentum right-hand side, u~ and U* - and the momentum solve in FP32 on
+   the increment e = u* - u^n (right-hand side c = b - A u^n formed in
+   FP32 without the O(1) cancellation, stopping test ||c - A e|| <
+   tol ||b|| / 2); FP64 for the state updates u^{n+1} = u^n + (e - dt G p'),
+   the face projection, p, the Poisson right-hand side (the FP64 divergence
+   of U*) and the pressure solve as IBM3D_MIXED_MG.  Its results differ
+   from the FP64 step by the FP32 rounding of O(dt) increments (~1e-7
+   relative velocity after a few hundred steps); max|div U| is driven to
+   the same bound.  IBM3D_MIXED32_IR: the same, with the pressure solved
+   as in IBM3D_MIXED (FP64 refinement around FP32 BiCGSTAB with the FP32
+   multigrid). */
+enum { IBM3D_FP64 = 0, IBM3D_MIXED = 1, IBM3D_MIXED_MG = 2, IBM3D_MIXED32 = 3, IBM3D_MIXED32_IR = 4 };
 void IBMSolver_set_precision(IBMSolver *, int mode);
 
 /* Step sequencing.  on (default): each time step runs as one recorded CUDA
@@ -92,6 +107,29 @@ void IBMSolver_set_multigrid(IBMSolver *, int nu_pre, int nu_post, int nuc_pre, 
    inner solve stops sooner; the stopping test (||r|| < tol ||b||) is the
    same.  The plain FP64 step always starts from zero, as the reference. */
 void IBMSolver_set_warm_start(IBMSolver *, int on);
+
+/* Self-test of the integer-pipe FP64 <-> FP32 conversions of the
+   IBM3D_MIXED32 stages against the hardware conversion instructions on
+   the GPU: each of the n values is converted both ways; *mismatches counts
+   the results that differ bit for bit (values on an exact rounding tie,
+   which these round away from zero and the hardware to even, and FP32
+   subnormals, which these flush to zero, are the expected differences).
+   Returns 0, or -1 on a CUDA error or bad argument. */
+int IBMSolver_check_fp32_conversions(long long n, const double *values, unsigned long long *mismatches);
+
+/* Initial guess of a warm-started pressure solve (the mixed modes):
+   0 (default) the last step's increment p'; 1 its linear extrapolation
+   2 p'_{n-1} - p'_{n-2} once two increments are known.  The solve stops
+   on the same test either way; both increments are part of the
+   exact-resume state. */
+void IBMSolver_set_pressure_guess(IBMSolver *, int mode);
+
+/* Krylov iteration caps of the momentum and pressure solves (defaults
+   200 and 1000, the reference's hypre settings, src/ibm3d_setup.c:1411-1563).
+   A solve that reaches its cap prints the reference's warning
+   ("warning: u0_star did not converge", "warning: p_prime did not
+   converge") and the step continues, as in the reference. */
+void IBMSolver_set_max_iters(IBMSolver *, int max_mom, int max_p);
 
 /* Coarsening of the pressure multigrid (before IBMSolver_assemble).
    IBM3D_COARSEN_SPACING (default): a coarse level merges neighbouring
@@ -163,6 +201,13 @@ typedef struct {
     int cpt_fallback;       /* level-set points settled by the full extrusion scan */
     int outer_u;            /* refinement cycles of the momentum solve (IBM3D_MIXED) */
     int outer_p;            /* refinement cycles of the pressure solve (IBM3D_MIXED) */
+    /* Totals over every step since IBMSolver_assemble (averages over a run
+       are differences of two reads). */
+    long long steps_total;
+    long long iters_u_total[3];
+    long long iters_p_total;
+    long long outer_p_total;
+    double max_div_max;     /* largest per-step max|div U| */
 } IBMSolverStats;
 void IBMSolver_get_stats(const IBMSolver *, IBMSolverStats *);
 
@@ -175,10 +220,23 @@ double IBMSolver_time_iterate(IBMSolver *, int nsteps);
    events on the solver's stream (ms), and its algorithmic bytes per launch
    in *bytes (for a roofline).  IBM3D_K_MG_COLOR: one colour pass of the
    pressure multigrid's fine-grid smoother; IBM3D_K_SPMV_P: one pressure
-   operator application.  Both run on scratch vectors of the pressure
-   solve; the flow state is untouched. */
-enum { IBM3D_K_MG_COLOR = 0, IBM3D_K_SPMV_P = 1 };
+   operator application (both on scratch vectors of the pressure solve).
+   IBM3D_K_CONV_RHS, IBM3D_K_USTAR_PRHS, IBM3D_K_UPDATE_NEXT: the step's
+   explicit kernels of the current mode (FP64, or the FP32 stages of
+   IBM3D_MIXED32), re-run on the last step's inputs; they write only
+   buffers the next step overwrites first.  Or IBM3D_K_COLD into which:
+   an L2-sized buffer is written before each launch and only the launches
+   are timed (cold cache), instead of back-to-back launches. */
+enum {
+    IBM3D_K_MG_COLOR = 0, IBM3D_K_SPMV_P = 1, IBM3D_K_CONV_RHS = 2, IBM3D_K_USTAR_PRHS = 3,
+    IBM3D_K_UPDATE_NEXT = 4, IBM3D_K_COLD = 256
+};
 double IBMSolver_time_kernel(IBMSolver *, int which, int reps, double *bytes);
+
+/* Register-only FMA throughput of this GPU (TFLOP/s, 2 flops per FMA):
+   which 0 FP64, 1 FP32.  A roofline denominator for the kernels that the
+   FP64 pipe, not HBM, bounds on this part. */
+double IBMSolver_measure_fma_rate(int which);
 
 /* Per-stage device time accumulated while profiling is on (CUDA events
    around each stage of each step).  Stage names: conv_rhs, tau, mom_solve,
