@@ -26,6 +26,8 @@
  *                                      (KIND pulse) or press / velper
  *                                      (KIND ramp); functions below
  *   forcefunc KIND                     VAL_FUNC body force (KIND swirl)
+ *   export NAME                        after the last call,
+ *                                      IBMSolver_export_result(out-dir/NAME)
  *
  * Dumped (little-endian raw, padded (N+4)^3 cell layout, k fastest):
  *   flag.i32 lvset.f64 coeffsum.f64 ghost.txt  after IBMSolver_assemble
@@ -102,6 +104,7 @@ int main(int argc, char **argv) {
     char stl[1024] = "";
     int init_field = 0;
     char init_dir[1024] = "";
+    char export_name[256] = "";
     double iu = 0, iv = 0, iw = 0, ip = 0;
 
     struct { int dir, type; double a, b, c; int func; } bcs[16];
@@ -145,6 +148,8 @@ int main(int argc, char **argv) {
             else if (!strcmp(type, "velper") && !strcmp(kind, "ramp")) bcs[nbc].type = BC_VELOCITY_PERIODIC;
             else { fprintf(stderr, "bad bcfunc %s %s\n", type, kind); return 2; }
             nbc++;
+        } else if (!strcmp(key, "export")) {
+            if (fscanf(cf, "%255s", export_name) != 1) return 2;
         } else if (!strcmp(key, "forcefunc")) {
             char kind[16];
             if (fscanf(cf, "%15s", kind) != 1 || strcmp(kind, "swirl")) return 2;
@@ -287,6 +292,10 @@ int main(int argc, char **argv) {
         fprintf(rf, "%d %d %d %.17g\n", s, calls[s - 1], shim_hypre_total_iterations(), solver->time);
     }
     fclose(rf);
+    if (export_name[0]) {
+        snprintf(path, sizeof path, "%s/%s", out, export_name);
+        IBMSolver_export_result(solver, path);
+    }
 
     IBMSolver_destroy(solver);
     HYPRE_Finalize();

@@ -1,8 +1,10 @@
 /*
  * netCDF stand-in so the reference's init/export translation units
  * (src/ibm3d_init.c, src/ibm3d_export.c) compile without libnetcdf.
- * Test infrastructure only: writers accept and discard, readers fail
- * with an error code (the reference then aborts, src/ibm3d_init.c:223).
+ * Test infrastructure only: writers record each variable's payload into
+ * $IBM3D_NC_DUMP_DIR/<variable>.bin when that is set (and discard it
+ * otherwise); readers fail with an error code (the reference then aborts,
+ * src/ibm3d_init.c:223).
  */
 #ifndef ORACLE_SHIM_NETCDF_H
 #define ORACLE_SHIM_NETCDF_H

@@ -11,6 +11,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <string>
 #include <vector>
 #include <algorithm>
 
@@ -89,17 +90,54 @@ void g_tree_destroy(GTree *t) {
 }
 
 // ------------------------------------------------------------- netCDF ----
+// Writers record: with IBM3D_NC_DUMP_DIR set, every nc_put_var_* payload of
+// the file being written goes to <dir>/<variable>.bin (raw, little-endian,
+// the variable's element type), so the reference's own exports can be
+// compared with the GPU library's.  Without it writes are discarded.
+// Readers fail (the reference then aborts, src/ibm3d_init.c:223).
+namespace {
+struct NcState {
+    std::vector<size_t> dims;
+    std::vector<std::pair<std::string, std::vector<int>>> vars;
+};
+NcState g_nc;
+
+void nc_record(int varid, const void *data, size_t elem) {
+    const char *dir = std::getenv("IBM3D_NC_DUMP_DIR");
+    if (!dir || varid < 0 || varid >= (int)g_nc.vars.size()) return;
+    size_t count = 1;
+    for (int d : g_nc.vars[varid].second) count *= g_nc.dims[d];
+    const std::string path = std::string(dir) + "/" + g_nc.vars[varid].first + ".bin";
+    FILE *f = std::fopen(path.c_str(), "wb");
+    if (!f) return;
+    std::fwrite(data, elem, count, f);
+    std::fclose(f);
+}
+}  // namespace
+
 extern "C" {
-int nc_create(const char *, int, int *ncidp) { *ncidp = 1; return NC_NOERR; }
+int nc_create(const char *, int, int *ncidp) {
+    g_nc = NcState();
+    *ncidp = 1;
+    return NC_NOERR;
+}
 int nc_open(const char *, int, int *) { return NC_ENOTNC; }
 int nc_close(int) { return NC_NOERR; }
 int nc_enddef(int) { return NC_NOERR; }
-int nc_def_dim(int, const char *, size_t, int *idp) { *idp = 0; return NC_NOERR; }
-int nc_def_var(int, const char *, nc_type, int, const int *, int *varidp) { *varidp = 0; return NC_NOERR; }
+int nc_def_dim(int, const char *, size_t len, int *idp) {
+    *idp = (int)g_nc.dims.size();
+    g_nc.dims.push_back(len);
+    return NC_NOERR;
+}
+int nc_def_var(int, const char *name, nc_type, int ndims, const int *dimidsp, int *varidp) {
+    *varidp = (int)g_nc.vars.size();
+    g_nc.vars.emplace_back(name, std::vector<int>(dimidsp, dimidsp + ndims));
+    return NC_NOERR;
+}
 int nc_put_att_text(int, int, const char *, size_t, const char *) { return NC_NOERR; }
-int nc_put_var_double(int, int, const double *) { return NC_NOERR; }
-int nc_put_var_float(int, int, const float *) { return NC_NOERR; }
-int nc_put_var_int(int, int, const int *) { return NC_NOERR; }
+int nc_put_var_double(int, int varid, const double *op) { nc_record(varid, op, sizeof(double)); return NC_NOERR; }
+int nc_put_var_float(int, int varid, const float *op) { nc_record(varid, op, sizeof(float)); return NC_NOERR; }
+int nc_put_var_int(int, int varid, const int *op) { nc_record(varid, op, sizeof(int)); return NC_NOERR; }
 int nc_inq_varid(int, const char *, int *) { return NC_ENOTNC; }
 int nc_get_var_double(int, int, double *) { return NC_ENOTNC; }
 int nc_get_var_float(int, int, float *) { return NC_ENOTNC; }

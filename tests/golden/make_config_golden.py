@@ -23,10 +23,17 @@ Written to tests/golden/configs/:
   keeps every 4th interior cell along each axis (a regular sample of
   24,576 cells) of u1, u2, u3 and p: a sampled relative L2 difference.
 
+* ``export_<case>.npz`` for the golden cases sphere, channel_les and
+  mixed_box - the reference's result file: what its IBMSolver_export_result
+  hands to netCDF after the case's calls (the stand-in records every
+  variable, see oracle/ref_shim): x, y, z, time, iter and the float u, v,
+  w, p, vorticity and Q in [z][y][x] order, beside the FP64 fields it was
+  made from (u1, u2, u3, p, padded layout).
+
 Needs the reference tree (see oracle/Makefile), so it runs where that is
 mounted; the fixtures are committed.
 
-    python tests/golden/make_config_golden.py [c1] [c2] [c3]
+    python tests/golden/make_config_golden.py [c1] [c2] [c3] [exports]
 """
 from __future__ import annotations
 
@@ -154,9 +161,43 @@ def c3():
     print("c3:", meta)
 
 
+EXPORT_CASES = ("sphere", "channel_les", "mixed_box")
+
+
+def exports():
+    from make_golden import cases
+    all_cases = cases()
+    for name in EXPORT_CASES:
+        c = all_cases[name]
+        nx, ny, nz = c["grid"]
+        cell = (nx + 4, ny + 4, nz + 4)
+        with tempfile.TemporaryDirectory() as tmp:
+            cf = os.path.join(tmp, "case.txt")
+            write_case_file(cf, c)
+            with open(cf, "a") as fh:
+                fh.write("export result\n")
+            dump = os.path.join(tmp, "nc")
+            os.makedirs(dump)
+            subprocess.run([DRIVER, cf, tmp], check=True, env=dict(os.environ, IBM3D_NC_DUMP_DIR=dump))
+            last = len(c["calls"])
+
+            def raw(var, dtype, shape):
+                return np.fromfile(os.path.join(dump, var + ".bin"), dtype=dtype).reshape(shape)
+
+            pad = (nz + 4, ny + 4, nx + 4)
+            out = {v: raw(v, "<f4", pad) for v in ("u", "v", "w", "p", "vorticity", "Q")}
+            out.update(x=raw("x", "<f8", (nx + 4,)), y=raw("y", "<f8", (ny + 4,)), z=raw("z", "<f8", (nz + 4,)),
+                       time=raw("time", "<f8", (1,)), iter=raw("iter", "<i4", (1,)))
+            for f in ("u1", "u2", "u3", "p"):
+                out["state_" + f] = np.fromfile(os.path.join(tmp, f"{f}_{last}.f64"), dtype="<f8").reshape(cell)
+        out["meta"] = np.array(json.dumps(dict(case=name, calls=c["calls"])))
+        np.savez_compressed(os.path.join(OUT, f"export_{name}.npz"), **out)
+        print("export:", name, {k: v.shape for k, v in out.items() if k != "meta"})
+
+
 if __name__ == "__main__":
     if not os.path.exists(DRIVER):
         subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True)
     os.makedirs(OUT, exist_ok=True)
-    for name in sys.argv[1:] or ["c1", "c2", "c3"]:
-        {"c1": c1, "c2": c2, "c3": c3}[name]()
+    for name in sys.argv[1:] or ["c1", "c2", "c3", "exports"]:
+        {"c1": c1, "c2": c2, "c3": c3, "exports": exports}[name]()

@@ -183,3 +183,30 @@ def _read_plain(path):
         out = {k: np.array(v.data) for k, v in f.variables.items()}
         out["_dims"] = dict(f.dimensions)
     return out
+
+
+@pytest.mark.parametrize("name", ["sphere", "channel_les", "mixed_box"])
+def test_export_matches_reference_file(ibm, tmp_path, name):
+    """The reference's own result file (tests/golden/configs/export_<case>:
+    what its IBMSolver_export_result wrote after the case's calls, recorded
+    by the netCDF stand-in): from the same FP64 fields, the library's file
+    holds the same coordinates and the same float u, v, w, p, vorticity and
+    Q, bit for bit."""
+    ref = np.load(os.path.join(ROOT, "tests", "golden", "configs", f"export_{name}.npz"))
+    case = load_golden(name)
+    s = build_case(ibm, case)
+    s.init_flow_array(*(ref["state_" + f] for f in FIELDS))
+    base = str(tmp_path / "res")
+    s.export_result(base)
+    f = _read(base + ".nc")
+    for var in ("x", "y", "z"):
+        assert np.array_equal(f[var], ref[var]), var
+    for var in ("u", "v", "w", "p", "vorticity", "Q"):
+        got = f[var][0]
+        assert got.dtype.kind == "f" and got.dtype.itemsize == 4 and got.shape == ref[var].shape, var
+        got = got.astype("<f4")            # the file is big-endian
+        assert np.array_equal(got, ref[var], equal_nan=True), \
+            f"{var}: {int((got != ref[var]).sum())} values differ from the reference's file"
+        # Bit for bit where finite (NaN payloads aside).
+        fin = np.isfinite(ref[var])
+        assert np.array_equal(got[fin].view(np.uint32), ref[var][fin].view(np.uint32)), var
