@@ -147,6 +147,8 @@ def load_library(path: str = LIB_PATH):
         "IBMBatch_remove": (i, [vp, vp]),
         "IBMBatch_size": (i, [vp]),
         "IBMBatch_iterate": (d, [vp, i]),
+        "IBMBatch_launch": (i, [vp]),
+        "IBMBatch_wait": (i, [vp]),
         "IBMBatch_last_status": (i, [vp]),
         "IBMBatch_set_combined": (None, [vp, i]),
         "Polyhedron_new": (vp, []),
@@ -527,6 +529,18 @@ class Batch:
         if ms < 0 or st not in (0, 1):
             raise IBM3DError(f"IBMBatch_iterate: {STATUS.get(st, st)}")
         return ms
+
+    def launch(self):
+        """Queues one batched step and returns at once (see wait)."""
+        if self._lib.IBMBatch_launch(self._b) != 0:
+            raise IBM3DError("IBMBatch_launch failed")
+
+    def wait(self):
+        """Waits for the step queued by launch and books it."""
+        rc = self._lib.IBMBatch_wait(self._b)
+        st = self._lib.IBMBatch_last_status(self._b)
+        if rc != 0 or st not in (0, 1):
+            raise IBM3DError(f"IBMBatch_wait: {STATUS.get(st, st)}")
 
     def __del__(self):
         if getattr(self, "_b", None):

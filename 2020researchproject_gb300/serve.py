@@ -100,8 +100,15 @@ class Server:
     a job is assembled (raised to what admitted jobs actually take)."""
 
     def __init__(self, ibm, precision="mixed", tol=1e-6, div_tol=1e-8, hbm_budget=None, bytes_per_cell=1500.0,
-                 keep_results=False, combined=False):
+                 keep_results=False, combined=False, overlap=True, admit_per_step=2):
         self.ibm = ibm
+        # overlap: while the GPU runs a batched step (IBMBatch_launch ..
+        # IBMBatch_wait) the host assembles at most `admit_per_step` queued
+        # jobs, which join at the next step, so arrivals do not hold up the
+        # resident jobs' steps; otherwise (or when nothing is resident) a job
+        # is assembled before the step it joins.
+        self.overlap = overlap
+        self.admit_per_step = admit_per_step
         # False: each member steps through its own recorded graph (nothing is
         # re-recorded when jobs arrive or finish); True: one graph per
         # batched step, re-recorded on every membership change.
@@ -143,26 +150,43 @@ class Server:
         batched_steps = 0
         max_active = 0
         t0 = time.perf_counter()
+        def admit_from_queue(limit):
+            nonlocal used
+            joined = []
+            while queue and len(joined) < limit:
+                if (active or joined) and used + self._estimate(queue[0]) > budget:
+                    break
+                job = queue.popleft()
+                self._admit(job, time.perf_counter() - t0)
+                used += job.device_bytes or self._estimate(job)
+                joined.append(job)
+            return joined
+
+        def join(jobs_in):
+            for job in jobs_in:
+                batch.add(job.solver)
+                active.append(job)
+
         while pending or queue or active:
             now = time.perf_counter() - t0
             if now > time_limit:
                 raise RuntimeError("serving run exceeded its time limit")
             while pending and pending[0].arrival <= now:
                 queue.append(pending.popleft())
-            while queue:
-                if active and used + self._estimate(queue[0]) > budget:
-                    break
-                job = queue.popleft()
-                s = self._admit(job, time.perf_counter() - t0)
-                used += job.device_bytes or self._estimate(job)
-                batch.add(s)
-                active.append(job)
+            if not active or not self.overlap:
+                join(admit_from_queue(len(queue)))
             if not active:
                 if pending:
                     time.sleep(max(0.0, min(pending[0].arrival - (time.perf_counter() - t0), 0.05)))
                 continue
             max_active = max(max_active, len(active))
-            batch.iterate(1)
+            joined = []
+            if self.overlap:
+                batch.launch()
+                joined = admit_from_queue(self.admit_per_step)
+                batch.wait()
+            else:
+                batch.iterate(1)
             batched_steps += 1
             for job in list(active):
                 job.done_steps += 1
@@ -177,6 +201,7 @@ class Server:
                     s.close()
                     job.solver = None
                     active.remove(job)
+            join(joined)
         wall = time.perf_counter() - t0
         lat = np.array([j.finished - j.arrival for j in jobs])
         cell_steps = sum(j.cells * j.steps for j in jobs)

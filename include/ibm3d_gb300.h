@@ -279,6 +279,13 @@ int IBMBatch_add(IBMBatch *, IBMSolver *);
 int IBMBatch_remove(IBMBatch *, IBMSolver *);
 int IBMBatch_size(const IBMBatch *);
 double IBMBatch_iterate(IBMBatch *, int nsteps);
+/* One batched step in two halves: IBMBatch_launch queues the step of every
+   member on the GPU and returns at once; IBMBatch_wait waits for it and
+   books it (as IBMBatch_iterate(b, 1) does).  Between the two the host is
+   free, e.g. to assemble solvers that join at the next step; members may
+   not be added or removed then.  Both return 0, or -1 on error. */
+int IBMBatch_launch(IBMBatch *);
+int IBMBatch_wait(IBMBatch *);
 int IBMBatch_last_status(const IBMBatch *);
 /* on (default): each batched step is one graph launch over all members,
    re-recorded when the membership changes.  off: each member's own step

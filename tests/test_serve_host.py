@@ -63,6 +63,17 @@ class FakeBatch:
             m.iter += n
         return 1.0
 
+    def launch(self):                      # a step in two halves: members are fixed in between
+        self.launched = list(self.members)
+        FakeBatch.log.append(("launch", len(self.members)))
+
+    def wait(self):
+        time.sleep(0.02)
+        assert self.launched == self.members, "membership changed while a step was in flight"
+        FakeBatch.log.append(("step", len(self.members)))
+        for m in self.members:
+            m.iter += 1
+
 
 class FakeIBM:
     MIXED, FP64 = 1, 0
@@ -133,3 +144,27 @@ def test_setup_failure_reaches_the_caller():
         assert "assembly failed" in str(e)
     else:
         raise AssertionError("the set-up error was swallowed")
+
+
+def test_arrivals_are_assembled_while_the_gpu_steps():
+    """A job that arrives while others are resident is assembled between
+    the launch of a batched step and its wait (the GPU keeps stepping the
+    resident jobs) and joins at the next step."""
+    class Logged(FakeIBM):
+        class IBMSolver(FakeSolver):
+            def assemble(self):
+                FakeBatch.log.append(("assemble", id(self)))
+
+    FakeSolver.made.clear()
+    FakeBatch.log.clear()
+    rng = np.random.Generator(np.random.Philox(2))
+    jobs = [serve.Job(id=0, case=serve.job_case("cavity", 32, 32, 32, 100.0, rng), steps=6, arrival=0.0,
+                      cells=32 ** 3),
+            serve.Job(id=1, case=serve.job_case("cavity", 36, 36, 36, 100.0, rng), steps=2, arrival=0.03,
+                      cells=36 ** 3)]
+    out = serve.Server(Logged(), hbm_budget=1 << 40, bytes_per_cell=100.0).run(jobs)
+    assert out["jobs"] == 2
+    log = FakeBatch.log
+    a1 = [i for i, e in enumerate(log) if e[0] == "assemble"][1]
+    assert log[a1 - 1][0] == "launch" and log[a1 + 1][0] == "step"   # inside a step in flight
+    assert all(j.done_steps == j.steps for j in jobs)
