@@ -154,6 +154,12 @@ struct Axis {
     const double *kp;    // Crank-Nicolson coefficient toward i+1 (kx_E)
 };
 
+// dt times the face-normal and cell-centred gradient reciprocals (FP64,
+// per axis, index i+2): one product fewer per face on the FP64 pipe.
+struct DtAxis {
+    const double *dtrdc, *dtrdcc;
+};
+
 // FP32 copies of the tables the FP32 explicit stages read.
 struct AxisF {
     const float *wm, *wp, *rd, *rdc, *rdcc, *km, *kp;

@@ -99,9 +99,6 @@ void launch_smagorinsky(cudaStream_t s, const Grid &g, const Axis &ax, const Axi
                         double cs);
 void launch_ustar_prhs(cudaStream_t s, const Grid &g, const Axis &ax, const Axis &ay, const Axis &az,
                        const BCSet &bc, const uint8_t *flag, const UstarArgs &a, double dt, double Re);
-void launch_update_next(cudaStream_t s, const Grid &g, const Axis &ax, const Axis &ay, const Axis &az,
-                        const BCSet &bc, const uint8_t *flag, const NextArgs &a, double dt, double *partials,
-                        unsigned int *counter, double *maxdiv_out, int nblocks);
 // when: 0 fills with the values at the step's start time, 1 at its end
 // time (the two differ only for VAL_FUNC faces).
 void launch_fill_outer(cudaStream_t s, const Grid &g, const BCSet &bc, double *const u[3], double *p, int when);
@@ -119,11 +116,20 @@ struct OpT;
 void launch_conv_rhs32(cudaStream_t s, const Grid &g, const AxisF axf[3], const OpT<float> &A, const BCSet &bc,
                        const uint8_t *flag, const Conv32Args &a, double dt, const double f[3], int les,
                        double *partials, unsigned int *counter, IRScal *out);
-void launch_ustar_prhs32(cudaStream_t s, const Grid &g, const AxisF axf[3], const Axis ax64[3], const BCSet &bc,
-                         const uint8_t *flag, const Ustar32Args &a, double dt, double Re);
-void launch_update_next32(cudaStream_t s, const Grid &g, const Axis ax64[3], const AxisF axf[3], const BCSet &bc,
-                          const uint8_t *flag, const Next32Args &a, double dt, double *partials,
-                          unsigned int *counter, double *maxdiv_out, int nblocks);
+// update_next over tiles of 32 (k) x 8 (j) columns marching over planes of
+// i: each face of U^{n+1} is computed once (x faces carried along i, y
+// faces exchanged in shared memory, z faces by warp shuffle).  a32: the
+// increment form of IBM3D_MIXED32, else the FP64 step (a64).
+void launch_update_next_tiled(cudaStream_t s, const Grid &g, const Axis ax64[3], const DtAxis dta[3],
+                              const AxisF axf[3], const BCSet &bc, const uint8_t *flag, const NextArgs *a64,
+                              const Next32Args *a32, double dt, double *partials, unsigned int *counter,
+                              double *maxdiv_out);
+// calc_u_tilde into ut (3 x ncell floats), then U* and the Poisson
+// right-hand side over tiles, then the outer rows (outer: padded indices of
+// the nout outer cells).
+void launch_ustar_prhs32_tiled(cudaStream_t s, const Grid &g, const AxisF axf[3], const Axis ax64[3],
+                               const BCSet &bc, const uint8_t *flag, const Ustar32Args &a, float *ut, double dt,
+                               double Re, const int *outer, int nout);
 void launch_widen_f32(cudaStream_t s, long long n, const float *x, double *y);
 void launch_ustar_from_increment(cudaStream_t s, long long n, const double *u, const float *e, double *y);
 // Compares d2f_int / f2d_int with the hardware conversions on n host

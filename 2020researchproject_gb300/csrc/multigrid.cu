@@ -782,71 +782,48 @@ constexpr size_t TAIL_SMEM_MAX = 200 * 1024;
 
 template <typename T>
 __global__ void __launch_bounds__(TAIL_THREADS)
-k_mg_tail(const MGLevel<T> *__restrict__ lv, const int first, const int nlev, const int nu1, const int nu2,
-          const int csweeps, const Per3 per, const int *gate) {
+k_mg_tail(const TailDesc<T> d, const uint4 *__restrict__ img, const int nu1, const int nu2, const int csweeps,
+          const Per3 per, const int *gate) {
     MG_GATE(gate);
     extern __shared__ __align__(16) unsigned char tail_smem[];
-    constexpr int MAXL = 16;
-    __shared__ MGLevel<T> loc[MAXL];
+    __shared__ MGLevel<T> loc[TAIL_MAXL];
     const int tid = threadIdx.x;
-    if (tid == 0) {
-        T *q = reinterpret_cast<T *>(tail_smem);
-        for (int l = first; l < nlev; l++) {
-            MGLevel<T> L = lv[l];
-            const long long n = L.n;
-            L.Tx = q; q += n;
-            L.Ty = q; q += n;
-            L.Tz = q; q += n;
-            L.diag = q; q += n;
-            L.R = q; q += n;
-            L.Z = q; q += n;
-            L.idiag = q; q += n;
-            loc[l - first] = L;
+    const int first = 0, nlev = d.ntl;
+    // The image: every level's constants and zeroed R, Z, in one pass of
+    // independent 16-byte loads.
+    uint4 *dst = reinterpret_cast<uint4 *>(tail_smem);
+    for (int q = tid; q < d.words16; q += TAIL_THREADS) dst[q] = __ldg(img + q);
+    if (tid < nlev) {
+        const TailLevel &t = d.lv[tid];
+        MGLevel<T> L{};
+        L.nx = t.nx;
+        L.ny = t.ny;
+        L.nz = t.nz;
+        L.n = t.n;
+        L.cx = t.cx;
+        L.cy = t.cy;
+        L.cz = t.cz;
+        T *arr[7];
+        for (int a = 0; a < 7; a++) arr[a] = reinterpret_cast<T *>(tail_smem + t.off[a]);
+        L.Tx = arr[0];
+        L.Ty = arr[1];
+        L.Tz = arr[2];
+        L.diag = arr[3];
+        L.R = arr[4];
+        L.Z = arr[5];
+        L.idiag = arr[6];
+        for (int a = 0; a < 3; a++) {
+            L.pw[a] = tid > 0 ? reinterpret_cast<const T *>(tail_smem + t.opw[a]) : nullptr;
+            L.po[a] = tid > 0 ? reinterpret_cast<const int *>(tail_smem + t.opo[a]) : nullptr;
+            L.pa[a] = tid > 0 ? reinterpret_cast<const int *>(tail_smem + t.opa[a]) : nullptr;
+            L.ch[a] = tid > 0 ? reinterpret_cast<const int *>(tail_smem + t.och[a]) : nullptr;
         }
-        // Transfer tables of the levels below `first` (toward their finer
-        // level): weights first (alignment of T), then the int tables.
-        for (int l = first + 1; l < nlev; l++) {
-            const int nf[3] = {lv[l - 1].nx, lv[l - 1].ny, lv[l - 1].nz};
-            for (int a = 0; a < 3; a++) {
-                loc[l - first].pw[a] = q;
-                q += nf[a];
-            }
-        }
-        int *qi = reinterpret_cast<int *>(q);
-        for (int l = first + 1; l < nlev; l++) {
-            MGLevel<T> &L = loc[l - first];
-            const int nf[3] = {lv[l - 1].nx, lv[l - 1].ny, lv[l - 1].nz}, nc[3] = {L.nx, L.ny, L.nz};
-            for (int a = 0; a < 3; a++) {
-                L.po[a] = qi; qi += nf[a];
-                L.pa[a] = qi; qi += nf[a];
-                L.ch[a] = qi; qi += nc[a] + 1;
-            }
-        }
+        loc[tid] = L;
     }
     __syncthreads();
-    for (int l = first + 1; l < nlev; l++) {
-        const MGLevel<T> &G = lv[l], &L = loc[l - first];
-        const int nf[3] = {lv[l - 1].nx, lv[l - 1].ny, lv[l - 1].nz}, nc[3] = {L.nx, L.ny, L.nz};
-        for (int a = 0; a < 3; a++) {
-            for (int c = tid; c < nf[a]; c += TAIL_THREADS) {
-                const_cast<T *>(L.pw[a])[c] = G.pw[a][c];
-                const_cast<int *>(L.po[a])[c] = G.po[a][c];
-                const_cast<int *>(L.pa[a])[c] = G.pa[a][c];
-            }
-            for (int c = tid; c <= nc[a]; c += TAIL_THREADS) const_cast<int *>(L.ch[a])[c] = G.ch[a][c];
-        }
-    }
-    for (int l = first; l < nlev; l++) {
-        const MGLevel<T> &G = lv[l], &L = loc[l - first];
-        for (int c = tid; c < L.n; c += TAIL_THREADS) {
-            L.Tx[c] = G.Tx[c];
-            L.Ty[c] = G.Ty[c];
-            L.Tz[c] = G.Tz[c];
-            L.diag[c] = G.diag[c];
-            L.idiag[c] = G.idiag[c];
-            L.R[c] = l == first ? G.R[c] : (T)0;
-            L.Z[c] = 0;
-        }
+    {
+        const MGLevel<T> &L = loc[0];
+        for (int c = tid; c < L.n; c += TAIL_THREADS) L.R[c] = d.R_first[c];
     }
     __syncthreads();
     // Thread tid takes cell tid of a level (a level holds at most
@@ -907,8 +884,8 @@ k_mg_tail(const MGLevel<T> *__restrict__ lv, const int first, const int nlev, co
         __syncthreads();
         sweep(L, nu2);
     }
-    const MGLevel<T> &G = lv[first], &L = loc[0];
-    for (int c = tid; c < L.n; c += TAIL_THREADS) G.Z[c] = L.Z[c];
+    const MGLevel<T> &L = loc[0];
+    for (int c = tid; c < L.n; c += TAIL_THREADS) d.Z_first[c] = L.Z[c];
 }
 
 // Shared memory the tail kernel needs for levels [first, nlev): seven
@@ -922,6 +899,67 @@ static size_t tail_bytes(const std::vector<MGLevel<T>> &lv, int first) {
         for (int a = 0; a < 3; a++) b += (sizeof(T) + 2 * sizeof(int)) * (size_t)nf[a] + sizeof(int) * (nc[a] + 1);
     }
     return b;
+}
+
+// The tail's image (see TailDesc): the same layout as tail_bytes counts,
+// arrays per level (Tx, Ty, Tz, diag, R, Z, idiag), then the weight tables
+// and the int tables of the levels below the first; 16-byte aligned.
+template <typename T>
+static int build_tail_image(const std::vector<MGLevel<T>> &lv, int first, TailDesc<T> &d,
+                            std::vector<unsigned char> &img) {
+    const int nl = (int)lv.size();
+    d.ntl = nl - first;
+    if (d.ntl > TAIL_MAXL) return -1;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        const size_t at = off;
+        off += bytes;
+        return (int)at;
+    };
+    for (int l = first; l < nl; l++) {
+        TailLevel &t = d.lv[l - first];
+        const MGLevel<T> &L = lv[l];
+        t.nx = L.nx, t.ny = L.ny, t.nz = L.nz, t.cx = L.cx, t.cy = L.cy, t.cz = L.cz, t.n = L.n;
+        for (int a = 0; a < 7; a++) t.off[a] = take(sizeof(T) * (size_t)L.n);
+    }
+    for (int l = first + 1; l < nl; l++) {
+        const int nf[3] = {lv[l - 1].nx, lv[l - 1].ny, lv[l - 1].nz};
+        for (int a = 0; a < 3; a++) d.lv[l - first].opw[a] = take(sizeof(T) * (size_t)nf[a]);
+    }
+    for (int l = first + 1; l < nl; l++) {
+        const int nf[3] = {lv[l - 1].nx, lv[l - 1].ny, lv[l - 1].nz}, nc[3] = {lv[l].nx, lv[l].ny, lv[l].nz};
+        for (int a = 0; a < 3; a++) {
+            d.lv[l - first].opo[a] = take(sizeof(int) * (size_t)nf[a]);
+            d.lv[l - first].opa[a] = take(sizeof(int) * (size_t)nf[a]);
+            d.lv[l - first].och[a] = take(sizeof(int) * (size_t)(nc[a] + 1));
+        }
+    }
+    img.assign((off + 15) & ~(size_t)15, 0);
+    d.words16 = (int)(img.size() / 16);
+    auto fetch = [&](int at, const void *src, size_t bytes) {
+        return cudaMemcpy(img.data() + at, src, bytes, cudaMemcpyDeviceToHost) == cudaSuccess;
+    };
+    bool ok = true;
+    for (int l = first; l < nl; l++) {
+        const TailLevel &t = d.lv[l - first];
+        const MGLevel<T> &L = lv[l];
+        const size_t b = sizeof(T) * (size_t)L.n;
+        ok = ok && fetch(t.off[0], L.Tx, b) && fetch(t.off[1], L.Ty, b) && fetch(t.off[2], L.Tz, b) &&
+             fetch(t.off[3], L.diag, b) && fetch(t.off[6], L.idiag, b);   // R, Z stay zero
+    }
+    for (int l = first + 1; l < nl; l++) {
+        const TailLevel &t = d.lv[l - first];
+        const int nf[3] = {lv[l - 1].nx, lv[l - 1].ny, lv[l - 1].nz}, nc[3] = {lv[l].nx, lv[l].ny, lv[l].nz};
+        for (int a = 0; a < 3; a++) {
+            ok = ok && fetch(t.opw[a], lv[l].pw[a], sizeof(T) * (size_t)nf[a]) &&
+                 fetch(t.opo[a], lv[l].po[a], sizeof(int) * (size_t)nf[a]) &&
+                 fetch(t.opa[a], lv[l].pa[a], sizeof(int) * (size_t)nf[a]) &&
+                 fetch(t.och[a], lv[l].ch[a], sizeof(int) * (size_t)(nc[a] + 1));
+        }
+    }
+    d.R_first = lv[first].R;
+    d.Z_first = lv[first].Z;
+    return ok ? 0 : -1;
 }
 
 // ------------------------------------------------------------- host --
@@ -1225,8 +1263,11 @@ int GMG<T>::setup(cudaStream_t s, const OpT<double> &A64, const OpT<T> &A, const
             return -1;
     }
     if (!levels_.empty()) {
-        dlevels_ = (MGLevel<T> *)dalloc(sizeof(MGLevel<T>) * levels_.size(), true);
-        cudaMemcpyAsync(dlevels_, levels_.data(), sizeof(MGLevel<T>) * levels_.size(), cudaMemcpyHostToDevice, s);
+        if (cudaStreamSynchronize(s) != cudaSuccess) return -1;
+        std::vector<unsigned char> img;
+        if (build_tail_image(levels_, tail_, tail_desc_, img) != 0) return -1;
+        tail_img_ = (const uint4 *)upload(img.data(), img.size(), true);
+        if (!tail_img_) return -1;
     }
     const bool ok = cudaStreamSynchronize(s) == cudaSuccess;
     for (void *p : tmp) cudaFree(p);
@@ -1344,8 +1385,8 @@ void GMG<T>::apply(cudaStream_t s, const T *r, T *z, const int *gate) {
     }
     te(tp);
     tp = tb("mg_tail");
-    launch_pdl(k_mg_tail<T>, 1, TAIL_THREADS, tail_smem_, s, dlevels_, tail_, nl, cfg_.nuc_pre, cfg_.nuc_post,
-                                                     cfg_.coarse_sweeps, per, gate);
+    launch_pdl(k_mg_tail<T>, 1, TAIL_THREADS, tail_smem_, s, tail_desc_, tail_img_, cfg_.nuc_pre, cfg_.nuc_post,
+               cfg_.coarse_sweeps, per, gate);
     k++;
     te(tp);
     tp = tb("mgc_up");

@@ -80,6 +80,29 @@ struct MGGeometry {
     std::vector<double> f[3];
 };
 
+// The coarsest levels, run inside one thread block (k_mg_tail): each
+// level's place in the block's shared memory, as byte offsets into an
+// image that setup builds once in global memory (conductances, diagonal,
+// zeroed R and Z, transfer tables) and every launch copies with 16-byte
+// loads.
+constexpr int TAIL_MAXL = 16;
+
+struct TailLevel {
+    int nx, ny, nz, cx, cy, cz;
+    long long n;
+    int off[7];                          // Tx, Ty, Tz, diag, R, Z, idiag
+    int opw[3], opo[3], opa[3], och[3];  // transfer tables toward the finer level (unused on level 0)
+};
+
+template <typename T>
+struct TailDesc {
+    int ntl;        // levels in the tail
+    int words16;    // image size in 16-byte words
+    TailLevel lv[TAIL_MAXL];
+    const T *R_first;   // R and Z of the first tail level in global memory
+    T *Z_first;
+};
+
 template <typename T>
 class GMG : public Preconditioner<T> {
   public:
@@ -118,7 +141,8 @@ class GMG : public Preconditioner<T> {
     int tail_ = 0;
     Prof *prof_ = nullptr;
     size_t tail_smem_ = 0;
-    MGLevel<T> *dlevels_ = nullptr;
+    TailDesc<T> tail_desc_{};
+    const uint4 *tail_img_ = nullptr;
     const int *ghost_cell_ = nullptr;
     int nghost_ = 0;
     T *ghost_tmp_ = nullptr;

@@ -72,6 +72,9 @@ struct ibm3d_device {
     // FP32 copies (wm, wp, rd, rdc, rdcc, km, kp) for the FP32 explicit stages.
     float *tabf[3] = {nullptr, nullptr, nullptr};
     AxisF axf[3];
+    // dt x rdc and dt x rdcc per axis (FP64).
+    double *dtab[3] = {nullptr, nullptr, nullptr};
+    DtAxis dta[3];
     BCSet bc{};
     // Fields.
     double *fields = nullptr;
@@ -87,6 +90,7 @@ struct ibm3d_device {
     // IBM3D_MIXED32: N and N_prev in FP32 (6 arrays of ncell floats).
     float *f32 = nullptr;
     float *N32[3], *Np32[3];
+    float *ut32 = nullptr;   // u~ (3 x ncell floats)
     // Ghost cells.
     int nghost = 0, nlevels = 0;
     int *g_mem = nullptr;
@@ -176,7 +180,6 @@ namespace {
 __attribute__((constructor)) void ibm3d_queues() { setenv("CUDA_DEVICE_MAX_CONNECTIONS", "32", 0); }
 
 constexpr double kNaN = __builtin_nan("");
-constexpr int kUpdateBlocks = 608;
 
 int ncell_of(const IBMSolver *s) { return (s->Nx + 4) * (s->Ny + 4) * (s->Nz + 4); }
 
@@ -309,6 +312,7 @@ void release_device(ibm3d_device *d) {
     for (int a = 0; a < 3; a++) {
         dfree(d->tab[a]);
         dfree(d->tabf[a]);
+        dfree(d->dtab[a]);
     }
     dfree(d->fields);
     dfree(d->f32);
@@ -416,6 +420,15 @@ bool upload_axes(IBMSolver *sv) {
         cudaMemcpyAsync(d->tabf[a], hf.data(), sizeof(float) * hf.size(), cudaMemcpyHostToDevice, d->s);
         float *f = d->tabf[a];
         d->axf[a] = AxisF{f, f + n, f + 2 * n, f + 3 * n, f + 4 * n, f + 5 * n, f + 6 * n};
+        std::vector<double> hd(2 * (size_t)n);
+        for (int q = 0; q < n; q++) {
+            hd[q] = sv->dt * rdc[q];
+            hd[n + q] = sv->dt * rdcc[q];
+        }
+        d->dtab[a] = dmalloc<double>(sv, hd.size(), "dt axis tables");
+        if (!d->dtab[a]) return false;
+        cudaMemcpyAsync(d->dtab[a], hd.data(), sizeof(double) * hd.size(), cudaMemcpyHostToDevice, d->s);
+        d->dta[a] = DtAxis{d->dtab[a], d->dtab[a] + n};
     }
     return true;
 }
@@ -448,8 +461,9 @@ bool alloc_fields(IBMSolver *sv) {
     d->b = take(3);
     d->lvset = take(1);
     d->dinv = take(1);
-    d->f32 = dmalloc<float>(sv, 6 * (size_t)n, "FP32 convection terms");
+    d->f32 = dmalloc<float>(sv, 9 * (size_t)n, "FP32 convection terms and u~");
     if (!d->f32) return false;
+    d->ut32 = d->f32 + 6 * (size_t)n;
     d->pp_prev = dmalloc<double>(sv, n, "pressure increment history");
     d->pp_hist = dmalloc<int>(sv, 1, "pressure increment count");
     if (!d->pp_prev || !d->pp_hist) return false;
@@ -459,7 +473,11 @@ bool alloc_fields(IBMSolver *sv) {
     }
     d->flag = dmalloc<uint8_t>(sv, n, "flags");
     d->gid = dmalloc<int>(sv, n, "ghost map");
-    d->red_partials = dmalloc<double>(sv, 8 * 4096, "reduction partials");
+    // Partials of the fused reductions: up to 8 values per block of the
+    // largest reducing launch (tiles at most one plane deep, plus blocks
+    // over the outer cells).
+    const long long tiles = (long long)((d->g.nz + 31) / 32) * ((d->g.ny + 7) / 8) * d->g.nx;
+    d->red_partials = dmalloc<double>(sv, 8 * (size_t)(tiles + n / 256 + 4096), "reduction partials");
     d->red_counter = dmalloc<unsigned int>(sv, 1, "reduction counter");
     d->maxdiv_d = dmalloc<double>(sv, 1, "max div");
     if (!d->flag || !d->gid || !d->red_partials || !d->red_counter || !d->maxdiv_d) return false;
@@ -1024,7 +1042,8 @@ void stage_ustar(IBMSolver *sv) {
         ua.dinv = d->dinv;
         ua.b = d->b;
         const int t = d->prof.begin("ustar_prhs");
-        launch_ustar_prhs32(d->s, d->g, d->axf, d->ax, d->bc, d->flag, ua, sv->dt, sv->Re);
+        launch_ustar_prhs32_tiled(d->s, d->g, d->axf, d->ax, d->bc, d->flag, ua, d->ut32, sv->dt, sv->Re,
+                                  d->A32.sw.outer, d->A32.sw.nout);
         d->prof.end(t);
         return;
     }
@@ -1055,8 +1074,8 @@ void stage_next(IBMSolver *sv) {
         na.pp = d->pp;
         na.pn = d->pn;
         const int t = d->prof.begin("update_next");
-        launch_update_next32(d->s, d->g, d->ax, d->axf, d->bc, d->flag, na, sv->dt, d->red_partials, d->red_counter,
-                             d->maxdiv_d, kUpdateBlocks);
+        launch_update_next_tiled(d->s, d->g, d->ax, d->dta, d->axf, d->bc, d->flag, nullptr, &na, sv->dt,
+                                 d->red_partials, d->red_counter, d->maxdiv_d);
         d->prof.end(t);
         return;
     }
@@ -1071,8 +1090,8 @@ void stage_next(IBMSolver *sv) {
     na.pp = d->pp;
     na.pn = d->pn;
     const int t = d->prof.begin("update_next");
-    launch_update_next(d->s, d->g, d->ax[0], d->ax[1], d->ax[2], d->bc, d->flag, na, sv->dt, d->red_partials,
-                       d->red_counter, d->maxdiv_d, kUpdateBlocks);
+    launch_update_next_tiled(d->s, d->g, d->ax, d->dta, d->axf, d->bc, d->flag, &na, nullptr, sv->dt,
+                             d->red_partials, d->red_counter, d->maxdiv_d);
     d->prof.end(t);
 }
 
@@ -2697,6 +2716,10 @@ struct IBMBatch {
     std::vector<Rec> cache;
     int combined = 1;  // 1: one graph for all members; 0: each member's own step graph
     int status = IBM3D_OK;
+    // A step launched by IBMBatch_launch and not yet finished.
+    bool pending = false;
+    Rec *pending_rec = nullptr;
+    std::vector<StepGraph *> pending_own;
 };
 
 namespace {
@@ -2760,8 +2783,13 @@ IBMBatch *IBMBatch_new(void) {
     return b;
 }
 
+namespace {
+bool batch_finish(IBMBatch *b);
+}
+
 void IBMBatch_destroy(IBMBatch *b) {
     if (!b) return;
+    batch_finish(b);
     batch_drop(b);
     for (auto e : b->join) cudaEventDestroy(e);
     if (b->fork) cudaEventDestroy(b->fork);
@@ -2772,6 +2800,10 @@ void IBMBatch_destroy(IBMBatch *b) {
 }
 
 int IBMBatch_add(IBMBatch *b, IBMSolver *s) {
+    if (b && b->pending) {
+        fprintf(stderr, "error: IBMBatch_add: a launched step has not been waited for\n");
+        return -1;
+    }
     if (!b || !s || !s->dev || !s->dev->assembled) {
         fprintf(stderr, "error: IBMBatch_add: the solver must be assembled first\n");
         return -1;
@@ -2790,6 +2822,10 @@ int IBMBatch_add(IBMBatch *b, IBMSolver *s) {
 }
 
 int IBMBatch_remove(IBMBatch *b, IBMSolver *s) {
+    if (b->pending) {
+        fprintf(stderr, "error: IBMBatch_remove: a launched step has not been waited for\n");
+        return -1;
+    }
     for (size_t q = 0; q < b->members.size(); q++)
         if (b->members[q] == s) {
             b->members.erase(b->members.begin() + q);
@@ -2806,96 +2842,113 @@ int IBMBatch_remove(IBMBatch *b, IBMSolver *s) {
 
 int IBMBatch_size(const IBMBatch *b) { return b ? (int)b->members.size() : 0; }
 
-double IBMBatch_iterate(IBMBatch *b, int nsteps) {
-    if (!b || b->members.empty() || nsteps < 1) return 0.0;
-    b->status = IBM3D_OK;
+namespace {
+
+// First half of a batched step: joins new members (their iterate
+// prologue), then launches the step of every member - one graph over all
+// members, or each member's own step graph on its stream - without
+// waiting for it.  Returns false on a recording or launch failure.
+bool batch_launch(IBMBatch *b) {
     for (size_t q = 0; q < b->members.size(); q++) {
         IBMSolver *m = b->members[q];
         if (b->next_iter[q] != m->iter) {  // joined, or stepped outside the batch: a new run
             b->run_start[q] = m->time;
             b->run_steps[q] = 0;
             iterate_prologue(m);
+            b->next_iter[q] = m->iter;
         }
         m->dev->status = IBM3D_OK;
         cudaEventRecord(b->join[q], m->dev->s);
         cudaStreamWaitEvent(b->s, b->join[q], 0);
     }
-    cudaEventRecord(b->t0, b->s);
-    std::vector<StepGraph *> own(b->members.size(), nullptr);
-    for (int i = 1; i <= nsteps; i++) {
-        if (!b->combined) {
-            // Each member's own recorded step on its own stream, all forked
-            // from and joined into the batch stream.
-            for (size_t q = 0; q < b->members.size(); q++) {
-                own[q] = step_graph(b->members[q]);
-                if (!own[q]) {
-                    fprintf(stderr, "error: IBMBatch_iterate: recording a member's step failed\n");
-                    b->status = IBM3D_ECUDA;
-                    return -1;
-                }
+    if (!b->combined) {
+        // Each member's own recorded step on its own stream, all forked
+        // from and joined into the batch stream.
+        b->pending_own.assign(b->members.size(), nullptr);
+        for (size_t q = 0; q < b->members.size(); q++) {
+            b->pending_own[q] = step_graph(b->members[q]);
+            if (!b->pending_own[q]) {
+                fprintf(stderr, "error: IBMBatch_iterate: recording a member's step failed\n");
+                return false;
             }
-            cudaEventRecord(b->fork, b->s);
-            for (size_t q = 0; q < b->members.size(); q++) {
-                IBMSolver *m = b->members[q];
-                cudaStreamWaitEvent(m->dev->s, b->fork, 0);
-                prepare_samples(m, m->dev->s, m->time, b->run_start[q] + m->dt * (b->run_steps[q] + 1));
-                cudaGraphLaunch(own[q]->exec, m->dev->s);
-                cudaEventRecord(b->join[q], m->dev->s);
-                cudaStreamWaitEvent(b->s, b->join[q], 0);
-            }
-            if (cudaStreamSynchronize(b->s) != cudaSuccess) {
-                fprintf(stderr, "error: IBMBatch_iterate: %s\n", cudaGetErrorString(cudaGetLastError()));
-                b->status = IBM3D_ECUDA;
-                return -1;
-            }
-            for (size_t q = 0; q < b->members.size(); q++) {
-                IBMSolver *m = b->members[q];
-                finish_step(m, *own[q]);
-                m->iter++;
-                b->run_steps[q]++;
-                b->next_iter[q] = m->iter;
-                m->time = b->run_start[q] + m->dt * b->run_steps[q];
-                m->dev->max_div = *m->dev->maxdiv_h;
-                account_step(m->dev);
-                if (m->dev->status != IBM3D_OK && m->dev->status != IBM3D_ENOCONV) b->status = m->dev->status;
-            }
-            continue;
         }
+        cudaEventRecord(b->fork, b->s);
         for (size_t q = 0; q < b->members.size(); q++) {
             IBMSolver *m = b->members[q];
-            prepare_samples(m, b->s, m->time, b->run_start[q] + m->dt * (b->run_steps[q] + 1));
+            cudaStreamWaitEvent(m->dev->s, b->fork, 0);
+            prepare_samples(m, m->dev->s, m->time, b->run_start[q] + m->dt * (b->run_steps[q] + 1));
+            cudaGraphLaunch(b->pending_own[q]->exec, m->dev->s);
+            cudaEventRecord(b->join[q], m->dev->s);
+            cudaStreamWaitEvent(b->s, b->join[q], 0);
         }
-        const std::vector<const void *> key = batch_key(b);
-        IBMBatch::Rec *R = nullptr;
-        for (auto &r : b->cache)
-            if (r.key == key) R = &r;
-        if (!R) {
-            if (b->cache.size() >= 4) batch_drop(b);
-            IBMBatch::Rec nr;
-            nr.key = key;
-            if (!batch_record(b, nr)) {
-                fprintf(stderr, "error: IBMBatch_iterate: recording the batched step failed\n");
-                b->status = IBM3D_ECUDA;
-                return -1;
-            }
-            b->cache.push_back(nr);
-            R = &b->cache.back();
+        b->pending = true;
+        return true;
+    }
+    for (size_t q = 0; q < b->members.size(); q++) {
+        IBMSolver *m = b->members[q];
+        prepare_samples(m, b->s, m->time, b->run_start[q] + m->dt * (b->run_steps[q] + 1));
+    }
+    const std::vector<const void *> key = batch_key(b);
+    IBMBatch::Rec *R = nullptr;
+    for (auto &r : b->cache)
+        if (r.key == key) R = &r;
+    if (!R) {
+        if (b->cache.size() >= 4) batch_drop(b);
+        IBMBatch::Rec nr;
+        nr.key = key;
+        if (!batch_record(b, nr)) {
+            fprintf(stderr, "error: IBMBatch_iterate: recording the batched step failed\n");
+            return false;
         }
-        if (cudaGraphLaunch(R->exec, b->s) != cudaSuccess || cudaStreamSynchronize(b->s) != cudaSuccess) {
-            fprintf(stderr, "error: IBMBatch_iterate: %s\n", cudaGetErrorString(cudaGetLastError()));
+        b->cache.push_back(nr);
+        R = &b->cache.back();
+    }
+    if (cudaGraphLaunch(R->exec, b->s) != cudaSuccess) {
+        fprintf(stderr, "error: IBMBatch_iterate: %s\n", cudaGetErrorString(cudaGetLastError()));
+        return false;
+    }
+    b->pending_rec = R;
+    b->pending = true;
+    return true;
+}
+
+// Second half: waits for the launched step and books it for every member
+// (solve reports, warnings, pointer swaps, iteration count and time).
+bool batch_finish(IBMBatch *b) {
+    if (!b->pending) return true;
+    b->pending = false;
+    if (cudaStreamSynchronize(b->s) != cudaSuccess) {
+        fprintf(stderr, "error: IBMBatch_iterate: %s\n", cudaGetErrorString(cudaGetLastError()));
+        return false;
+    }
+    for (size_t q = 0; q < b->members.size(); q++) {
+        IBMSolver *m = b->members[q];
+        finish_step(m, b->combined ? b->pending_rec->parts[q] : *b->pending_own[q]);
+        m->iter++;
+        b->run_steps[q]++;
+        b->next_iter[q] = m->iter;
+        m->time = b->run_start[q] + m->dt * b->run_steps[q];
+        m->dev->max_div = *m->dev->maxdiv_h;
+        account_step(m->dev);
+        if (m->dev->status != IBM3D_OK && m->dev->status != IBM3D_ENOCONV) b->status = m->dev->status;
+    }
+    return true;
+}
+
+}  // namespace
+
+double IBMBatch_iterate(IBMBatch *b, int nsteps) {
+    if (!b || b->members.empty() || nsteps < 1) return 0.0;
+    if (b->pending && !batch_finish(b)) {
+        b->status = IBM3D_ECUDA;
+        return -1;
+    }
+    b->status = IBM3D_OK;
+    cudaEventRecord(b->t0, b->s);
+    for (int i = 1; i <= nsteps; i++) {
+        if (!batch_launch(b) || !batch_finish(b)) {
             b->status = IBM3D_ECUDA;
             return -1;
-        }
-        for (size_t q = 0; q < b->members.size(); q++) {
-            IBMSolver *m = b->members[q];
-            finish_step(m, R->parts[q]);
-            m->iter++;
-            b->run_steps[q]++;
-            b->next_iter[q] = m->iter;
-            m->time = b->run_start[q] + m->dt * b->run_steps[q];
-            m->dev->max_div = *m->dev->maxdiv_h;
-            account_step(m->dev);
-            if (m->dev->status != IBM3D_OK && m->dev->status != IBM3D_ENOCONV) b->status = m->dev->status;
         }
     }
     cudaEventRecord(b->t1, b->s);
@@ -2903,6 +2956,25 @@ double IBMBatch_iterate(IBMBatch *b, int nsteps) {
     float ms = 0;
     cudaEventElapsedTime(&ms, b->t0, b->t1);
     return ms;
+}
+
+int IBMBatch_launch(IBMBatch *b) {
+    if (!b || b->members.empty() || b->pending) return -1;
+    b->status = IBM3D_OK;
+    if (!batch_launch(b)) {
+        b->status = IBM3D_ECUDA;
+        return -1;
+    }
+    return 0;
+}
+
+int IBMBatch_wait(IBMBatch *b) {
+    if (!b) return -1;
+    if (!batch_finish(b)) {
+        b->status = IBM3D_ECUDA;
+        return -1;
+    }
+    return 0;
 }
 
 int IBMBatch_last_status(const IBMBatch *b) { return b ? b->status : IBM3D_EARG; }

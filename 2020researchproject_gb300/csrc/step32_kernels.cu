@@ -25,6 +25,8 @@
 //
 // FP64 fields are read as FP32 with d2f_int / written with f2d_int
 // (integer pipe; see common.cuh).
+#include <algorithm>
+
 #include "common.cuh"
 #include "kernels.h"
 #include "krylov.h"
@@ -36,6 +38,8 @@ namespace {
 
 constexpr int K32_THREADS = 256;
 constexpr int K32_BLOCKS = 1216;  // 8 per SM on 152 SMs; grid-stride
+// Tiles of the marching kernels: 32 (k) x 8 (j) columns, UN_PLANES planes of i.
+constexpr int UN_TK = 32, UN_TJ = 8, UN_PLANES = 8;
 
 // An FP64 field value in FP32; NaN (solid cells) becomes 0, the value the
 // momentum solve gives solid rows.
@@ -79,8 +83,27 @@ k_conv_rhs32(const Grid g, const AxisF ax, const AxisF ay, const AxisF az, const
     float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // ||b||^2 (3), ||c||^2 (3)
     const long long n = g.ncell;
     const float NaNf = __int_as_float(0x7fc00000);
-    for (long long P = blockIdx.x * (long long)blockDim.x + threadIdx.x; P < n;
-         P += (long long)gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    // Block-uniform loop: the lanes of a warp hold consecutive padded cells,
+    // so the k neighbours (P -/+ 1) of the values every lane converts for
+    // its own cell come by shuffle; lanes 0 and 31 load theirs.
+    for (long long base = blockIdx.x * (long long)blockDim.x; base < n; base += (long long)gridDim.x * blockDim.x) {
+        const long long P = base + threadIdx.x;
+        const bool act = P < n;
+        float own[5] = {0.f, 0.f, 0.f, 0.f, 0.f};   // u1, u2, u3, p, W (low z face)
+        if (act) {
+            own[0] = ld32(a.u[0], P);
+            own[1] = ld32(a.u[1], P);
+            own[2] = ld32(a.u[2], P);
+            own[3] = ldp32(a.p, P);
+            own[4] = ldp32(a.U[2], P);
+        }
+        float dn[4], up[5];
+#pragma unroll
+        for (int q = 0; q < 4; q++) dn[q] = __shfl_up_sync(0xffffffffu, own[q], 1);
+#pragma unroll
+        for (int q = 0; q < 5; q++) up[q] = __shfl_down_sync(0xffffffffu, own[q], 1);
+        if (!act) continue;
         int i, j, k;
         cijk_g(g, P, i, j, k);
         int layer;
@@ -121,12 +144,23 @@ k_conv_rhs32(const Grid g, const AxisF ax, const AxisF ay, const AxisF az, const
         } else {
             const long long sx = g.sx, sy = g.sy;
             const int I = i + 2, J = j + 2, K = k + 2;
+            // A fluid cell is interior, so P -/+ 1 are cells of the grid:
+            // the warp's edge lanes load them here.
+            if (lane == 0) {
+                for (int q = 0; q < 3; q++) dn[q] = ld32(a.u[q], P - 1);
+                dn[3] = ldp32(a.p, P - 1);
+            }
+            if (lane == 31) {
+                for (int q = 0; q < 3; q++) up[q] = ld32(a.u[q], P + 1);
+                up[3] = ldp32(a.p, P + 1);
+                up[4] = ldp32(a.U[2], P + 1);
+            }
             const float wmx0 = ax.wm[I], wpx0 = ax.wp[I], wmx1 = ax.wm[I + 1], wpx1 = ax.wp[I + 1];
             const float wmy0 = ay.wm[J], wpy0 = ay.wp[J], wmy1 = ay.wm[J + 1], wpy1 = ay.wp[J + 1];
             const float wmz0 = az.wm[K], wpz0 = az.wp[K], wmz1 = az.wm[K + 1], wpz1 = az.wp[K + 1];
             const float Uw = ldp32(a.U[0], P), Ue = ldp32(a.U[0], P + sx);
             const float Vs = ldp32(a.U[1], P), Vn = ldp32(a.U[1], P + sy);
-            const float Wd = ldp32(a.U[2], P), Wu = ldp32(a.U[2], P + 1);
+            const float Wd = own[4], Wu = up[4];
             const float rdx = ax.rd[I], rdy = ay.rd[J], rdz = az.rd[K];
             const float kW = ax.km[I], kE = ax.kp[I], kS = ay.km[J], kN = ay.kp[J], kD = az.km[K], kU = az.kp[K];
             const float gx = ax.rdcc[I], gy = ay.rdcc[J], gz = az.rdcc[K];
@@ -134,9 +168,9 @@ k_conv_rhs32(const Grid g, const AxisF ax, const AxisF ay, const AxisF az, const
 #pragma unroll
             for (int l = 0; l < 3; l++) {
                 const double *u = a.u[l];
-                const float uc = ld32(u, P);
+                const float uc = own[l];
                 const float uW = ld32(u, P - sx), uE = ld32(u, P + sx), uS = ld32(u, P - sy), uN = ld32(u, P + sy);
-                const float uD = ld32(u, P - 1), uU = ld32(u, P + 1);
+                const float uD = dn[l], uU = up[l];
                 const float fw = uW * wmx0 + uc * wpx0, fe = uc * wmx1 + uE * wpx1;
                 const float fs = uS * wmy0 + uc * wpy0, fn = uc * wmy1 + uN * wpy1;
                 const float fd = uD * wmz0 + uc * wpz0, fu = uc * wmz1 + uU * wpz1;
@@ -145,7 +179,7 @@ k_conv_rhs32(const Grid g, const AxisF ax, const AxisF ay, const AxisF az, const
                 float dp;
                 if (l == 0) dp = (ldp32(a.p, P + sx) - ldp32(a.p, P - sx)) * gx;
                 else if (l == 1) dp = (ldp32(a.p, P + sy) - ldp32(a.p, P - sy)) * gy;
-                else dp = (ldp32(a.p, P + 1) - ldp32(a.p, P - 1)) * gz;
+                else dp = (up[3] - dn[3]) * gz;
                 float divtau = 0.0f;
                 if (les) {
                     const int t1 = l == 0 ? 0 : l == 1 ? 1 : 2;
@@ -201,8 +235,14 @@ void launch_conv_rhs32(cudaStream_t s, const Grid &g, const AxisF axf[3], const 
 
 // ------------------------------------------------------------------------
 // calc_u_tilde + calc_U_star (src/ibm3d_fracstep.c:388-487) in FP32 from
-// u* = u^n + e, fused with the pressure-Poisson right-hand side
-// (src/ibm3d_fracstep.c:530-647) in FP64 from the stored faces.
+// u* = u^n + e, with the pressure-Poisson right-hand side
+// (src/ibm3d_fracstep.c:530-647) in FP64 from the stored faces, in two
+// passes: u~ = u* + dt G_c p in FP32 on every cell the faces read (i, j, k
+// in [-1, N]), then the faces and the right-hand side over tiles of 32 (k)
+// x 8 (j) columns marching over planes of i, each face computed once (x
+// faces carried along i, y faces in shared memory, z faces by warp
+// shuffle).  Tile-edge threads compute their high faces as well; face32t is
+// explicitly rounded, so both computations of such a face give its bits.
 // ------------------------------------------------------------------------
 namespace {
 
@@ -210,152 +250,294 @@ __device__ __forceinline__ float ustar_at(const double *__restrict__ u, const fl
     return __fadd_rn(ld32(u, P), e[P]);
 }
 
-// Face between cells Pm (index ii-1) and Pp (index ii) along stride s;
-// explicitly rounded so that both cells sharing the face get its bits.
-__device__ __forceinline__ float face32(const double *__restrict__ u, const float *__restrict__ e,
-                                        const double *__restrict__ p, const AxisF &a, int ii, long long Pm,
-                                        long long Pp, long long s, bool fluid_ghost, float dt) {
-    const float um = ustar_at(u, e, Pm), up = ustar_at(u, e, Pp);
-    const float wm = a.wm[ii + 2], wp = a.wp[ii + 2];
-    if (fluid_ghost) return __fadd_rn(__fmul_rn(um, wm), __fmul_rn(up, wp));
-    const float gm = __fmul_rn(__fsub_rn(ldp32(p, Pm + s), ldp32(p, Pm - s)), a.rdcc[ii + 1]);
-    const float gp = __fmul_rn(__fsub_rn(ldp32(p, Pp + s), ldp32(p, Pp - s)), a.rdcc[ii + 2]);
-    const float tm = __fadd_rn(um, __fmul_rn(dt, gm));
-    const float tp = __fadd_rn(up, __fmul_rn(dt, gp));
-    const float gf = __fmul_rn(__fsub_rn(ldp32(p, Pp), ldp32(p, Pm)), a.rdc[ii + 2]);
-    return __fsub_rn(__fadd_rn(__fmul_rn(tm, wm), __fmul_rn(tp, wp)), __fmul_rn(dt, gf));
-}
-
 __device__ __forceinline__ bool fg_pair32(uint8_t a, uint8_t b) {
     return (a == FLUID && b == GHOST) || (a == GHOST && b == FLUID);
 }
 
+// U* on the face between Pm (index ii-1) and Pp (index ii) from u~ (ut)
+// or, across a fluid-ghost pair, from u*.
+__device__ __forceinline__ float face32t(const double *__restrict__ u, const float *__restrict__ e,
+                                         const float *__restrict__ ut, const double *__restrict__ p, const AxisF &a,
+                                         int ii, long long Pm, long long Pp, bool fluid_ghost, float dt) {
+    const float wm = a.wm[ii + 2], wp = a.wp[ii + 2];
+    if (fluid_ghost) return __fadd_rn(__fmul_rn(ustar_at(u, e, Pm), wm), __fmul_rn(ustar_at(u, e, Pp), wp));
+    const float gf = __fmul_rn(__fsub_rn(ldp32(p, Pp), ldp32(p, Pm)), a.rdc[ii + 2]);
+    return __fsub_rn(__fadd_rn(__fmul_rn(ut[Pm], wm), __fmul_rn(ut[Pp], wp)), __fmul_rn(dt, gf));
+}
+
 }  // namespace
 
-__global__ void __launch_bounds__(K32_THREADS)
-k_ustar_prhs32(const Grid g, const AxisF ax, const AxisF ay, const AxisF az, const Axis ax64, const Axis ay64,
-               const Axis az64, const BCSet bc, const uint8_t *__restrict__ flag, const Ustar32Args a, const float dt,
-               const double m2re) {
-    const long long n = g.ncell;
-    for (long long P = blockIdx.x * (long long)blockDim.x + threadIdx.x; P < n;
-         P += (long long)gridDim.x * blockDim.x) {
-        int i, j, k;
-        cijk_g(g, P, i, j, k);
-        int layer;
-        const int face = owner_face(g, i, j, k, layer);
-        if (face >= 0) {
-            // Pressure-Dirichlet rows: p_bc(t + dt) - p_bc(t) (0 for constants).
-            const BCFace &F = bc.f[face];
-            double v = 0.0;
-            if (F.scur && (F.type == BCT_PRESSURE || F.type == BCT_VELPERIODIC)) {
-                const int t = 3 * F.nt + face_line(g, face, i, j, k);
-                v = F.snxt[t] - F.scur[t];
-            }
-            a.b[P] = v;
-            continue;
-        }
-        const long long sx = g.sx, sy = g.sy;
-        const uint8_t fc = flag[P];
-        const float Uw = face32(a.u[0], a.e[0], a.p, ax, i, P - sx, P, sx, fg_pair32(flag[P - sx], fc), dt);
-        const float Ue = face32(a.u[0], a.e[0], a.p, ax, i + 1, P, P + sx, sx, fg_pair32(fc, flag[P + sx]), dt);
-        const float Vs = face32(a.u[1], a.e[1], a.p, ay, j, P - sy, P, sy, fg_pair32(flag[P - sy], fc), dt);
-        const float Vn = face32(a.u[1], a.e[1], a.p, ay, j + 1, P, P + sy, sy, fg_pair32(fc, flag[P + sy]), dt);
-        const float Wd = face32(a.u[2], a.e[2], a.p, az, k, P - 1, P, 1, fg_pair32(flag[P - 1], fc), dt);
-        const float Wu = face32(a.u[2], a.e[2], a.p, az, k + 1, P, P + 1, 1, fg_pair32(fc, flag[P + 1]), dt);
-        const double Uw64 = f2d_int(Uw), Ue64 = f2d_int(Ue), Vs64 = f2d_int(Vs), Vn64 = f2d_int(Vn);
-        const double Wd64 = f2d_int(Wd), Wu64 = f2d_int(Wu);
-        a.Us[0][P] = Uw64;
-        a.Us[1][P] = Vs64;
-        a.Us[2][P] = Wd64;
-        if (i == g.nx - 1) a.Us[0][P + sx] = Ue64;
-        if (j == g.ny - 1) a.Us[1][P + sy] = Vn64;
-        if (k == g.nz - 1) a.Us[2][P + 1] = Wu64;
-        double rhs = 0.0;
-        if (fc == FLUID && !(bc.p_singular && i == 0 && j == 0 && k == 0)) {
-            const double div = (Ue64 - Uw64) * ax64.rd[i + 2] + (Vn64 - Vs64) * ay64.rd[j + 2] +
-                               (Wu64 - Wd64) * az64.rd[k + 2];
-            rhs = div * m2re * a.dinv[P];   // -div / (2 Re coeffsum)
-        }
-        a.b[P] = rhs;
-    }
-}
-
-void launch_ustar_prhs32(cudaStream_t s, const Grid &g, const AxisF axf[3], const Axis ax64[3], const BCSet &bc,
-                         const uint8_t *flag, const Ustar32Args &a, double dt, double Re) {
-    k_ustar_prhs32<<<K32_BLOCKS, K32_THREADS, 0, s>>>(g, axf[0], axf[1], axf[2], ax64[0], ax64[1], ax64[2], bc, flag,
-                                                      a, (float)dt, -1.0 / (2.0 * Re));
-    note_launches(1);
-}
-
-// ------------------------------------------------------------------------
-// update_next (src/ibm3d_fracstep.c:709-805) for the increment form: the
-// cell velocity u^{n+1} = u^n + (e - dt G_c p') with the increment in
-// FP32; faces U^{n+1} = U* - dt G_f p', p^{n+1} = p + p' and the
-// divergence check max|div U^{n+1}| in FP64, as the FP64 step.
-// ------------------------------------------------------------------------
 __global__ void __launch_bounds__(256)
-k_update_next32(const Grid g, const Axis ax, const Axis ay, const Axis az, const AxisF axf, const AxisF ayf,
-                const AxisF azf, const BCSet bc, const uint8_t *__restrict__ flag, const Next32Args a, const double dt,
-                double *partials, unsigned int *counter, double *maxdiv_out) {
-    __shared__ double smem[32];
-    const long long n = (long long)g.nx * g.ny * g.nz;
-    double mdiv[1] = {0.0};
-    const double NaN = __longlong_as_double(0x7ff8000000000000LL);
-    const float dtf = (float)dt;
+k_utilde32(const Grid g, const AxisF ax, const AxisF ay, const AxisF az, const Ustar32Args a, float *__restrict__ ut,
+           const float dt) {
+    const long long nx2 = g.nx + 2, ny2 = g.ny + 2, nz2 = g.nz + 2, n = nx2 * ny2 * nz2;
+    const long long sx = g.sx, sy = g.sy;
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
          q += (long long)gridDim.x * blockDim.x) {
-        int i, j, k;
-        ijk_interior(g, q, i, j, k);
+        const int k = (int)(q % nz2) - 1;
+        const long long r = q / nz2;
+        const int j = (int)(r % ny2) - 1, i = (int)(r / ny2) - 1;
         const long long P = cidx(g, i, j, k);
-        const long long sx = g.sx, sy = g.sy;
-        const int I = i + 2, J = j + 2, K = k + 2;
-        const uint8_t fc = flag[P];
-        const double pp = a.pp[P];
-        a.pn[P] = (fc == FLUID || fc == GHOST) ? a.p[P] + pp : NaN;
-        if (fc == FLUID) {
-            const float gx = (ldp32(a.pp, P + sx) - ldp32(a.pp, P - sx)) * axf.rdcc[I];
-            const float gy = (ldp32(a.pp, P + sy) - ldp32(a.pp, P - sy)) * ayf.rdcc[J];
-            const float gz = (ldp32(a.pp, P + 1) - ldp32(a.pp, P - 1)) * azf.rdcc[K];
-            a.un[0][P] = a.u[0][P] + f2d_int(a.e[0][P] - dtf * gx);
-            a.un[1][P] = a.u[1][P] + f2d_int(a.e[1][P] - dtf * gy);
-            a.un[2][P] = a.u[2][P] + f2d_int(a.e[2][P] - dtf * gz);
-        } else if (fc == SOLID) {
-            a.un[0][P] = a.un[1][P] = a.un[2][P] = NaN;
-        }
-        const uint8_t fw = flag[P - sx], fe = flag[P + sx], fs = flag[P - sy], fn = flag[P + sy];
-        const uint8_t fd = flag[P - 1], fu = flag[P + 1];
-        const double Uw = (fw != SOLID && fc != SOLID) ? a.Us[0][P] - dt * (pp - a.pp[P - sx]) * ax.rdc[I] : NaN;
-        const double Ue = (fc != SOLID && fe != SOLID) ? a.Us[0][P + sx] - dt * (a.pp[P + sx] - pp) * ax.rdc[I + 1] : NaN;
-        const double Vs = (fs != SOLID && fc != SOLID) ? a.Us[1][P] - dt * (pp - a.pp[P - sy]) * ay.rdc[J] : NaN;
-        const double Vn = (fc != SOLID && fn != SOLID) ? a.Us[1][P + sy] - dt * (a.pp[P + sy] - pp) * ay.rdc[J + 1] : NaN;
-        const double Wd = (fd != SOLID && fc != SOLID) ? a.Us[2][P] - dt * (pp - a.pp[P - 1]) * az.rdc[K] : NaN;
-        const double Wu = (fc != SOLID && fu != SOLID) ? a.Us[2][P + 1] - dt * (a.pp[P + 1] - pp) * az.rdc[K + 1] : NaN;
-        a.Un[0][P] = Uw;
-        a.Un[1][P] = Vs;
-        a.Un[2][P] = Wd;
-        if (i == g.nx - 1) a.Un[0][P + sx] = Ue;
-        if (j == g.ny - 1) a.Un[1][P + sy] = Vn;
-        if (k == g.nz - 1) a.Un[2][P + 1] = Wu;
-        if (fc == FLUID && !(bc.p_singular && i == 0 && j == 0 && k == 0)) {
-            const double div = (Ue - Uw) * ax.rd[I] + (Vn - Vs) * ay.rd[J] + (Wu - Wd) * az.rd[K];
-            mdiv[0] = nanmax(mdiv[0], fabs(div));
-        }
+        const float gx = (ldp32(a.p, P + sx) - ldp32(a.p, P - sx)) * ax.rdcc[i + 2];
+        const float gy = (ldp32(a.p, P + sy) - ldp32(a.p, P - sy)) * ay.rdcc[j + 2];
+        const float gz = (ldp32(a.p, P + 1) - ldp32(a.p, P - 1)) * az.rdcc[k + 2];
+        ut[P] = ustar_at(a.u[0], a.e[0], P) + dt * gx;
+        ut[g.ncell + P] = ustar_at(a.u[1], a.e[1], P) + dt * gy;
+        ut[2 * g.ncell + P] = ustar_at(a.u[2], a.e[2], P) + dt * gz;
     }
-    block_max<1>(mdiv, smem);
-    if (!publish_partials<1>(mdiv, partials, counter)) return;
-    double m[1];
-    reduce_partials<1, 0>(partials, gridDim.x, m, smem);
-    if (threadIdx.x == 0) {
-        *maxdiv_out = m[0];
+}
+
+__global__ void __launch_bounds__(UN_TK * UN_TJ)
+k_ustar_faces32(const Grid g, const AxisF ax, const AxisF ay, const AxisF az, const Axis ax64, const Axis ay64,
+                const Axis az64, const BCSet bc, const uint8_t *__restrict__ flag, const Ustar32Args a,
+                const float *__restrict__ ut, const float dt, const double m2re, const int tk, const int tj,
+                const int planes) {
+    __shared__ float sVs[2][UN_TJ][UN_TK];
+    int b = blockIdx.x;
+    const int bk = b % tk;
+    b /= tk;
+    const int bj = b % tj, bi = b / tj;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int k = bk * UN_TK + tx, j = bj * UN_TJ + ty;
+    const int i0 = bi * planes, i1 = min(i0 + planes, g.nx);
+    const bool live = j < g.ny && k < g.nz;
+    const bool own_vn = ty == UN_TJ - 1 || j == g.ny - 1;
+    const bool own_wu = tx == UN_TK - 1 || k == g.nz - 1;
+    const long long sx = g.sx, sy = g.sy, n = g.ncell;
+    const float *ut0 = ut, *ut1 = ut + n, *ut2 = ut + 2 * n;
+    long long P = live ? cidx(g, i0, j, k) : 0;
+    uint8_t fc = live ? flag[P] : (uint8_t)SOLID;
+    float Uw = 0.0f;
+    if (live) Uw = face32t(a.u[0], a.e[0], ut0, a.p, ax, i0, P - sx, P, fg_pair32(flag[P - sx], fc), dt);
+    int buf = 0;
+    for (int i = i0; i < i1; i++, P += sx) {
+        float Ue = 0.f, Vs = 0.f, Wd = 0.f, Vn = 0.f, Wu = 0.f;
+        uint8_t fe = SOLID;
+        if (live) {
+            fe = flag[P + sx];
+            Ue = face32t(a.u[0], a.e[0], ut0, a.p, ax, i + 1, P, P + sx, fg_pair32(fc, fe), dt);
+            Vs = face32t(a.u[1], a.e[1], ut1, a.p, ay, j, P - sy, P, fg_pair32(flag[P - sy], fc), dt);
+            Wd = face32t(a.u[2], a.e[2], ut2, a.p, az, k, P - 1, P, fg_pair32(flag[P - 1], fc), dt);
+            if (own_vn) Vn = face32t(a.u[1], a.e[1], ut1, a.p, ay, j + 1, P, P + sy, fg_pair32(fc, flag[P + sy]), dt);
+            if (own_wu) Wu = face32t(a.u[2], a.e[2], ut2, a.p, az, k + 1, P, P + 1, fg_pair32(fc, flag[P + 1]), dt);
+        }
+        sVs[buf][ty][tx] = Vs;
+        const float wnext = __shfl_down_sync(0xffffffffu, Wd, 1);
+        __syncthreads();
+        if (!own_vn) Vn = sVs[buf][ty + 1][tx];
+        if (!own_wu) Wu = wnext;
+        buf ^= 1;
+        if (live) {
+            const double Uw64 = f2d_int(Uw), Ue64 = f2d_int(Ue), Vs64 = f2d_int(Vs), Vn64 = f2d_int(Vn);
+            const double Wd64 = f2d_int(Wd), Wu64 = f2d_int(Wu);
+            a.Us[0][P] = Uw64;
+            a.Us[1][P] = Vs64;
+            a.Us[2][P] = Wd64;
+            if (i == g.nx - 1) a.Us[0][P + sx] = Ue64;
+            if (j == g.ny - 1) a.Us[1][P + sy] = Vn64;
+            if (k == g.nz - 1) a.Us[2][P + 1] = Wu64;
+            double rhs = 0.0;
+            if (fc == FLUID && !(bc.p_singular && i == 0 && j == 0 && k == 0)) {
+                const double div = (Ue64 - Uw64) * ax64.rd[i + 2] + (Vn64 - Vs64) * ay64.rd[j + 2] +
+                                   (Wu64 - Wd64) * az64.rd[k + 2];
+                rhs = div * m2re * a.dinv[P];   // -div / (2 Re coeffsum)
+            }
+            a.b[P] = rhs;
+        }
+        Uw = Ue;
+        fc = fe;
+    }
+}
+
+// Outer rows of the Poisson right-hand side: the pressure-BC increments
+// p_bc(t + dt) - p_bc(t) (0 for constant values), over the outer-cell list.
+__global__ void __launch_bounds__(256)
+k_prhs_outer(const Grid g, const BCSet bc, const int *__restrict__ outer, const int nout, double *b) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nout) return;
+    const long long P = outer[t];
+    int i, j, k;
+    cijk_g(g, P, i, j, k);
+    int layer;
+    const int face = owner_face(g, i, j, k, layer);
+    const BCFace &F = bc.f[face];
+    double v = 0.0;
+    if (F.scur && (F.type == BCT_PRESSURE || F.type == BCT_VELPERIODIC)) {
+        const int q = 3 * F.nt + face_line(g, face, i, j, k);
+        v = F.snxt[q] - F.scur[q];
+    }
+    b[P] = v;
+}
+
+void launch_ustar_prhs32_tiled(cudaStream_t s, const Grid &g, const AxisF axf[3], const Axis ax64[3],
+                               const BCSet &bc, const uint8_t *flag, const Ustar32Args &a, float *ut, double dt,
+                               double Re, const int *outer, int nout) {
+    const long long nt = (long long)(g.nx + 2) * (g.ny + 2) * (g.nz + 2);
+    k_utilde32<<<(unsigned)std::min<long long>((nt + 255) / 256, 8 * K32_BLOCKS), 256, 0, s>>>(
+        g, axf[0], axf[1], axf[2], a, ut, (float)dt);
+    const int tk = (g.nz + UN_TK - 1) / UN_TK, tj = (g.ny + UN_TJ - 1) / UN_TJ, planes = UN_PLANES;
+    const int nb = tk * tj * ((g.nx + planes - 1) / planes);
+    k_ustar_faces32<<<nb, dim3(UN_TK, UN_TJ), 0, s>>>(g, axf[0], axf[1], axf[2], ax64[0], ax64[1], ax64[2], bc, flag, a,
+                                                      ut, (float)dt, -1.0 / (2.0 * Re), tk, tj, planes);
+    if (nout > 0) k_prhs_outer<<<(nout + 255) / 256, 256, 0, s>>>(g, bc, outer, nout, a.b);
+    note_launches(nout > 0 ? 3 : 2);
+}
+
+// ------------------------------------------------------------------------
+// update_next (src/ibm3d_fracstep.c:709-805) on tiles: each thread owns a
+// (j, k) column of a 32 x 8 tile and marches over the planes of i of its
+// tile.  The x face between cells i and i+1 is computed once and carried
+// to the next plane as its low face; the high y face of a cell is the low
+// y face of the thread at j+1 (shared memory, one barrier per plane); the
+// high z face is the low z face of the next lane (warp shuffle).  Tile-edge
+// threads compute their high faces themselves.  Per fluid cell that is 3
+// face updates on the FP64 pipe instead of 6.  F32: the increment form of
+// the FP32-stage step (the cell velocity takes the FP32 increment
+// e - dt G_c p'); otherwise the FP64 step.
+// ------------------------------------------------------------------------
+template <bool F32>
+__global__ void __launch_bounds__(UN_TK * UN_TJ)
+k_update_next_tiled(const Grid g, const Axis ax, const Axis ay, const Axis az, const DtAxis dx, const DtAxis dy,
+                    const DtAxis dz, const AxisF axf, const AxisF ayf, const AxisF azf, const BCSet bc,
+                    const uint8_t *__restrict__ flag, const NextArgs a64, const Next32Args a32, const double dt,
+                    const int tk, const int tj, const int planes, double *partials, unsigned int *counter,
+                    double *maxdiv_out) {
+    __shared__ double smem[32];
+    __shared__ double sVs[2][UN_TJ][UN_TK];
+    const double NaN = __longlong_as_double(0x7ff8000000000000LL);
+    int b = blockIdx.x;
+    const int bk = b % tk;
+    b /= tk;
+    const int bj = b % tj, bi = b / tj;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int k = bk * UN_TK + tx, j = bj * UN_TJ + ty;
+    const int i0 = bi * planes, i1 = min(i0 + planes, g.nx);
+    const bool live = j < g.ny && k < g.nz;
+    const bool own_vn = ty == UN_TJ - 1 || j == g.ny - 1;
+    const bool own_wu = tx == UN_TK - 1 || k == g.nz - 1;
+    const long long sx = g.sx, sy = g.sy;
+    const double *Us0 = F32 ? a32.Us[0] : a64.Us[0], *Us1 = F32 ? a32.Us[1] : a64.Us[1],
+                 *Us2 = F32 ? a32.Us[2] : a64.Us[2];
+    const double *pp = F32 ? a32.pp : a64.pp, *p = F32 ? a32.p : a64.p;
+    double *const *Un = F32 ? a32.Un : a64.Un;
+    double *const *un = F32 ? a32.un : a64.un;
+    double *pn = F32 ? a32.pn : a64.pn;
+    const int J = j + 2, K = k + 2;
+    double mdiv = 0.0;
+    long long P = live ? cidx(g, i0, j, k) : 0;
+    uint8_t fc = live ? flag[P] : (uint8_t)SOLID;
+    double ppc = live ? pp[P] : 0.0;
+    double Uw = NaN;
+    if (live && flag[P - sx] != SOLID && fc != SOLID) Uw = Us0[P] - dx.dtrdc[i0 + 2] * (ppc - pp[P - sx]);
+    int buf = 0;
+    for (int i = i0; i < i1; i++, P += sx) {
+        const int I = i + 2;
+        double Ue = NaN, Vs = NaN, Wd = NaN, Vn = NaN, Wu = NaN;
+        uint8_t fe = SOLID;
+        double ppe = 0.0;
+        if (live) {
+            fe = flag[P + sx];
+            ppe = pp[P + sx];
+            if (fc != SOLID && fe != SOLID) Ue = Us0[P + sx] - dx.dtrdc[I + 1] * (ppe - ppc);
+            if (fc != SOLID && flag[P - sy] != SOLID) Vs = Us1[P] - dy.dtrdc[J] * (ppc - pp[P - sy]);
+            if (fc != SOLID && flag[P - 1] != SOLID) Wd = Us2[P] - dz.dtrdc[K] * (ppc - pp[P - 1]);
+            if (own_vn && fc != SOLID && flag[P + sy] != SOLID) Vn = Us1[P + sy] - dy.dtrdc[J + 1] * (pp[P + sy] - ppc);
+            if (own_wu && fc != SOLID && flag[P + 1] != SOLID) Wu = Us2[P + 1] - dz.dtrdc[K + 1] * (pp[P + 1] - ppc);
+        }
+        sVs[buf][ty][tx] = Vs;
+        const double wnext = __shfl_down_sync(0xffffffffu, Wd, 1);
+        __syncthreads();
+        if (!own_vn) Vn = sVs[buf][ty + 1][tx];
+        if (!own_wu) Wu = wnext;
+        buf ^= 1;
+        if (live) {
+            Un[0][P] = Uw;
+            Un[1][P] = Vs;
+            Un[2][P] = Wd;
+            if (i == g.nx - 1) Un[0][P + sx] = Ue;
+            if (j == g.ny - 1) Un[1][P + sy] = Vn;
+            if (k == g.nz - 1) Un[2][P + 1] = Wu;
+            pn[P] = (fc == FLUID || fc == GHOST) ? p[P] + ppc : NaN;
+            if (fc == FLUID) {
+                const double ppw = pp[P - sx], pps = pp[P - sy], ppn = pp[P + sy], ppd = pp[P - 1], ppu = pp[P + 1];
+                if (F32) {
+                    const float gx = (d2f_int(ppe) - d2f_int(ppw)) * axf.rdcc[I];
+                    const float gy = (d2f_int(ppn) - d2f_int(pps)) * ayf.rdcc[J];
+                    const float gz = (d2f_int(ppu) - d2f_int(ppd)) * azf.rdcc[K];
+                    const float dtf = (float)dt;
+                    un[0][P] = a32.u[0][P] + f2d_int(a32.e[0][P] - dtf * gx);
+                    un[1][P] = a32.u[1][P] + f2d_int(a32.e[1][P] - dtf * gy);
+                    un[2][P] = a32.u[2][P] + f2d_int(a32.e[2][P] - dtf * gz);
+                } else {
+                    un[0][P] = a64.us[0][P] - dx.dtrdcc[I] * (ppe - ppw);
+                    un[1][P] = a64.us[1][P] - dy.dtrdcc[J] * (ppn - pps);
+                    un[2][P] = a64.us[2][P] - dz.dtrdcc[K] * (ppu - ppd);
+                }
+                if (!(bc.p_singular && i == 0 && j == 0 && k == 0)) {
+                    const double div = (Ue - Uw) * ax.rd[I] + (Vn - Vs) * ay.rd[J] + (Wu - Wd) * az.rd[K];
+                    mdiv = nanmax(mdiv, fabs(div));
+                }
+            } else if (fc == SOLID) {
+                un[0][P] = un[1][P] = un[2][P] = NaN;
+            }
+        }
+        Uw = Ue;
+        fc = fe;
+        ppc = ppe;
+    }
+    // Maximum over the block, then over the blocks (the last block to
+    // finish reduces every block's value in a fixed order).
+    const int t = ty * UN_TK + tx, lane = t & 31, warp = t >> 5;
+    double x = mdiv;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x = nanmax(x, __shfl_down_sync(0xffffffffu, x, o));
+    if (lane == 0) smem[warp] = x;
+    __syncthreads();
+    __shared__ bool last;
+    if (t == 0) {
+        double m = 0.0;
+        for (int w = 0; w < (UN_TK * UN_TJ) / 32; w++) m = nanmax(m, smem[w]);
+        partials[blockIdx.x] = m;
+        __threadfence();
+        last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double m = 0.0;
+    for (int q = t; q < (int)gridDim.x; q += UN_TK * UN_TJ) m = nanmax(m, __ldcg(partials + q));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = nanmax(m, __shfl_down_sync(0xffffffffu, m, o));
+    __syncthreads();
+    if (lane == 0) smem[warp] = m;
+    __syncthreads();
+    if (t == 0) {
+        double r = 0.0;
+        for (int w = 0; w < (UN_TK * UN_TJ) / 32; w++) r = nanmax(r, smem[w]);
+        *maxdiv_out = r;
         *counter = 0;
     }
 }
 
-void launch_update_next32(cudaStream_t s, const Grid &g, const Axis ax64[3], const AxisF axf[3], const BCSet &bc,
-                          const uint8_t *flag, const Next32Args &a, double dt, double *partials,
-                          unsigned int *counter, double *maxdiv_out, int nblocks) {
-    k_update_next32<<<nblocks, 256, 0, s>>>(g, ax64[0], ax64[1], ax64[2], axf[0], axf[1], axf[2], bc, flag, a, dt,
-                                            partials, counter, maxdiv_out);
+void launch_update_next_tiled(cudaStream_t s, const Grid &g, const Axis ax64[3], const DtAxis dta[3],
+                              const AxisF axf[3], const BCSet &bc, const uint8_t *flag, const NextArgs *a64,
+                              const Next32Args *a32, double dt, double *partials, unsigned int *counter,
+                              double *maxdiv_out) {
+    const int tk = (g.nz + UN_TK - 1) / UN_TK, tj = (g.ny + UN_TJ - 1) / UN_TJ;
+    // UN_PLANES planes per tile, more on grids whose tiles would outnumber
+    // the reduction's partials (8 x 4096).
+    int planes = UN_PLANES;
+    while ((long long)tk * tj * ((g.nx + planes - 1) / planes) > 8 * 4096) planes *= 2;
+    const int nb = tk * tj * ((g.nx + planes - 1) / planes);
+    const dim3 blk(UN_TK, UN_TJ);
+    if (a32)
+        k_update_next_tiled<true><<<nb, blk, 0, s>>>(g, ax64[0], ax64[1], ax64[2], dta[0], dta[1], dta[2], axf[0],
+                                                    axf[1], axf[2], bc, flag, NextArgs{}, *a32, dt, tk, tj, planes,
+                                                    partials, counter, maxdiv_out);
+    else
+        k_update_next_tiled<false><<<nb, blk, 0, s>>>(g, ax64[0], ax64[1], ax64[2], dta[0], dta[1], dta[2], axf[0],
+                                                     axf[1], axf[2], bc, flag, *a64, Next32Args{}, dt, tk, tj,
+                                                     planes, partials, counter, maxdiv_out);
     note_launches(1);
 }
 

@@ -249,71 +249,6 @@ void launch_ustar_prhs(cudaStream_t s, const Grid &g, const Axis &ax, const Axis
 }
 
 // ------------------------------------------------------------------------
-// update_next (src/ibm3d_fracstep.c:709-805) fused with the post-projection
-// divergence check max|div U^{n+1}| over fluid cells (pinned cell excluded).
-// ------------------------------------------------------------------------
-__global__ void __launch_bounds__(256)
-k_update_next(const Grid g, const Axis ax, const Axis ay, const Axis az, const BCSet bc,
-              const uint8_t *__restrict__ flag, NextArgs a, const double dt, double *partials,
-              unsigned int *counter, double *maxdiv_out) {
-    __shared__ double smem[32];
-    const long long n = (long long)g.nx * g.ny * g.nz;
-    double mdiv[1] = {0.0};
-    const double NaN = __longlong_as_double(0x7ff8000000000000LL);
-    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
-         q += (long long)gridDim.x * blockDim.x) {
-        int i, j, k;
-        ijk_interior(g, q, i, j, k);
-        const long long P = cidx(g, i, j, k);
-        const long long sx = g.sx, sy = g.sy;
-        const int I = i + 2, J = j + 2, K = k + 2;
-        const uint8_t fc = flag[P];
-        const double pp = a.pp[P];
-        a.pn[P] = (fc == FLUID || fc == GHOST) ? a.p[P] + pp : NaN;
-        if (fc == FLUID) {
-            a.un[0][P] = a.us[0][P] - dt * (a.pp[P + sx] - a.pp[P - sx]) * ax.rdcc[I];
-            a.un[1][P] = a.us[1][P] - dt * (a.pp[P + sy] - a.pp[P - sy]) * ay.rdcc[J];
-            a.un[2][P] = a.us[2][P] - dt * (a.pp[P + 1] - a.pp[P - 1]) * az.rdcc[K];
-        } else if (fc == SOLID) {
-            a.un[0][P] = a.un[1][P] = a.un[2][P] = NaN;
-        }
-        const uint8_t fw = flag[P - sx], fe = flag[P + sx], fs = flag[P - sy], fn = flag[P + sy];
-        const uint8_t fd = flag[P - 1], fu = flag[P + 1];
-        const double Uw = (fw != SOLID && fc != SOLID) ? a.Us[0][P] - dt * (pp - a.pp[P - sx]) * ax.rdc[I] : NaN;
-        const double Ue = (fc != SOLID && fe != SOLID) ? a.Us[0][P + sx] - dt * (a.pp[P + sx] - pp) * ax.rdc[I + 1] : NaN;
-        const double Vs = (fs != SOLID && fc != SOLID) ? a.Us[1][P] - dt * (pp - a.pp[P - sy]) * ay.rdc[J] : NaN;
-        const double Vn = (fc != SOLID && fn != SOLID) ? a.Us[1][P + sy] - dt * (a.pp[P + sy] - pp) * ay.rdc[J + 1] : NaN;
-        const double Wd = (fd != SOLID && fc != SOLID) ? a.Us[2][P] - dt * (pp - a.pp[P - 1]) * az.rdc[K] : NaN;
-        const double Wu = (fc != SOLID && fu != SOLID) ? a.Us[2][P + 1] - dt * (a.pp[P + 1] - pp) * az.rdc[K + 1] : NaN;
-        a.Un[0][P] = Uw;
-        a.Un[1][P] = Vs;
-        a.Un[2][P] = Wd;
-        if (i == g.nx - 1) a.Un[0][P + sx] = Ue;
-        if (j == g.ny - 1) a.Un[1][P + sy] = Vn;
-        if (k == g.nz - 1) a.Un[2][P + 1] = Wu;
-        if (fc == FLUID && !(bc.p_singular && i == 0 && j == 0 && k == 0)) {
-            const double div = (Ue - Uw) * ax.rd[I] + (Vn - Vs) * ay.rd[J] + (Wu - Wd) * az.rd[K];
-            mdiv[0] = nanmax(mdiv[0], fabs(div));
-        }
-    }
-    block_max<1>(mdiv, smem);
-    if (!publish_partials<1>(mdiv, partials, counter)) return;
-    double m[1];
-    reduce_partials<1, 0>(partials, gridDim.x, m, smem);
-    if (threadIdx.x == 0) {
-        *maxdiv_out = m[0];
-        *counter = 0;
-    }
-}
-
-void launch_update_next(cudaStream_t s, const Grid &g, const Axis &ax, const Axis &ay, const Axis &az,
-                        const BCSet &bc, const uint8_t *flag, const NextArgs &a, double dt, double *partials,
-                        unsigned int *counter, double *maxdiv_out, int nblocks) {
-    k_update_next<<<nblocks, 256, 0, s>>>(g, ax, ay, az, bc, flag, a, dt, partials, counter, maxdiv_out);
-    note_launches(1);
-}
-
-// ------------------------------------------------------------------------
 // update_outer (src/ibm3d_fracstep.c:855-1906): velocity and pressure
 // outer-layer fills.  Three launches keep the reference's face order
 // (x faces, then y faces reading the x-filled edges, then z faces).
