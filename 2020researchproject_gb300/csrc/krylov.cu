@@ -199,9 +199,10 @@ __device__ __forceinline__ void sweep_rows(const OpT<T> &A, const bool (&run)[NC
 }
 
 // The same with x holding an initial guess: r = r0 = b - A x, p = v = 0,
-// ||b||^2 (the relative test stays relative to b), ||r||^2 and the
-// divergence max of r; a guess that already passes the stopping test ends
-// the solve before its first iteration.
+// ||b||^2 (the relative test stays relative to b; to the initial residual
+// where b = 0, whose solution x = 0 a relative test to 0 would never
+// reach), ||r||^2 and the divergence max of r; a guess that already passes
+// the stopping test ends the solve before its first iteration.
 template <typename T, int NC>
 __global__ void __launch_bounds__(SW_THREADS)
 k_bicg_init_guess(const OpT<T> A, const int op, const long long n, const T *__restrict__ b, const T *__restrict__ x,
@@ -239,7 +240,7 @@ k_bicg_init_guess(const OpT<T> A, const int op, const long long n, const T *__re
         bool go = false;
         for (int c = 0; c < NC; c++) {
             KScal &s = sc[c];
-            s.bnorm2 = tot[c];
+            s.bnorm2 = tot[c] > 0.0 ? tot[c] : tot[NC + c];
             s.rnorm2 = tot[NC + c];
             s.rho = tot[NC + c];
             s.alpha = 1.0;
@@ -249,7 +250,7 @@ k_bicg_init_guess(const OpT<T> A, const int op, const long long n, const T *__re
             s.tol = tol;
             s.divtol = divtol;
             s.divmax = tot[2 * NC];
-            const bool done = tot[NC + c] == 0.0 || converged(tot[NC + c], tot[c], tot[2 * NC], tol, divtol);
+            const bool done = tot[NC + c] == 0.0 || converged(tot[NC + c], s.bnorm2, tot[2 * NC], tol, divtol);
             s.state = done ? KS_DONE : KS_RUN;
             go = go || !done;
         }

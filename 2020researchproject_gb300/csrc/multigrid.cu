@@ -312,63 +312,132 @@ static inline dim3 l3_block() { return dim3(L3_TK, L3_TJ, 1); }
 // uneven.  Tiles: coarse ranges [segj[b], segj[b+1]) x [segk[b], segk[b+1])
 // cut on the host so that each covers at most 8 fine rows and 32 fine
 // columns (as many as fit), ending on group boundaries.  A block takes one
-// tile of coarse plane I; its 32 x 8 threads each take one fine (j, k)
-// (coalesced rows along k), summed over the plane group in x, into shared
-// memory; then one thread per coarse cell adds up its one to four entries.
-// Grid (nsegk, nsegj, nx1).
+// tile of MG0_RPLANES consecutive coarse planes; its 32 x 8 threads each
+// take one fine (j, k) (coalesced rows along k) and, per coarse plane, sum
+// the one or two fine planes of its group into shared memory - in FP32 both
+// fine planes loaded before either is tested (a one-plane group reads its
+// plane twice and adds it once), every plane's loads in flight together;
+// the tile's tables read once; then one thread per coarse cell and plane
+// adds up its one to four entries.  Grid (nsegk, nsegj, ceil(nx1 /
+// MG0_RPLANES)).
+constexpr int MG0_RPLANES = 4;
+
 template <typename T>
 __global__ void __launch_bounds__(256)
 k_mg0_restrict_g(const OpT<T> c, const T *__restrict__ r, const T *__restrict__ z, MGLevel<T> L1,
                  const int *__restrict__ segj, const int *__restrict__ segk, const int *gate) {
     MG_GATE(gate);
-    __shared__ T part[8][33];
+    __shared__ T part[MG0_RPLANES][8][33];
     const Grid &g = c.g;
-    const int I = blockIdx.z;
     const int J0 = segj[blockIdx.y], J1 = segj[blockIdx.y + 1];
     const int K0 = segk[blockIdx.x], K1 = segk[blockIdx.x + 1];
     const int jb = L1.ch[1][J0], je = L1.ch[1][J1];
     const int kb = L1.ch[2][K0], ke = L1.ch[2][K1];
-    const int j = jb + threadIdx.y, k = kb + threadIdx.x;
-    T acc = 0;
-    if (j < je && k < ke) {
-        const int Jj = j + 2, Kk = k + 2;
-        const T vyz = c.d[1][Jj] * c.d[2][Kk];
-        const T kyz = c.ks[1][Jj] + c.ks[2][Kk];
-        const T kmy = c.km[1][Jj], kpy = c.kp[1][Jj], kmz = c.km[2][Kk], kpz = c.kp[2][Kk];
-        const int i0 = L1.ch[0][I], i1 = L1.ch[0][I + 1];
-        for (int i = i0; i < i1; i++) {
+    const bool live = (int)threadIdx.y < je - jb && (int)threadIdx.x < ke - kb;
+    const int j = live ? jb + threadIdx.y : jb, k = live ? kb + threadIdx.x : kb;
+    const int Jj = j + 2, Kk = k + 2;
+    const T vyz = c.d[1][Jj] * c.d[2][Kk];
+    const T kyz = c.ks[1][Jj] + c.ks[2][Kk];
+    const T kmy = c.km[1][Jj], kpy = c.kp[1][Jj], kmz = c.km[2][Kk], kpz = c.kp[2][Kk];
+    const int Ib = blockIdx.z * MG0_RPLANES;
+#pragma unroll
+    for (int q = 0; q < MG0_RPLANES; q++) {
+        const int I = min(Ib + q, L1.nx - 1);
+        const int i0 = L1.ch[0][I], two = L1.ch[0][I + 1] - i0 > 1;
+        T res[2] = {0, 0}, w[2] = {0, 0};
+        bool use[2];
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int i = i0 + (h & two);
             const long long P = cidx(g, i, j, k);
-            if (c.flag[P] != FLUID || (c.p_singular && P == c.pinned)) continue;
             const int Ii = i + 2;
-            const T nb = c.km[0][Ii] * z[P - g.sx] + c.kp[0][Ii] * z[P + g.sx] + kmy * z[P - g.sy] +
-                         kpy * z[P + g.sy] + kmz * z[P - 1] + kpz * z[P + 1];
-            const T res = r[P] - (z[P] - c.dinv[P] * nb);
-            acc += c.d[0][Ii] * vyz * (c.ks[0][Ii] + kyz) * res;
+            use[h] = live && (h == 0 || two) && c.flag[P] == FLUID && !(c.p_singular && P == c.pinned);
+            // FP64 rows are computed only where used: the FP64 pipe, not
+            // the latency, bounds that form.
+            if (sizeof(T) == 4 || use[h]) {
+                const T nb = c.km[0][Ii] * z[P - g.sx] + c.kp[0][Ii] * z[P + g.sx] + kmy * z[P - g.sy] +
+                             kpy * z[P + g.sy] + kmz * z[P - 1] + kpz * z[P + 1];
+                res[h] = r[P] - (z[P] - c.dinv[P] * nb);
+                w[h] = c.d[0][Ii] * vyz * (c.ks[0][Ii] + kyz);
+            }
         }
+        T acc = 0;
+#pragma unroll
+        for (int h = 0; h < 2; h++) acc = use[h] ? acc + w[h] * res[h] : acc;
+        part[q][threadIdx.y][threadIdx.x] = acc;
     }
-    part[threadIdx.y][threadIdx.x] = acc;
     __syncthreads();
-    const int t = threadIdx.y * 32 + threadIdx.x, nk = K1 - K0;
-    if (t >= (J1 - J0) * nk) return;
-    const int J = J0 + t / nk, K = K0 + t % nk;
-    const int ja = L1.ch[1][J] - jb, jz = L1.ch[1][J + 1] - jb;
-    const int ka = L1.ch[2][K] - kb, kz = L1.ch[2][K + 1] - kb;
-    T sum = 0;
-    for (int y = ja; y < jz; y++)
-        for (int x = ka; x < kz; x++) sum += part[y][x];
-    L1.R[lidx(L1, I, J, K)] = sum;
+    const int nk = K1 - K0, ncell = (J1 - J0) * nk;
+    for (int t = threadIdx.y * 32 + threadIdx.x; t < MG0_RPLANES * ncell; t += 256) {
+        const int q = t / ncell, e = t - q * ncell;
+        const int I = Ib + q;
+        if (I >= L1.nx) break;
+        const int J = J0 + e / nk, K = K0 + e % nk;
+        const int ja = L1.ch[1][J] - jb, jz = L1.ch[1][J + 1] - jb;
+        const int ka = L1.ch[2][K] - kb, kz = L1.ch[2][K + 1] - kb;
+        T sum = 0;
+        for (int y = ja; y < jz; y++)
+            for (int x = ka; x < kz; x++) sum += part[q][y][x];
+        L1.R[lidx(L1, I, J, K)] = sum;
+    }
 }
+
+// Prolongation into the fine grid from a level 1 of uneven groups: each
+// thread takes one fine (j, k) on MG0_PPLANES consecutive planes, reads its
+// j and k transfer tables once, addresses coarse cells in 32-bit
+// arithmetic (a level has fewer than 2^31 cells) and issues every load
+// (flags, z, the x tables, the coarse values) before any store; a cell that
+// takes no correction stores z back.  Same arithmetic as prolong_value.
+// Grid (ceil(nz/32), ceil(ny/8), ceil(nx/MG0_PPLANES)) of 32 x 8 threads.
+constexpr int MG0_PPLANES = 4;
 
 template <typename T>
 __global__ void __launch_bounds__(256)
-k_mg0_prolong(const OpT<T> c, T *z, const MGLevel<T> L1, const int *gate) {
+k_mg0_prolong(const OpT<T> c, T *z, const MGLevel<T> C, const int *gate) {
     MG_GATE(gate);
-    L3_INDEX(i, j, k, c.g.ny, c.g.nz);
-    const long long P = cidx(c.g, i, j, k);
-    const uint8_t fl = c.flag[P];
-    if (fl != FLUID && fl != GHOST) return;
-    if (c.p_singular && P == c.pinned) return;
-    z[P] += prolong_value(L1, i, j, k);
+    const Grid &g = c.g;
+    const int k = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 8 + threadIdx.y;
+    if (k >= g.nz || j >= g.ny) return;
+    const int cny = C.ny, cnz = C.nz;
+    const int ys[2] = {C.pa[1][j], C.po[1][j]}, zs[2] = {C.pa[2][k], C.po[2][k]};
+    const T wy = C.pw[1][j], wz = C.pw[2][k];
+    const T wys[2] = {wy, (T)1 - wy}, wzs[2] = {wz, (T)1 - wz};
+    const int i0 = blockIdx.z * MG0_PPLANES;
+    long long Ps[MG0_PPLANES];
+    T out[MG0_PPLANES];
+#pragma unroll
+    for (int p = 0; p < MG0_PPLANES; p++) {
+        const int i = min(i0 + p, g.nx - 1);
+        const long long P = cidx(g, i, j, k);
+        const uint8_t fl = c.flag[P];
+        const T zp = z[P];
+        const int xs[2] = {C.pa[0][i], C.po[0][i]};
+        const T wx = C.pw[0][i];
+        const T wxs[2] = {wx, (T)1 - wx};
+        T v[2][2][2];
+        bool act[2][2][2];
+#pragma unroll
+        for (int a = 0; a < 2; a++)
+#pragma unroll
+            for (int b = 0; b < 2; b++)
+#pragma unroll
+                for (int cc = 0; cc < 2; cc++) {
+                    v[a][b][cc] = 0;
+                    act[a][b][cc] = false;
+                    if (xs[a] < 0 || ys[b] < 0 || zs[cc] < 0) continue;
+                    const int q = (xs[a] * cny + ys[b]) * cnz + zs[cc];
+                    v[a][b][cc] = C.Z[q];
+                    act[a][b][cc] = active_bits(C.diag[q]);
+                }
+        const bool take = (fl == FLUID || fl == GHOST) && !(c.p_singular && P == c.pinned);
+        // As in the restriction: the FP64 blend only where it is used.
+        const T corr = sizeof(T) == 4 || take ? trilinear(v, act, wxs, wys, wzs) : (T)0;
+        out[p] = take ? zp + corr : zp;
+        Ps[p] = P;
+    }
+#pragma unroll
+    for (int p = 0; p < MG0_PPLANES; p++)
+        if (i0 + p < g.nx) z[Ps[p]] = out[p];
 }
 
 // Restriction when level 1 halves every axis: one thread per fine (j, k)
@@ -844,17 +913,44 @@ k_mg_tail(const TailDesc<T> d, const uint4 *__restrict__ img, const int nu1, con
         }
         return p;
     };
-    // Colour passes of a level; a level of at most 32 cells runs in warp 0
-    // alone, its passes separated by warp barriers, and one block barrier
-    // after the last.
+    // Colour passes of a level.  With two colours thread t takes (k, k+1)
+    // pair t of the level and relaxes its cell of the pass's colour (half
+    // the warps of one cell per thread, and no lane idles on the other
+    // colour), through the branch-free relaxation on levels without
+    // periodic axes; with four, cell t and a colour test.  Work of at most
+    // 32 threads runs in warp 0 alone, its passes separated by warp
+    // barriers, and one block barrier after the last.
+    const bool open = !per.p[0] && !per.p[1] && !per.p[2];
     auto sweep = [&](const MGLevel<T> &L, int nsw) {
-        const Pos p = pos(L);
         const int ncol = level_colors(L, per.p);
-        if (L.n <= 32) {
+        const bool pairs = ncol == 2;
+        const int nzw = pairs ? (L.nz + 1) / 2 : L.nz;
+        const int items = L.nx * L.ny * nzw;
+        int I = 0, J = 0, kw = 0, cc = -1;
+        if (tid < items) {
+            const int nyz = L.ny * nzw;
+            I = tid / nyz;
+            const int rem = tid - I * nyz;
+            J = rem / nzw;
+            kw = rem - J * nzw;
+            if (!pairs) cc = cell_color(I, J, kw, L.nx, L.ny, L.nz, per.p);
+        }
+        auto pass = [&](int col) {
+            if (tid >= items) return;
+            if (pairs) {
+                const int K = 2 * kw + ((I + J + col) & 1);
+                if (K >= L.nz) return;
+                if (open) coarse_relax_open(L, I, J, K);
+                else coarse_relax(L, I, J, K, per.p);
+            } else if (cc == col) {
+                coarse_relax(L, I, J, kw, per.p);
+            }
+        };
+        if (items <= 32) {
             if (tid < 32)
                 for (int s = 0; s < nsw; s++)
                     for (int col = 0; col < ncol; col++) {
-                        if (p.col == col) coarse_relax(L, p.I, p.J, p.K, per.p);
+                        pass(col);
                         __syncwarp();
                     }
             __syncthreads();
@@ -862,7 +958,7 @@ k_mg_tail(const TailDesc<T> d, const uint4 *__restrict__ img, const int nu1, con
         }
         for (int s = 0; s < nsw; s++)
             for (int col = 0; col < ncol; col++) {
-                if (p.col == col) coarse_relax(L, p.I, p.J, p.K, per.p);
+                pass(col);
                 __syncthreads();
             }
     };
@@ -1351,18 +1447,22 @@ void GMG<T>::apply(cudaStream_t s, const T *r, T *z, const int *gate) {
     auto te = [&](int t) {
         if (prof_) prof_->end(t);
     };
+    if (cfg_.nu_pre == 0) {   // no pre-smoothing: the cycle restricts r itself (z = 0)
+        launch_pdl(k_fill0<T>, nblk(g.ncell, 256), 256, 0, s, z, (long long)g.ncell, gate);
+        k++;
+    }
     k += smooth0(s, r, z, cfg_.nu_pre, true, gate);
     const MGLevel<T> &L1 = levels_[0];
     int tp = tb("mg0_restrict");
     if (L1.cx && L1.cy && L1.cz)
         launch_pdl(k_mg0_restrict2<T>, dim3((g.nz + 31) / 32, (g.ny + 7) / 8, L1.nx), dim3(32, 8), 0, s, A_, r, z, L1, gate);
     else
-        launch_pdl(k_mg0_restrict_g<T>, dim3(nsegk_, nsegj_, L1.nx), dim3(32, 8), 0, s, A_, r, z, L1,
+        launch_pdl(k_mg0_restrict_g<T>, dim3(nsegk_, nsegj_, (L1.nx + MG0_RPLANES - 1) / MG0_RPLANES), dim3(32, 8), 0, s,
+                   A_, r, z, L1,
                    (const int *)segj_, (const int *)segk_, gate);
     k++;
     te(tp);
     tp = tb("mgc_down");
-    const int nl = (int)levels_.size();
     for (int l = 0; l < tail_; l++) {
         MGLevel<T> &L = levels_[l];
         const MGLevel<T> &C = levels_[l + 1];
@@ -1404,7 +1504,8 @@ void GMG<T>::apply(cudaStream_t s, const T *r, T *z, const int *gate) {
     if (L1.cx && L1.cy && L1.cz)
         launch_pdl(k_mg0_prolong2<T>, l3_grid(g.nx, g.ny, g.nz), l3_block(), 0, s, A_, z, L1, gate);
     else
-        launch_pdl(k_mg0_prolong<T>, l3_grid(g.nx, g.ny, g.nz), l3_block(), 0, s, A_, z, L1, gate);
+        launch_pdl(k_mg0_prolong<T>, dim3((g.nz + 31) / 32, (g.ny + 7) / 8, (g.nx + MG0_PPLANES - 1) / MG0_PPLANES),
+                   dim3(32, 8), 0, s, A_, z, L1, gate);
     k++;
     te(tp);
     k += smooth0(s, r, z, cfg_.nu_post, false, gate);

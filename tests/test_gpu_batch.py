@@ -25,12 +25,12 @@ def _same(a, b):
 
 
 @pytest.mark.parametrize("combined", [True, False])
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed32"])
 def test_batch_members_equal_solo_runs(precision, combined):
     ibm = package()
     names = ["cavity", "sphere", "channel_les", "mixed_box", "func_sphere"]
     cases = [load_golden(n) for n in names]
-    mode = ibm.MIXED if precision == "mixed" else ibm.FP64
+    mode = {"mixed": ibm.MIXED, "mixed32": ibm.MIXED32, "fp64": ibm.FP64}[precision]
 
     solo = []
     for c in cases:

@@ -63,10 +63,11 @@ def test_export_matches_oracle(ibm, tmp_path, name):
     assert np.isfinite(vort).sum() > 0
 
 
-@pytest.mark.parametrize("precision", ["FP64", "MIXED_MG", "MIXED"])
+@pytest.mark.parametrize("precision", ["FP64", "MIXED_MG", "MIXED", "MIXED32"])
 def test_exact_resume_from_state_file(ibm, tmp_path, precision):
     """The mixed modes' warm starts read the last pressure increment: it is
-    part of the state, so a resumed run still continues bit for bit."""
+    part of the state, so a resumed run still continues bit for bit (the
+    FP32-stage step's momentum increment starts from zero in every step)."""
     case = load_golden("sphere")
     a = build_case(ibm, case, tol=1e-8)
     a.set_precision(getattr(ibm, precision))

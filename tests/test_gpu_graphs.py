@@ -67,20 +67,21 @@ def test_graph_equals_host_loop_other_solvers(ibm, solver, precision):
             assert a[k] == b[k], f"{k}: {a[k]} != {b[k]}"
 
 
-def test_autotune_leaves_the_run_unchanged(ibm):
+@pytest.mark.parametrize("precision", ["MIXED", "MIXED32"])
+def test_autotune_leaves_the_run_unchanged(ibm, precision):
     """The autotuner times candidate sweep settings from the current state
     and restores it: a run continued after tuning equals the same run with
     the chosen setting and no tuning."""
     case = load_golden("sphere")
     a = build_case(ibm, case, tol=1e-8)
-    a.set_precision(ibm.MIXED)
+    a.set_precision(getattr(ibm, precision))
     a.iterate(1)
     ms, best = a.autotune(steps=1)
     assert ms > 0 and len(best) == 5
     assert a.stats()["iter"] == 1
     a.iterate(2)
     b = build_case(ibm, case, tol=1e-8)
-    b.set_precision(ibm.MIXED)
+    b.set_precision(getattr(ibm, precision))
     b.iterate(1)
     b.set_multigrid(*best, 1.0)
     b.iterate(2)
