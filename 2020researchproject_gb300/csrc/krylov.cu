@@ -816,14 +816,14 @@ __global__ void __launch_bounds__(KTHREADS)
 k_narrow(const long long n, const double *__restrict__ r, float *r32, const int *gate) {
     pdl_enter();
     if (gate && *gate != KS_RUN) return;
-    GRID_STRIDE(P, n) r32[P] = (float)r[P];
+    GRID_STRIDE(P, n) r32[P] = d2f_int(r[P]);   // on the integer pipe: conversions run at the FP64 rate
 }
 
 __global__ void __launch_bounds__(KTHREADS)
 k_widen(const long long n, const float *__restrict__ z32, double *z, const int *gate) {
     pdl_enter();
     if (gate && *gate != KS_RUN) return;
-    GRID_STRIDE(P, n) z[P] = (double)z32[P];
+    GRID_STRIDE(P, n) z[P] = f2d_int(z32[P]);
 }
 
 int WidenedPreconditioner::allocate(long long ncell, Preconditioner<float> *m) {
@@ -847,10 +847,14 @@ void WidenedPreconditioner::release() {
 }
 
 void WidenedPreconditioner::apply(cudaStream_t s, const double *r, double *z, const int *gate) {
-    launch_pdl(k_narrow, nblk, KTHREADS, 0, s, n, r, r32, gate);
-    m32->apply(s, r32, z32, gate);
+    fused_narrow = m32->apply_from64(s, r, z32, gate);
+    if (!fused_narrow) {
+        launch_pdl(k_narrow, nblk, KTHREADS, 0, s, n, r, r32, gate);
+        note_launches(1);
+        m32->apply(s, r32, z32, gate);
+    }
     launch_pdl(k_widen, nblk, KTHREADS, 0, s, n, z32, z, gate);
-    note_launches(2);
+    note_launches(1);
 }
 
 static void launch_update(cudaStream_t st, IRWork &w, double *x) {

@@ -86,6 +86,9 @@ template <typename T>
 struct Preconditioner {
     virtual ~Preconditioner() {}
     virtual void apply(cudaStream_t s, const T *r, T *z, const int *gate) = 0;
+    // The same from an FP64 r, rounded to T inside the application (one
+    // pass fewer than rounding first); false: not available, nothing ran.
+    virtual bool apply_from64(cudaStream_t, const double *, T *, const int *) { return false; }
     // Kernels one application launches.
     virtual int launches() const = 0;
 };
@@ -103,7 +106,8 @@ struct WidenedPreconditioner : Preconditioner<double> {
     int allocate(long long ncell, Preconditioner<float> *m);
     void release();
     void apply(cudaStream_t s, const double *r, double *z, const int *gate) override;
-    int launches() const override { return m32->launches() + 2; }
+    int launches() const override { return m32->launches() + (fused_narrow ? 1 : 2); }
+    bool fused_narrow = false;   // the last application rounded r inside m32
 };
 
 template <typename T>

@@ -126,9 +126,9 @@ __device__ inline T prolong_value(const MGLevel<T> &C, int i, int j, int k) {
 // sweep over all cells then covers the whole array).
 constexpr int MG0_PLANES = 2;
 
-template <typename T>
+template <typename T, bool SPLIT>
 __global__ void __launch_bounds__(256)
-k_mg0_color(const OpT<T> c, const T *__restrict__ r, T *__restrict__ z, const int color, const int pairs,
+k_mg0_color(const OpT<T> c, const FineRows<T> fr, T *__restrict__ z, const int color, const int pairs,
             const Per3 per, const T omega, const int *gate) {
     MG_GATE(gate);
     const Grid &g = c.g;
@@ -156,9 +156,9 @@ k_mg0_color(const OpT<T> c, const T *__restrict__ r, T *__restrict__ z, const in
         }
         ok = ok && k < g.nz;
         k = min(k, g.nz - 1);
-        const long long P = cidx(g, i, jj, k);
-        const uint8_t fl = c.flag[P];
-        const T rv = r[P], dv = c.dinv[P];
+        const long long P = cidx(g, i, jj, k), q = SPLIT ? fr.split_index(i, jj, k) : P;
+        const uint8_t fl = fr.flag[q];
+        const T rv = fr.r[q], dv = fr.dinv[q];
         const T zw = z[P - sx], ze = z[P + sx], zs = z[P - sy], zn = z[P + sy], zd = z[P - 1], zu = z[P + 1];
         const T zc = z[P];
         const int I = i + 2, K = k + 2;
@@ -177,22 +177,79 @@ k_mg0_color(const OpT<T> c, const T *__restrict__ r, T *__restrict__ z, const in
 // The first colour pass of a V-cycle on z = 0, as one pass over the whole
 // padded array: colour-0 interior rows take r (r + dinv * 0, and r for
 // solid and pinned rows), every other cell 0.  A 3-D launch over the
-// padded box (threads along k, no index division): grid
-// (ceil((nz+4)/32), ceil((ny+4)/8), nx+4).
-template <typename T>
+// padded box (threads along k, no index division), each thread on
+// MG0_IPLANES consecutive planes: grid (ceil((nz+4)/32), ceil((ny+4)/8),
+// ceil((nx+4)/MG0_IPLANES)).
+constexpr int MG0_IPLANES = 4;
+
+template <typename T, bool SPLIT>
 __global__ void __launch_bounds__(256)
-k_mg0_init3(const OpT<T> c, const T *__restrict__ r, T *__restrict__ z, const Per3 per, const int *gate) {
+k_mg0_init3(const OpT<T> c, const FineRows<T> fr, T *__restrict__ z, const Per3 per, const int *gate) {
     MG_GATE(gate);
     const Grid &g = c.g;
-    const int K = blockIdx.x * 32 + threadIdx.x, J = blockIdx.y * 8 + threadIdx.y, I = blockIdx.z;
+    const int K = blockIdx.x * 32 + threadIdx.x, J = blockIdx.y * 8 + threadIdx.y;
     if (K >= g.nz + 4 || J >= g.ny + 4) return;
-    const int i = I - 2, j = J - 2, k = K - 2;
-    const long long P = (long long)I * g.sx + (long long)J * g.sy + K;
-    T v = 0;
-    if (i >= 0 && i < g.nx && j >= 0 && j < g.ny && k >= 0 && k < g.nz &&
-        cell_color(i, j, k, g.nx, g.ny, g.nz, per.p) == 0 && c.flag[P] != GHOST)
-        v = r[P];
-    z[P] = v;
+    const int j = J - 2, k = K - 2;
+    const bool jk = j >= 0 && j < g.ny && k >= 0 && k < g.nz;
+#pragma unroll
+    for (int q = 0; q < MG0_IPLANES; q++) {
+        const int I = blockIdx.z * MG0_IPLANES + q, i = I - 2;
+        if (I >= g.nx + 4) break;
+        const long long P = (long long)I * g.sx + (long long)J * g.sy + K;
+        T v = 0;
+        if (jk && i >= 0 && i < g.nx && cell_color(i, j, k, g.nx, g.ny, g.nz, per.p) == 0 && c.flag[P] != GHOST)
+            v = fr.r[SPLIT ? fr.split_index(i, j, k) : P];
+        z[P] = v;
+    }
+}
+
+// A padded natural array into the colour-split layout of FineRows (at
+// set-up: 1/coeffsum and the flags).  3-D launch over the padded box: grid
+// (ceil(NZ/32), ceil(NY/8), NX) of 32 x 8 threads.
+template <typename D, typename S>
+__global__ void __launch_bounds__(256)
+k_to_split(const S *__restrict__ a, D *__restrict__ b, const int NY, const int NZ, const int NZH, const long long H,
+           const int *gate) {
+    MG_GATE(gate);
+    const int K = blockIdx.x * 32 + threadIdx.x, J = blockIdx.y * 8 + threadIdx.y, I = blockIdx.z;
+    if (K >= NZ || J >= NY) return;
+    const long long row = (long long)I * NY + J;
+    b[((I + J + K) & 1) * H + row * NZH + (K >> 1)] = (D)a[row * NZ + K];
+}
+
+// The right-hand side of an FP32 cycle (FP64, or FP32 from an FP32 solve)
+// into the colour-split layout: each thread takes one (K, K+1) pair of a
+// padded row on MG0_NPLANES consecutive planes; its two values go to the
+// two colour halves at the same position (coalesced reads and writes), an
+// FP64 value rounded on the integer pipe (d2f_int: FP64 <-> FP32
+// conversions issue at the FP64 rate on this part).  Grid (ceil(NZH/32),
+// ceil(NY/8), ceil(NX/MG0_NPLANES)).
+constexpr int MG0_NPLANES = 4;
+
+__device__ __forceinline__ float to32(double x) { return d2f_int(x); }
+__device__ __forceinline__ float to32(float x) { return x; }
+
+template <typename S>
+__global__ void __launch_bounds__(256)
+k_narrow_split(const S *__restrict__ r, float *__restrict__ rs, const int NX, const int NY, const int NZ,
+               const int NZH, const long long H, const int *gate) {
+    MG_GATE(gate);
+    const int kp = blockIdx.x * 32 + threadIdx.x, J = blockIdx.y * 8 + threadIdx.y;
+    if (kp >= NZH || J >= NY) return;
+    const int K = 2 * kp;
+    const bool two = K + 1 < NZ;
+    const int I0 = blockIdx.z * MG0_NPLANES;
+#pragma unroll
+    for (int p = 0; p < MG0_NPLANES; p++) {
+        const int I = I0 + p;
+        if (I >= NX) break;
+        const long long row = (long long)I * NY + J;
+        const S a = r[row * NZ + K];
+        const S b = two ? r[row * NZ + K + 1] : (S)0;
+        const long long c = (I + J) & 1;   // colour of the even K
+        rs[c * H + row * NZH + kp] = to32(a);
+        if (two) rs[(1 - c) * H + row * NZH + kp] = to32(b);
+    }
 }
 
 // Ghost rows of the smoother, Jacobi-style among ghosts (each reads the
@@ -206,7 +263,7 @@ k_mg0_init3(const OpT<T> c, const T *__restrict__ r, T *__restrict__ z, const Pe
 // leaves a slowly converging error that doubled the Krylov iterations.
 
 template <typename T>
-__device__ __forceinline__ T ghost_value(const OpT<T> &c, const T *__restrict__ r, const T *__restrict__ z, int P,
+__device__ __forceinline__ T ghost_value(const OpT<T> &c, const T rP, const T *__restrict__ z, int P,
                                          const T *__restrict__ gidiv) {
     const int id = c.gid[P];
     T sum = 0;
@@ -215,7 +272,7 @@ __device__ __forceinline__ T ghost_value(const OpT<T> &c, const T *__restrict__ 
         if (q >= 0) sum += c.gw[8 * id + e] * z[q];
     }
     const T zp = z[P];
-    return zp + (r[P] + sum - ((T)1 - c.gwself[id]) * zp) * gidiv[id];
+    return zp + (rP + sum - ((T)1 - c.gwself[id]) * zp) * gidiv[id];
 }
 
 template <typename T>
@@ -234,7 +291,7 @@ __global__ void k_mg0_ghost_scatter(const int *__restrict__ gcell, const int ng,
 // interior values alone: one launch, no ordering between outer cells, and
 // no thread reads an outer value another thread writes.
 template <typename T>
-__device__ __forceinline__ T outer_chain_value(const OpT<T> &c, const T *__restrict__ r, const T *z, long long P0) {
+__device__ __forceinline__ T outer_chain_value(const OpT<T> &c, const FineRows<T> &fr, const T *z, long long P0) {
     long long chain[4];
     int face[4], layer[4];
     int n = 0;
@@ -248,7 +305,7 @@ __device__ __forceinline__ T outer_chain_value(const OpT<T> &c, const T *__restr
             v = z[Q];
             break;
         }
-        chain[n] = Q;
+        chain[n] = fr.at(Q, i, j, k);
         face[n] = f;
         layer[n] = L;
         n++;
@@ -263,11 +320,11 @@ __device__ __forceinline__ T outer_chain_value(const OpT<T> &c, const T *__restr
     }
     for (int q = n - 1; q >= 0; q--) {
         const BCRow<T> &F = c.bc[face[q]];
-        const long long P = chain[q];
+        const T rv = fr.r[chain[q]];
         switch (F.type) {
         case BCT_PRESSURE:
-        case BCT_VELPERIODIC: v = (r[P] - F.dir_m[layer[q] - 1] * v) / F.dir_o[layer[q] - 1]; break;
-        default: v = r[P] + v; break;
+        case BCT_VELPERIODIC: v = (rv - F.dir_m[layer[q] - 1] * v) / F.dir_o[layer[q] - 1]; break;
+        default: v = rv + v; break;
         }
     }
     return v;
@@ -280,18 +337,18 @@ __device__ __forceinline__ T outer_chain_value(const OpT<T> &c, const T *__restr
 // ghost values reach z in the following scatter launch.
 template <typename T>
 __global__ void __launch_bounds__(256)
-k_mg0_outer(const OpT<T> c, const T *__restrict__ r, T *z, const int *__restrict__ outer, const int nout,
-            const int *__restrict__ gcell, const int ng, const int gblocks, T *tmp, const T *__restrict__ gidiv,
-            const int *gate) {
+k_mg0_outer(const OpT<T> c, const FineRows<T> fr, T *z, const int *__restrict__ outer, const int nout,
+            const int *__restrict__ gcell, const long long *__restrict__ grow, const int ng, const int gblocks, T *tmp,
+            const T *__restrict__ gidiv, const int *gate) {
     MG_GATE(gate);
     if ((int)blockIdx.x < gblocks) {
         const int g = blockIdx.x * blockDim.x + threadIdx.x;
-        if (g < ng) tmp[g] = ghost_value(c, r, z, gcell[g], gidiv);
+        if (g < ng) tmp[g] = ghost_value(c, fr.r[grow[g]], z, gcell[g], gidiv);
         return;
     }
     const int t = (blockIdx.x - gblocks) * blockDim.x + threadIdx.x;
     if (t >= nout) return;
-    z[outer[t]] = outer_chain_value(c, r, z, outer[t]);
+    z[outer[t]] = outer_chain_value(c, fr, z, outer[t]);
 }
 
 // 3-D launch over an (nx, ny, nz) box: threads along k, blocks along
@@ -322,9 +379,9 @@ static inline dim3 l3_block() { return dim3(L3_TK, L3_TJ, 1); }
 // MG0_RPLANES)).
 constexpr int MG0_RPLANES = 4;
 
-template <typename T>
+template <typename T, bool SPLIT>
 __global__ void __launch_bounds__(256)
-k_mg0_restrict_g(const OpT<T> c, const T *__restrict__ r, const T *__restrict__ z, MGLevel<T> L1,
+k_mg0_restrict_g(const OpT<T> c, const FineRows<T> fr, const T *__restrict__ z, MGLevel<T> L1,
                  const int *__restrict__ segj, const int *__restrict__ segk, const int *gate) {
     MG_GATE(gate);
     __shared__ T part[MG0_RPLANES][8][33];
@@ -349,15 +406,15 @@ k_mg0_restrict_g(const OpT<T> c, const T *__restrict__ r, const T *__restrict__ 
 #pragma unroll
         for (int h = 0; h < 2; h++) {
             const int i = i0 + (h & two);
-            const long long P = cidx(g, i, j, k);
+            const long long P = cidx(g, i, j, k), q = SPLIT ? fr.split_index(i, j, k) : P;
             const int Ii = i + 2;
-            use[h] = live && (h == 0 || two) && c.flag[P] == FLUID && !(c.p_singular && P == c.pinned);
+            use[h] = live && (h == 0 || two) && fr.flag[q] == FLUID && !(c.p_singular && P == c.pinned);
             // FP64 rows are computed only where used: the FP64 pipe, not
             // the latency, bounds that form.
             if (sizeof(T) == 4 || use[h]) {
                 const T nb = c.km[0][Ii] * z[P - g.sx] + c.kp[0][Ii] * z[P + g.sx] + kmy * z[P - g.sy] +
                              kpy * z[P + g.sy] + kmz * z[P - 1] + kpz * z[P + 1];
-                res[h] = r[P] - (z[P] - c.dinv[P] * nb);
+                res[h] = fr.r[q] - (z[P] - fr.dinv[q] * nb);
                 w[h] = c.d[0][Ii] * vyz * (c.ks[0][Ii] + kyz);
             }
         }
@@ -445,9 +502,9 @@ k_mg0_prolong(const OpT<T> c, T *z, const MGLevel<T> C, const int *gate) {
 // lane shuffle and the j pair through shared memory, so every load is a
 // coalesced row and the whole fine grid is in flight at once.  Grid
 // (ceil(nz/32), ceil(ny/8), L1.nx) of 32 x 8 threads.
-template <typename T>
+template <typename T, bool SPLIT>
 __global__ void __launch_bounds__(256)
-k_mg0_restrict2(const OpT<T> c, const T *__restrict__ r, const T *__restrict__ z, MGLevel<T> L1, const int *gate) {
+k_mg0_restrict2(const OpT<T> c, const FineRows<T> fr, const T *__restrict__ z, MGLevel<T> L1, const int *gate) {
     MG_GATE(gate);
     __shared__ T part[8][33];
     const Grid &g = c.g;
@@ -462,12 +519,12 @@ k_mg0_restrict2(const OpT<T> c, const T *__restrict__ r, const T *__restrict__ z
         for (int h = 0; h < 2; h++) {
             const int i = 2 * I + h;
             if (i >= g.nx) break;
-            const long long P = cidx(g, i, j, k);
-            if (c.flag[P] != FLUID || (c.p_singular && P == c.pinned)) continue;
+            const long long P = cidx(g, i, j, k), q = SPLIT ? fr.split_index(i, j, k) : P;
+            if (fr.flag[q] != FLUID || (c.p_singular && P == c.pinned)) continue;
             const int Ii = i + 2;
             const T nb = c.km[0][Ii] * z[P - g.sx] + c.kp[0][Ii] * z[P + g.sx] + kmy * z[P - g.sy] +
                          kpy * z[P + g.sy] + kmz * z[P - 1] + kpz * z[P + 1];
-            const T res = r[P] - (z[P] - c.dinv[P] * nb);
+            const T res = fr.r[q] - (z[P] - fr.dinv[q] * nb);
             acc += c.d[0][Ii] * vyz * (c.ks[0][Ii] + kyz) * res;
         }
     }
@@ -1152,6 +1209,11 @@ int GMG<T>::setup(cudaStream_t s, const OpT<double> &A64, const OpT<T> &A, const
     per_[0] = A.bc[F_W].type == BCT_PERIODIC;
     per_[1] = A.bc[F_S].type == BCT_PERIODIC;
     per_[2] = A.bc[F_D].type == BCT_PERIODIC;
+    // Colour-split fine rows for FP32 cycles on grids without a seam.
+    const bool seam = (per_[0] && (g.nx & 1)) || (per_[1] && (g.ny & 1)) || (per_[2] && (g.nz & 1));
+    NZH_ = (g.nz + 5) / 2;
+    H_ = (long long)(g.nx + 4) * (g.ny + 4) * NZH_;
+    split_ = sizeof(T) == 4 && !seam && 2 * H_ < (1LL << 31);
     std::vector<void *> tmp;
     auto dalloc = [&](size_t bytes, bool keep) -> void * {
         void *p = nullptr;
@@ -1161,6 +1223,15 @@ int GMG<T>::setup(cudaStream_t s, const OpT<double> &A64, const OpT<T> &A, const
         return p;
     };
     if (nghost > 0) ghost_tmp_ = (T *)dalloc(sizeof(T) * nghost, true);
+    if (split_) {
+        rs_ = (T *)dalloc(sizeof(T) * 2 * H_, true);
+        ds_ = (T *)dalloc(sizeof(T) * 2 * H_, true);
+        fs_ = (uint8_t *)dalloc(2 * H_, true);
+        if (!rs_ || !ds_ || !fs_) return -1;
+        const dim3 gs((g.nz + 35) / 32, (g.ny + 11) / 8, g.nx + 4);
+        k_to_split<T, T><<<gs, dim3(32, 8), 0, s>>>(A.dinv, ds_, g.ny + 4, g.nz + 4, NZH_, H_, nullptr);
+        k_to_split<uint8_t, uint8_t><<<gs, dim3(32, 8), 0, s>>>(A.flag, fs_, g.ny + 4, g.nz + 4, NZH_, H_, nullptr);
+    }
     // Does any ghost interpolation stencil reach an outer cell?  Then the
     // ghost and outer rows of a sweep cannot share a launch.
     {
@@ -1183,6 +1254,21 @@ int GMG<T>::setup(cudaStream_t s, const OpT<double> &A64, const OpT<T> &A, const
         std::vector<double> gw(8 * (size_t)nghost), gws(nghost);
         cudaMemcpy(gidx.data(), A.gidx, sizeof(int) * gidx.size(), cudaMemcpyDeviceToHost);
         cudaMemcpy(gcell.data(), ghost_cell, sizeof(int) * nghost, cudaMemcpyDeviceToHost);
+        // Each ghost's row in the fine-row layout in use.
+        {
+            const FineRows<T> fr{nullptr, nullptr, nullptr, split_ ? 1 : 0, H_, g.ny + 4, NZH_,
+                                 (long long)(g.ny + 4) * NZH_};
+            std::vector<long long> grow(nghost);
+            for (int t = 0; t < nghost; t++) {
+                int i, j, k;
+                cijk(g, gcell[t], i, j, k);
+                grow[t] = fr.at(gcell[t], i, j, k);
+            }
+            grow_ = (long long *)dalloc(sizeof(long long) * nghost, true);
+            if (!grow_) return -1;
+            // After dalloc's clearing, on the same stream (pageable source: staged at the call).
+            cudaMemcpyAsync(grow_, grow.data(), sizeof(long long) * nghost, cudaMemcpyHostToDevice, s);
+        }
         cudaMemcpy(gw.data(), A64.gw, sizeof(double) * gw.size(), cudaMemcpyDeviceToHost);
         cudaMemcpy(gws.data(), A64.gwself, sizeof(double) * nghost, cudaMemcpyDeviceToHost);
         for (int q : gidx) {
@@ -1378,7 +1464,7 @@ static dim3 cgrid(const MGLevel<T> &L, int ncol) {
 }
 
 template <typename T>
-int GMG<T>::smooth0(cudaStream_t s, const T *r, T *z, int sweeps, bool from_zero, const int *gate) {
+int GMG<T>::smooth0(cudaStream_t s, const FineRows<T> &fr, T *z, int sweeps, bool from_zero, const int *gate) {
     const Grid &g = A_.g;
     Per3 per{{per_[0], per_[1], per_[2]}};
     const bool seam = (per_[0] && (g.nx & 1)) || (per_[1] && (g.ny & 1)) || (per_[2] && (g.nz & 1));
@@ -1393,10 +1479,12 @@ int GMG<T>::smooth0(cudaStream_t s, const T *r, T *z, int sweeps, bool from_zero
         const int tc = tb("mg0_color");
         for (int col = 0; col < (seam ? 4 : 2); col++, k++) {
             if (it == 0 && col == 0 && from_zero)
-                launch_pdl(k_mg0_init3<T>, dim3((g.nz + 35) / 32, (g.ny + 11) / 8, g.nx + 4), dim3(32, 8), 0, s, A_, r, z,
-                                                                                                   per, gate);
+                launch_pdl(fr.split ? k_mg0_init3<T, true> : k_mg0_init3<T, false>,
+                           dim3((g.nz + 35) / 32, (g.ny + 11) / 8, (g.nx + 3 + MG0_IPLANES) / MG0_IPLANES),
+                           dim3(32, 8), 0, s, A_, fr, z, per, gate);
             else
-                launch_pdl(k_mg0_color<T>, grd, blk, 0, s, A_, r, z, col, seam ? 0 : 1, per, (T)cfg_.omega, gate);
+                launch_pdl(fr.split ? k_mg0_color<T, true> : k_mg0_color<T, false>, grd, blk, 0, s, A_, fr, z, col,
+                           seam ? 0 : 1, per, (T)cfg_.omega, gate);
         }
         te(tc);
         const int to = tb("mg0_outer_ghost");
@@ -1407,12 +1495,12 @@ int GMG<T>::smooth0(cudaStream_t s, const T *r, T *z, int sweeps, bool from_zero
             const bool last = it == sweeps - 1;
             const int *ol = last ? A_.sw.outer : outer1_;
             const int no = last ? A_.sw.nout : nout1_;
-            launch_pdl(k_mg0_outer<T>, gb + (no + 255) / 256, 256, 0, s, A_, r, z, ol, no, ghost_cell_, nghost_, gb, ghost_tmp_,
-                       (const T *)ghost_idiv_, gate);
+            launch_pdl(k_mg0_outer<T>, gb + (no + 255) / 256, 256, 0, s, A_, fr, z, ol, no, ghost_cell_,
+                       (const long long *)grow_, nghost_, gb, ghost_tmp_, (const T *)ghost_idiv_, gate);
             k++;
         } else {  // a ghost stencil reaches an outer cell: ghosts first, outer rows after the scatter
-            launch_pdl(k_mg0_outer<T>, gb, 256, 0, s, A_, r, z, A_.sw.outer, 0, ghost_cell_, nghost_, gb, ghost_tmp_,
-                       (const T *)ghost_idiv_, gate);
+            launch_pdl(k_mg0_outer<T>, gb, 256, 0, s, A_, fr, z, A_.sw.outer, 0, ghost_cell_, (const long long *)grow_,
+                       nghost_, gb, ghost_tmp_, (const T *)ghost_idiv_, gate);
             k++;
         }
         if (nghost_ > 0) {
@@ -1420,8 +1508,8 @@ int GMG<T>::smooth0(cudaStream_t s, const T *r, T *z, int sweeps, bool from_zero
             k++;
         }
         if (ghost_reads_outer_) {
-            launch_pdl(k_mg0_outer<T>, ob, 256, 0, s, A_, r, z, A_.sw.outer, A_.sw.nout, ghost_cell_, 0, 0, ghost_tmp_,
-                       (const T *)ghost_idiv_, gate);
+            launch_pdl(k_mg0_outer<T>, ob, 256, 0, s, A_, fr, z, A_.sw.outer, A_.sw.nout, ghost_cell_,
+                       (const long long *)grow_, 0, 0, ghost_tmp_, (const T *)ghost_idiv_, gate);
             k++;
         }
         te(to);
@@ -1429,15 +1517,58 @@ int GMG<T>::smooth0(cudaStream_t s, const T *r, T *z, int sweeps, bool from_zero
     return k;
 }
 
+// The fine rows of an application with right-hand side r: r itself and
+// the operator's 1/coeffsum and flags, or their colour-split copies (r
+// split by the caller into rs_).
+template <typename T>
+FineRows<T> GMG<T>::rows(const T *r) const {
+    const Grid &g = A_.g;
+    if (split_) return FineRows<T>{rs_, ds_, fs_, 1, H_, g.ny + 4, NZH_, (long long)(g.ny + 4) * NZH_};
+    return FineRows<T>{r, A_.dinv, A_.flag, 0, 0, g.ny + 4, 0, 0};
+}
+
+template <typename T>
+void GMG<T>::apply(cudaStream_t s, const T *r, T *z, const int *gate) {
+    if constexpr (sizeof(T) == 4) {
+        if (split_) {
+            const Grid &g = A_.g;
+            launch_pdl(k_narrow_split<float>,
+                       dim3((NZH_ + 31) / 32, (g.ny + 11) / 8, (g.nx + 3 + MG0_NPLANES) / MG0_NPLANES), dim3(32, 8), 0,
+                       s, r, rs_, g.nx + 4, g.ny + 4, g.nz + 4, NZH_, H_, gate);
+            note_launches(1);
+            cycle(s, rows(r), z, gate);
+            launches_++;
+            return;
+        }
+    }
+    cycle(s, rows(r), z, gate);
+}
+
+template <typename T>
+bool GMG<T>::apply_from64(cudaStream_t s, const double *r, T *z, const int *gate) {
+    if constexpr (sizeof(T) != 4) {
+        return false;   // FP64 cycles keep the natural layout
+    } else {
+        if (!split_) return false;
+        const Grid &g = A_.g;
+        launch_pdl(k_narrow_split<double>, dim3((NZH_ + 31) / 32, (g.ny + 11) / 8, (g.nx + 3 + MG0_NPLANES) / MG0_NPLANES),
+                   dim3(32, 8), 0, s, r, rs_, g.nx + 4, g.ny + 4, g.nz + 4, NZH_, H_, gate);
+        note_launches(1);
+        cycle(s, rows(nullptr), z, gate);
+        launches_++;
+        return true;
+    }
+}
+
 // One V-cycle from z = 0: pre-smoothing on the fine rows, restriction, the
 // coarse levels above the tail (each starting from Z = 0), the tail, then
 // prolongation and post-smoothing back up.
 template <typename T>
-void GMG<T>::apply(cudaStream_t s, const T *r, T *z, const int *gate) {
+void GMG<T>::cycle(cudaStream_t s, const FineRows<T> &fr, T *z, const int *gate) {
     const Grid &g = A_.g;
     int k = 0;
     if (levels_.empty()) {
-        k += smooth0(s, r, z, cfg_.nu_pre + cfg_.nu_post + 4, true, gate);
+        k += smooth0(s, fr, z, cfg_.nu_pre + cfg_.nu_post + 4, true, gate);
         note_launches(k);
         launches_ = k;
         return;
@@ -1451,14 +1582,15 @@ void GMG<T>::apply(cudaStream_t s, const T *r, T *z, const int *gate) {
         launch_pdl(k_fill0<T>, nblk(g.ncell, 256), 256, 0, s, z, (long long)g.ncell, gate);
         k++;
     }
-    k += smooth0(s, r, z, cfg_.nu_pre, true, gate);
+    k += smooth0(s, fr, z, cfg_.nu_pre, true, gate);
     const MGLevel<T> &L1 = levels_[0];
     int tp = tb("mg0_restrict");
     if (L1.cx && L1.cy && L1.cz)
-        launch_pdl(k_mg0_restrict2<T>, dim3((g.nz + 31) / 32, (g.ny + 7) / 8, L1.nx), dim3(32, 8), 0, s, A_, r, z, L1, gate);
+        launch_pdl(fr.split ? k_mg0_restrict2<T, true> : k_mg0_restrict2<T, false>,
+                   dim3((g.nz + 31) / 32, (g.ny + 7) / 8, L1.nx), dim3(32, 8), 0, s, A_, fr, z, L1, gate);
     else
-        launch_pdl(k_mg0_restrict_g<T>, dim3(nsegk_, nsegj_, (L1.nx + MG0_RPLANES - 1) / MG0_RPLANES), dim3(32, 8), 0, s,
-                   A_, r, z, L1,
+        launch_pdl(fr.split ? k_mg0_restrict_g<T, true> : k_mg0_restrict_g<T, false>,
+                   dim3(nsegk_, nsegj_, (L1.nx + MG0_RPLANES - 1) / MG0_RPLANES), dim3(32, 8), 0, s, A_, fr, z, L1,
                    (const int *)segj_, (const int *)segk_, gate);
     k++;
     te(tp);
@@ -1508,7 +1640,7 @@ void GMG<T>::apply(cudaStream_t s, const T *r, T *z, const int *gate) {
                    dim3(32, 8), 0, s, A_, z, L1, gate);
     k++;
     te(tp);
-    k += smooth0(s, r, z, cfg_.nu_post, false, gate);
+    k += smooth0(s, fr, z, cfg_.nu_post, false, gate);
     note_launches(k);
     launches_ = k;
 }
@@ -1520,11 +1652,13 @@ float GMG<T>::time_color(cudaStream_t s, const T *r, T *z, int reps, double *byt
     const bool seam = (per_[0] && (g.nx & 1)) || (per_[1] && (g.ny & 1)) || (per_[2] && (g.nz & 1));
     const dim3 blk(32, 8, 1);
     const dim3 grd(seam ? (g.nz + 31) / 32 : (g.nz + 63) / 64, (g.ny + 7) / 8, (g.nx + MG0_PLANES - 1) / MG0_PLANES);
+    void (*color)(const OpT<T>, const FineRows<T>, T *, int, int, Per3, T, const int *) =
+        split_ ? k_mg0_color<T, true> : k_mg0_color<T, false>;
     const double nint = (double)g.nx * g.ny * g.nz;
     *bytes = nint * sizeof(T) + 0.5 * nint * (3 * sizeof(T) + 1);
     if (!timed) {
         for (int q = 0; q < reps; q++)
-            k_mg0_color<T><<<grd, blk, 0, s>>>(A_, r, z, 1, seam ? 0 : 1, per, (T)cfg_.omega, nullptr);
+            color<<<grd, blk, 0, s>>>(A_, rows(r), z, 1, seam ? 0 : 1, per, (T)cfg_.omega, nullptr);
         note_launches(reps);
         return 0.0f;
     }
@@ -1533,7 +1667,7 @@ float GMG<T>::time_color(cudaStream_t s, const T *r, T *z, int reps, double *byt
     cudaEventCreate(&b);
     cudaEventRecord(a, s);
     for (int q = 0; q < reps; q++)
-        k_mg0_color<T><<<grd, blk, 0, s>>>(A_, r, z, 1, seam ? 0 : 1, per, (T)cfg_.omega, nullptr);
+        color<<<grd, blk, 0, s>>>(A_, rows(r), z, 1, seam ? 0 : 1, per, (T)cfg_.omega, nullptr);
     cudaEventRecord(b, s);
     cudaEventSynchronize(b);
     float ms = 0;

@@ -64,6 +64,32 @@ struct MGLevel {
     const int *pa[3];
 };
 
+// The fine rows' right-hand side r, 1/coeffsum and flags as the V-cycle's
+// fine-level kernels read them.  split = 1 (the FP32 cycle on grids
+// without a periodic seam): colour-split - two halves, red ((I+J+K) even)
+// then black, each ordered by (I, J, K/2) over the padded box (padded
+// coordinates I = i + 2, ...) - so that a colour pass reads only its
+// colour's entries, contiguous along k; split = 0: the padded natural
+// layout (index P).
+template <typename T>
+struct FineRows {
+    const T *r;
+    const T *dinv;
+    const uint8_t *flag;
+    int split;
+    long long H;     // entries per colour half
+    int NY, NZH;     // padded y extent; padded z extent halved, rounded up
+    long long NYZH;  // NY * NZH: one padded plane of a half
+    // Index of interior-relative cell (i, j, k) in the split layout, in
+    // 32-bit arithmetic (the layout is used only below 2^31 entries).
+    __host__ __device__ __forceinline__ int split_index(int i, int j, int k) const {
+        return ((i + j + k) & 1) * (int)H + (i + 2) * (int)NYZH + (j + 2) * NZH + ((k + 2) >> 1);
+    }
+    __host__ __device__ __forceinline__ long long at(long long P, int i, int j, int k) const {
+        return split ? split_index(i, j, k) : P;
+    }
+};
+
 enum { MG_COARSEN_HALVE = 0, MG_COARSEN_SPACING = 1 };
 
 struct GMGConfig {
@@ -112,6 +138,9 @@ class GMG : public Preconditioner<T> {
     int setup(cudaStream_t s, const OpT<double> &A64, const OpT<T> &A, const int *ghost_cell, int nghost,
               const MGGeometry &geom, const GMGConfig &cfg);
     void apply(cudaStream_t s, const T *r, T *z, const int *gate) override;
+    // FP32 cycles with colour-split fine rows round an FP64 r straight into
+    // the split layout.
+    bool apply_from64(cudaStream_t s, const double *r, T *z, const int *gate) override;
     int launches() const override { return launches_; }
     // Smoother sweeps (pre, post) on the fine grid and on the coarse levels,
     // and on the coarsest level; takes effect at the next apply.
@@ -133,6 +162,8 @@ class GMG : public Preconditioner<T> {
     // updated half of the interior cells).
     // timed = false: launches only (the caller times them).
     float time_color(cudaStream_t s, const T *r, T *z, int reps, double *bytes, bool timed = true);
+    // Whether the fine rows are colour-split (FineRows).
+    bool split() const { return split_; }
 
   private:
     OpT<T> A_{};
@@ -153,6 +184,15 @@ class GMG : public Preconditioner<T> {
     // last sweep of each smoothing).
     int *outer1_ = nullptr;
     int nout1_ = 0;
+    // Colour-split fine rows (FP32 cycles without a periodic seam): the
+    // cycle's right-hand side (filled per application), 1/coeffsum and
+    // flags; and per ghost the index of its row in the layout in use.
+    bool split_ = false;
+    T *rs_ = nullptr, *ds_ = nullptr;
+    uint8_t *fs_ = nullptr;
+    long long H_ = 0;
+    int NZH_ = 0;
+    long long *grow_ = nullptr;
     int per_[3] = {0, 0, 0};
     // Level 1's groups (host copy) and the restriction tiles cut from them.
     std::vector<int> ch1_[3];
@@ -161,7 +201,9 @@ class GMG : public Preconditioner<T> {
     std::vector<void *> allocs_;
     int launches_ = 0;
     // sweeps of the fine-grid smoother; from_zero: z is taken as 0 on entry
-    int smooth0(cudaStream_t s, const T *r, T *z, int sweeps, bool from_zero, const int *gate);
+    int smooth0(cudaStream_t s, const FineRows<T> &fr, T *z, int sweeps, bool from_zero, const int *gate);
+    FineRows<T> rows(const T *r) const;
+    void cycle(cudaStream_t s, const FineRows<T> &fr, T *z, const int *gate);
 };
 
 }  // namespace ibm

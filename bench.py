@@ -515,12 +515,20 @@ def bench_gb300(args):
     head["solver"] = None
     sec["solver"].close()
     sec["solver"] = None
+    def phase(name):   # marks the log, so that a solver warning can be placed
+        print(f"[bench] {name}", file=sys.stderr, flush=True)
+
     if rank == 0 and world == 1 and not args.no_oracle:
+        phase("error against the oracle")
         line["error_vs_oracle"] = error_vs_oracle(ibm, wl, case, u0, lv, mixed_mode)
     if rank == 0 and world == 1 and not args.no_extras:
+        phase("configurations")
         line["configs"] = configs_arm(ibm, wl, args)
+        phase("ensemble")
         line["ensemble"] = ensemble_arm(ibm, wl, args)
+        phase("serving")
         line["serving"] = serving_arm(ibm, wl, args)
+        phase("large-body set-up")
         line["large_body_setup"] = large_body_arm(ibm, wl)
     if rank == 0 and world == 1 and not args.no_cpu:
         cv, done, secs, _ = run_cpu(case, lv, steps=2, warmup=0, threads=os.cpu_count() or 1, sample_budget_s=25)
