@@ -440,17 +440,21 @@ k_mg0_restrict_g(const OpT<T> c, const FineRows<T> fr, const T *__restrict__ z, 
 }
 
 // Prolongation into the fine grid from a level 1 of uneven groups: each
-// thread takes one fine (j, k) on MG0_PPLANES consecutive planes, reads its
-// j and k transfer tables once, addresses coarse cells in 32-bit
-// arithmetic (a level has fewer than 2^31 cells) and issues every load
-// (flags, z, the x tables, the coarse values) before any store; a cell that
-// takes no correction stores z back.  Same arithmetic as prolong_value.
-// Grid (ceil(nz/32), ceil(ny/8), ceil(nx/MG0_PPLANES)) of 32 x 8 threads.
-constexpr int MG0_PPLANES = 4;
+// thread takes one fine (j, k) on mg0_pplanes<T>() consecutive planes (four
+// in FP32; one in FP64, whose blend is bound by the FP64 pipe rather than
+// by latency), reads its j and k transfer tables once, addresses coarse
+// cells in 32-bit arithmetic (a level has fewer than 2^31 cells) and
+// issues every load (flags, z, the x tables, the coarse values) before any
+// store; a cell that takes no correction stores z back.  Same arithmetic
+// as prolong_value.  Grid (ceil(nz/32), ceil(ny/8), ceil(nx/planes)) of
+// 32 x 8 threads.
+template <typename T>
+__host__ __device__ constexpr int mg0_pplanes() { return sizeof(T) == 4 ? 4 : 1; }
 
 template <typename T>
 __global__ void __launch_bounds__(256)
 k_mg0_prolong(const OpT<T> c, T *z, const MGLevel<T> C, const int *gate) {
+    constexpr int MG0_PPLANES = mg0_pplanes<T>();
     MG_GATE(gate);
     const Grid &g = c.g;
     const int k = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 8 + threadIdx.y;
@@ -1636,8 +1640,9 @@ void GMG<T>::cycle(cudaStream_t s, const FineRows<T> &fr, T *z, const int *gate)
     if (L1.cx && L1.cy && L1.cz)
         launch_pdl(k_mg0_prolong2<T>, l3_grid(g.nx, g.ny, g.nz), l3_block(), 0, s, A_, z, L1, gate);
     else
-        launch_pdl(k_mg0_prolong<T>, dim3((g.nz + 31) / 32, (g.ny + 7) / 8, (g.nx + MG0_PPLANES - 1) / MG0_PPLANES),
-                   dim3(32, 8), 0, s, A_, z, L1, gate);
+        launch_pdl(k_mg0_prolong<T>,
+                   dim3((g.nz + 31) / 32, (g.ny + 7) / 8, (g.nx + mg0_pplanes<T>() - 1) / mg0_pplanes<T>()), dim3(32, 8), 0,
+                   s, A_, z, L1, gate);
     k++;
     te(tp);
     k += smooth0(s, fr, z, cfg_.nu_post, false, gate);
