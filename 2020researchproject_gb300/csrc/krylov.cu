@@ -131,6 +131,7 @@ k_bicg_init(const long long n, const T *__restrict__ b, T *x, T *r, T *r0, T *p,
             s.iters = 0;
             s.state = tot[c] == 0.0 ? KS_DONE : KS_RUN;
             s.divmax = 0.0;
+            s.restart = 0;
             s.tol = tol;
             s.divtol = divtol;
             if (outer) {
@@ -147,13 +148,22 @@ k_bicg_init(const long long n, const T *__restrict__ b, T *x, T *r, T *r0, T *p,
 // ------------------------------------------------- p = r + beta (p - w v) --
 template <typename T, int NC, bool VEC>
 __global__ void __launch_bounds__(KTHREADS)
-k_bicg_p(const long long n, const T *__restrict__ r, T *__restrict__ p, const T *__restrict__ v, const KScal *sc) {
+k_bicg_p(const long long n, const T *__restrict__ r, T *__restrict__ p, const T *__restrict__ v, T *__restrict__ r0,
+         const KScal *sc) {
     pdl_enter();
 #pragma unroll
     for (int c = 0; c < NC; c++) {
         if (sc[c].state != KS_RUN) continue;
         const T beta = (T)sc[c].beta, om = (T)sc[c].omega;
         const long long o = c * n;
+        if (sc[c].restart) {   // the recurrence restarts from the current residual
+            GRID_STRIDE(P, n) {
+                const T rv = r[o + P];
+                p[o + P] = rv;
+                r0[o + P] = rv;
+            }
+            continue;
+        }
         if (VEC) {
             const long long np = n / PW<T>, op = o / PW<T>;
             GRID_STRIDE(q, np) {
@@ -250,6 +260,7 @@ k_bicg_init_guess(const OpT<T> A, const int op, const long long n, const T *__re
             s.tol = tol;
             s.divtol = divtol;
             s.divmax = tot[2 * NC];
+            s.restart = 0;
             const bool done = tot[NC + c] == 0.0 || converged(tot[NC + c], s.bnorm2, tot[2 * NC], tol, divtol);
             s.state = done ? KS_DONE : KS_RUN;
             go = go || !done;
@@ -289,6 +300,7 @@ k_bicg_spmv_v(const OpT<T> A, const int op, const long long n, const T *__restri
     reduce_and_finish<NC, NC>(a, smem, partials, counter, [&](const double *tot) {
         for (int c = 0; c < NC; c++) {
             KScal &s = sc[c];
+            s.restart = 0;   // k_bicg_p, the only reader, has finished
             if (s.state != KS_RUN) continue;
             // A zero or non-finite (r0, v) ends the solve: NaN or Inf in
             // the operands would otherwise run it to its iteration cap.
@@ -485,8 +497,12 @@ k_bicg_xr(const OpT<T> A, const long long n, T *__restrict__ x, T *__restrict__ 
             if (converged(tot[2 * c], st.bnorm2, tot[2 * NC], st.tol, st.divtol)) {
                 st.state = KS_DONE;
                 st.divmax = tot[2 * NC];
-            } else if (rho1 == 0.0 || !isfinite(rho1) || !isfinite(tot[2 * c])) {
+            } else if (!isfinite(rho1) || !isfinite(tot[2 * c])) {
                 st.state = KS_BREAKDOWN;
+            } else if (st.iters % KRESTART == 0 || rho1 == 0.0) {
+                st.restart = 1;
+                st.rho = tot[2 * c];
+                st.beta = 0.0;
             }
             run = run || (st.state == KS_RUN && st.iters < maxit);
         }
@@ -736,10 +752,10 @@ static void first_half(cudaStream_t st, const OpT<T> &A, int op, KrylovWork<T> &
     const int nc = w.nc;
     const int *gate = nc == 1 ? &w.scal[0].state : nullptr;
     const bool vec = n % 4 == 0;
-    if (nc == 3 && vec) launch_pdl(k_bicg_p<T, 3, true>, w.nblk, KTHREADS, 0, st, n, w.r, w.p, w.v, w.scal);
-    else if (nc == 3) launch_pdl(k_bicg_p<T, 3, false>, w.nblk, KTHREADS, 0, st, n, w.r, w.p, w.v, w.scal);
-    else if (vec) launch_pdl(k_bicg_p<T, 1, true>, w.nblk, KTHREADS, 0, st, n, w.r, w.p, w.v, w.scal);
-    else launch_pdl(k_bicg_p<T, 1, false>, w.nblk, KTHREADS, 0, st, n, w.r, w.p, w.v, w.scal);
+    if (nc == 3 && vec) launch_pdl(k_bicg_p<T, 3, true>, w.nblk, KTHREADS, 0, st, n, w.r, w.p, w.v, w.r0, w.scal);
+    else if (nc == 3) launch_pdl(k_bicg_p<T, 3, false>, w.nblk, KTHREADS, 0, st, n, w.r, w.p, w.v, w.r0, w.scal);
+    else if (vec) launch_pdl(k_bicg_p<T, 1, true>, w.nblk, KTHREADS, 0, st, n, w.r, w.p, w.v, w.r0, w.scal);
+    else launch_pdl(k_bicg_p<T, 1, false>, w.nblk, KTHREADS, 0, st, n, w.r, w.p, w.v, w.r0, w.scal);
     note_launches(1);
     if (M) {
         const int tm = prof_begin(pf, "mg_vcycle");

@@ -45,7 +45,16 @@ struct KScal {
     double tol, divtol;  // this solve's stopping test (set by the init kernel)
     int iters;
     int state;
+    int restart;   // the next p update restarts the recurrence (r0 = r, p = r)
 };
+
+// BiCGSTAB restarts its recurrence every KRESTART iterations of a solve
+// that has not converged: the current residual becomes the shadow residual
+// r0 and the search direction (rho = ||r||^2, beta = 0), which ends the
+// stagnation that a near-breakdown ((r0, r) -> 0) or an inexact FP32
+// preconditioner can cause; a converging solve (4-20 iterations) never
+// reaches it.
+constexpr int KRESTART = 30;
 
 // Outer (FP64) state of an iterative-refinement solve, per component.
 struct IRScal {

@@ -913,7 +913,7 @@ constexpr size_t TAIL_SMEM_MAX = 200 * 1024;
 template <typename T>
 __global__ void __launch_bounds__(TAIL_THREADS)
 k_mg_tail(const TailDesc<T> d, const uint4 *__restrict__ img, const int nu1, const int nu2, const int csweeps,
-          const Per3 per, const int *gate) {
+          const Per3 per, const int singular, const int *gate) {
     MG_GATE(gate);
     extern __shared__ __align__(16) unsigned char tail_smem[];
     __shared__ MGLevel<T> loc[TAIL_MAXL];
@@ -1025,6 +1025,29 @@ k_mg_tail(const TailDesc<T> d, const uint4 *__restrict__ img, const int nu1, con
     };
     for (int l = first; l < nlev; l++) {
         const MGLevel<T> &L = loc[l - first];
+        if (l == nlev - 1 && singular && tid < 32) {
+            // Without a pressure boundary value the coarse operators are
+            // singular (constants are their null space) and the restricted
+            // residual need not sum to zero (the fine grid's pinned row
+            // absorbs the difference): the coarsest sweeps would drift along
+            // the constants.  Its right-hand side is made consistent first:
+            // the mean over active cells is removed.
+            T sum = 0, cnt = 0;
+            for (int c = tid; c < L.n; c += 32)
+                if (L.diag[c] != (T)0) {
+                    sum += L.R[c];
+                    cnt += (T)1;
+                }
+            for (int o = 16; o > 0; o >>= 1) {
+                sum += __shfl_xor_sync(0xffffffffu, sum, o);
+                cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+            }
+            const T mean = cnt > (T)0 ? sum / cnt : (T)0;
+            __syncwarp();
+            for (int c = tid; c < L.n; c += 32)
+                if (L.diag[c] != (T)0) L.R[c] -= mean;
+        }
+        if (l == nlev - 1) __syncthreads();
         sweep(L, l == nlev - 1 ? csweeps : nu1);
         if (l < nlev - 1) {
             const MGLevel<T> &C = loc[l + 1 - first];
@@ -1622,7 +1645,7 @@ void GMG<T>::cycle(cudaStream_t s, const FineRows<T> &fr, T *z, const int *gate)
     te(tp);
     tp = tb("mg_tail");
     launch_pdl(k_mg_tail<T>, 1, TAIL_THREADS, tail_smem_, s, tail_desc_, tail_img_, cfg_.nuc_pre, cfg_.nuc_post,
-               cfg_.coarse_sweeps, per, gate);
+               cfg_.coarse_sweeps, per, A_.p_singular ? 1 : 0, gate);
     k++;
     te(tp);
     tp = tb("mgc_up");
