@@ -36,6 +36,15 @@ struct Per3 {
     int p[3];
 };
 
+// The first colour pass of a coarse level on Z = 0, applied to one cell by
+// the restriction that has just computed its R (saves the level its
+// separate init launch): colour-0 cells take R / diag, the others 0.
+template <typename T>
+__device__ __forceinline__ void restrict_init(const MGLevel<T> &L, long long q, int I, int J, int K, T R,
+                                              const Per3 &per) {
+    L.Z[q] = cell_color(I, J, K, L.nx, L.ny, L.nz, per.p) == 0 ? R * L.idiag[q] : (T)0;
+}
+
 // Every V-cycle kernel returns at once while *gate (when given) is not
 // KS_RUN: the solve it serves has converged.
 #define MG_GATE(gate)                       \
@@ -382,7 +391,8 @@ constexpr int MG0_RPLANES = 4;
 template <typename T, bool SPLIT>
 __global__ void __launch_bounds__(256)
 k_mg0_restrict_g(const OpT<T> c, const FineRows<T> fr, const T *__restrict__ z, MGLevel<T> L1,
-                 const int *__restrict__ segj, const int *__restrict__ segk, const int *gate) {
+                 const int *__restrict__ segj, const int *__restrict__ segk, const Per3 per, const int init,
+                 const int *gate) {
     MG_GATE(gate);
     __shared__ T part[MG0_RPLANES][8][33];
     const Grid &g = c.g;
@@ -435,7 +445,9 @@ k_mg0_restrict_g(const OpT<T> c, const FineRows<T> fr, const T *__restrict__ z, 
         T sum = 0;
         for (int y = ja; y < jz; y++)
             for (int x = ka; x < kz; x++) sum += part[q][y][x];
-        L1.R[lidx(L1, I, J, K)] = sum;
+        const long long c1 = lidx(L1, I, J, K);
+        L1.R[c1] = sum;
+        if (init) restrict_init(L1, c1, I, J, K, sum, per);
     }
 }
 
@@ -508,7 +520,8 @@ k_mg0_prolong(const OpT<T> c, T *z, const MGLevel<T> C, const int *gate) {
 // (ceil(nz/32), ceil(ny/8), L1.nx) of 32 x 8 threads.
 template <typename T, bool SPLIT>
 __global__ void __launch_bounds__(256)
-k_mg0_restrict2(const OpT<T> c, const FineRows<T> fr, const T *__restrict__ z, MGLevel<T> L1, const int *gate) {
+k_mg0_restrict2(const OpT<T> c, const FineRows<T> fr, const T *__restrict__ z, MGLevel<T> L1, const Per3 per,
+                const int init, const int *gate) {
     MG_GATE(gate);
     __shared__ T part[8][33];
     const Grid &g = c.g;
@@ -537,7 +550,12 @@ k_mg0_restrict2(const OpT<T> c, const FineRows<T> fr, const T *__restrict__ z, M
     __syncthreads();
     if ((threadIdx.y & 1) || (threadIdx.x & 1)) return;
     const int J = blockIdx.y * 4 + (threadIdx.y >> 1), K = blockIdx.x * 16 + (threadIdx.x >> 1);
-    if (J < L1.ny && K < L1.nz) L1.R[lidx(L1, I, J, K)] = part[threadIdx.y][threadIdx.x] + part[threadIdx.y + 1][threadIdx.x];
+    if (J < L1.ny && K < L1.nz) {
+        const long long c1 = lidx(L1, I, J, K);
+        const T R = part[threadIdx.y][threadIdx.x] + part[threadIdx.y + 1][threadIdx.x];
+        L1.R[c1] = R;
+        if (init) restrict_init(L1, c1, I, J, K, R, per);
+    }
 }
 
 // Prolongation when level 1 halves every axis: the block's fine tile (one
@@ -827,16 +845,6 @@ __global__ void k_fill0(T *z, const long long n, const int *gate) {
 }
 
 
-// The first colour pass of a coarse level on Z = 0: colour-0 cells take
-// R / diag (0 where inactive), every other cell 0.
-template <typename T>
-__global__ void __launch_bounds__(256) k_mgc_init(MGLevel<T> L, const Per3 per, const int *gate) {
-    MG_GATE(gate);
-    L3_INDEX(I, J, K, L.ny, L.nz);
-    const long long q = lidx(L, I, J, K);
-    L.Z[q] = cell_color(I, J, K, L.nx, L.ny, L.nz, per.p) == 0 ? L.R[q] * L.idiag[q] : (T)0;
-}
-
 // Branch-free relaxation of coarse cell (I, J, K) on a level without
 // periodic axes: every load is issued up front (low-face conductances are
 // 0 on the first cell of an axis; high neighbours off the level are read
@@ -886,10 +894,13 @@ k_mgc_color(MGLevel<T> L, const int color, const int pairs, const Per3 per, cons
 
 template <typename T>
 __global__ void __launch_bounds__(256)
-k_mgc_restrict(const MGLevel<T> F, MGLevel<T> C, const Per3 per, const int skip, const int *gate) {
+k_mgc_restrict(const MGLevel<T> F, MGLevel<T> C, const Per3 per, const int skip, const int init, const int *gate) {
     MG_GATE(gate);
     L3_INDEX(I, J, K, C.ny, C.nz);
-    C.R[lidx(C, I, J, K)] = coarse_restrict_value(F, C, I, J, K, per.p, skip);
+    const long long q = lidx(C, I, J, K);
+    const T R = coarse_restrict_value(F, C, I, J, K, per.p, skip);
+    C.R[q] = R;
+    if (init) restrict_init(C, q, I, J, K, R, per);
 }
 
 template <typename T>
@@ -1611,14 +1622,18 @@ void GMG<T>::cycle(cudaStream_t s, const FineRows<T> &fr, T *z, const int *gate)
     }
     k += smooth0(s, fr, z, cfg_.nu_pre, true, gate);
     const MGLevel<T> &L1 = levels_[0];
+    // The restriction into a coarse level above the tail also applies its
+    // first colour pass (Z = R / diag on colour 0), so the level's own init
+    // launch is left out.
+    const int init1 = cfg_.nuc_pre > 0 && tail_ > 0 ? 1 : 0;
     int tp = tb("mg0_restrict");
     if (L1.cx && L1.cy && L1.cz)
         launch_pdl(fr.split ? k_mg0_restrict2<T, true> : k_mg0_restrict2<T, false>,
-                   dim3((g.nz + 31) / 32, (g.ny + 7) / 8, L1.nx), dim3(32, 8), 0, s, A_, fr, z, L1, gate);
+                   dim3((g.nz + 31) / 32, (g.ny + 7) / 8, L1.nx), dim3(32, 8), 0, s, A_, fr, z, L1, per, init1, gate);
     else
         launch_pdl(fr.split ? k_mg0_restrict_g<T, true> : k_mg0_restrict_g<T, false>,
                    dim3(nsegk_, nsegj_, (L1.nx + MG0_RPLANES - 1) / MG0_RPLANES), dim3(32, 8), 0, s, A_, fr, z, L1,
-                   (const int *)segj_, (const int *)segk_, gate);
+                   (const int *)segj_, (const int *)segk_, per, init1, gate);
     k++;
     te(tp);
     tp = tb("mgc_down");
@@ -1627,19 +1642,16 @@ void GMG<T>::cycle(cudaStream_t s, const FineRows<T> &fr, T *z, const int *gate)
         const MGLevel<T> &C = levels_[l + 1];
         const int ncol = level_colors(L, per_);
         for (int it = 0; it < cfg_.nuc_pre; it++)
-            for (int col = 0; col < ncol; col++, k++) {
-                if (it == 0 && col == 0)
-                    launch_pdl(k_mgc_init<T>, l3_grid(L.nx, L.ny, L.nz), l3_block(), 0, s, L, per, gate);
-                else
-                    launch_pdl(k_mgc_color<T>, cgrid(L, ncol), l3_block(), 0, s, L, col, ncol == 2, per, gate);
-            }
+            for (int col = it == 0 ? 1 : 0; col < ncol; col++, k++)   // colour 0 of the first sweep: the restriction
+                launch_pdl(k_mgc_color<T>, cgrid(L, ncol), l3_block(), 0, s, L, col, ncol == 2, per, gate);
         if (cfg_.nuc_pre == 0) {
             launch_pdl(k_fill0<T>, nblk(L.n, 256), 256, 0, s, L.Z, L.n, gate);
             k++;
         }
         // After a red/black pre-smoothing the last colour's residuals are 0.
         const int skip = cfg_.nuc_pre > 0 && ncol == 2 ? 1 : -1;
-        launch_pdl(k_mgc_restrict<T>, l3_grid(C.nx, C.ny, C.nz), l3_block(), 0, s, L, C, per, skip, gate);
+        launch_pdl(k_mgc_restrict<T>, l3_grid(C.nx, C.ny, C.nz), l3_block(), 0, s, L, C, per, skip,
+                   cfg_.nuc_pre > 0 && l + 1 < tail_ ? 1 : 0, gate);
         k++;
     }
     te(tp);
