@@ -333,6 +333,37 @@ def e2e_loop(ibm, s, steps, world):
     return secs, 4 * host[0].nbytes, pinned
 
 
+def fp64_step_ops(arm):
+    """FP64 operations (FMA = 2) of one step of `arm` (fp64 / mixed) on the
+    sphere, from the committed ncu summary (profiles/fp64_step_ops.txt:
+    '<arm> <workload> <ops> <momentum iterations> <pressure iterations>'
+    of the profiled step), or None."""
+    path = os.path.join(ROOT, "profiles", "fp64_step_ops.txt")
+    try:
+        for line in open(path):
+            t = line.split()
+            if len(t) >= 5 and not line.startswith("#") and t[0] == arm:
+                return float(t[2]), float(t[3]), float(t[4])
+    except OSError:
+        pass
+    return None
+
+
+def fp64_roofline(arm, ms_per_step, fp64_tf):
+    """The step against the FP64 pipe: the FP64 operations of a profiled
+    step (ncu; its iteration counts are stated, close to the timed steps'
+    means) over the measured time per step, as a fraction of the measured
+    FP64 FMA rate."""
+    rec = fp64_step_ops(arm)
+    if rec is None:
+        return None
+    ops, it_u, it_p = rec
+    tf = ops / (ms_per_step / 1e3) / 1e12
+    return {"fp64_ops_per_step": ops, "achieved_tflops": round(tf, 3), "peak_tflops": round(fp64_tf, 3),
+            "frac": round(tf / fp64_tf, 4), "peak_source": "measured FP64 FMA rate (fma_rate_tflops)",
+            "ops_source": f"ncu, one profiled step ({it_u:g} momentum and {it_p:g} pressure iterations)"}
+
+
 def fp64_ops_per_launch(kernel):
     """FP64 operations per launch (FMA = 2) of `kernel` from the committed
     ncu summary (profiles/fp64_ops.txt: '<kernel> <workload> <ops>'), or
@@ -388,7 +419,7 @@ def bench_gb300(args):
         os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
     ibm = importlib.import_module("2020researchproject_gb300")
     wl = importlib.import_module("2020researchproject_gb300.workloads")
-    case = wl.sphere()
+    case = {"sphere": wl.sphere, "cavity64": lambda: wl.cavity(64, 1000.0, 1e-3), "channel": wl.channel}[args.workload]()
     ncell = (len(case["xf"]) - 1) * (len(case["yf"]) - 1) * (len(case["zf"]) - 1)
     u0 = wl.initial_state(case)
     other = "fp64" if args.precision == "mixed" else "mixed"
@@ -498,7 +529,8 @@ def bench_gb300(args):
                 "gpu_launches": int(sec["launches"]), "clocks": sec["clocks"],
                 "e2e": {"value": round(e2e2, 3), "unit": "Mcell-steps/s", "h2d_bytes_per_step": bytes_io,
                         "d2h_bytes_per_step": bytes_io},
-                "roofline_step": roof_step[other]},
+                "roofline_step": roof_step[other],
+                "roofline_fp64": fp64_roofline(other, sec["ms"] / args.steps, fp64_tf)},
         "mixed_vs_fp64": round((mixed_arm["ms"] and fp64_arm["ms"] / mixed_arm["ms"]) or 0, 3),
         "error_vs_fp64": {"velocity_rel_l2": err, "max_div_mixed": mixed_arm["stats"]["max_div"],
                           "max_div_fp64": fp64_arm["stats"]["max_div"],
@@ -508,6 +540,7 @@ def bench_gb300(args):
         "fma_rate_tflops": {"fp64": round(fp64_tf, 3), "fp32": round(fp32_tf, 2),
                             "how": "register-only FMA chains, 8 blocks of 256 per SM, best of 3"},
         "explicit_kernels": explicit,
+        "roofline_fp64": fp64_roofline(args.precision, head["ms"] / args.steps, fp64_tf),
         "profile_ms": {k: [v[0], round(v[1], 3)] for k, v in sorted(prof.items())},
     }
     lv = s.get_field("lvset")
@@ -697,11 +730,15 @@ def main():
                     help="headline arm only (set-up, warm-up, timed region) for profiler runs")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"],
                     help="arithmetic of the headline arm (the other one is measured beside it)")
+    ap.add_argument("--workload", default="sphere", choices=["sphere", "cavity64", "channel"],
+                    help="with --profile-only: the case of the profiled steps (the headline is the sphere)")
     ap.add_argument("--lvset-from-gpu", action="store_true",
                     help="reference arm: take the level set from the GPU set-up instead of the CPU transform")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
+    if args.workload != "sphere" and not args.profile_only:
+        ap.error("--workload selects the case of --profile-only runs")
     if args.impl == "reference":
         return bench_reference(args)
     return bench_gb300(args)
