@@ -51,10 +51,16 @@ __device__ __forceinline__ void stp(T *p, long long q, const Pack<T> &x) {
     reinterpret_cast<Pack<T> *>(p)[q] = x;
 }
 
-// Weighted |r| for the divergence criterion (FP32 is ample for a stopping test).
+// Weighted |r| for the divergence criterion (FP32 is ample for a stopping
+// test; an FP64 y is rounded on the integer pipe, since an FP64 -> FP32
+// conversion instruction runs at the FP64 rate and these kernels are
+// FP64-pipe bound).
+__device__ __forceinline__ float to_f32(double y) { return d2f_int(y); }
+__device__ __forceinline__ float to_f32(float y) { return y; }
+
 template <typename T>
 __device__ __forceinline__ float divw(const OpT<T> &c, long long P, T y) {
-    return c.wdiv[P] * fabsf((float)y);
+    return c.wdiv[P] * fabsf(to_f32(y));
 }
 
 // Stopping test: ||r|| < tol ||b|| (tol > 0) or max weighted |r| <= divtol
@@ -89,7 +95,9 @@ __device__ __forceinline__ void reduce_and_finish(const A (&v)[NV], double *smem
 }
 
 // ---------------------------------------------------------------- init --
-// x = 0, r = r0 = b, p = v = 0, ||b||^2.  The stopping test of the solve is
+// x = 0, r = b, ||b||^2; the first p update of the loop sets p = r0 = r
+// (restart flag), so nothing reads p, r0 or v before it writes them.  The
+// stopping test of the solve is
 // fixed here: (tol, divtol) as given, or, for the inner solve of a
 // refinement cycle (outer != null), derived from the outer state: the
 // relative tolerance is raised to what the outer FP64 test still needs
@@ -97,7 +105,7 @@ __device__ __forceinline__ void reduce_and_finish(const A (&v)[NV], double *smem
 // scaled units of the inner right-hand side.
 template <typename T, int NC>
 __global__ void __launch_bounds__(KTHREADS)
-k_bicg_init(const long long n, const T *__restrict__ b, T *x, T *r, T *r0, T *p, T *v, KScal *sc, double *partials,
+k_bicg_init(const long long n, const T *__restrict__ b, T *x, T *r, KScal *sc, double *partials,
             unsigned int *counter, const double tol, const double divtol, const IRScal *__restrict__ outer,
             const double outer_tol, const double outer_divtol, const LoopCtl lc) {
     pdl_enter();
@@ -112,9 +120,6 @@ k_bicg_init(const long long n, const T *__restrict__ b, T *x, T *r, T *r0, T *p,
             const T bv = b[o + P];
             x[o + P] = 0;
             r[o + P] = bv;
-            r0[o + P] = bv;
-            p[o + P] = 0;
-            v[o + P] = 0;
             a[c] += bv * bv;
         }
     }
@@ -131,7 +136,7 @@ k_bicg_init(const long long n, const T *__restrict__ b, T *x, T *r, T *r0, T *p,
             s.iters = 0;
             s.state = tot[c] == 0.0 ? KS_DONE : KS_RUN;
             s.divmax = 0.0;
-            s.restart = 0;
+            s.restart = 1;   // the first p update sets p = r0 = r
             s.tol = tol;
             s.divtol = divtol;
             if (outer) {
@@ -208,7 +213,8 @@ __device__ __forceinline__ void sweep_rows(const OpT<T> &A, const bool (&run)[NC
     }
 }
 
-// The same with x holding an initial guess: r = r0 = b - A x, p = v = 0,
+// The same with x holding an initial guess: r = b - A x (p = r0 = r at the
+// first p update),
 // ||b||^2 (the relative test stays relative to b; to the initial residual
 // where b = 0, whose solution x = 0 a relative test to 0 would never
 // reach), ||r||^2 and the divergence max of r; a guess that already passes
@@ -216,7 +222,7 @@ __device__ __forceinline__ void sweep_rows(const OpT<T> &A, const bool (&run)[NC
 template <typename T, int NC>
 __global__ void __launch_bounds__(SW_THREADS)
 k_bicg_init_guess(const OpT<T> A, const int op, const long long n, const T *__restrict__ b, const T *__restrict__ x,
-                  T *r, T *r0, T *p, T *v, KScal *sc, double *partials, unsigned int *counter, const double tol,
+                  T *r, KScal *sc, double *partials, unsigned int *counter, const double tol,
                   const double divtol, const LoopCtl lc) {
     pdl_enter();
     __shared__ double smem[32 * (2 * NC + 1)];
@@ -232,9 +238,6 @@ k_bicg_init_guess(const OpT<T> A, const int op, const long long n, const T *__re
         const long long o = c * n;
         const T bv = b[o + P];
         r[o + P] = y;
-        r0[o + P] = y;
-        p[o + P] = 0;
-        v[o + P] = 0;
         a[c] += bv * bv;
         a[NC + c] += y * y;
         if (divtol > 0) dmax = fmaxf(dmax, divw(A, P, y));
@@ -260,7 +263,7 @@ k_bicg_init_guess(const OpT<T> A, const int op, const long long n, const T *__re
             s.tol = tol;
             s.divtol = divtol;
             s.divmax = tot[2 * NC];
-            s.restart = 0;
+            s.restart = 1;   // the first p update sets p = r0 = r
             const bool done = tot[NC + c] == 0.0 || converged(tot[NC + c], s.bnorm2, tot[2 * NC], tol, divtol);
             s.state = done ? KS_DONE : KS_RUN;
             go = go || !done;
@@ -601,7 +604,7 @@ k_ir_to32(const long long n, const double *__restrict__ r, const IRScal *sc, flo
     for (int c = 0; c < NC; c++) {
         const double s = sc[c].scale;
         const long long o = c * n;
-        GRID_STRIDE(P, n) b32[o + P] = (float)(r[o + P] * s);
+        GRID_STRIDE(P, n) b32[o + P] = d2f_int(r[o + P] * s);
     }
 }
 
@@ -725,10 +728,10 @@ template <typename T>
 static void launch_init(cudaStream_t st, KrylovWork<T> &w, const T *b, T *x, double tol, double divtol,
                         const IRScal *outer, double outer_tol, double outer_divtol, LoopCtl lc) {
     if (w.nc == 3)
-        launch_pdl(k_bicg_init<T, 3>, w.nblk, KTHREADS, 0, st, w.n, b, x, w.r, w.r0, w.p, w.v, w.scal, w.partials,
+        launch_pdl(k_bicg_init<T, 3>, w.nblk, KTHREADS, 0, st, w.n, b, x, w.r, w.scal, w.partials,
                                                        w.counter, tol, divtol, outer, outer_tol, outer_divtol, lc);
     else
-        launch_pdl(k_bicg_init<T, 1>, w.nblk, KTHREADS, 0, st, w.n, b, x, w.r, w.r0, w.p, w.v, w.scal, w.partials,
+        launch_pdl(k_bicg_init<T, 1>, w.nblk, KTHREADS, 0, st, w.n, b, x, w.r, w.scal, w.partials,
                                                        w.counter, tol, divtol, outer, outer_tol, outer_divtol, lc);
     note_launches(1);
 }
@@ -737,11 +740,11 @@ template <typename T>
 static void launch_init_guess(cudaStream_t st, const OpT<T> &A, int op, KrylovWork<T> &w, const T *b, const T *x,
                               double tol, double divtol, LoopCtl lc) {
     if (w.nc == 3)
-        launch_pdl(k_bicg_init_guess<T, 3>, A.sw.nblocks, SW_THREADS, 0, st, A, op, w.n, b, x, w.r, w.r0, w.p, w.v,
-                   w.scal, w.partials, w.counter, tol, divtol, lc);
+        launch_pdl(k_bicg_init_guess<T, 3>, A.sw.nblocks, SW_THREADS, 0, st, A, op, w.n, b, x, w.r, w.scal,
+                   w.partials, w.counter, tol, divtol, lc);
     else
-        launch_pdl(k_bicg_init_guess<T, 1>, A.sw.nblocks, SW_THREADS, 0, st, A, op, w.n, b, x, w.r, w.r0, w.p, w.v,
-                   w.scal, w.partials, w.counter, tol, divtol, lc);
+        launch_pdl(k_bicg_init_guess<T, 1>, A.sw.nblocks, SW_THREADS, 0, st, A, op, w.n, b, x, w.r, w.scal,
+                   w.partials, w.counter, tol, divtol, lc);
     note_launches(1);
 }
 
