@@ -89,6 +89,7 @@ struct GhostArgs {
     const double *w;         // [8*g+e] normalised weights (0 where skipped)
     const double *wself;     // weight of the ghost cell in its own stencil
     double *old;             // [4*g]: snapshot of u1,u2,u3,p
+    const int *hlevel_start; // host copy of level_start (launch sizes; not read on the device)
 };
 
 void launch_conv_rhs(cudaStream_t s, const Grid &g, const Axis &ax, const Axis &ay, const Axis &az,

@@ -93,6 +93,7 @@ struct ibm3d_device {
     float *ut32 = nullptr;   // u~ (3 x ncell floats)
     // Ghost cells.
     int nghost = 0, nlevels = 0;
+    std::vector<int> ghost_level_start;   // host copy of the ghosts' level starts (launch sizes)
     int *g_mem = nullptr;
     double *g_dmem = nullptr;
     int8_t *g_kind = nullptr;
@@ -616,7 +617,9 @@ bool build_ghosts(IBMSolver *sv) {
         cudaMemcpyAsync(dm, w.data(), sizeof(double) * 8 * ng, cudaMemcpyHostToDevice, d->s);
         cudaMemcpyAsync(dm + 8 * ng, wself.data(), sizeof(double) * ng, cudaMemcpyHostToDevice, d->s);
         cudaMemcpyAsync(d->g_kind, kind.data(), 8 * ng, cudaMemcpyHostToDevice, d->s);
-        d->gargs = GhostArgs{ng, nlev, im + 17 * ng, im, im + ng, d->g_kind, dm, dm + 8 * ng, dm + 9 * ng};
+        d->ghost_level_start = lstart;
+        d->gargs = GhostArgs{ng, nlev, im + 17 * ng, im, im + ng, d->g_kind, dm, dm + 8 * ng, dm + 9 * ng,
+                             d->ghost_level_start.data()};
         d->g_gidx = im + 9 * ng;
         d->g_gw = dm;
         d->g_gwself = dm + 8 * ng;

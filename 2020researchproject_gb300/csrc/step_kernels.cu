@@ -397,54 +397,64 @@ void launch_interp_stag(cudaStream_t s, const Grid &g, const Axis &ax, const Axi
 // into dependency levels at assembly; values of "higher" ghosts are
 // snapshotted first, then the levels run in order inside one block.
 // ------------------------------------------------------------------------
-__global__ void __launch_bounds__(1024)
-k_ghost_update(GhostArgs a, double *u0, double *u1, double *u2, double *p) {
-    const int ng = a.nghost;
-    for (int g = threadIdx.x; g < ng; g += blockDim.x) {
-        const long long c = a.cell[g];
-        a.old[4 * g + 0] = u0[c];
-        a.old[4 * g + 1] = u1[c];
-        a.old[4 * g + 2] = u2[c];
-        a.old[4 * g + 3] = p[c];
-    }
-    __syncthreads();
-    for (int lev = 0; lev < a.nlevels; lev++) {
-        const int g0 = a.level_start[lev], g1 = a.level_start[lev + 1];
-        for (int g = g0 + threadIdx.x; g < g1; g += blockDim.x) {
-            double s0 = 0, s1 = 0, s2 = 0, s3 = 0;
-            for (int e = 0; e < 8; e++) {
-                const int kind = a.kind[8 * g + e];
-                if (kind == GK_SKIP) continue;
-                const double w = a.w[8 * g + e];
-                if (kind == GK_OLD) {
-                    const int h = a.ref[8 * g + e];
-                    s0 += w * a.old[4 * h + 0];
-                    s1 += w * a.old[4 * h + 1];
-                    s2 += w * a.old[4 * h + 2];
-                    s3 += w * a.old[4 * h + 3];
-                } else {
-                    const long long c = a.ref[8 * g + e];
-                    s0 += w * u0[c];
-                    s1 += w * u1[c];
-                    s2 += w * u2[c];
-                    s3 += w * p[c];
-                }
-            }
-            const long long c = a.cell[g];
-            const double lu = 1 + a.wself[g], lp = 1 - a.wself[g];
-            u0[c] = -s0 / lu;
-            u1[c] = -s1 / lu;
-            u2[c] = -s2 / lu;
-            if (lp != 0) p[c] = s3 / lp;
+// The ghosts' rows are FP64 (interpolation sums and the reference's
+// divisions): spread over the whole GPU - one launch snapshots the values
+// "higher" ghosts read, then one launch per level (a level reads only the
+// snapshot, fluid cells and earlier levels) - rather than inside one
+// block, whose single SM's FP64 pipe bound it.
+__global__ void __launch_bounds__(256)
+k_ghost_snapshot(GhostArgs a, const double *u0, const double *u1, const double *u2, const double *p) {
+    pdl_enter();
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= a.nghost) return;
+    const long long c = a.cell[g];
+    a.old[4 * g + 0] = u0[c];
+    a.old[4 * g + 1] = u1[c];
+    a.old[4 * g + 2] = u2[c];
+    a.old[4 * g + 3] = p[c];
+}
+
+__global__ void __launch_bounds__(128)
+k_ghost_level(GhostArgs a, const int g0, const int g1, double *u0, double *u1, double *u2, double *p) {
+    pdl_enter();
+    const int g = g0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= g1) return;
+    double s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+    for (int e = 0; e < 8; e++) {
+        const int kind = a.kind[8 * g + e];
+        if (kind == GK_SKIP) continue;
+        const double w = a.w[8 * g + e];
+        if (kind == GK_OLD) {
+            const int h = a.ref[8 * g + e];
+            s0 += w * a.old[4 * h + 0];
+            s1 += w * a.old[4 * h + 1];
+            s2 += w * a.old[4 * h + 2];
+            s3 += w * a.old[4 * h + 3];
+        } else {
+            const long long c = a.ref[8 * g + e];
+            s0 += w * u0[c];
+            s1 += w * u1[c];
+            s2 += w * u2[c];
+            s3 += w * p[c];
         }
-        __syncthreads();
     }
+    const long long c = a.cell[g];
+    const double lu = 1 + a.wself[g], lp = 1 - a.wself[g];
+    u0[c] = -s0 / lu;
+    u1[c] = -s1 / lu;
+    u2[c] = -s2 / lu;
+    if (lp != 0) p[c] = s3 / lp;
 }
 
 void launch_ghost_update(cudaStream_t s, const GhostArgs &a, double *const u[3], double *p) {
     if (a.nghost == 0) return;
-    k_ghost_update<<<1, 1024, 0, s>>>(a, u[0], u[1], u[2], p);
-    note_launches(1);
+    launch_pdl(k_ghost_snapshot, (a.nghost + 255) / 256, 256, 0, s, a, (const double *)u[0], (const double *)u[1],
+               (const double *)u[2], (const double *)p);
+    for (int lev = 0; lev < a.nlevels; lev++) {
+        const int g0 = a.hlevel_start[lev], g1 = a.hlevel_start[lev + 1];
+        if (g1 > g0) launch_pdl(k_ghost_level, (g1 - g0 + 127) / 128, 128, 0, s, a, g0, g1, u[0], u[1], u[2], p);
+    }
+    note_launches(1 + a.nlevels);
 }
 
 // Interior solid cells -> NaN (the SOLID branch of update_ghost).
