@@ -183,6 +183,68 @@ k_mg0_color(const OpT<T> c, const FineRows<T> fr, T *__restrict__ z, const int c
         if (upd[p]) z[Ps[p]] = val[p];
 }
 
+// The first sweep's two colour passes on z = 0 in one launch (red/black
+// without a periodic seam, where no ghost stencil reaches an outer cell):
+// each thread takes the (k, k+1) pair of each of its planes.  The colour-0
+// cell takes its value after the first pass (r, or 0 on a ghost row), the
+// colour-1 cell the Gauss-Seidel update from its neighbours' values after
+// that pass (r of interior non-ghost neighbours, 0 elsewhere; 0 on a ghost
+// row): the same arithmetic as k_mg0_init3 followed by the colour-1 pass of
+// k_mg0_color, one launch fewer per V-cycle.  Outer cells are left as they
+// are: nothing reads them before the sweep's outer rows set them.
+template <typename T, bool SPLIT>
+__global__ void __launch_bounds__(256)
+k_mg0_first(const OpT<T> c, const FineRows<T> fr, T *__restrict__ z, const T omega, const int *gate) {
+    MG_GATE(gate);
+    const Grid &g = c.g;
+    const int j = blockIdx.y * 8 + threadIdx.y;
+    const int i0 = blockIdx.z * MG0_PLANES;
+    const long long sx = g.sx, sy = g.sy;
+    const int jj = min(j, g.ny - 1);
+    const T kmy = c.km[1][jj + 2], kpy = c.kp[1][jj + 2];
+    long long P0s[MG0_PLANES], P1s[MG0_PLANES];
+    T v0[MG0_PLANES], v1[MG0_PLANES];
+    bool ok0[MG0_PLANES], ok1[MG0_PLANES];
+    // A colour-0 cell's value after the first pass (a neighbour of the
+    // colour-1 cell; its padded index Q and layout index always exist).
+    auto first = [&](int a, int b, int e, long long Q) -> T {
+        const bool in = a >= 0 && a < g.nx && b >= 0 && b < g.ny && e >= 0 && e < g.nz;
+        const T rn = fr.r[SPLIT ? fr.split_index(a, b, e) : Q];
+        return in && c.flag[Q] != GHOST ? rn : (T)0;
+    };
+#pragma unroll
+    for (int p = 0; p < MG0_PLANES; p++) {
+        const int i = min(i0 + p, g.nx - 1);
+        const bool okp = j < g.ny && i0 + p < g.nx;
+        const int kb = 2 * (blockIdx.x * 32 + threadIdx.x);
+        const int k0 = kb + ((i + jj) & 1), k1 = kb + ((i + jj + 1) & 1);
+        ok0[p] = okp && k0 < g.nz;
+        ok1[p] = okp && k1 < g.nz;
+        const int k0c = min(k0, g.nz - 1), k1c = min(k1, g.nz - 1);
+        const long long P0 = cidx(g, i, jj, k0c), P1 = cidx(g, i, jj, k1c);
+        const long long q0 = SPLIT ? fr.split_index(i, jj, k0c) : P0, q1 = SPLIT ? fr.split_index(i, jj, k1c) : P1;
+        v0[p] = c.flag[P0] != GHOST ? fr.r[q0] : (T)0;
+        const uint8_t fl = fr.flag[q1];
+        const T rv = fr.r[q1], dv = fr.dinv[q1];
+        const T zw = first(i - 1, jj, k1c, P1 - sx), ze = first(i + 1, jj, k1c, P1 + sx);
+        const T zs = first(i, jj - 1, k1c, P1 - sy), zn = first(i, jj + 1, k1c, P1 + sy);
+        const T zd = first(i, jj, k1c - 1, P1 - 1), zu = first(i, jj, k1c + 1, P1 + 1);
+        const T zc = 0;
+        const int I = i + 2, K = k1c + 2;
+        const T nb = c.km[0][I] * zw + c.kp[0][I] * ze + kmy * zs + kpy * zn + c.km[2][K] * zd + c.kp[2][K] * zu;
+        const bool fluid = fl == FLUID && !(c.p_singular && P1 == c.pinned);
+        const T gs = rv + dv * nb;
+        v1[p] = fl == GHOST ? (T)0 : fluid ? (omega == (T)1 ? gs : zc + omega * (gs - zc)) : rv;
+        P0s[p] = P0;
+        P1s[p] = P1;
+    }
+#pragma unroll
+    for (int p = 0; p < MG0_PLANES; p++) {
+        if (ok0[p]) z[P0s[p]] = v0[p];
+        if (ok1[p]) z[P1s[p]] = v1[p];
+    }
+}
+
 // The first colour pass of a V-cycle on z = 0, as one pass over the whole
 // padded array: colour-0 interior rows take r (r + dinv * 0, and r for
 // solid and pinned rows), every other cell 0.  A 3-D launch over the
@@ -1515,14 +1577,20 @@ int GMG<T>::smooth0(cudaStream_t s, const FineRows<T> &fr, T *z, int sweeps, boo
     };
     for (int it = 0; it < sweeps; it++) {
         const int tc = tb("mg0_color");
-        for (int col = 0; col < (seam ? 4 : 2); col++, k++) {
-            if (it == 0 && col == 0 && from_zero)
-                launch_pdl(fr.split ? k_mg0_init3<T, true> : k_mg0_init3<T, false>,
-                           dim3((g.nz + 35) / 32, (g.ny + 11) / 8, (g.nx + 3 + MG0_IPLANES) / MG0_IPLANES),
-                           dim3(32, 8), 0, s, A_, fr, z, per, gate);
-            else
-                launch_pdl(fr.split ? k_mg0_color<T, true> : k_mg0_color<T, false>, grd, blk, 0, s, A_, fr, z, col,
-                           seam ? 0 : 1, per, (T)cfg_.omega, gate);
+        if (it == 0 && from_zero && !seam && !ghost_reads_outer_) {
+            launch_pdl(fr.split ? k_mg0_first<T, true> : k_mg0_first<T, false>, grd, blk, 0, s, A_, fr, z, (T)cfg_.omega,
+                       gate);
+            k++;
+        } else {
+            for (int col = 0; col < (seam ? 4 : 2); col++, k++) {
+                if (it == 0 && col == 0 && from_zero)
+                    launch_pdl(fr.split ? k_mg0_init3<T, true> : k_mg0_init3<T, false>,
+                               dim3((g.nz + 35) / 32, (g.ny + 11) / 8, (g.nx + 3 + MG0_IPLANES) / MG0_IPLANES),
+                               dim3(32, 8), 0, s, A_, fr, z, per, gate);
+                else
+                    launch_pdl(fr.split ? k_mg0_color<T, true> : k_mg0_color<T, false>, grd, blk, 0, s, A_, fr, z,
+                               col, seam ? 0 : 1, per, (T)cfg_.omega, gate);
+            }
         }
         te(tc);
         const int to = tb("mg0_outer_ghost");
