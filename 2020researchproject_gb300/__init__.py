@@ -33,6 +33,7 @@ LIB_PATH = os.path.join(_PKG, "libibm3d_gb300.so")
 SOLVER_AMG, SOLVER_PCG, SOLVER_BiCGSTAB, SOLVER_GMRES = range(4)
 PRECOND_NONE, PRECOND_AMG = range(2)
 FP64, MIXED, MIXED_MG, MIXED32, MIXED32_IR = 0, 1, 2, 3, 4
+PVEC_FP64, PVEC_DFLOAT = 0, 1
 COARSEN_HALVE, COARSEN_SPACING = 0, 1
 DIR_NORTH, DIR_EAST, DIR_SOUTH, DIR_WEST, DIR_DOWN, DIR_UP = (1 << i for i in range(6))
 (BC_VELOCITY_COMPONENT, BC_PRESSURE, BC_STATIONARY_WALL, BC_FREE_SLIP_WALL,
@@ -101,6 +102,7 @@ def load_library(path: str = LIB_PATH):
         "IBMSolver_set_warm_start": (None, [vp, i]),
         "IBMSolver_set_max_iters": (None, [vp, i, i]),
         "IBMSolver_set_pressure_guess": (None, [vp, i]),
+        "IBMSolver_set_pressure_vectors": (None, [vp, i]),
         "IBMSolver_measure_fma_rate": (d, [i]),
         "IBMSolver_check_fp32_conversions": (i, [ctypes.c_longlong, dp, ctypes.POINTER(ctypes.c_ulonglong)]),
         "IBMSolver_autotune": (d, [vp, i, ip]),
@@ -347,6 +349,11 @@ class IBMSolver:
         linear extrapolation from the last two (1)."""
         self._lib.IBMSolver_set_pressure_guess(self._s, int(mode))
         self._check("set_pressure_guess")
+
+    def set_pressure_vectors(self, kind=PVEC_DFLOAT):
+        """MIXED32 pressure BiCGSTAB vectors: double-float (default) or FP64."""
+        self._lib.IBMSolver_set_pressure_vectors(self._s, int(kind))
+        self._check("set_pressure_vectors")
 
     def set_max_iters(self, max_mom=200, max_p=1000):
         """Krylov iteration caps (the reference's 200 and 1000 by default)."""

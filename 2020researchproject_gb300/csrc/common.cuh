@@ -141,6 +141,120 @@ __device__ __forceinline__ double f2d_int(float f) {
     return __hiloint2double((int)hi, (int)lo);
 }
 
+// ------------------------------------------------------- double-float --
+// dfloat: the unevaluated sum hi + lo of two FP32 values with
+// |lo| <= ulp(hi) / 2, a 48-bit significand with FP32's exponent range
+// (magnitudes below ~1e-38 lose the low word).  Its operations are
+// error-free transformations on the FP32 pipe: TwoSum (Knuth, TAOCP vol. 2,
+// 4.2.2, Theorem B), FastTwoSum (Dekker, "A floating-point technique for
+// extending the available precision", Numer. Math. 18, 1971) and TwoProduct
+// with one fused multiply-add, combined as in the double-double addition
+// and multiplication of Hida, Li and Bailey ("Algorithms for quad-double
+// precision floating point arithmetic", ARITH-15, 2001) with FP32 words.
+// An add takes 20 FP32 operations and a multiply 7, against one FP64
+// operation at 1/72 of the FP32 issue rate on this part, so FP64-bound
+// vector kernels run several times faster on double-float vectors.  The
+// _rn intrinsics keep the compiler from contracting the transformations
+// into fused operations, which would break their exactness.
+struct dfloat {
+    float hi, lo;
+    dfloat() = default;
+    __host__ __device__ constexpr dfloat(float h, float l) : hi(h), lo(l) {}
+    __host__ __device__ constexpr dfloat(int v) : hi((float)v), lo(0.0f) {}
+    __host__ __device__ constexpr dfloat(float v) : hi(v), lo(0.0f) {}
+    // Nearest double-float of an FP64 value: hi = x rounded to FP32, lo = the
+    // rest (x - hi is exact in FP64) rounded to FP32.  On the device both
+    // roundings run on the integer pipe; the subtraction is one FP64 add.
+    __host__ __device__ dfloat(double x) {
+#ifdef __CUDA_ARCH__
+        hi = d2f_int(x);
+        lo = d2f_int(x - f2d_int(hi));
+#else
+        hi = (float)x;
+        lo = (float)(x - (double)hi);
+#endif
+    }
+    // hi + lo in FP64 (one FP64 add; exact when the two words' bits span at
+    // most 53 places).
+    __host__ __device__ explicit operator double() const {
+#ifdef __CUDA_ARCH__
+        return f2d_int(hi) + f2d_int(lo);
+#else
+        return (double)hi + (double)lo;
+#endif
+    }
+};
+
+__device__ __forceinline__ dfloat two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return dfloat(s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb)));
+}
+// |a| >= |b| (or a = 0).
+__device__ __forceinline__ dfloat fast_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    return dfloat(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+
+__device__ __forceinline__ dfloat operator+(dfloat a, dfloat b) {
+    const dfloat s = two_sum(a.hi, b.hi), t = two_sum(a.lo, b.lo);
+    dfloat u = fast_two_sum(s.hi, __fadd_rn(s.lo, t.hi));
+    return fast_two_sum(u.hi, __fadd_rn(u.lo, t.lo));
+}
+__device__ __forceinline__ dfloat operator-(dfloat a) { return dfloat(-a.hi, -a.lo); }
+__device__ __forceinline__ dfloat operator-(dfloat a, dfloat b) { return a + (-b); }
+__device__ __forceinline__ dfloat operator*(dfloat a, dfloat b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);
+    e = __fmaf_rn(a.hi, b.lo, e);
+    e = __fmaf_rn(a.lo, b.hi, e);
+    return fast_two_sum(p, e);
+}
+__device__ __forceinline__ dfloat &operator+=(dfloat &a, dfloat b) { return a = a + b; }
+__device__ __forceinline__ dfloat &operator-=(dfloat &a, dfloat b) { return a = a - b; }
+
+// Lazy accumulation of a sum of products (Ogita, Rump and Oishi, "Accurate
+// sum and dot product", SIAM J. Sci. Comput. 26, 2005, Algorithm Dot2, with
+// double-float factors): acc.hi carries the FP32 running sum, acc.lo the
+// FP32 sum of every rounding error of the products and additions and of the
+// products' low-word terms, not renormalised between terms (the
+// double-float addition that combines such sums accepts them as they are).
+// 12 FP32 operations per term against 27 for a double-float multiply and
+// add; its error, a few units of 2^-48 of the sum of the terms'
+// magnitudes up to a factor of the number of terms, is larger than the
+// chained operations', which the vector updates keep.
+__device__ __forceinline__ void df_mac(dfloat &acc, dfloat a, dfloat b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);
+    e = __fmaf_rn(a.hi, b.lo, e);
+    e = __fmaf_rn(a.lo, b.hi, e);
+    const dfloat s = two_sum(acc.hi, p);
+    acc.hi = s.hi;
+    acc.lo = __fadd_rn(acc.lo, __fadd_rn(s.lo, e));
+}
+
+// The expressions the Krylov and operator kernels build from products,
+// written once for FP32, FP64 and double-float entries (the same arithmetic
+// as the inline expressions they replace).  Dot-product accumulation alone
+// is lazy for double-floats: it only feeds the iteration's scalars.
+template <typename T>
+__device__ __forceinline__ void mac(T &acc, T a, T b) { acc += a * b; }
+__device__ __forceinline__ void mac(dfloat &acc, dfloat a, dfloat b) { df_mac(acc, a, b); }
+// x - a b
+template <typename T>
+__device__ __forceinline__ T sub_mul(T x, T a, T b) { return x - a * b; }
+// x + (a p + b s)
+template <typename T>
+__device__ __forceinline__ T add_mul2(T x, T a, T p, T b, T s) { return x + (a * p + b * s); }
+// r + beta (p - omega v)
+template <typename T>
+__device__ __forceinline__ T p_update(T r, T beta, T p, T om, T v) { return r + beta * (p - om * v); }
+// a0 x0 + a1 x1 + ... + a5 x5 (a stencil's neighbour sum)
+template <typename T>
+__device__ __forceinline__ T sum6(T a0, T x0, T a1, T x1, T a2, T x2, T a3, T x3, T a4, T x4, T a5, T x5) {
+    return a0 * x0 + a1 * x1 + a2 * x2 + a3 * x3 + a4 * x4 + a5 * x5;
+}
+
 // Per-axis 1-D tables (device pointers, N+4 entries, index i+2).
 struct Axis {
     const double *d;     // cell width
@@ -270,6 +384,16 @@ inline void launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t sme
 // maximum reduction reaches the host, which turns it into a status.
 __device__ __forceinline__ double nanmax(double a, double b) { return (a != a || b != b) ? a + b : fmax(a, b); }
 __device__ __forceinline__ float nanmax(float a, float b) { return (a != a || b != b) ? a + b : fmaxf(a, b); }
+__device__ __forceinline__ dfloat nanmax(dfloat a, dfloat b) {
+    return (a.hi != a.hi || b.hi != b.hi) ? a + b : (a.hi > b.hi || (a.hi == b.hi && a.lo >= b.lo)) ? a : b;
+}
+
+// Warp shuffle of a reduction's accumulator type.
+__device__ __forceinline__ double shfl_down(double x, int o) { return __shfl_down_sync(0xffffffffu, x, o); }
+__device__ __forceinline__ float shfl_down(float x, int o) { return __shfl_down_sync(0xffffffffu, x, o); }
+__device__ __forceinline__ dfloat shfl_down(dfloat x, int o) {
+    return dfloat(__shfl_down_sync(0xffffffffu, x.hi, o), __shfl_down_sync(0xffffffffu, x.lo, o));
+}
 
 // Deterministic two-level reductions: every block writes its partials to
 // partials[block][v]; the last block to finish reduces them in a fixed
@@ -342,7 +466,7 @@ __device__ inline void block_reduce(const A (&v)[NV], double (&out)[NV], double 
         A x = v[q];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
-            const A y = __shfl_down_sync(0xffffffffu, x, o);
+            const A y = shfl_down(x, o);
             x = q < NS ? x + y : nanmax(x, y);
         }
         if (lane == 0) smem[warp * NV + q] = (double)x;

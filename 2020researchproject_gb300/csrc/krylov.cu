@@ -14,6 +14,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "common.cuh"
@@ -32,6 +33,7 @@ namespace ibm {
 template <typename T> struct AccT;
 template <> struct AccT<double> { using type = double; };
 template <> struct AccT<float> { using type = float; };
+template <> struct AccT<dfloat> { using type = dfloat; };
 
 // 16-byte packs for the streaming vector kernels: with n % 4 == 0 every
 // vector (and every component of a 3-component vector) starts on a 16-byte
@@ -50,6 +52,16 @@ template <typename T>
 __device__ __forceinline__ void stp(T *p, long long q, const Pack<T> &x) {
     reinterpret_cast<Pack<T> *>(p)[q] = x;
 }
+// PW<T> entries of type E (the FP32 p^ and s^ of double-float vectors; a
+// Pack<T> when E = T).
+template <typename E, int N>
+struct alignas(sizeof(E) * N) PackN {
+    E v[N];
+};
+template <typename T, typename E>
+__device__ __forceinline__ PackN<E, PW<T>> ldpn(const E *p, long long q) {
+    return reinterpret_cast<const PackN<E, PW<T>> *>(p)[q];
+}
 
 // Weighted |r| for the divergence criterion (FP32 is ample for a stopping
 // test; an FP64 y is rounded on the integer pipe, since an FP64 -> FP32
@@ -57,6 +69,7 @@ __device__ __forceinline__ void stp(T *p, long long q, const Pack<T> &x) {
 // FP64-pipe bound).
 __device__ __forceinline__ float to_f32(double y) { return d2f_int(y); }
 __device__ __forceinline__ float to_f32(float y) { return y; }
+__device__ __forceinline__ float to_f32(dfloat y) { return y.hi; }
 
 template <typename T>
 __device__ __forceinline__ float divw(const OpT<T> &c, long long P, T y) {
@@ -102,10 +115,11 @@ __device__ __forceinline__ void reduce_and_finish(const A (&v)[NV], double *smem
 // refinement cycle (outer != null), derived from the outer state: the
 // relative tolerance is raised to what the outer FP64 test still needs
 // (half of it, as margin) and the divergence bound is expressed in the
-// scaled units of the inner right-hand side.
-template <typename T, int NC>
+// scaled units of the inner right-hand side.  b may be FP64 under
+// double-float vectors (B = double, T = dfloat), converted as it is read.
+template <typename T, int NC, typename B = T>
 __global__ void __launch_bounds__(KTHREADS)
-k_bicg_init(const long long n, const T *__restrict__ b, T *x, T *r, KScal *sc, double *partials,
+k_bicg_init(const long long n, const B *__restrict__ b, T *x, T *r, KScal *sc, double *partials,
             unsigned int *counter, const double tol, const double divtol, const IRScal *__restrict__ outer,
             const double outer_tol, const double outer_divtol, const LoopCtl lc) {
     pdl_enter();
@@ -117,10 +131,10 @@ k_bicg_init(const long long n, const T *__restrict__ b, T *x, T *r, KScal *sc, d
     for (int c = 0; c < NC; c++) {
         const long long o = c * n;
         GRID_STRIDE(P, n) {
-            const T bv = b[o + P];
+            const T bv = (T)b[o + P];
             x[o + P] = 0;
             r[o + P] = bv;
-            a[c] += bv * bv;
+            mac(a[c], bv, bv);
         }
     }
     reduce_and_finish<NC, NC>(a, smem, partials, counter, [&](const double *tot) {
@@ -175,11 +189,11 @@ k_bicg_p(const long long n, const T *__restrict__ r, T *__restrict__ p, const T 
                 const Pack<T> rr = ldp(r, op + q), vv = ldp(v, op + q);
                 Pack<T> pp = ldp(p, op + q);
 #pragma unroll
-                for (int l = 0; l < PW<T>; l++) pp.v[l] = rr.v[l] + beta * (pp.v[l] - om * vv.v[l]);
+                for (int l = 0; l < PW<T>; l++) pp.v[l] = p_update(rr.v[l], beta, pp.v[l], om, vv.v[l]);
                 stp(p, op + q, pp);
             }
         } else {
-            GRID_STRIDE(P, n) { p[o + P] = r[o + P] + beta * (p[o + P] - om * v[o + P]); }
+            GRID_STRIDE(P, n) { p[o + P] = p_update(r[o + P], beta, p[o + P], om, v[o + P]); }
         }
     }
 }
@@ -218,10 +232,11 @@ __device__ __forceinline__ void sweep_rows(const OpT<T> &A, const bool (&run)[NC
 // ||b||^2 (the relative test stays relative to b; to the initial residual
 // where b = 0, whose solution x = 0 a relative test to 0 would never
 // reach), ||r||^2 and the divergence max of r; a guess that already passes
-// the stopping test ends the solve before its first iteration.
-template <typename T, int NC>
-__global__ void __launch_bounds__(SW_THREADS)
-k_bicg_init_guess(const OpT<T> A, const int op, const long long n, const T *__restrict__ b, const T *__restrict__ x,
+// the stopping test ends the solve before its first iteration.  b as in
+// k_bicg_init.
+template <typename T, int NC, typename B = T>
+__global__ void __launch_bounds__(SW_THREADS, std::is_same<T, dfloat>::value ? 4 : 1)
+k_bicg_init_guess(const OpT<T> A, const int op, const long long n, const B *__restrict__ b, const T *__restrict__ x,
                   T *r, KScal *sc, double *partials, unsigned int *counter, const double tol,
                   const double divtol, const LoopCtl lc) {
     pdl_enter();
@@ -234,20 +249,22 @@ k_bicg_init_guess(const OpT<T> A, const int op, const long long n, const T *__re
         run[c] = true;
     }
     float dmax = 0.0f;
-    auto put = [&](int c, long long P, T y) {
-        const long long o = c * n;
-        const T bv = b[o + P];
-        r[o + P] = y;
-        a[c] += bv * bv;
-        a[NC + c] += y * y;
+    auto put = [&](int c, long long P, T bv, T y) {
+        r[c * n + P] = y;
+        mac(a[c], bv, bv);
+        mac(a[NC + c], y, y);
         if (divtol > 0) dmax = fmaxf(dmax, divw(A, P, y));
     };
     sweep_rows<T, NC>(
         A, run,
         [&](int c, long long P, int i, const Column<T> &q) {
-            put(c, P, b[c * n + P] - interior_row(A, op, x + c * n, P, i, q));
+            const T bv = (T)b[c * n + P];
+            put(c, P, bv, bv - interior_row(A, op, x + c * n, P, i, q));
         },
-        [&](int c, long long P) { put(c, P, b[c * n + P] - op_row(A, op, c, x + c * n, P)); });
+        [&](int c, long long P) {
+            const T bv = (T)b[c * n + P];
+            put(c, P, bv, bv - op_row(A, op, c, x + c * n, P));
+        });
     a[2 * NC] = dmax;
     reduce_and_finish<2 * NC + 1, 2 * NC>(a, smem, partials, counter, [&](const double *tot) {
         bool go = false;
@@ -275,7 +292,8 @@ k_bicg_init_guess(const OpT<T> A, const int op, const long long n, const T *__re
 // ------------------------------------------- v = A ph, alpha = rho/(r0,v) --
 template <typename T, int NC>
 __global__ void __launch_bounds__(SW_THREADS, (sizeof(T) == 4 || NC == 1) ? 4 : 2)
-k_bicg_spmv_v(const OpT<T> A, const int op, const long long n, const T *__restrict__ ph, T *__restrict__ v,
+k_bicg_spmv_v(const OpT<T> A, const int op, const long long n, const typename PrecT<T>::type *__restrict__ ph,
+              T *__restrict__ v,
               const T *__restrict__ r0, KScal *sc, double *partials, unsigned int *counter) {
     pdl_enter();
     __shared__ double smem[32 * NC];
@@ -292,13 +310,13 @@ k_bicg_spmv_v(const OpT<T> A, const int op, const long long n, const T *__restri
             const long long o = c * n;
             const T y = interior_row(A, op, ph + o, P, i, q);
             v[o + P] = y;
-            a[c] += r0[o + P] * y;
+            mac(a[c], r0[o + P], y);
         },
         [&](int c, long long P) {
             const long long o = c * n;
             const T y = op_row(A, op, c, ph + o, P);
             v[o + P] = y;
-            a[c] += r0[o + P] * y;
+            mac(a[c], r0[o + P], y);
         });
     reduce_and_finish<NC, NC>(a, smem, partials, counter, [&](const double *tot) {
         for (int c = 0; c < NC; c++) {
@@ -340,18 +358,18 @@ k_bicg_s(const OpT<T> A, const long long n, const T *__restrict__ r, const T *__
                 Pack<T> ss;
 #pragma unroll
                 for (int l = 0; l < PW<T>; l++) {
-                    const T y = rr.v[l] - al * vv.v[l];
+                    const T y = sub_mul(rr.v[l], al, vv.v[l]);
                     ss.v[l] = y;
-                    a[c] += y * y;
+                    mac(a[c], y, y);
                     if (want_div) dmax = fmaxf(dmax, divw(A, q * PW<T> + l, y));
                 }
                 stp(s, op + q, ss);
             }
         } else {
             GRID_STRIDE(P, n) {
-                const T y = r[o + P] - al * v[o + P];
+                const T y = sub_mul(r[o + P], al, v[o + P]);
                 s[o + P] = y;
-                a[c] += y * y;
+                mac(a[c], y, y);
                 if (want_div) dmax = fmaxf(dmax, divw(A, P, y));
             }
         }
@@ -376,7 +394,8 @@ k_bicg_s(const OpT<T> A, const long long n, const T *__restrict__ r, const T *__
 // --------------------------------------- t = A sh, omega = (t,s)/(t,t) --
 template <typename T, int NC>
 __global__ void __launch_bounds__(SW_THREADS, (sizeof(T) == 4 || NC == 1) ? 4 : 2)
-k_bicg_spmv_t(const OpT<T> A, const int op, const long long n, const T *__restrict__ sh, T *__restrict__ t,
+k_bicg_spmv_t(const OpT<T> A, const int op, const long long n, const typename PrecT<T>::type *__restrict__ sh,
+              T *__restrict__ t,
               const T *__restrict__ s, KScal *sc, double *partials, unsigned int *counter) {
     pdl_enter();
     __shared__ double smem[32 * 2 * NC];
@@ -393,15 +412,15 @@ k_bicg_spmv_t(const OpT<T> A, const int op, const long long n, const T *__restri
             const long long o = c * n;
             const T y = interior_row(A, op, sh + o, P, i, q);
             t[o + P] = y;
-            a[2 * c] += y * s[o + P];
-            a[2 * c + 1] += y * y;
+            mac(a[2 * c], y, s[o + P]);
+            mac(a[2 * c + 1], y, y);
         },
         [&](int c, long long P) {
             const long long o = c * n;
             const T y = op_row(A, op, c, sh + o, P);
             t[o + P] = y;
-            a[2 * c] += y * s[o + P];
-            a[2 * c + 1] += y * y;
+            mac(a[2 * c], y, s[o + P]);
+            mac(a[2 * c + 1], y, y);
         });
     reduce_and_finish<2 * NC, 2 * NC>(a, smem, partials, counter, [&](const double *tot) {
         for (int c = 0; c < NC; c++) {
@@ -423,7 +442,8 @@ k_bicg_spmv_t(const OpT<T> A, const int op, const long long n, const T *__restri
 template <typename T, int NC, bool VEC>
 __global__ void __launch_bounds__(KTHREADS)
 k_bicg_xr(const OpT<T> A, const long long n, T *__restrict__ x, T *__restrict__ r, const T *__restrict__ r0,
-          const T *__restrict__ ph, const T *__restrict__ sh, const T *__restrict__ s, const T *__restrict__ t,
+          const typename PrecT<T>::type *__restrict__ ph, const typename PrecT<T>::type *__restrict__ sh,
+          const T *__restrict__ s, const T *__restrict__ t,
           KScal *sc, double *partials, unsigned int *counter, const int maxit, const LoopCtl lc) {
     pdl_enter();
     __shared__ double smem[32 * (2 * NC + 1)];
@@ -440,7 +460,7 @@ k_bicg_xr(const OpT<T> A, const long long n, T *__restrict__ x, T *__restrict__ 
             // Converged on s: x += alpha ph, r = s.
             const T al = (T)sc[c].alpha;
             GRID_STRIDE(P, n) {
-                x[o + P] += al * ph[o + P];
+                x[o + P] += al * T(ph[o + P]);
                 r[o + P] = s[o + P];
             }
             continue;
@@ -451,16 +471,16 @@ k_bicg_xr(const OpT<T> A, const long long n, T *__restrict__ x, T *__restrict__ 
             const long long np = n / PW<T>, op = o / PW<T>;
             GRID_STRIDE(q, np) {
                 Pack<T> xx = ldp(x, op + q);
-                const Pack<T> pp = ldp(ph, op + q), ss = ldp(sh, op + q), s0 = ldp(s, op + q), tt = ldp(t, op + q),
-                              rr0 = ldp(r0, op + q);
+                const auto pp = ldpn<T>(ph, op + q), ss = ldpn<T>(sh, op + q);
+                const Pack<T> s0 = ldp(s, op + q), tt = ldp(t, op + q), rr0 = ldp(r0, op + q);
                 Pack<T> rr;
 #pragma unroll
                 for (int l = 0; l < PW<T>; l++) {
-                    xx.v[l] += al * pp.v[l] + om * ss.v[l];
-                    const T y = s0.v[l] - om * tt.v[l];
+                    xx.v[l] = add_mul2(xx.v[l], al, T(pp.v[l]), om, T(ss.v[l]));
+                    const T y = sub_mul(s0.v[l], om, tt.v[l]);
                     rr.v[l] = y;
-                    a[2 * c] += y * y;
-                    a[2 * c + 1] += rr0.v[l] * y;
+                    mac(a[2 * c], y, y);
+                    mac(a[2 * c + 1], rr0.v[l], y);
                     if (want_div) dmax = fmaxf(dmax, divw(A, q * PW<T> + l, y));
                 }
                 stp(x, op + q, xx);
@@ -468,11 +488,11 @@ k_bicg_xr(const OpT<T> A, const long long n, T *__restrict__ x, T *__restrict__ 
             }
         } else {
             GRID_STRIDE(P, n) {
-                x[o + P] += al * ph[o + P] + om * sh[o + P];
-                const T y = s[o + P] - om * t[o + P];
+                x[o + P] = add_mul2(x[o + P], al, T(ph[o + P]), om, T(sh[o + P]));
+                const T y = sub_mul(s[o + P], om, t[o + P]);
                 r[o + P] = y;
-                a[2 * c] += y * y;
-                a[2 * c + 1] += r0[o + P] * y;
+                mac(a[2 * c], y, y);
+                mac(a[2 * c + 1], r0[o + P], y);
                 if (want_div) dmax = fmaxf(dmax, divw(A, P, y));
             }
         }
@@ -628,6 +648,10 @@ k_ir_update(const long long n, double *x, const float *__restrict__ e, IRScal *s
 // ------------------------------------------------------------ workspace --
 template <typename T>
 void KrylovWork<T>::release() {
+    if (!owner) {   // a view: the buffers belong to another work
+        *this = KrylovWork<T>();
+        return;
+    }
     if (base) cudaFree(base);
     if (scal) cudaFree(scal);
     if (scal_h) cudaFreeHost(scal_h);
@@ -659,9 +683,9 @@ int KrylovWork<T>::allocate(long long ncell, int ncomp, bool precond, int maxblo
     s = q; q += m;
     t = q; q += m;
     if (precond) {
-        ph = q; q += m;
-        sh = q; q += m;
-    } else {
+        ph = reinterpret_cast<PT *>(q); q += m;
+        sh = reinterpret_cast<PT *>(q); q += m;
+    } else if constexpr (std::is_same<PT, T>::value) {
         ph = p;
         sh = s;
     }
@@ -676,6 +700,31 @@ int KrylovWork<T>::allocate(long long ncell, int ncomp, bool precond, int maxblo
 
 template struct KrylovWork<double>;
 template struct KrylovWork<float>;
+template void KrylovWork<dfloat>::release();
+
+KrylovWork<dfloat> dfloat_view(const KrylovWork<double> &w) {
+    static_assert(sizeof(dfloat) == sizeof(double), "double-float vectors take the FP64 vectors' place");
+    KrylovWork<dfloat> v;
+    v.owner = false;
+    v.n = w.n;
+    v.nc = w.nc;
+    v.nblk = w.nblk;
+    auto as = [](double *q) { return reinterpret_cast<dfloat *>(q); };
+    v.base = as(w.base);
+    v.r = as(w.r);
+    v.r0 = as(w.r0);
+    v.p = as(w.p);
+    v.v = as(w.v);
+    v.s = as(w.s);
+    v.t = as(w.t);
+    v.ph = reinterpret_cast<float *>(w.ph);
+    v.sh = reinterpret_cast<float *>(w.sh);
+    v.scal = w.scal;
+    v.scal_h = w.scal_h;
+    v.partials = w.partials;
+    v.counter = w.counter;
+    return v;
+}
 
 void IRWork::release() {
     if (r) cudaFree(r);
@@ -724,26 +773,26 @@ static bool all_in(const SC *s, int nc, int a, int b, int c2) {
     return true;
 }
 
-template <typename T>
-static void launch_init(cudaStream_t st, KrylovWork<T> &w, const T *b, T *x, double tol, double divtol,
+template <typename T, typename B>
+static void launch_init(cudaStream_t st, KrylovWork<T> &w, const B *b, T *x, double tol, double divtol,
                         const IRScal *outer, double outer_tol, double outer_divtol, LoopCtl lc) {
     if (w.nc == 3)
-        launch_pdl(k_bicg_init<T, 3>, w.nblk, KTHREADS, 0, st, w.n, b, x, w.r, w.scal, w.partials,
+        launch_pdl(k_bicg_init<T, 3, B>, w.nblk, KTHREADS, 0, st, w.n, b, x, w.r, w.scal, w.partials,
                                                        w.counter, tol, divtol, outer, outer_tol, outer_divtol, lc);
     else
-        launch_pdl(k_bicg_init<T, 1>, w.nblk, KTHREADS, 0, st, w.n, b, x, w.r, w.scal, w.partials,
+        launch_pdl(k_bicg_init<T, 1, B>, w.nblk, KTHREADS, 0, st, w.n, b, x, w.r, w.scal, w.partials,
                                                        w.counter, tol, divtol, outer, outer_tol, outer_divtol, lc);
     note_launches(1);
 }
 
-template <typename T>
-static void launch_init_guess(cudaStream_t st, const OpT<T> &A, int op, KrylovWork<T> &w, const T *b, const T *x,
+template <typename T, typename B>
+static void launch_init_guess(cudaStream_t st, const OpT<T> &A, int op, KrylovWork<T> &w, const B *b, const T *x,
                               double tol, double divtol, LoopCtl lc) {
     if (w.nc == 3)
-        launch_pdl(k_bicg_init_guess<T, 3>, A.sw.nblocks, SW_THREADS, 0, st, A, op, w.n, b, x, w.r, w.scal,
+        launch_pdl(k_bicg_init_guess<T, 3, B>, A.sw.nblocks, SW_THREADS, 0, st, A, op, w.n, b, x, w.r, w.scal,
                    w.partials, w.counter, tol, divtol, lc);
     else
-        launch_pdl(k_bicg_init_guess<T, 1>, A.sw.nblocks, SW_THREADS, 0, st, A, op, w.n, b, x, w.r, w.scal,
+        launch_pdl(k_bicg_init_guess<T, 1, B>, A.sw.nblocks, SW_THREADS, 0, st, A, op, w.n, b, x, w.r, w.scal,
                    w.partials, w.counter, tol, divtol, lc);
     note_launches(1);
 }
@@ -767,10 +816,10 @@ static void first_half(cudaStream_t st, const OpT<T> &A, int op, KrylovWork<T> &
     }
     const int tm = prof_begin(pf, op == OP_MOM ? "spmv_mom" : "spmv_p");
     if (nc == 3)
-        launch_pdl(k_bicg_spmv_v<T, 3>, A.sw.nblocks, SW_THREADS, 0, st, A, op, n, w.ph, w.v, w.r0, w.scal, w.partials,
+        launch_pdl(k_bicg_spmv_v<T, 3>, A.sw.nblocks, SW_THREADS, 0, st, A, op, n, w.phat(M), w.v, w.r0, w.scal, w.partials,
                                                                 w.counter);
     else
-        launch_pdl(k_bicg_spmv_v<T, 1>, A.sw.nblocks, SW_THREADS, 0, st, A, op, n, w.ph, w.v, w.r0, w.scal, w.partials,
+        launch_pdl(k_bicg_spmv_v<T, 1>, A.sw.nblocks, SW_THREADS, 0, st, A, op, n, w.phat(M), w.v, w.r0, w.scal, w.partials,
                                                                 w.counter);
     note_launches(1);
     prof_end(pf, tm);
@@ -792,18 +841,19 @@ static void second_half(cudaStream_t st, const OpT<T> &A, int op, KrylovWork<T> 
     }
     const int tm = prof_begin(pf, op == OP_MOM ? "spmv_mom" : "spmv_p");
     if (w.nc == 3)
-        launch_pdl(k_bicg_spmv_t<T, 3>, A.sw.nblocks, SW_THREADS, 0, st, A, op, w.n, w.sh, w.t, w.s, w.scal, w.partials,
+        launch_pdl(k_bicg_spmv_t<T, 3>, A.sw.nblocks, SW_THREADS, 0, st, A, op, w.n, w.shat(M), w.t, w.s, w.scal, w.partials,
                                                                 w.counter);
     else
-        launch_pdl(k_bicg_spmv_t<T, 1>, A.sw.nblocks, SW_THREADS, 0, st, A, op, w.n, w.sh, w.t, w.s, w.scal, w.partials,
+        launch_pdl(k_bicg_spmv_t<T, 1>, A.sw.nblocks, SW_THREADS, 0, st, A, op, w.n, w.shat(M), w.t, w.s, w.scal, w.partials,
                                                                 w.counter);
     note_launches(1);
     prof_end(pf, tm);
 }
 
 template <typename T>
-static void launch_xr(cudaStream_t st, const OpT<T> &A, KrylovWork<T> &w, T *x, int maxit, LoopCtl lc) {
-#define XR_ARGS A, w.n, x, w.r, w.r0, w.ph, w.sh, w.s, w.t, w.scal, w.partials, w.counter, maxit, lc
+static void launch_xr(cudaStream_t st, const OpT<T> &A, KrylovWork<T> &w, T *x, int maxit, const void *M,
+                      LoopCtl lc) {
+#define XR_ARGS A, w.n, x, w.r, w.r0, w.phat(M), w.shat(M), w.s, w.t, w.scal, w.partials, w.counter, maxit, lc
     const bool vec = w.n % 4 == 0;
     if (w.nc == 3 && vec) launch_pdl(k_bicg_xr<T, 3, true>, w.nblk, KTHREADS, 0, st, XR_ARGS);
     else if (w.nc == 3) launch_pdl(k_bicg_xr<T, 3, false>, w.nblk, KTHREADS, 0, st, XR_ARGS);
@@ -876,6 +926,38 @@ void WidenedPreconditioner::apply(cudaStream_t s, const double *r, double *z, co
     note_launches(1);
 }
 
+// Double-float vectors: the FP32 preconditioner takes the high words (r
+// rounded to FP32) when it cannot read them itself.
+__global__ void __launch_bounds__(KTHREADS)
+k_narrow_df(const long long n, const dfloat *__restrict__ r, float *r32, const int *gate) {
+    pdl_enter();
+    if (gate && *gate != KS_RUN) return;
+    GRID_STRIDE(P, n) r32[P] = r[P].hi;
+}
+
+
+// FP64 <-> double-float at the ends of a double-float solve.
+__global__ void __launch_bounds__(KTHREADS)
+k_to_dfloat(const long long n, const double *__restrict__ x, dfloat *y) {
+    pdl_enter();
+    GRID_STRIDE(P, n) y[P] = dfloat(x[P]);
+}
+
+__global__ void __launch_bounds__(KTHREADS)
+k_from_dfloat(const long long n, const dfloat *__restrict__ x, double *y) {
+    pdl_enter();
+    GRID_STRIDE(P, n) y[P] = (double)x[P];
+}
+
+void DFloatPreconditioner::apply(cudaStream_t s, const dfloat *r, float *z, const int *gate) {
+    fused_narrow = m32->apply_from_df(s, r, z, gate);
+    if (!fused_narrow) {
+        launch_pdl(k_narrow_df, nblk, KTHREADS, 0, s, n, r, r32, gate);
+        note_launches(1);
+        m32->apply(s, r32, z, gate);
+    }
+}
+
 static void launch_update(cudaStream_t st, IRWork &w, double *x) {
     if (w.nc == 3) launch_pdl(k_ir_update<3>, w.nblk, KTHREADS, 0, st, w.n, x, w.e32, w.scal, w.inner.scal);
     else launch_pdl(k_ir_update<1>, w.nblk, KTHREADS, 0, st, w.n, x, w.e32, w.scal, w.inner.scal);
@@ -905,6 +987,7 @@ int report(const KrylovWork<T> &w, SolveReport &rep) {
 
 template int report<double>(const KrylovWork<double> &, SolveReport &);
 template int report<float>(const KrylovWork<float> &, SolveReport &);
+template int report<dfloat>(const KrylovWork<dfloat> &, SolveReport &);
 
 int report(const IRWork &w, SolveReport &rep) {
     rep = SolveReport();
@@ -938,12 +1021,12 @@ static void host_loop(cudaStream_t st, const OpT<T> &A, int op, KrylovWork<T> &w
         first_half(st, A, op, w, M, pf);
         fetch(st, w);
         if (all_in(w.scal_h, w.nc, KS_HALF, KS_DONE, KS_BREAKDOWN)) {
-            launch_xr(st, A, w, x, maxit, none);
+            launch_xr(st, A, w, x, maxit, M, none);
             fetch(st, w);
             break;
         }
         second_half(st, A, op, w, M, pf);
-        launch_xr(st, A, w, x, maxit, none);
+        launch_xr(st, A, w, x, maxit, M, none);
         fetch(st, w);
     }
 }
@@ -961,6 +1044,31 @@ template int bicgstab<double>(cudaStream_t, const OpT<double> &, int, KrylovWork
                               double *, const SolveParams &, Preconditioner<double> *, SolveReport &);
 template int bicgstab<float>(cudaStream_t, const OpT<float> &, int, KrylovWork<float> &, const float *, float *,
                              const SolveParams &, Preconditioner<float> *, SolveReport &);
+
+static void launch_to_dfloat(cudaStream_t st, long long n, const double *x, dfloat *y) {
+    launch_pdl(k_to_dfloat, vector_blocks(n), KTHREADS, 0, st, n, x, y);
+    note_launches(1);
+}
+
+static void launch_from_dfloat(cudaStream_t st, long long n, const dfloat *x, double *y) {
+    launch_pdl(k_from_dfloat, vector_blocks(n), KTHREADS, 0, st, n, x, y);
+    note_launches(1);
+}
+
+int bicgstab_df(cudaStream_t st, const OpT<dfloat> &A, int op, KrylovWork<dfloat> &w, dfloat *xw, const double *b,
+                double *x, const SolveParams &prm, Preconditioner<dfloat> *M, SolveReport &rep) {
+    if (!M) return 2;   // p^ and s^ are the preconditioner's FP32 output
+    const long long m = w.n * w.nc;
+    if (prm.x_given) {
+        launch_to_dfloat(st, m, x, xw);
+        launch_init_guess(st, A, op, w, b, xw, prm.tol, prm.divtol, LoopCtl());
+    } else {
+        launch_init(st, w, b, xw, prm.tol, prm.divtol, nullptr, 0.0, 0.0, LoopCtl());
+    }
+    host_loop(st, A, op, w, xw, prm.maxit, M, prm.prof);
+    launch_from_dfloat(st, m, xw, x);
+    return report(w, rep);
+}
 
 int solve_ir(cudaStream_t st, const OpT<double> &A64, const OpT<float> &A32, int op, IRWork &w, const double *b,
              double *x, const SolveParams &prm, Preconditioner<float> *M32, SolveReport &rep) {
@@ -1062,7 +1170,7 @@ static int record_loop(cudaStream_t st, cudaStream_t body, const OpT<T> &A, int 
     if (begin_while(st, lc, body) != 0) return -1;
     first_half(body, A, op, w, M, nullptr);
     second_half(body, A, op, w, M, nullptr);
-    launch_xr(body, A, w, x, maxit, lc);
+    launch_xr(body, A, w, x, maxit, M, lc);
     if (end_while(body) != 0) return -1;
     *per_iter = 5 + (M ? 2 * M->launches() : 0);
     return 0;
@@ -1087,6 +1195,26 @@ template int record_bicgstab<double>(cudaStream_t, const cudaStream_t *, const O
 template int record_bicgstab<float>(cudaStream_t, const cudaStream_t *, const OpT<float> &, int, KrylovWork<float> &,
                                     const float *, float *, const SolveParams &, Preconditioner<float> *, int *,
                                     int *);
+
+int record_bicgstab_df(cudaStream_t st, const cudaStream_t *aux, const OpT<dfloat> &A, int op, KrylovWork<dfloat> &w,
+                       dfloat *xw, const double *b, double *x, const SolveParams &prm, Preconditioner<dfloat> *M,
+                       int *fixed, int *per_iter) {
+    if (!M) return -1;   // p^ and s^ are the preconditioner's FP32 output
+    const long long m = w.n * w.nc;
+    LoopCtl lc;
+    if (new_loop(st, lc) != 0) return -1;
+    if (prm.x_given) {
+        launch_to_dfloat(st, m, x, xw);
+        launch_init_guess(st, A, op, w, b, xw, prm.tol, prm.divtol, lc);
+    } else {
+        launch_init(st, w, b, xw, prm.tol, prm.divtol, nullptr, 0.0, 0.0, lc);
+    }
+    if (record_loop(st, aux[0], A, op, w, xw, prm.maxit, M, lc, per_iter) != 0) return -1;
+    launch_from_dfloat(st, m, xw, x);
+    cudaMemcpyAsync(w.scal_h, w.scal, sizeof(KScal) * w.nc, cudaMemcpyDeviceToHost, st);
+    *fixed = prm.x_given ? 3 : 2;
+    return 0;
+}
 
 int record_ir(cudaStream_t st, const cudaStream_t *aux, const OpT<double> &A64, const OpT<float> &A32, int op,
               IRWork &w, const double *b, double *x, const SolveParams &prm, Preconditioner<float> *M32, int *fixed,

@@ -18,6 +18,8 @@
 
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "kernels.h"
 #include "ops.cuh"
 
@@ -88,16 +90,30 @@ struct LoopCtl {
     int use = 0;
 };
 
+// Entry type of the preconditioned vectors p^ = M p and s^ = M s: T, or
+// FP32 under double-float Krylov vectors, whose preconditioner (the FP32
+// V-cycle) produces FP32 values, so p^ and s^ are stored as they come.
+template <typename T>
+struct PrecT {
+    using type = T;
+};
+template <>
+struct PrecT<dfloat> {
+    using type = float;
+};
+
 // gate (device pointer or null): when it points to a value other than
 // KS_RUN every kernel of the application returns at once, so a recorded
 // loop iteration after convergence costs only empty launches.
 template <typename T>
 struct Preconditioner {
     virtual ~Preconditioner() {}
-    virtual void apply(cudaStream_t s, const T *r, T *z, const int *gate) = 0;
+    virtual void apply(cudaStream_t s, const T *r, typename PrecT<T>::type *z, const int *gate) = 0;
     // The same from an FP64 r, rounded to T inside the application (one
     // pass fewer than rounding first); false: not available, nothing ran.
     virtual bool apply_from64(cudaStream_t, const double *, T *, const int *) { return false; }
+    // The same from double-float r (its high words).
+    virtual bool apply_from_df(cudaStream_t, const dfloat *, T *, const int *) { return false; }
     // Kernels one application launches.
     virtual int launches() const = 0;
 };
@@ -119,14 +135,47 @@ struct WidenedPreconditioner : Preconditioner<double> {
     bool fused_narrow = false;   // the last application rounded r inside m32
 };
 
+// Double-float Krylov vectors (the pressure solve of IBM3D_MIXED32) with
+// the FP32 preconditioner: its right-hand side is the vector's high words
+// (r rounded to FP32), its FP32 output is the preconditioned vector.
+// Shares the FP32 buffer of a WidenedPreconditioner (the two never run at
+// once).
+struct DFloatPreconditioner : Preconditioner<dfloat> {
+    Preconditioner<float> *m32 = nullptr;
+    float *r32 = nullptr;
+    long long n = 0;
+    int nblk = KBLOCKS;
+    void attach(const WidenedPreconditioner &w) {
+        m32 = w.m32;
+        r32 = w.r32;
+        n = w.n;
+        nblk = w.nblk;
+    }
+    void apply(cudaStream_t s, const dfloat *r, float *z, const int *gate) override;
+    int launches() const override { return m32->launches() + (fused_narrow ? 0 : 1); }
+    bool fused_narrow = false;
+};
+
 template <typename T>
 struct KrylovWork {
+    bool owner = true;   // false for a view of another work's buffers
     long long n = 0;
     int nc = 0;
     int nblk = KBLOCKS;  // blocks of the vector kernels
     T *base = nullptr;
+    using PT = typename PrecT<T>::type;
     T *r = nullptr, *r0 = nullptr, *p = nullptr, *v = nullptr, *s = nullptr, *t = nullptr;
-    T *ph = nullptr, *sh = nullptr;
+    PT *ph = nullptr, *sh = nullptr;   // p and s themselves when allocated without a preconditioner
+    // p^ and s^ of a solve with preconditioner M, or p and s themselves
+    // when it has none (a double-float solve always has one).
+    const PT *phat(const void *M) const {
+        if constexpr (std::is_same<PT, T>::value) return M ? ph : p;
+        else return ph;
+    }
+    const PT *shat(const void *M) const {
+        if constexpr (std::is_same<PT, T>::value) return M ? sh : s;
+        else return sh;
+    }
     KScal *scal = nullptr, *scal_h = nullptr;
     double *partials = nullptr;
     unsigned int *counter = nullptr;
@@ -135,6 +184,12 @@ struct KrylovWork {
     int allocate(long long ncell, int ncomp, bool precond, int maxblocks);
     void release();
 };
+
+// The FP64 work's vectors seen as double-float vectors (the same bytes per
+// entry; p^ and s^ as FP32 in the first half of theirs), with its scalars,
+// partials and counter: a non-owning view.  Double-float solves always
+// take the FP32 preconditioner.
+KrylovWork<dfloat> dfloat_view(const KrylovWork<double> &w);
 
 // FP64 outer vectors of an iterative-refinement solve plus its FP32 inner work.
 struct IRWork {
@@ -217,6 +272,18 @@ int solve_ir(cudaStream_t st, const OpT<double> &A64, const OpT<float> &A32, int
 template <typename T>
 int record_bicgstab(cudaStream_t st, const cudaStream_t *aux, const OpT<T> &A, int op, KrylovWork<T> &w, const T *b,
                     T *x, const SolveParams &prm, Preconditioner<T> *M, int *fixed, int *per_iter);
+
+// BiCGSTAB on double-float vectors and the double-float operator, FP64 b
+// and x: x (the initial guess when prm.x_given) is converted into xw at the
+// start, the residual r = b - A xw formed from the FP64 b, and xw
+// converted back into x at the end.  The scalars (alpha, omega, rho, the
+// norms) and the combination of the dot products across threads stay
+// FP64; the stopping test is bicgstab's.  Host loop and recorded form.
+int bicgstab_df(cudaStream_t st, const OpT<dfloat> &A, int op, KrylovWork<dfloat> &w, dfloat *xw, const double *b,
+                double *x, const SolveParams &prm, Preconditioner<dfloat> *M, SolveReport &rep);
+int record_bicgstab_df(cudaStream_t st, const cudaStream_t *aux, const OpT<dfloat> &A, int op, KrylovWork<dfloat> &w,
+                       dfloat *xw, const double *b, double *x, const SolveParams &prm, Preconditioner<dfloat> *M,
+                       int *fixed, int *per_iter);
 int record_ir(cudaStream_t st, const cudaStream_t *aux, const OpT<double> &A64, const OpT<float> &A32, int op,
               IRWork &w, const double *b, double *x, const SolveParams &prm, Preconditioner<float> *M32, int *fixed,
               int *per_outer, int *per_iter);

@@ -288,8 +288,8 @@ k_to_split(const S *__restrict__ a, D *__restrict__ b, const int NY, const int N
     b[((I + J + K) & 1) * H + row * NZH + (K >> 1)] = (D)a[row * NZ + K];
 }
 
-// The right-hand side of an FP32 cycle (FP64, or FP32 from an FP32 solve)
-// into the colour-split layout: each thread takes one (K, K+1) pair of a
+// The right-hand side of an FP32 cycle (FP64, double-float (its high
+// word), or FP32 from an FP32 solve) into the colour-split layout: each thread takes one (K, K+1) pair of a
 // padded row on MG0_NPLANES consecutive planes; its two values go to the
 // two colour halves at the same position (coalesced reads and writes), an
 // FP64 value rounded on the integer pipe (d2f_int: FP64 <-> FP32
@@ -299,6 +299,7 @@ constexpr int MG0_NPLANES = 4;
 
 __device__ __forceinline__ float to32(double x) { return d2f_int(x); }
 __device__ __forceinline__ float to32(float x) { return x; }
+__device__ __forceinline__ float to32(dfloat x) { return x.hi; }
 
 template <typename S>
 __global__ void __launch_bounds__(256)
@@ -1658,6 +1659,22 @@ bool GMG<T>::apply_from64(cudaStream_t s, const double *r, T *z, const int *gate
         if (!split_) return false;
         const Grid &g = A_.g;
         launch_pdl(k_narrow_split<double>, dim3((NZH_ + 31) / 32, (g.ny + 11) / 8, (g.nx + 3 + MG0_NPLANES) / MG0_NPLANES),
+                   dim3(32, 8), 0, s, r, rs_, g.nx + 4, g.ny + 4, g.nz + 4, NZH_, H_, gate);
+        note_launches(1);
+        cycle(s, rows(nullptr), z, gate);
+        launches_++;
+        return true;
+    }
+}
+
+template <typename T>
+bool GMG<T>::apply_from_df(cudaStream_t s, const dfloat *r, T *z, const int *gate) {
+    if constexpr (sizeof(T) != 4) {
+        return false;
+    } else {
+        if (!split_) return false;
+        const Grid &g = A_.g;
+        launch_pdl(k_narrow_split<dfloat>, dim3((NZH_ + 31) / 32, (g.ny + 11) / 8, (g.nx + 3 + MG0_NPLANES) / MG0_NPLANES),
                    dim3(32, 8), 0, s, r, rs_, g.nx + 4, g.ny + 4, g.nz + 4, NZH_, H_, gate);
         note_launches(1);
         cycle(s, rows(nullptr), z, gate);

@@ -141,6 +141,7 @@ class GMG : public Preconditioner<T> {
     // FP32 cycles with colour-split fine rows round an FP64 r straight into
     // the split layout.
     bool apply_from64(cudaStream_t s, const double *r, T *z, const int *gate) override;
+    bool apply_from_df(cudaStream_t s, const dfloat *r, T *z, const int *gate) override;
     int launches() const override { return launches_; }
     // Smoother sweeps (pre, post) on the fine grid and on the coarse levels,
     // and on the coarsest level; takes effect at the next apply.

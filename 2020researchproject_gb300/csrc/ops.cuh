@@ -82,18 +82,20 @@ __host__ __device__ inline int outer_row_kind(int op, int type, int comp, int ax
     }
 }
 
-template <typename T>
-__device__ __forceinline__ T outer_row(const OpT<T> &c, int op, int comp, const T *__restrict__ x, long long P, int i,
+// x may hold entries of another type X (FP32 entries under double-float
+// rows), converted to T as they are read.
+template <typename T, typename X>
+__device__ __forceinline__ T outer_row(const OpT<T> &c, int op, int comp, const X *__restrict__ x, long long P, int i,
                                        int j, int k, int f, int L) {
     const BCRow<T> &F = c.bc[f];
     const int axis = face_axis(f);
     const long long s = axis == 0 ? c.g.sx : axis == 1 ? c.g.sy : 1;
     const long long in = face_low(f) ? s : -s;
     switch (outer_row_kind(op, F.type, comp, axis)) {
-    case ROW_DIR: return F.dir_o[L - 1] * x[P] + F.dir_m[L - 1] * x[P + (2 * L - 1) * in];
-    case ROW_NEU: return x[P] - x[P + (2 * L - 1) * in];
-    case ROW_PER: return x[P] - x[periodic_image(c.g, i, j, k)];
-    default: return F.ext_o[L - 1] * x[P] - x[P + in] + F.ext_2[L - 1] * x[P + 2 * in];
+    case ROW_DIR: return F.dir_o[L - 1] * T(x[P]) + F.dir_m[L - 1] * T(x[P + (2 * L - 1) * in]);
+    case ROW_NEU: return T(x[P]) - T(x[P + (2 * L - 1) * in]);
+    case ROW_PER: return T(x[P]) - T(x[periodic_image(c.g, i, j, k)]);
+    default: return F.ext_o[L - 1] * T(x[P]) - T(x[P + in]) + F.ext_2[L - 1] * T(x[P + 2 * in]);
     }
 }
 
@@ -140,17 +142,18 @@ __device__ __forceinline__ Column<T> column(const OpT<T> &c, int j, int k) {
 // as op_row without the index decode and the outer-face test, and
 // branch-free for fluid, solid and pinned rows (every load issued up
 // front, the result selected); ghost rows, a few per thousand, branch.
-template <typename T>
-__device__ __forceinline__ T interior_row(const OpT<T> &c, int op, const T *__restrict__ x, long long P, int i,
+template <typename T, typename X>
+__device__ __forceinline__ T interior_row(const OpT<T> &c, int op, const X *__restrict__ x, long long P, int i,
                                           const Column<T> &q) {
     const uint8_t fl = c.flag[P];
     const int I = i + 2;
     const long long sx = c.g.sx, sy = c.g.sy;
-    const T xc = x[P], xw = x[P - sx], xe = x[P + sx], xs = x[P - sy], xn = x[P + sy], xd = x[P - 1], xu = x[P + 1];
-    const T nb = c.km[0][I] * xw + c.kp[0][I] * xe + q.kmy * xs + q.kpy * xn + q.kmz * xd + q.kpz * xu;
+    const T xc = T(x[P]), xw = T(x[P - sx]), xe = T(x[P + sx]), xs = T(x[P - sy]), xn = T(x[P + sy]),
+            xd = T(x[P - 1]), xu = T(x[P + 1]);
+    const T nb = sum6(c.km[0][I], xw, c.kp[0][I], xe, q.kmy, xs, q.kpy, xn, q.kmz, xd, q.kpz, xu);
     T y;
     if (op == OP_MOM) y = ((T)1 + c.ks[0][I] + q.ksy + q.ksz) * xc - nb;
-    else y = xc - c.dinv[P] * nb;
+    else y = sub_mul(xc, c.dinv[P], nb);
     const bool pinned = op == OP_PRES && c.p_singular && P == c.pinned;
     if (fl != FLUID || pinned) y = xc;
     if (fl == GHOST && !pinned) {
@@ -159,7 +162,7 @@ __device__ __forceinline__ T interior_row(const OpT<T> &c, int op, const T *__re
 #pragma unroll
         for (int e = 0; e < 8; e++) {
             const int m = c.gidx[8 * g + e];
-            if (m >= 0) sum += c.gw[8 * g + e] * x[m];
+            if (m >= 0) sum += c.gw[8 * g + e] * T(x[m]);
         }
         const T ws = c.gwself[g];
         y = op == OP_MOM ? ((T)1 + ws) * xc + sum : ((T)1 - ws) * xc - sum;
@@ -168,22 +171,22 @@ __device__ __forceinline__ T interior_row(const OpT<T> &c, int op, const T *__re
 }
 
 // One row of A applied to x (op OP_MOM with component comp, or OP_PRES).
-template <typename T>
-__device__ __forceinline__ T op_row(const OpT<T> &c, int op, int comp, const T *__restrict__ x, long long P) {
+template <typename T, typename X>
+__device__ __forceinline__ T op_row(const OpT<T> &c, int op, int comp, const X *__restrict__ x, long long P) {
     int i, j, k;
     cijk_fast(c.g, c.fdx, c.fdy, P, i, j, k);
     int L;
     const int f = owner_face(c.g, i, j, k, L);
     if (f >= 0) return outer_row(c, op, comp, x, P, i, j, k, f, L);
-    if (op == OP_PRES && c.p_singular && P == c.pinned) return x[P];
+    if (op == OP_PRES && c.p_singular && P == c.pinned) return T(x[P]);
     const uint8_t fl = c.flag[P];
     if (fl == FLUID) {
         const int I = i + 2, J = j + 2, K = k + 2;
         const long long sx = c.g.sx, sy = c.g.sy;
-        const T nb = c.km[0][I] * x[P - sx] + c.kp[0][I] * x[P + sx] + c.km[1][J] * x[P - sy] +
-                     c.kp[1][J] * x[P + sy] + c.km[2][K] * x[P - 1] + c.kp[2][K] * x[P + 1];
-        if (op == OP_MOM) return ((T)1 + c.ks[0][I] + c.ks[1][J] + c.ks[2][K]) * x[P] - nb;
-        return x[P] - c.dinv[P] * nb;
+        const T nb = c.km[0][I] * T(x[P - sx]) + c.kp[0][I] * T(x[P + sx]) + c.km[1][J] * T(x[P - sy]) +
+                     c.kp[1][J] * T(x[P + sy]) + c.km[2][K] * T(x[P - 1]) + c.kp[2][K] * T(x[P + 1]);
+        if (op == OP_MOM) return ((T)1 + c.ks[0][I] + c.ks[1][J] + c.ks[2][K]) * T(x[P]) - nb;
+        return T(x[P]) - c.dinv[P] * nb;
     }
     if (fl == GHOST) {
         const int g = c.gid[P];
@@ -191,12 +194,12 @@ __device__ __forceinline__ T op_row(const OpT<T> &c, int op, int comp, const T *
 #pragma unroll
         for (int e = 0; e < 8; e++) {
             const int q = c.gidx[8 * g + e];
-            if (q >= 0) sum += c.gw[8 * g + e] * x[q];
+            if (q >= 0) sum += c.gw[8 * g + e] * T(x[q]);
         }
         const T ws = c.gwself[g];
-        return op == OP_MOM ? ((T)1 + ws) * x[P] + sum : ((T)1 - ws) * x[P] - sum;
+        return op == OP_MOM ? ((T)1 + ws) * T(x[P]) + sum : ((T)1 - ws) * T(x[P]) - sum;
     }
-    return x[P];
+    return T(x[P]);
 }
 
 }  // namespace ibm

@@ -56,7 +56,7 @@ struct StepGraph {
 
 // Host parameters baked into recorded graphs.
 struct GraphSig {
-    int precision, les, use_mg, max_outer, solver, gm_restart, warm, p_guess;
+    int precision, les, use_mg, max_outer, solver, gm_restart, warm, p_guess, pvec;
     double tol, divtol, Re, dt, f[3], cs, inner_tol[2];
     bool operator==(const GraphSig &o) const { return memcmp(this, &o, sizeof *this) == 0; }
 };
@@ -106,9 +106,11 @@ struct ibm3d_device {
     // km, kp, ks, d per axis, then dinv, wdiv (n each), ghost weights.
     double *op64 = nullptr;
     float *op32 = nullptr;
+    dfloat *opdf = nullptr;       // the FP64 tables as double-floats: km, kp, ks, d per axis, dinv, ghost weights
     int *sweep_outer = nullptr;   // outer cells of the padded grid (sweep launches)
     OpT<double> A64{};
     OpT<float> A32{};
+    OpT<dfloat> Adf{};
     // Solvers: FP64 BiCGSTAB (plain path) and FP64 refinement around FP32
     // BiCGSTAB (mixed path), each with its multigrid preconditioner.
     KrylovWork<double> kmom, kpres;
@@ -116,6 +118,12 @@ struct ibm3d_device {
     GMG<double> *mg = nullptr;
     GMG<float> *mg32 = nullptr;
     WidenedPreconditioner pc64;   // FP32 multigrid under an FP64 Krylov solve
+    // IBM3D_MIXED32 pressure solve on double-float vectors: a view of
+    // kpres's buffers, the solution vector and the FP32 multigrid behind it.
+    KrylovWork<dfloat> kpres_df;
+    dfloat *pp_df = nullptr;
+    DFloatPreconditioner pcdf;
+    int pvec = IBM3D_PVEC_DFLOAT;
     GmresWork gm;                 // SOLVER_GMRES pressure solves
     int gm_restart = 10;          // restart length (the reference's KDim, src/ibm3d_setup.c:1474)
     double *red_partials = nullptr;
@@ -303,13 +311,17 @@ void release_device(ibm3d_device *d) {
     d->gm.release();
     d->kmom.release();
     d->kpres.release();
+    d->kpres_df.release();
+    dfree(d->pp_df);
     d->irmom.release();
     d->irpres.release();
     dfree(d->op64);
     dfree(d->op32);
+    dfree(d->opdf);
     dfree(d->sweep_outer);
     d->A64 = OpT<double>{};
     d->A32 = OpT<float>{};
+    d->Adf = OpT<dfloat>{};
     for (int a = 0; a < 3; a++) {
         dfree(d->tab[a]);
         dfree(d->tabf[a]);
@@ -673,24 +685,36 @@ bool build_ops(IBMSolver *sv) {
     n32 += 2 * (size_t)n + 9 * (size_t)ng;
     std::vector<double> h64(n64, 0.0);
     std::vector<float> h32(n32, 0.0f);
+    // Double-float tables: the FP64 values of km, kp, ks, d per axis, then
+    // dinv (n) and the ghost weights (9 per ghost), each split in two words.
+    const size_t ndf = n32 - (size_t)n;
+    std::vector<dfloat> hdf(ndf, dfloat(0));
     d->op64 = dmalloc<double>(sv, n64, "operator tables");
     d->op32 = dmalloc<float>(sv, n32, "operator tables");
-    if (!d->op64 || !d->op32) return false;
+    d->opdf = dmalloc<dfloat>(sv, ndf, "operator tables");
+    if (!d->op64 || !d->op32 || !d->opdf) return false;
     OpT<double> &A = d->A64;
     OpT<float> &B = d->A32;
+    OpT<dfloat> &C = d->Adf;
     A = OpT<double>{};
     B = OpT<float>{};
+    C = OpT<dfloat>{};
     size_t o64 = 0, o32 = 0;
     for (int a = 0; a < 3; a++) {
         const int m = Ns[a] + 4;
         double *ks = &h64[o64];
         float *km = &h32[o32], *kp = km + m, *ks32 = km + 2 * m, *dd = km + 3 * m;
+        dfloat *kmd = &hdf[o32], *kpd = kmd + m, *ksd = kmd + 2 * m, *ddd = kmd + 3 * m;
         for (int q = 0; q < m; q++) {
             ks[q] = KM[a][q] + KP[a][q];
             km[q] = (float)KM[a][q];
             kp[q] = (float)KP[a][q];
             ks32[q] = (float)ks[q];
             dd[q] = (float)D[a][q];
+            kmd[q] = dfloat(KM[a][q]);
+            kpd[q] = dfloat(KP[a][q]);
+            ksd[q] = dfloat(ks[q]);
+            ddd[q] = dfloat(D[a][q]);
         }
         A.km[a] = d->ax[a].km;
         A.kp[a] = d->ax[a].kp;
@@ -700,6 +724,10 @@ bool build_ops(IBMSolver *sv) {
         B.kp[a] = d->op32 + o32 + m;
         B.ks[a] = d->op32 + o32 + 2 * m;
         B.d[a] = d->op32 + o32 + 3 * m;
+        C.km[a] = d->opdf + o32;
+        C.kp[a] = d->opdf + o32 + m;
+        C.ks[a] = d->opdf + o32 + 2 * m;
+        C.d[a] = d->opdf + o32 + 3 * m;
         o64 += m;
         o32 += 4 * (size_t)m;
     }
@@ -719,13 +747,22 @@ bool build_ops(IBMSolver *sv) {
     }
     for (size_t q = 0; q < gw.size(); q++) gw32[q] = (float)gw[q];
     for (int q = 0; q < ng; q++) gws32[q] = (float)gws[q];
+    dfloat *dinvd = &hdf[o32], *gwd = dinvd + n, *gwsd = gwd + 8 * (size_t)ng;
+    for (long long P = 0; P < n; P++) dinvd[P] = dfloat(dinv[P]);
+    for (size_t q = 0; q < gw.size(); q++) gwd[q] = dfloat(gw[q]);
+    for (int q = 0; q < ng; q++) gwsd[q] = dfloat(gws[q]);
+    cudaMemcpyAsync(d->opdf, hdf.data(), sizeof(dfloat) * ndf, cudaMemcpyHostToDevice, d->s);
     cudaMemcpyAsync(d->op64, h64.data(), sizeof(double) * n64, cudaMemcpyHostToDevice, d->s);
     cudaMemcpyAsync(d->op32, h32.data(), sizeof(float) * n32, cudaMemcpyHostToDevice, d->s);
     float *f32 = d->op32 + o32;
     for (int f = 0; f < 6; f++) {
         const BCFace &F = d->bc.f[f];
-        A.bc[f].type = B.bc[f].type = F.type;
+        A.bc[f].type = B.bc[f].type = C.bc[f].type = F.type;
         for (int L = 0; L < 2; L++) {
+            C.bc[f].dir_o[L] = dfloat(F.dir_o[L]);
+            C.bc[f].dir_m[L] = dfloat(F.dir_m[L]);
+            C.bc[f].ext_o[L] = dfloat(F.ext_o[L]);
+            C.bc[f].ext_2[L] = dfloat(F.ext_2[L]);
             A.bc[f].dir_o[L] = F.dir_o[L];
             A.bc[f].dir_m[L] = F.dir_m[L];
             A.bc[f].ext_o[L] = F.ext_o[L];
@@ -776,6 +813,21 @@ bool build_ops(IBMSolver *sv) {
     A.wdiv = B.wdiv = f32 + n;
     B.gw = ng ? f32 + 2 * n : nullptr;
     B.gwself = ng ? f32 + 2 * n + 8 * (size_t)ng : nullptr;
+    // The double-float operator: the FP64 operator's index tables, its
+    // values split in two words.
+    C.g = g;
+    C.fdx = fdx;
+    C.fdy = fdy;
+    C.sw = sw;
+    C.p_singular = A.p_singular;
+    C.pinned = A.pinned;
+    C.flag = A.flag;
+    C.gid = A.gid;
+    C.gidx = A.gidx;
+    C.wdiv = A.wdiv;
+    C.dinv = d->opdf + o32;
+    C.gw = ng ? d->opdf + o32 + n : nullptr;
+    C.gwself = ng ? d->opdf + o32 + n + 8 * (size_t)ng : nullptr;
     return cuda_check(sv, cudaStreamSynchronize(d->s), "operator tables");
 }
 
@@ -1009,6 +1061,16 @@ bool pres_ir(const IBMSolver *sv) {
     return (sv->dev->precision == IBM3D_MIXED || sv->dev->precision == IBM3D_MIXED32_IR) && !pres_gmres(sv);
 }
 
+// The IBM3D_MIXED32 pressure BiCGSTAB on double-float vectors
+// (IBMSolver_set_pressure_vectors; with the FP32 multigrid, whose FP32
+// output the double-float solve stores as it comes), and its
+// preconditioner.
+bool pres_df(const IBMSolver *sv) {
+    const ibm3d_device *d = sv->dev;
+    return d->precision == IBM3D_MIXED32 && d->pvec == IBM3D_PVEC_DFLOAT && !pres_gmres(sv) && use_mg(sv);
+}
+Preconditioner<dfloat> *pres_pcdf(IBMSolver *sv) { return &sv->dev->pcdf; }
+
 // Preconditioner of an FP64 pressure Krylov solve.
 Preconditioner<double> *pres_pc64(IBMSolver *sv) {
     ibm3d_device *d = sv->dev;
@@ -1162,6 +1224,8 @@ void one_step(IBMSolver *sv) {
     else if (pres_ir(sv))
         rc = solve_ir(d->s, d->A64, d->A32, OP_PRES, d->irpres, d->b, d->pp, pp, use_mg(sv) ? d->mg32 : nullptr,
                       d->rep_p);
+    else if (pres_df(sv))
+        rc = bicgstab_df(d->s, d->Adf, OP_PRES, d->kpres_df, d->pp_df, d->b, d->pp, pp, pres_pcdf(sv), d->rep_p);
     else
         rc = bicgstab<double>(d->s, d->A64, OP_PRES, d->kpres, d->b, d->pp, pp, pres_pc64(sv), d->rep_p);
     pf.end(t);
@@ -1191,6 +1255,7 @@ GraphSig graph_sig(const IBMSolver *sv) {
     g.solver = sv->linear_solver_type;
     g.gm_restart = sv->dev->gm_restart;
     g.p_guess = sv->dev->p_guess;
+    g.pvec = sv->dev->pvec;
     return g;
 }
 
@@ -1229,6 +1294,9 @@ bool record_step_into(IBMSolver *sv, StepGraph &G) {
         else if (pres_ir(sv))
             ok = record_ir(d->s, d->aux, d->A64, d->A32, OP_PRES, d->irpres, d->b, d->pp, pp,
                            use_mg(sv) ? d->mg32 : nullptr, &pf, &po, &pi) == 0;
+        else if (pres_df(sv))
+            ok = record_bicgstab_df(d->s, d->aux, d->Adf, OP_PRES, d->kpres_df, d->pp_df, d->b, d->pp, pp,
+                                    pres_pcdf(sv), &pf, &pi) == 0;
         else
             ok = record_bicgstab<double>(d->s, d->aux, d->A64, OP_PRES, d->kpres, d->b, d->pp, pp, pres_pc64(sv),
                                          &pf, &pi) == 0;
@@ -1658,6 +1726,9 @@ void IBMSolver_assemble(IBMSolver *s) {
         set_status(s, IBM3D_ECUDA, "Krylov workspace allocation failed");
         return;
     }
+    d->kpres_df = dfloat_view(d->kpres);
+    d->pp_df = dmalloc<dfloat>(s, g.ncell, "Krylov workspace");
+    if (!d->pp_df) return;
     MGGeometry geom;
     const double *D[3] = {s->dx, s->dy, s->dz};
     const int Ns[3] = {s->Nx, s->Ny, s->Nz};
@@ -1688,6 +1759,7 @@ void IBMSolver_assemble(IBMSolver *s) {
         set_status(s, IBM3D_ECUDA, "preconditioner workspace allocation failed");
         return;
     }
+    d->pcdf.attach(d->pc64);
     if (pres_gmres(s) && d->gm.allocate(g.ncell, d->gm_restart, mb) != 0) {
         set_status(s, IBM3D_ECUDA, "GMRES workspace allocation failed");
         return;
@@ -2282,6 +2354,15 @@ void IBMSolver_set_pressure_guess(IBMSolver *s, int mode) {
         return;
     }
     s->dev->p_guess = mode;
+    drop_graphs(s->dev);
+}
+
+void IBMSolver_set_pressure_vectors(IBMSolver *s, int kind) {
+    if (!s || !s->dev || (kind != IBM3D_PVEC_FP64 && kind != IBM3D_PVEC_DFLOAT)) {
+        set_status(s, IBM3D_EARG, "IBMSolver_set_pressure_vectors: kind %d", kind);
+        return;
+    }
+    s->dev->pvec = kind;
     drop_graphs(s->dev);
 }
 

@@ -124,6 +124,23 @@ int IBMSolver_check_fp32_conversions(long long n, const double *values, unsigned
    exact-resume state. */
 void IBMSolver_set_pressure_guess(IBMSolver *, int mode);
 
+/* Storage and arithmetic of the IBM3D_MIXED32 pressure BiCGSTAB's vectors:
+   IBM3D_PVEC_DFLOAT (default) keeps each entry as a double-float, the
+   unevaluated sum of two FP32 words (48-bit significand), and runs the
+   vector and operator arithmetic as error-free FP32 transformations;
+   IBM3D_PVEC_FP64 keeps FP64 vectors.  Either way the right-hand side,
+   the solution p' and the scalars of the iteration (alpha, omega, rho, the
+   norms and the combination of the dot products) are FP64, the stopping
+   test is the same and max|div U| is checked in FP64 after the
+   projection.  GB300 issues FP64 operations at 1/72 of its FP32 rate:
+   the FP64 vectors make the solve FP64-bound, the double-float ones bring
+   it near the memory bound.  The preconditioned vectors are the FP32
+   multigrid's output as it comes (FP32 entries); without the multigrid
+   preconditioner (PRECOND_AMG) the vectors stay FP64.  Other precision
+   modes ignore the setting. */
+enum { IBM3D_PVEC_FP64 = 0, IBM3D_PVEC_DFLOAT = 1 };
+void IBMSolver_set_pressure_vectors(IBMSolver *, int kind);
+
 /* Krylov iteration caps of the momentum and pressure solves (defaults
    200 and 1000, the reference's hypre settings, src/ibm3d_setup.c:1411-1563).
    A solve that reaches its cap prints the reference's warning

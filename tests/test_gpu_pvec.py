@@ -1,0 +1,81 @@
+"""Double-float vectors in the IBM3D_MIXED32 pressure BiCGSTAB
+(IBMSolver_set_pressure_vectors).
+
+The default keeps the Krylov vectors as double-floats (two FP32 words,
+48-bit significand) and the preconditioned vectors as the FP32 multigrid's
+output; IBM3D_PVEC_FP64 keeps FP64 vectors.  On the golden fixtures:
+
+* both reach the same divergence bound with the same iteration counts (to
+  one iteration per step) and fields within 5e-7 (velocity) and 1e-5
+  (pressure) relative L2 of each other (two solves stopped at the same
+  bound, not the same iterates: 1.7e-7 on the LES channel); both stay
+  within the IBM3D_MIXED32 bounds of the reference's fields;
+* down to max|div U| <= 1e-10 every step meets the bound (the double-float
+  residual floor measured on these fixtures is ~5e-11, the FP64 one
+  ~5e-13).
+"""
+import numpy as np
+import pytest
+
+from conftest import load_golden, rel_l2
+from test_gpu_golden import build_case
+
+pytestmark = pytest.mark.gpu
+
+CASES = ["sphere", "channel_les", "cavity", "bumpy_stl", "func_sphere", "mixed_box"]
+
+
+def _run(ibm, case, pvec, divtol):
+    s = build_case(ibm, case, tol=1e-7)
+    s.set_div_tol(divtol)
+    s.set_precision(ibm.MIXED32)
+    s.set_pressure_vectors(pvec)
+    for n in case["meta"]["calls"]:
+        s.iterate(n)
+    return s
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_dfloat_vectors_match_fp64_vectors(ibm, name):
+    case = load_golden(name)
+    last = len(case["meta"]["calls"])
+    a = _run(ibm, case, ibm.PVEC_FP64, 1e-10)
+    b = _run(ibm, case, ibm.PVEC_DFLOAT, 1e-10)
+    sa, sb = a.stats(), b.stats()
+    steps = sb["steps_total"]
+    print(name, "max|div U|", sa["max_div_max"], sb["max_div_max"], "pressure iterations",
+          sa["iters_p_total"], sb["iters_p_total"])
+    assert sa["max_div_max"] <= 1e-10 and sb["max_div_max"] <= 1e-10
+    assert abs(sa["iters_p_total"] - sb["iters_p_total"]) <= steps
+    for f in ("u1", "u2", "u3", "p"):
+        ga, gb = a.get_field(f), b.get_field(f)
+        assert np.array_equal(np.isnan(ga), np.isnan(gb)), f
+        assert rel_l2(gb, ga) < (1e-5 if f == "p" else 5e-7), (f, rel_l2(gb, ga))
+        assert rel_l2(gb, case[f"{f}_{last}"]) < (1e-5 if f == "p" else 2e-6), f
+
+
+@pytest.mark.parametrize("mode", ["FP64", "MIXED32"])
+def test_unpreconditioned_pressure_solve(ibm, mode):
+    """PRECOND_NONE: BiCGSTAB iterates on p and s themselves (p^ = p,
+    s^ = s) and converges; the double-float vectors need the multigrid, so
+    without it the setting changes nothing."""
+    case = load_golden("sphere")
+    out = []
+    for pvec in (ibm.PVEC_FP64, ibm.PVEC_DFLOAT):
+        s = build_case(ibm, case, tol=1e-7)
+        s.set_linear_solver(ibm.SOLVER_BiCGSTAB, ibm.PRECOND_NONE, 1e-7)
+        s.set_div_tol(1e-9)
+        s.set_precision(getattr(ibm, mode))
+        s.set_pressure_vectors(pvec)
+        s.iterate(3)
+        st = s.stats()
+        assert st["max_div_max"] <= 1e-9, st["max_div_max"]
+        assert 0 < st["iters_p_total"] < 3000, st["iters_p_total"]
+        out.append(s.get_field("p"))
+    assert np.array_equal(out[0], out[1], equal_nan=True)   # NaN on solid cells
+
+
+def test_pressure_vectors_argument(ibm):
+    s = ibm.IBMSolver()
+    with pytest.raises(ibm.IBM3DError):
+        s.set_pressure_vectors(7)
