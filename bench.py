@@ -9,10 +9,13 @@ momentum to the reference drivers' relative tolerance 1e-6.  Synthetic,
 seeded inputs (the reference has no public dataset).
 
 Metric: Mcell-steps/s = interior cells x steps / seconds, for the
-mixed-precision step (FP32 Krylov/multigrid inner solves inside FP64
-iterative refinement, everything else FP64), with the plain FP64 step
-measured beside it on the same state ("fp64", "mixed_vs_fp64") and the
-velocity difference between the two after the run ("error_vs_fp64").
+mixed-precision step (the autotuner's choice among the mixed forms; on this
+workload IBM3D_MIXED32: FP32 explicit stages and momentum solve, the
+pressure BiCGSTAB on double-float vectors with the FP32 multigrid, FP64
+right-hand side, solution, scalars and divergence check), with the plain
+FP64 step measured beside it on the same state ("fp64", "mixed_vs_fp64")
+and the velocity difference between the two after the run
+("error_vs_fp64").
   value : device time (CUDA events on the solver's stream) of K steps with
           the state resident in HBM (the step's working set, >1 GB, is far
           larger than the 129 MB L2).  Each step is one recorded CUDA graph.
