@@ -346,7 +346,7 @@ class IBMSolver:
 
     def set_pressure_guess(self, mode=1):
         """Warm-started pressure solves from the last increment (0) or its
-        linear extrapolation from the last two (1)."""
+        linear extrapolation from the last two (1, the default)."""
         self._lib.IBMSolver_set_pressure_guess(self._s, int(mode))
         self._check("set_pressure_guess")
 

@@ -86,7 +86,7 @@ struct ibm3d_device {
     // increment before the last one, and how many increments are known.
     double *pp_prev = nullptr;
     int *pp_hist = nullptr;
-    int p_guess = 0;
+    int p_guess = 1;   // warm-started (mixed) pressure solves start from the extrapolation
     // IBM3D_MIXED32: N and N_prev in FP32 (6 arrays of ncell floats).
     float *f32 = nullptr;
     float *N32[3], *Np32[3];
