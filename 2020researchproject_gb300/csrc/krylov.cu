@@ -543,6 +543,56 @@ k_apply(const OpT<T> A, const int op, const int comp, const T *__restrict__ x, T
         [&](int, long long P) { y[P] = op_row(A, op, comp, x, P); });
 }
 
+// ------------------------------------------------- true-residual check --
+// Runs after k_bicg_xr of a one-component solve and acts only when that
+// iteration ended the solve (KS_DONE): r = b - A x from the solution
+// itself, and the stopping test on it.  A pass keeps the solve done (the
+// reported norms become the true residual's); a miss restarts the
+// recurrence from the true residual (r0 = p = r at the next p update) and
+// keeps the loop going below maxit.  Used by the double-float solve, whose
+// recursive residual can drift from the true one by more than the
+// divergence bound's margin over a long solve.
+template <typename T, typename B>
+__global__ void __launch_bounds__(SW_THREADS, std::is_same<T, dfloat>::value ? 4 : 1)
+k_bicg_verify(const OpT<T> A, const int op, const long long n, const B *__restrict__ b, const T *__restrict__ x,
+              T *r, KScal *sc, double *partials, unsigned int *counter, const int maxit, const LoopCtl lc) {
+    pdl_enter();
+    if (sc[0].state != KS_DONE) return;   // the same value in every block: written only by the last one below
+    __shared__ double smem[32 * 2];
+    typename AccT<T>::type a[1] = {0};
+    float dmax = 0.0f;
+    const bool run[1] = {true};
+    const bool want_div = sc[0].divtol > 0;
+    auto put = [&](long long P, T y) {
+        r[P] = y;
+        mac(a[0], y, y);
+        if (want_div) dmax = fmaxf(dmax, divw(A, P, y));
+    };
+    sweep_rows<T, 1>(
+        A, run, [&](int, long long P, int i, const Column<T> &q) { put(P, (T)b[P] - interior_row(A, op, x, P, i, q)); },
+        [&](int, long long P) { put(P, (T)b[P] - op_row(A, op, 0, x, P)); });
+    typename AccT<T>::type acc[2] = {a[0], dmax};
+    reduce_and_finish<2, 1>(acc, smem, partials, counter, [&](const double *tot) {
+        KScal &st = sc[0];
+        st.rnorm2 = tot[0];
+        if (!isfinite(tot[0])) {
+            st.state = KS_BREAKDOWN;
+            set_loop(lc, false);
+            return;
+        }
+        if (converged(tot[0], st.bnorm2, tot[1], st.tol, st.divtol)) {
+            st.divmax = tot[1];
+            set_loop(lc, false);
+            return;
+        }
+        st.state = KS_RUN;
+        st.restart = 1;
+        st.rho = tot[0];
+        st.beta = 0.0;
+        set_loop(lc, st.iters < maxit);
+    });
+}
+
 // --------------------------------------------- iterative refinement (FP64) --
 // r = b - A x (or r = b while x is still zero), with per-component ||r||^2,
 // max|r| and the divergence max; the last block derives each component's
@@ -863,6 +913,14 @@ static void launch_xr(cudaStream_t st, const OpT<T> &A, KrylovWork<T> &w, T *x, 
     note_launches(1);
 }
 
+template <typename T, typename B>
+static void launch_verify(cudaStream_t st, const OpT<T> &A, int op, KrylovWork<T> &w, const B *b, const T *x,
+                          int maxit, LoopCtl lc) {
+    launch_pdl(k_bicg_verify<T, B>, A.sw.nblocks, SW_THREADS, 0, st, A, op, w.n, b, x, w.r, w.scal, w.partials,
+               w.counter, maxit, lc);
+    note_launches(1);
+}
+
 static void launch_residual(cudaStream_t st, const OpT<double> &A64, int op, IRWork &w, const double *b,
                             const double *x, int mode, const SolveParams &prm, LoopCtl lc) {
     if (w.nc == 3)
@@ -1010,9 +1068,11 @@ static void fetch(cudaStream_t st, KrylovWork<T> &w) {
     cudaStreamSynchronize(st);
 }
 
-template <typename T>
+// vb (one-component solves): the right-hand side, to check the true
+// residual after the iteration that ends the solve (k_bicg_verify).
+template <typename T, typename B = T>
 static void host_loop(cudaStream_t st, const OpT<T> &A, int op, KrylovWork<T> &w, T *x, int maxit,
-                      Preconditioner<T> *M, Prof *pf) {
+                      Preconditioner<T> *M, Prof *pf, const B *vb = nullptr) {
     const LoopCtl none;
     fetch(st, w);
     int it = 0;
@@ -1020,13 +1080,11 @@ static void host_loop(cudaStream_t st, const OpT<T> &A, int op, KrylovWork<T> &w
         it++;
         first_half(st, A, op, w, M, pf);
         fetch(st, w);
-        if (all_in(w.scal_h, w.nc, KS_HALF, KS_DONE, KS_BREAKDOWN)) {
-            launch_xr(st, A, w, x, maxit, M, none);
-            fetch(st, w);
-            break;
-        }
-        second_half(st, A, op, w, M, pf);
+        // Components converged on s skip the second half (its kernels would
+        // return at once for them).
+        if (!all_in(w.scal_h, w.nc, KS_HALF, KS_DONE, KS_BREAKDOWN)) second_half(st, A, op, w, M, pf);
         launch_xr(st, A, w, x, maxit, M, none);
+        if (vb) launch_verify(st, A, op, w, vb, x, maxit, none);
         fetch(st, w);
     }
 }
@@ -1065,7 +1123,7 @@ int bicgstab_df(cudaStream_t st, const OpT<dfloat> &A, int op, KrylovWork<dfloat
     } else {
         launch_init(st, w, b, xw, prm.tol, prm.divtol, nullptr, 0.0, 0.0, LoopCtl());
     }
-    host_loop(st, A, op, w, xw, prm.maxit, M, prm.prof);
+    host_loop(st, A, op, w, xw, prm.maxit, M, prm.prof, b);
     launch_from_dfloat(st, m, xw, x);
     return report(w, rep);
 }
@@ -1163,16 +1221,18 @@ static int end_while(cudaStream_t body_stream) {
     return cudaStreamEndCapture(body_stream, &g) == cudaSuccess ? 0 : -1;
 }
 
-// Init (already recorded by the caller with lc) + while loop of iterations.
-template <typename T>
+// Init (already recorded by the caller with lc) + while loop of iterations
+// (vb as in host_loop).
+template <typename T, typename B = T>
 static int record_loop(cudaStream_t st, cudaStream_t body, const OpT<T> &A, int op, KrylovWork<T> &w, T *x,
-                       int maxit, Preconditioner<T> *M, const LoopCtl &lc, int *per_iter) {
+                       int maxit, Preconditioner<T> *M, const LoopCtl &lc, int *per_iter, const B *vb = nullptr) {
     if (begin_while(st, lc, body) != 0) return -1;
     first_half(body, A, op, w, M, nullptr);
     second_half(body, A, op, w, M, nullptr);
     launch_xr(body, A, w, x, maxit, M, lc);
+    if (vb) launch_verify(body, A, op, w, vb, x, maxit, lc);
     if (end_while(body) != 0) return -1;
-    *per_iter = 5 + (M ? 2 * M->launches() : 0);
+    *per_iter = 5 + (vb ? 1 : 0) + (M ? 2 * M->launches() : 0);
     return 0;
 }
 
@@ -1209,7 +1269,7 @@ int record_bicgstab_df(cudaStream_t st, const cudaStream_t *aux, const OpT<dfloa
     } else {
         launch_init(st, w, b, xw, prm.tol, prm.divtol, nullptr, 0.0, 0.0, lc);
     }
-    if (record_loop(st, aux[0], A, op, w, xw, prm.maxit, M, lc, per_iter) != 0) return -1;
+    if (record_loop(st, aux[0], A, op, w, xw, prm.maxit, M, lc, per_iter, b) != 0) return -1;
     launch_from_dfloat(st, m, xw, x);
     cudaMemcpyAsync(w.scal_h, w.scal, sizeof(KScal) * w.nc, cudaMemcpyDeviceToHost, st);
     *fixed = prm.x_given ? 3 : 2;

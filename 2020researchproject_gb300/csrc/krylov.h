@@ -278,7 +278,10 @@ int record_bicgstab(cudaStream_t st, const cudaStream_t *aux, const OpT<T> &A, i
 // start, the residual r = b - A xw formed from the FP64 b, and xw
 // converted back into x at the end.  The scalars (alpha, omega, rho, the
 // norms) and the combination of the dot products across threads stay
-// FP64; the stopping test is bicgstab's.  Host loop and recorded form.
+// FP64; the stopping test is bicgstab's, and an iteration that passes it
+// on the recursive residual has it checked on the true residual b - A x
+// (a miss restarts the recurrence from that residual).  Host loop and
+// recorded form.
 int bicgstab_df(cudaStream_t st, const OpT<dfloat> &A, int op, KrylovWork<dfloat> &w, dfloat *xw, const double *b,
                 double *x, const SolveParams &prm, Preconditioner<dfloat> *M, SolveReport &rep);
 int record_bicgstab_df(cudaStream_t st, const cudaStream_t *aux, const OpT<dfloat> &A, int op, KrylovWork<dfloat> &w,

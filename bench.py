@@ -254,14 +254,17 @@ def _timed_arm(ibm, wl, case, precision, args, world, u0, headline=False):
         # The autotuner picks the multigrid sweeps (and, for the mixed step,
         # which of the mixed solver forms) from the state after three
         # steps (past the start-up transient, whose harder solves favour
-        # other settings); the state is restored, and warm-up follows.
+        # other settings), timing 8 steps per candidate (4-step trials
+        # ranked sweeps that differ by 4 % in the timed steps either way
+        # from one run to the next); the state is restored, and warm-up
+        # follows.
         s.iterate(3)
         modes = ([("MIXED", ibm.MIXED), ("MIXED_MG", ibm.MIXED_MG), ("MIXED32", ibm.MIXED32)]
                  if precision == "mixed" else [("FP64", ibm.FP64)])
         trials = []
         for name, mode in modes:
             s.set_precision(mode)
-            ms_t, sweeps = s.autotune(steps=4)
+            ms_t, sweeps = s.autotune(steps=8)
             trials.append((ms_t, name, mode, sweeps))
         ms_t, name, mode, sweeps = min(trials)
         s.set_precision(mode)

@@ -75,6 +75,24 @@ def test_unpreconditioned_pressure_solve(ibm, mode):
     assert np.array_equal(out[0], out[1], equal_nan=True)   # NaN on solid cells
 
 
+def test_long_solves_meet_the_divergence_bound(ibm):
+    """The LES channel (128x96x128, 13-16 pressure iterations per step):
+    over many iterations the double-float recursive residual can drift from
+    the true one by more than the bound's margin (one step of an earlier
+    version ended at max|div U| = 1.27e-8 against 1e-8).  Every solve now
+    checks the true residual before it stops, so every step meets the
+    bound."""
+    wl = __import__("importlib").import_module("2020researchproject_gb300.workloads")
+    case = wl.channel()
+    s = wl.build_solver(ibm, case, tol=1e-6, div_tol=1e-8)
+    s.set_precision(ibm.MIXED32)
+    s.init_flow_array(*wl.initial_state(case))
+    s.iterate(53)
+    st = s.stats()
+    s.close()
+    assert st["max_div_max"] <= 1e-8, st["max_div_max"]
+
+
 def test_pressure_vectors_argument(ibm):
     s = ibm.IBMSolver()
     with pytest.raises(ibm.IBM3DError):
